@@ -1,0 +1,400 @@
+#!/usr/bin/env python
+"""Bundle-adjustment throughput on GB300: LM iterations/s and observations/s
+of the mixed-precision form against the plain FP64 form on the same scene,
+with the final-cost agreement, a live roofline of the dominant phase, an
+end-to-end number through the C ABI with host buffers, and a CPU baseline.
+
+Workload (default): the 1M-observation random-walk scene (200 keyframes,
+50,000 landmarks, ~1.02M observations, 20 LM iterations), synthetic and
+seeded. A step is one full 20-iteration solve from the initial state.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank solves its own replica (independent problems, no
+collective): value = iterations of all ranks / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BA LM iters/s & obs/s, mixed vs FP64 GPU at <=1e-6 rel cost; CPU ref beside"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="walk", choices=["walk", "arc", "loop"])
+    ap.add_argument("--iterations", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int, enabled: bool = True):
+        self.proc = None
+        self.path = None
+        if not enabled:
+            return
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_scene(name: str):
+    from zeroslam_gb300 import scenes
+
+    if name == "walk":
+        return scenes.large_scene()
+    if name == "loop":
+        return scenes.loop_large_scene()
+    return scenes.small_scene()
+
+
+def schur_triples(sc) -> int:
+    valid = (sc.pose_fixed[sc.obs_pose] == 0) & (sc.landmark_fixed[sc.obs_landmark] == 0)
+    d = np.bincount(sc.obs_landmark[valid], minlength=sc.L).astype(np.int64)
+    return int(np.sum(d * (d + 1) // 2))
+
+
+def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) -> dict:
+    """Roofline of the phase with the largest device time (algorithmic work
+    per call / measured average call duration)."""
+    s = 8 if precision == 0 else 4
+    K, L, M = sc.K, sc.L, sc.M
+    n = 6 * K
+    d = M / max(1, L)
+    T = schur_triples(sc)
+    pipe = peaks["fp64_tflops"] if precision == 0 else peaks["fp32_tflops"]
+    pipe_name = "fp64" if precision == 0 else "fp32"
+    work = {
+        # bytes: read observation + write H_pl, and H_ll / H_pp / b once
+        "linearize": ("hbm", M * (24 + 18 * s) + L * 12 * s + K * 42 * s, None),
+        "invert": ("hbm", L * (9 * 8 * 2) + M * 18 * s * 2, None),
+        # flops of the pair products W_i H_j^T (6x6x3 multiply-adds per triple)
+        "schur": (pipe_name, None, T * 216.0 + M * 36.0),
+        "factor": (pipe_name, None, n ** 3 / 3.0),
+        "trisolve": ("hbm", n * n * s * 2, None),
+        "update": ("hbm", M * 18 * s + L * 48 + K * 112, None),
+        "cost": ("hbm", M * 24 + L * 32 + K * 64, None),
+    }
+    ms = prof["ms_phase"]
+    calls = prof["phase_calls"]
+    top = max((p for p in work if calls.get(p, 0) > 0), key=lambda p: ms[p])
+    bound, nbytes, flops = work[top]
+    per_call_ms = ms[top] / calls[top]
+    if nbytes is not None:
+        achieved = nbytes / (per_call_ms * 1e-3) / 1e9
+        peak, unit, fallback = hbm_gbs, "GB/s", "MEASURED_PEAKS.json hbm_gbs"
+    else:
+        achieved = flops / (per_call_ms * 1e-3) / 1e12
+        peak, unit, fallback = pipe, "TFLOP/s", f"zs_pipe_peaks {pipe_name} FMA chain, measured in this run"
+    return {"phase": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak if peak else None, "traffic": None, "peak_source": fallback,
+            "ms_per_call": per_call_ms, "calls": calls[top],
+            "phase_share": ms[top] / max(1e-9, sum(ms.values()))}
+
+
+def run_solves(sc, precision: int, steps: int, warmup: int, iters: int, device: int, dist: Dist):
+    from zeroslam_gb300 import ba
+
+    h = ba.BundleAdjuster(precision=precision, device=device)
+    h.set_problem(sc)
+    for _ in range(warmup):
+        h.reset_state()
+        h.solve(iters)
+    dist.barrier()
+    ms = 0.0
+    it = 0
+    launches = 0
+    reps = []
+    for _ in range(steps):
+        h.reset_state()
+        rep = h.solve(iters)
+        ms += rep.ms_total
+        it += rep.iterations
+        launches += rep.kernel_launches
+        reps.append(rep)
+    dist.barrier()
+    final_chi2 = h.chi2()
+    h.close()
+    return dict(ms=ms, iterations=it, launches=launches, chi2=final_chi2, rep=reps[-1].as_dict())
+
+
+def profile_solve(sc, precision: int, iters: int, device: int) -> dict:
+    from zeroslam_gb300 import ba
+
+    with ba.BundleAdjuster(precision=precision, device=device, profile=1) as h:
+        h.set_problem(sc)
+        return h.solve(iters).as_dict()
+
+
+def e2e_run(sc, precision: int, steps: int, iters: int, device: int, dist: Dist):
+    """Through the C ABI with host buffers: upload + structure analysis +
+    solve + state read-back, every step."""
+    from zeroslam_gb300 import ba
+
+    h = ba.BundleAdjuster(precision=precision, device=device)
+    h.set_problem(sc)
+    h.solve(1)
+    h2d = (sc.poses.nbytes + sc.pose_fixed.nbytes + sc.landmarks.nbytes + sc.landmark_fixed.nbytes +
+           sc.obs_pose.nbytes + sc.obs_landmark.nbytes + sc.obs_uv.nbytes)
+    dist.barrier()
+    t0 = time.perf_counter()
+    it = 0
+    attempts = 0
+    for _ in range(steps):
+        h.set_problem(sc)
+        rep = h.solve(iters)
+        h.get_state()
+        it += rep.iterations
+        attempts += rep.attempts + 1
+    dist.barrier()
+    dt = time.perf_counter() - t0
+    h.close()
+    # per-attempt LM state read-backs (one 104-byte record each) plus the state
+    d2h = (7 * sc.K + 3 * sc.L) * 8 + 104 * attempts // steps
+    return dict(seconds=dt, iterations=it, h2d=h2d, d2h=d2h)
+
+
+def cpu_port_baseline(sc, kind: str):
+    """Seconds per LM iteration of a CPU implementation on the full scene,
+    from two landmark subsamples of it (every pose kept): t = a * M + c."""
+    from oracle.oracle import Oracle, Reference
+    from zeroslam_gb300 import scenes
+
+    impl = Reference() if kind == "reference" else Oracle()
+    pts = []
+    fracs = (0.02, 0.04) if kind == "reference" else (0.05, 0.10)
+    for frac in fracs:
+        Ls = max(10, int(sc.L * frac))
+        keep = sc.obs_landmark < Ls
+        sub = scenes.Scene(name="sample", poses=sc.poses.copy(), pose_fixed=sc.pose_fixed.copy(),
+                           landmarks=sc.landmarks[:Ls].copy(), landmark_fixed=sc.landmark_fixed[:Ls].copy(),
+                           obs_pose=sc.obs_pose[keep].copy(), obs_landmark=sc.obs_landmark[keep].copy(),
+                           obs_uv=sc.obs_uv[keep].copy())
+        t0 = time.perf_counter()
+        if kind == "reference":
+            _, _, _, _, _, _, solve_s = impl.solve(sub, 1)
+            dt = solve_s
+        else:
+            impl.solve(sub, 1)
+            dt = time.perf_counter() - t0
+        pts.append((sub.M, dt, Ls))
+    (m1, t1, l1), (m2, t2, l2) = pts
+    a = (t2 - t1) / max(1, (m2 - m1))
+    c = max(0.0, t1 - a * m1)
+    t_full = a * sc.M + c
+    sample = (f"one LM iteration (solve(1)) on landmark subsamples of the same scene: L={l1} (M={m1}) took "
+              f"{t1:.2f} s, L={l2} (M={m2}) took {t2:.2f} s; extrapolated linearly in M to the full "
+              f"M={sc.M}: {t_full:.1f} s per iteration")
+    return 1.0 / t_full, sample, t1 + t2
+
+
+def reference_arm(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    from oracle import build as ob
+
+    sc = make_scene(args.workload)
+    iters = args.iterations or sc.iterations
+    kind = "reference" if os.path.exists(ob.REF_SO) and ob.reference_available() else "port"
+    vals = []
+    sample = ""
+    for _ in range(max(1, args.steps)):
+        v, sample, _ = cpu_port_baseline(sc, kind)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "LM iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * iters / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"{args.workload}: K={sc.K} poses, L={sc.L} landmarks, M={sc.M} observations",
+                       "iterations": iters},
+            "cpu_baseline": {"value": value, "unit": "LM iters/s", "cores": 1, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "LM iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def ours_arm(args, dist: Dist):
+    from zeroslam_gb300 import ba
+
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else open(os.devnull) as f:
+        try:
+            mp = json.load(f)
+        except Exception:
+            mp = {}
+    hbm = float(mp.get("hbm_gbs", 6800.0))
+    device = dist.local
+    sc = make_scene(args.workload)
+    iters = args.iterations or sc.iterations
+    f64, f32 = ba.pipe_peaks(device)
+    peaks = {"fp64_tflops": f64, "fp32_tflops": f32}
+
+    clocks = Clocks(device, enabled=not args.no_clocks)
+    mixed = run_solves(sc, ba.MIXED, args.steps, args.warmup, iters, device, dist)
+    fp64 = run_solves(sc, ba.FP64, args.steps, args.warmup, iters, device, dist)
+    clk = clocks.stop()
+
+    prof_m = profile_solve(sc, ba.MIXED, iters, device)
+    prof_d = profile_solve(sc, ba.FP64, iters, device)
+    roof_m = phase_roofline(sc, prof_m, 1, peaks, hbm)
+    roof_d = phase_roofline(sc, prof_d, 0, peaks, hbm)
+
+    max_ms_m = dist.max(mixed["ms"])
+    max_ms_d = dist.max(fp64["ms"])
+    it_m = dist.sum(mixed["iterations"])
+    it_d = dist.sum(fp64["iterations"])
+    value = it_m / (max_ms_m * 1e-3)
+    value_d = it_d / (max_ms_d * 1e-3)
+    rel_cost = abs(mixed["chi2"] - fp64["chi2"]) / fp64["chi2"]
+
+    e2e = None
+    if not args.no_e2e:
+        e = e2e_run(sc, ba.MIXED, args.steps, iters, device, dist)
+        e2e_val = dist.sum(e["iterations"]) / dist.max(e["seconds"])
+        e2e = {"value": e2e_val, "unit": "LM iters/s", "h2d_bytes_per_step": int(e["h2d"]),
+               "d2h_bytes_per_step": int(e["d2h"]),
+               "includes": "zs_ba_set_problem (H2D + structure analysis) + zs_ba_solve + zs_ba_get_state"}
+
+    cpu = None
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        from oracle import build as ob
+
+        kind = "reference" if os.path.exists(ob.REF_SO) and ob.reference_available() else "port"
+        v, sample, _ = cpu_port_baseline(sc, kind)
+        cpu = {"value": v, "unit": "LM iters/s", "cores": 1, "kind": kind, "sample": sample}
+
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "LM iters/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms_m / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (mixed form)", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": f"{args.workload}: K={sc.K} poses, L={sc.L} landmarks, M={sc.M} observations, "
+                               f"{iters} LM iterations per step",
+                   "iterations": iters, "precision": "mixed", "parallelism": f"replicas x{dist.world}",
+                   "l2": "working set > L2 (no flush needed)"},
+        "obs_per_s": value * sc.M,
+        "fp64": {"value": value_d, "unit": "LM iters/s", "obs_per_s": value_d * sc.M,
+                 "ms_per_step": max_ms_d / args.steps, "final_chi2": fp64["chi2"], "rep": fp64["rep"],
+                 "roofline": roof_d, "profile_ms": prof_d["ms_phase"]},
+        "mixed_over_fp64": value / value_d,
+        "mixed_final_chi2": mixed["chi2"], "mixed_rel_cost_vs_fp64": rel_cost, "mixed_rep": mixed["rep"],
+        "profile_ms": prof_m["ms_phase"],
+        "roofline": roof_m,
+        "pipe_peaks": peaks,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": int(dist.sum(mixed["launches"])),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        reference_arm(args, dist)
+    else:
+        ours_arm(args, dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * zeroslam_ba.h — C ABI of the GB300 (sm_103a) sparse-block bundle adjuster.
+ *
+ * This library replaces the Levenberg-Marquardt / Schur-complement solve of
+ * zeroslam's factor graph for SE(3) keyframe poses and 3-D landmarks joined
+ * by pinhole reprojection edges. Every entry point takes plain host pointers
+ * and sizes; the handle owns all device memory and one CUDA stream. No CPU
+ * fallback exists: without a usable CUDA device every call that needs one
+ * returns ZS_ERR_CUDA.
+ *
+ * Entry point -> reference interface it replaces (paths inside gpdaniels/zeroslam):
+ *   zs_ba_create / zs_ba_destroy  factor_graph::factor_graph(bool)          source/factor_graph.hpp:379
+ *   zs_ba_set_problem             add_vertex / add_edge / set_observation /
+ *                                 set_information / set_loss_function      source/factor_graph.hpp:385,444,
+ *                                                                          198-277; graph build source/map.hpp:129-179
+ *   zs_ba_solve                   int factor_graph::solve(int, bool)       source/factor_graph.hpp:489-615
+ *   zs_ba_chi2                    double get_current_chi(bool)             source/factor_graph.hpp:618-629
+ *   zs_ba_get_state/zs_ba_set_state vertex_base::get/set_parameters        source/factor_graph.hpp:123-129
+ *   zs_ba_linear_step             make_hessian + solve_linear_system       source/factor_graph.hpp:648-806
+ *   zs_dense_cholesky_solve       matrix::decompose_cholesky +
+ *                                 matrix::solve_cholesky                   source/matrix_decomposition_cholesky.hpp:26-95
+ *   zs_ba_reset_state             vertex_base::restore                     source/factor_graph.hpp:135-137
+ *   zs_ba_status_string           (stderr diagnostics of solve)           source/factor_graph.hpp:495,786
+ *
+ * Conventions: return values are status codes (0 = ok, negative = error);
+ * nothing throws or aborts across this boundary. Host buffers stay owned by
+ * the caller and are copied. A handle is not thread-safe; use one handle per
+ * host thread. Results are bit-for-bit reproducible from run to run on the
+ * same device (no floating-point atomics).
+ */
+#ifndef ZEROSLAM_BA_H
+#define ZEROSLAM_BA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZS_BA_ABI_VERSION 1
+
+/* Status codes. */
+#define ZS_OK 0
+#define ZS_ERR_INVALID (-1)      /* bad argument or problem (index out of range, NULL pointer) */
+#define ZS_ERR_CUDA (-2)         /* CUDA runtime error or no usable device */
+#define ZS_ERR_UNSUPPORTED (-3)  /* vertex / edge / loss kind the device path does not implement */
+#define ZS_ERR_TIMEOUT (-4)      /* a bounded device wait ran out */
+#define ZS_ERR_NONFINITE (-5)    /* non-finite values in the inputs */
+#define ZS_ERR_NO_PROBLEM (-6)   /* solve/get before set_problem */
+#define ZS_ERR_OUT_OF_MEMORY (-7)
+#define ZS_ERR_CHOLESKY (-8)     /* dense Cholesky factor or solve failed its pivot test */
+
+/* Arithmetic of the solve. */
+#define ZS_PRECISION_FP64 0  /* everything in double: the reference's arithmetic */
+#define ZS_PRECISION_MIXED 1 /* FP32 Jacobians/Hessian/Schur, FP32 factor, FP64 refinement, FP64 cost */
+
+/* Robust losses of source/factor_graph.hpp:851-934. */
+#define ZS_LOSS_NONE 0
+#define ZS_LOSS_HUBER 1
+#define ZS_LOSS_CAUCHY 2
+#define ZS_LOSS_TUKEY 3
+
+typedef struct zs_ba_handle zs_ba_handle;
+
+/* Solver settings. zs_ba_default_options() gives the reference's constants
+ * (source/factor_graph.hpp:511-536). */
+typedef struct zs_ba_options {
+    int32_t precision;          /* ZS_PRECISION_* */
+    int32_t max_failures;       /* 10: failed attempts per outer iteration */
+    double tau;                 /* 1e-5: initial damping = tau * min(clamp, max diag) */
+    double diagonal_clamp;      /* 5e10 */
+    double legacy_stop;         /* 1e-10: stop when the gain < legacy_stop * chi2_initial */
+    double relative_tolerance;  /* 1e-6: stop when the gain < tol * max(last, floor) */
+    double chi2_floor;          /* 1e-12 */
+    int32_t refine_iterations;  /* mixed form: FP64 refinement sweeps at most (8) */
+    double refine_tolerance;    /* mixed form: stop refining at ||b - S x|| <= tol ||b|| (1e-12) */
+    int32_t device;             /* CUDA device ordinal (0) */
+    int32_t verbose;            /* 1: print [INIT]/[GOOD]/[ BAD] lines to stderr */
+    int32_t profile;            /* 1: time each phase with CUDA events into zs_ba_report.ms_phase */
+} zs_ba_options;
+
+/* A bundle-adjustment problem as structure of arrays (host pointers).
+ * Pose parameters are zeroslam's vertex_pose layout (tx, ty, tz, qx, qy, qz, qw),
+ * world->camera (source/factor_graph.hpp:941). Quaternions are used as given,
+ * without renormalisation, as the reference does. */
+typedef struct zs_ba_problem {
+    int32_t num_poses;              /* K */
+    int32_t num_landmarks;          /* L */
+    int64_t num_obs;                /* M: one edge_reprojection each */
+    const double* poses;            /* [K*7] */
+    const uint8_t* pose_fixed;      /* [K] nonzero = fixed (still ordered into the reduced system) */
+    const double* landmarks;        /* [L*3] */
+    const uint8_t* landmark_fixed;  /* [L] */
+    const int32_t* obs_pose;        /* [M] pose index of each observation */
+    const int32_t* obs_landmark;    /* [M] landmark index of each observation */
+    const double* obs_uv;           /* [M*2] observed pixel */
+    const double* obs_info;         /* [M*4] row-major 2x2 information, or NULL for identity */
+    double intrinsics[4];           /* fx, fy, cx, cy of camera::pinhole */
+    int32_t loss_kind;              /* ZS_LOSS_* shared by all edges */
+    double loss_delta;
+} zs_ba_problem;
+
+/* What a solve did. */
+typedef struct zs_ba_report {
+    int32_t status;            /* ZS_OK or the error returned */
+    int32_t iterations;        /* outer LM iterations run */
+    int32_t accepted;          /* accepted steps (the reference's solve() return value) */
+    int32_t attempts;          /* damped linear solves attempted */
+    int32_t cholesky_failures; /* attempts whose reduced Cholesky failed */
+    int32_t refine_sweeps;     /* mixed form: refinement sweeps over all attempts */
+    double chi2_initial;
+    double chi2_final;
+    double lambda_final;
+    double ms_total;           /* device time of the solve (CUDA events) */
+    /* With options.profile: device milliseconds and launch counts per phase
+     * (ZS_PHASE_*), summed over the solve. */
+    double ms_phase[8];
+    int32_t phase_calls[8];
+    int64_t kernel_launches;   /* kernels this library launched during the solve */
+} zs_ba_report;
+
+/* Phases of zs_ba_report.ms_phase. */
+#define ZS_PHASE_LINEARIZE 0 /* residuals, Jacobians, H_pp / H_pl / H_ll / b assembly */
+#define ZS_PHASE_INVERT 1    /* damped H_ll inverses and W = H_pl H_ll^-1 */
+#define ZS_PHASE_SCHUR 2     /* S = H_pp - W H_lp and b_s */
+#define ZS_PHASE_FACTOR 3    /* reduced Cholesky factorisation */
+#define ZS_PHASE_TRISOLVE 4  /* triangular solves and refinement */
+#define ZS_PHASE_UPDATE 5    /* back-substitution, state update, gain scale */
+#define ZS_PHASE_COST 6      /* robust chi2, LM decision, rollback */
+#define ZS_PHASE_OTHER 7
+
+void zs_ba_default_options(zs_ba_options* opt);
+
+int zs_ba_create(zs_ba_handle** out, const zs_ba_options* opt);
+void zs_ba_destroy(zs_ba_handle* h);
+
+/* Uploads a problem and analyses its structure (landmark- and pose-major
+ * orderings, Schur pair lists). Replaces any previous problem. */
+int zs_ba_set_problem(zs_ba_handle* h, const zs_ba_problem* p);
+
+/* Overwrites / reads the current vertex parameters ([K*7], [L*3]). */
+int zs_ba_set_state(zs_ba_handle* h, const double* poses, const double* landmarks);
+int zs_ba_get_state(zs_ba_handle* h, double* poses, double* landmarks);
+
+/* Restores the vertex parameters uploaded by zs_ba_set_problem (a device
+ * copy), so a problem can be solved again from the same initial guess. */
+int zs_ba_reset_state(zs_ba_handle* h);
+
+/* Levenberg-Marquardt with Schur complement, `iterations` outer iterations,
+ * stop rule as source/factor_graph.hpp:608-611. Returns the accepted-step
+ * count (>= 0) or a negative status; `rep` may be NULL. */
+int zs_ba_solve(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* rep);
+
+/* Robust chi2 of the current state. */
+int zs_ba_chi2(zs_ba_handle* h, double* chi2);
+
+/* One linearisation at the current state and one damped solve at `lambda`,
+ * without changing the state. Outputs (each may be NULL): S [n*n] the damped
+ * reduced camera matrix (n = 6K, row-major), bs [n] its right-hand side,
+ * delta [6K+3L] the step (poses then landmarks), b [6K+3L] the gradient
+ * vector. Returns ZS_OK or ZS_ERR_CHOLESKY. */
+int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b);
+
+/* Initial damping tau * min(clamp, max diagonal of H) at the current state. */
+int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda);
+
+/* Dense SPD solve on the device with the reference's pivot tests: factors the
+ * row-major n x n matrix A = L L^T and solves L L^T x = b. L (n*n, lower, zero
+ * above the diagonal) and x may be NULL. precision: ZS_PRECISION_FP64, or
+ * ZS_PRECISION_MIXED (FP32 factor + FP64 refinement of x).
+ * Returns ZS_OK or ZS_ERR_CHOLESKY. */
+int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, double* x, int precision);
+
+/* Measures the FP64 and FP32 fused multiply-add pipe peaks of `device` with
+ * a register-resident FMA chain on every SM (TFLOP/s, 2 flops per FMA). A
+ * measurement utility for roofline reports; no reference counterpart. */
+int zs_pipe_peaks(int device, double* fp64_tflops, double* fp32_tflops);
+
+const char* zs_ba_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ZEROSLAM_BA_H */

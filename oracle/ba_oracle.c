@@ -1,0 +1,624 @@
+/*
+ * CPU restatement of zeroslam's factor-graph bundle adjustment (the oracle).
+ * TEST INFRASTRUCTURE ONLY: see ba_oracle.h. Every function names the
+ * reference lines it follows.
+ */
+#include "ba_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PENALTY 0.3 /* source/factor_graph.hpp:981 */
+
+/* ---------------------------------------------------------------- lie / camera */
+
+/* Quaternion product (w, x, y, z), term order of source/lie.hpp:337-344. */
+static void qmul(const double a[4], const double b[4], double o[4]) {
+    o[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+    o[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+    o[2] = a[0] * b[2] - a[1] * b[3] + a[2] * b[0] + a[3] * b[1];
+    o[3] = a[0] * b[3] + a[1] * b[2] - a[2] * b[1] + a[3] * b[0];
+}
+
+/* Rotate a point by q (w, x, y, z) as q (0, p) q*, source/lie.hpp:347-362;
+ * the quaternion is not normalised. */
+static void qrotate(const double q[4], const double p[3], double o[3]) {
+    const double pq[4] = {0.0, p[0], p[1], p[2]};
+    const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
+    double t[4], r[4];
+    qmul(q, pq, t);
+    qmul(t, qc, r);
+    o[0] = r[1];
+    o[1] = r[2];
+    o[2] = r[3];
+}
+
+/* Rotation matrix of q, source/lie.hpp:188-204 (assumes a unit quaternion). */
+static void qmatrix(const double q[4], double R[9]) {
+    const double tx = 2.0 * q[1], ty = 2.0 * q[2], tz = 2.0 * q[3];
+    const double txx = tx * q[1], txy = tx * q[2], txz = tx * q[3], txw = tx * q[0];
+    const double tyy = ty * q[2], tyz = ty * q[3], tyw = ty * q[0];
+    const double tzz = tz * q[3], tzw = tz * q[0];
+    R[0] = 1.0 - (tyy + tzz); R[1] = txy - tzw;         R[2] = txz + tyw;
+    R[3] = txy + tzw;         R[4] = 1.0 - (txx + tzz); R[5] = tyz - txw;
+    R[6] = txz - tyw;         R[7] = tyz + txw;         R[8] = 1.0 - (txx + tyy);
+}
+
+/* so3::exp, source/lie.hpp:247-264. */
+static void so3_exp(const double w[3], double q[4]) {
+    const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    double re, sc;
+    if (th2 < 1e-6 * 1e-6) {
+        const double th4 = th2 * th2;
+        re = 1.0 - (1.0 / 8.0) * th2 + (1.0 / 384.0) * th4;
+        sc = 0.5 - (1.0 / 48.0) * th2 + (1.0 / 3840.0) * th4;
+    } else {
+        const double th = sqrt(th2);
+        const double h = 0.5 * th;
+        re = cos(h);
+        sc = sin(h) / th;
+    }
+    q[0] = re;
+    q[1] = w[0] * sc;
+    q[2] = w[1] * sc;
+    q[3] = w[2] * sc;
+}
+
+/* so3::left_jacobian, source/lie.hpp:284-294. */
+static void so3_left_jacobian(const double w[3], double J[9]) {
+    const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    const double H[9] = {0.0, -w[2], w[1], w[2], 0.0, -w[0], -w[1], w[0], 0.0};
+    double H2[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 3; ++k) s += H[i * 3 + k] * H[k * 3 + j];
+            H2[i * 3 + j] = s;
+        }
+    double a, b;
+    if (th2 < 1e-6 * 1e-6) {
+        a = 0.5;
+        b = 1.0 / 6.0;
+    } else {
+        const double th = sqrt(th2);
+        a = (1.0 - cos(th)) / th2;
+        b = (th - sin(th)) / (th2 * th);
+    }
+    for (int i = 0; i < 9; ++i) J[i] = ((i % 4 == 0) ? 1.0 : 0.0) + a * H[i] + b * H2[i];
+}
+
+void zso_pose_plus(double p[7], const double d[6]) {
+    /* vertex_pose::plus, source/factor_graph.hpp:947-960: T <- exp(d) T with
+     * se3::exp (source/lie.hpp:446-450) and se3 * se3 (source/lie.hpp:521-526). */
+    const double q[4] = {p[6], p[3], p[4], p[5]};
+    const double t[3] = {p[0], p[1], p[2]};
+    double dq[4], J[9], dt[3], nq[4], rt[3];
+    so3_exp(d, dq);
+    so3_left_jacobian(d, J);
+    for (int i = 0; i < 3; ++i) dt[i] = J[i * 3 + 0] * d[3] + J[i * 3 + 1] * d[4] + J[i * 3 + 2] * d[5];
+    qmul(dq, q, nq);
+    qrotate(dq, t, rt);
+    p[0] = rt[0] + dt[0];
+    p[1] = rt[1] + dt[1];
+    p[2] = rt[2] + dt[2];
+    p[3] = nq[1];
+    p[4] = nq[2];
+    p[5] = nq[3];
+    p[6] = nq[0];
+}
+
+int zso_edge(const double pose[7], const double X[3], const double uv[2], const double intr[4],
+             double r[2], double Jp[12], double Jl[6]) {
+    /* edge_reprojection::compute_residual / compute_jacobians,
+     * source/factor_graph.hpp:990-1048, and pinhole::project, source/camera.hpp:91-126. */
+    const double q[4] = {pose[6], pose[3], pose[4], pose[5]};
+    double Xc[3];
+    qrotate(q, X, Xc);
+    Xc[0] += pose[0];
+    Xc[1] += pose[1];
+    Xc[2] += pose[2];
+    double Jc[6];
+    int front = !(Xc[2] < 1.0e-12);
+    if (front) {
+        const double iz = 1.0 / Xc[2];
+        const double u = intr[0] * (Xc[0] * iz) + intr[2];
+        const double v = intr[1] * (Xc[1] * iz) + intr[3];
+        r[0] = uv[0] - u;
+        r[1] = uv[1] - v;
+        const double iz2 = iz * iz;
+        Jc[0] = intr[0] * iz; Jc[1] = 0.0; Jc[2] = -intr[0] * Xc[0] * iz2;
+        Jc[3] = 0.0; Jc[4] = intr[1] * iz; Jc[5] = -intr[1] * Xc[1] * iz2;
+    } else {
+        const double pen = -PENALTY * Xc[2];
+        r[0] = pen;
+        r[1] = pen;
+        Jc[0] = 0.0; Jc[1] = 0.0; Jc[2] = PENALTY;
+        Jc[3] = 0.0; Jc[4] = 0.0; Jc[5] = PENALTY;
+    }
+    if (Jp) {
+        const double Xv = Xc[0], Yv = Xc[1], Zv = Xc[2];
+        const double P[18] = {0.0, Zv, -Yv, 1.0, 0.0, 0.0,
+                              -Zv, 0.0, Xv, 0.0, 1.0, 0.0,
+                              Yv, -Xv, 0.0, 0.0, 0.0, 1.0};
+        for (int i = 0; i < 2; ++i)
+            for (int c = 0; c < 6; ++c) {
+                double s = 0.0;
+                for (int k = 0; k < 3; ++k) s += Jc[i * 3 + k] * P[k * 6 + c];
+                Jp[i * 6 + c] = -s;
+            }
+    }
+    if (Jl) {
+        double R[9];
+        qmatrix(q, R);
+        for (int i = 0; i < 2; ++i)
+            for (int c = 0; c < 3; ++c) {
+                double s = 0.0;
+                for (int k = 0; k < 3; ++k) s += Jc[i * 3 + k] * R[k * 3 + c];
+                Jl[i * 3 + c] = -s;
+            }
+    }
+    return front;
+}
+
+void zso_loss(int kind, double delta, double e2, double rho[3]) {
+    /* source/factor_graph.hpp:851-934 */
+    const double d2 = delta * delta;
+    if (kind == 1) {
+        if (e2 <= d2) {
+            rho[0] = e2; rho[1] = 1.0; rho[2] = 0.0;
+        } else {
+            const double e = sqrt(e2);
+            rho[0] = 2.0 * e * delta - d2;
+            rho[1] = delta / e;
+            rho[2] = -0.5 * rho[1] / e2;
+        }
+    } else if (kind == 2) {
+        const double inv = 1.0 / d2;
+        const double aux = inv * e2 + 1.0;
+        rho[0] = d2 * log(aux);
+        rho[1] = 1.0 / aux;
+        rho[2] = -inv * (rho[1] * rho[1]);
+    } else if (kind == 3) {
+        if (e2 <= d2) {
+            const double aux = e2 / d2;
+            const double om = 1.0 - aux;
+            const double om2 = om * om;
+            const double om3 = om2 * om;
+            rho[0] = d2 * (1.0 - om3) / 3.0;
+            rho[1] = om2;
+            rho[2] = -2.0 * om / d2;
+        } else {
+            rho[0] = d2 / 3.0; rho[1] = 0.0; rho[2] = 0.0;
+        }
+    } else {
+        rho[0] = e2; rho[1] = 1.0; rho[2] = 0.0;
+    }
+}
+
+static const double IDENT2[4] = {1.0, 0.0, 0.0, 1.0};
+
+static double edge_chi2(const double r[2], const double* om) {
+    /* r^T Omega r, source/factor_graph.hpp:217-219 */
+    const double a = r[0] * om[0] + r[1] * om[2];
+    const double b = r[0] * om[1] + r[1] * om[3];
+    return a * r[0] + b * r[1];
+}
+
+double zso_chi2(const zso_problem* p) {
+    /* get_current_chi, source/factor_graph.hpp:618-629 */
+    double total = 0.0;
+    for (long long o = 0; o < p->num_obs; ++o) {
+        const double* pose = p->poses + 7LL * p->obs_pose[o];
+        const double* X = p->landmarks + 3LL * p->obs_landmark[o];
+        double r[2];
+        zso_edge(pose, X, p->obs_uv + 2 * o, p->intrinsics, r, NULL, NULL);
+        const double* om = p->obs_info ? p->obs_info + 4 * o : IDENT2;
+        const double e2 = edge_chi2(r, om);
+        double rho[3];
+        zso_loss(p->loss_kind, p->loss_delta, e2, rho);
+        total += (p->loss_kind ? rho[0] : e2);
+    }
+    return total;
+}
+
+int zso_invert3(const double a[9], double o[9]) {
+    /* matrix::invert<3>, source/matrix.hpp:749-774 */
+    const double det = +a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                       a[2] * (a[3] * a[7] - a[4] * a[6]);
+    double scale = 0.0;
+    for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
+    if (!(fabs(det) > scale * scale * scale * 1e-12)) {
+        memset(o, 0, 9 * sizeof(double));
+        return 0;
+    }
+    const double id = 1.0 / det;
+    o[0] = (a[4] * a[8] - a[7] * a[5]) * id;
+    o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+    o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+    o[3] = (a[5] * a[6] - a[3] * a[8]) * id;
+    o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+    o[5] = (a[3] * a[2] - a[0] * a[5]) * id;
+    o[6] = (a[3] * a[7] - a[6] * a[4]) * id;
+    o[7] = (a[6] * a[1] - a[0] * a[7]) * id;
+    o[8] = (a[0] * a[4] - a[3] * a[1]) * id;
+    return 1;
+}
+
+int zso_cholesky(const double* A, int n, double* L) {
+    /* decompose_cholesky, source/matrix_decomposition_cholesky.hpp:26-59 */
+    memset(L, 0, (size_t)n * n * sizeof(double));
+    double scale = 0.0;
+    for (int i = 0; i < n; ++i) scale = fmax(scale, fabs(A[(size_t)i * n + i]));
+    const double eps = scale * 1e-14;
+    for (int i = 0; i < n; ++i) {
+        const double* Li = L + (size_t)i * n;
+        for (int k = 0; k < i; ++k) {
+            const double* Lk = L + (size_t)k * n;
+            double v = A[(size_t)i * n + k];
+            for (int j = 0; j < k; ++j) v -= Li[j] * Lk[j];
+            L[(size_t)i * n + k] = v / Lk[k];
+        }
+        double v = A[(size_t)i * n + i];
+        for (int j = 0; j < i; ++j) v -= Li[j] * Li[j];
+        if (!(v > eps)) return 0;
+        L[(size_t)i * n + i] = sqrt(v);
+    }
+    return 1;
+}
+
+int zso_cholesky_solve(const double* L, const double* b, int n, double* x) {
+    /* solve_cholesky, source/matrix_decomposition_cholesky.hpp:61-95 */
+    double scale = 0.0;
+    for (int i = 0; i < n; ++i) scale = fmax(scale, fabs(L[(size_t)i * n + i]));
+    const double eps = scale * 1e-7;
+    for (int i = 0; i < n; ++i) {
+        x[i] = b[i];
+        for (int j = 0; j < i; ++j) x[i] -= L[(size_t)i * n + j] * x[j];
+        if (!(fabs(L[(size_t)i * n + i]) > eps)) return 0;
+        x[i] /= L[(size_t)i * n + i];
+    }
+    for (int i = n; i-- > 0;) {
+        for (int j = i + 1; j < n; ++j) x[i] -= L[(size_t)j * n + i] * x[j];
+        if (!(fabs(L[(size_t)i * n + i]) > eps)) return 0;
+        x[i] /= L[(size_t)i * n + i];
+    }
+    return 1;
+}
+
+/* ---------------------------------------------------------------- linearisation */
+
+typedef struct lin {
+    int K, L;
+    double* hpp;   /* K*36 */
+    double* hll;   /* L*9 */
+    double* b;     /* 6K + 3L */
+    /* H_pl blocks grouped by landmark, one per distinct non-fixed pose: */
+    int* lm_ptr;   /* L+1 */
+    int* blk_pose; /* nblk */
+    double* hpl;   /* nblk*18 */
+    int nblk;
+} lin;
+
+static void lin_free(lin* s) {
+    free(s->hpp); free(s->hll); free(s->b); free(s->lm_ptr); free(s->blk_pose); free(s->hpl);
+}
+
+/* make_hessian, source/factor_graph.hpp:648-732. */
+static int linearise(const zso_problem* p, lin* s) {
+    const int K = p->num_poses, L = p->num_landmarks;
+    const long long M = p->num_obs;
+    const int n = 6 * K;
+    memset(s, 0, sizeof(*s));
+    s->K = K; s->L = L;
+    s->hpp = calloc((size_t)K * 36, sizeof(double));
+    s->hll = calloc((size_t)L * 9 + 1, sizeof(double));
+    s->b = calloc((size_t)n + 3 * (size_t)L + 1, sizeof(double));
+    s->lm_ptr = calloc((size_t)L + 1, sizeof(int));
+    double* hpl_obs = calloc((size_t)M * 18 + 1, sizeof(double));
+    if (!s->hpp || !s->hll || !s->b || !s->lm_ptr || !hpl_obs) { free(hpl_obs); lin_free(s); return 0; }
+    for (long long o = 0; o < M; ++o) {
+        const int pi = p->obs_pose[o], li = p->obs_landmark[o];
+        const int pf = p->pose_fixed[pi], lf = p->landmark_fixed[li];
+        double r[2], Jp[12], Jl[6];
+        zso_edge(p->poses + 7LL * pi, p->landmarks + 3LL * li, p->obs_uv + 2 * o, p->intrinsics, r, Jp, Jl);
+        const double* om = p->obs_info ? p->obs_info + 4 * o : IDENT2;
+        /* edge_base::robust_info, source/factor_graph.hpp:254-269 */
+        double W[4] = {om[0], om[1], om[2], om[3]};
+        double drho = 1.0;
+        if (p->loss_kind) {
+            const double e2 = edge_chi2(r, om);
+            double rho[3];
+            zso_loss(p->loss_kind, p->loss_delta, e2, rho);
+            drho = rho[1];
+            for (int i = 0; i < 4; ++i) W[i] = rho[1] * om[i];
+            if ((rho[1] + 2.0 * rho[2] * e2) > 0.0) {
+                const double we0 = om[0] * r[0] + om[1] * r[1];
+                const double we1 = om[2] * r[0] + om[3] * r[1];
+                W[0] += 2.0 * rho[2] * we0 * we0;
+                W[1] += 2.0 * rho[2] * we0 * we1;
+                W[2] += 2.0 * rho[2] * we1 * we0;
+                W[3] += 2.0 * rho[2] * we1 * we1;
+            }
+        }
+        /* Omega r for the gradient (the non-robust information scaled by drho). */
+        const double orr[2] = {om[0] * r[0] + om[1] * r[1], om[2] * r[0] + om[3] * r[1]};
+        if (!pf) {
+            double JtW[12]; /* 6x2 */
+            for (int a = 0; a < 6; ++a) {
+                JtW[a * 2 + 0] = Jp[0 * 6 + a] * W[0] + Jp[1 * 6 + a] * W[2];
+                JtW[a * 2 + 1] = Jp[0 * 6 + a] * W[1] + Jp[1 * 6 + a] * W[3];
+            }
+            double* H = s->hpp + 36LL * pi;
+            for (int a = 0; a < 6; ++a)
+                for (int c = 0; c < 6; ++c) H[a * 6 + c] += JtW[a * 2] * Jp[c] + JtW[a * 2 + 1] * Jp[6 + c];
+            if (!lf) {
+                double* B = hpl_obs + 18 * o;
+                for (int a = 0; a < 6; ++a)
+                    for (int c = 0; c < 3; ++c) B[a * 3 + c] = JtW[a * 2] * Jl[c] + JtW[a * 2 + 1] * Jl[3 + c];
+            }
+            for (int a = 0; a < 6; ++a) s->b[6 * pi + a] -= drho * (Jp[a] * orr[0] + Jp[6 + a] * orr[1]);
+        }
+        if (!lf) {
+            double JtW[6]; /* 3x2 */
+            for (int a = 0; a < 3; ++a) {
+                JtW[a * 2 + 0] = Jl[0 * 3 + a] * W[0] + Jl[1 * 3 + a] * W[2];
+                JtW[a * 2 + 1] = Jl[0 * 3 + a] * W[1] + Jl[1 * 3 + a] * W[3];
+            }
+            double* H = s->hll + 9LL * li;
+            for (int a = 0; a < 3; ++a)
+                for (int c = 0; c < 3; ++c) H[a * 3 + c] += JtW[a * 2] * Jl[c] + JtW[a * 2 + 1] * Jl[3 + c];
+            for (int a = 0; a < 3; ++a) s->b[n + 3 * li + a] -= drho * (Jl[a] * orr[0] + Jl[3 + a] * orr[1]);
+        }
+    }
+    /* Group the pose-landmark blocks by landmark, one block per distinct pose
+     * (duplicate observations of a pair add up, as the hash map does). */
+    int* cnt = calloc((size_t)L + 1, sizeof(int));
+    long long* order = malloc(((size_t)M + 1) * sizeof(long long));
+    for (long long o = 0; o < M; ++o) cnt[p->obs_landmark[o] + 1]++;
+    for (int l = 0; l < L; ++l) cnt[l + 1] += cnt[l];
+    int* fill = calloc((size_t)L + 1, sizeof(int));
+    for (long long o = 0; o < M; ++o) {
+        const int l = p->obs_landmark[o];
+        order[cnt[l] + fill[l]++] = o;
+    }
+    s->blk_pose = malloc(((size_t)M + 1) * sizeof(int));
+    s->hpl = calloc((size_t)M * 18 + 1, sizeof(double));
+    int nb = 0;
+    for (int l = 0; l < L; ++l) {
+        s->lm_ptr[l] = nb;
+        long long* seg = order + cnt[l];
+        const int d = cnt[l + 1] - cnt[l];
+        /* insertion sort by pose, stable */
+        for (int i = 1; i < d; ++i) {
+            long long v = seg[i];
+            int j = i - 1;
+            while (j >= 0 && p->obs_pose[seg[j]] > p->obs_pose[v]) { seg[j + 1] = seg[j]; --j; }
+            seg[j + 1] = v;
+        }
+        if (p->landmark_fixed[l]) continue;
+        for (int i = 0; i < d; ++i) {
+            const long long o = seg[i];
+            const int pi = p->obs_pose[o];
+            if (p->pose_fixed[pi]) continue;
+            if (nb > s->lm_ptr[l] && s->blk_pose[nb - 1] == pi) {
+                for (int k = 0; k < 18; ++k) s->hpl[18LL * (nb - 1) + k] += hpl_obs[18 * o + k];
+            } else {
+                s->blk_pose[nb] = pi;
+                memcpy(s->hpl + 18LL * nb, hpl_obs + 18 * o, 18 * sizeof(double));
+                ++nb;
+            }
+        }
+    }
+    s->lm_ptr[L] = nb;
+    s->nblk = nb;
+    free(cnt); free(order); free(fill); free(hpl_obs);
+    return 1;
+}
+
+/* solve_linear_system, source/factor_graph.hpp:736-806. */
+static int solve_system(const zso_problem* p, const lin* s, double lambda, double* S_out, double* bs_out,
+                        double* delta) {
+    const int K = s->K, L = s->L, n = 6 * K;
+    double* S = calloc((size_t)n * n + 1, sizeof(double));
+    double* Lf = malloc(((size_t)n * n + 1) * sizeof(double));
+    double* bs = malloc(((size_t)n + 1) * sizeof(double));
+    double* hinv = calloc((size_t)L * 9 + 1, sizeof(double));
+    double* Wb = malloc(((size_t)s->nblk * 18 + 1) * sizeof(double));
+    int ok = 0;
+    if (!S || !Lf || !bs || !hinv || !Wb) goto done;
+    /* damped H_ll inverses; fixed landmarks keep a zero block, a singular
+     * block is left zero as the ignored invert() result does. */
+    for (int l = 0; l < L; ++l) {
+        if (p->landmark_fixed[l]) continue;
+        double A[9];
+        memcpy(A, s->hll + 9LL * l, sizeof(A));
+        A[0] += lambda; A[4] += lambda; A[8] += lambda;
+        zso_invert3(A, hinv + 9LL * l);
+    }
+    /* W = H_pl H_ll^-1 per block */
+    for (int l = 0; l < L; ++l)
+        for (int k = s->lm_ptr[l]; k < s->lm_ptr[l + 1]; ++k) {
+            const double* H = s->hpl + 18LL * k;
+            const double* I = hinv + 9LL * l;
+            double* W = Wb + 18LL * k;
+            for (int a = 0; a < 6; ++a)
+                for (int c = 0; c < 3; ++c)
+                    W[a * 3 + c] = H[a * 3 + 0] * I[0 * 3 + c] + H[a * 3 + 1] * I[1 * 3 + c] + H[a * 3 + 2] * I[2 * 3 + c];
+        }
+    /* b_s = b_p - W b_l */
+    memcpy(bs, s->b, (size_t)n * sizeof(double));
+    for (int l = 0; l < L; ++l)
+        for (int k = s->lm_ptr[l]; k < s->lm_ptr[l + 1]; ++k) {
+            const double* W = Wb + 18LL * k;
+            const double* bl = s->b + n + 3LL * l;
+            double* t = bs + 6LL * s->blk_pose[k];
+            for (int a = 0; a < 6; ++a) t[a] -= W[a * 3] * bl[0] + W[a * 3 + 1] * bl[1] + W[a * 3 + 2] * bl[2];
+        }
+    /* C = sum_l W_l H_l^T accumulated into S, then S = (H_pp + lambda I) - C */
+    for (int l = 0; l < L; ++l)
+        for (int ka = s->lm_ptr[l]; ka < s->lm_ptr[l + 1]; ++ka) {
+            const double* W = Wb + 18LL * ka;
+            const int ia = s->blk_pose[ka];
+            for (int kb = s->lm_ptr[l]; kb < s->lm_ptr[l + 1]; ++kb) {
+                const double* H = s->hpl + 18LL * kb;
+                const int ib = s->blk_pose[kb];
+                for (int a = 0; a < 6; ++a) {
+                    double* row = S + (size_t)(6 * ia + a) * n + 6 * ib;
+                    for (int c = 0; c < 6; ++c)
+                        row[c] += W[a * 3] * H[c * 3] + W[a * 3 + 1] * H[c * 3 + 1] + W[a * 3 + 2] * H[c * 3 + 2];
+                }
+            }
+        }
+    for (size_t i = 0; i < (size_t)n * n; ++i) S[i] = -S[i];
+    for (int k = 0; k < K; ++k)
+        for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 6; ++c) {
+                double h = s->hpp[36LL * k + a * 6 + c];
+                if (a == c) h += lambda;
+                S[(size_t)(6 * k + a) * n + 6 * k + c] += h;
+            }
+    if (S_out) memcpy(S_out, S, (size_t)n * n * sizeof(double));
+    if (bs_out) memcpy(bs_out, bs, (size_t)n * sizeof(double));
+    memset(delta, 0, ((size_t)n + 3 * (size_t)L) * sizeof(double));
+    if (!zso_cholesky(S, n, Lf) || !zso_cholesky_solve(Lf, bs, n, delta)) goto done;
+    /* delta_l = H_ll^-1 (b_l - H_lp delta_p) */
+    for (int l = 0; l < L; ++l) {
+        double v[3] = {s->b[n + 3 * l], s->b[n + 3 * l + 1], s->b[n + 3 * l + 2]};
+        for (int k = s->lm_ptr[l]; k < s->lm_ptr[l + 1]; ++k) {
+            const double* H = s->hpl + 18LL * k;
+            const double* dp = delta + 6LL * s->blk_pose[k];
+            for (int c = 0; c < 3; ++c) {
+                double acc = 0.0;
+                for (int a = 0; a < 6; ++a) acc += H[a * 3 + c] * dp[a];
+                v[c] -= acc;
+            }
+        }
+        const double* I = hinv + 9LL * l;
+        for (int c = 0; c < 3; ++c) delta[n + 3 * l + c] = I[c * 3] * v[0] + I[c * 3 + 1] * v[1] + I[c * 3 + 2] * v[2];
+    }
+    ok = 1;
+done:
+    free(S); free(Lf); free(bs); free(hinv); free(Wb);
+    return ok;
+}
+
+static double max_diag(const lin* s) {
+    /* source/factor_graph.hpp:513-520 */
+    double m = 0.0;
+    for (int k = 0; k < s->K; ++k)
+        for (int a = 0; a < 6; ++a) m = fmax(fabs(s->hpp[36LL * k + 7 * a]), m);
+    for (int l = 0; l < s->L; ++l)
+        for (int a = 0; a < 3; ++a) m = fmax(fabs(s->hll[9LL * l + 4 * a]), m);
+    return fmin(5e10, m);
+}
+
+double zso_initial_lambda(const zso_problem* p) {
+    lin s;
+    if (!linearise(p, &s)) return NAN;
+    const double v = 1e-5 * max_diag(&s);
+    lin_free(&s);
+    return v;
+}
+
+int zso_linear_step(const zso_problem* p, double lambda, double* S, double* bs, double* delta, double* b,
+                    double* hpp, double* hll) {
+    lin s;
+    if (!linearise(p, &s)) return 0;
+    const size_t nall = 6 * (size_t)p->num_poses + 3 * (size_t)p->num_landmarks;
+    double* d = delta ? delta : malloc((nall + 1) * sizeof(double));
+    const int ok = solve_system(p, &s, lambda, S, bs, d);
+    if (b) memcpy(b, s.b, nall * sizeof(double));
+    if (hpp) memcpy(hpp, s.hpp, (size_t)p->num_poses * 36 * sizeof(double));
+    if (hll) memcpy(hll, s.hll, (size_t)p->num_landmarks * 9 * sizeof(double));
+    if (!delta) free(d);
+    lin_free(&s);
+    return ok;
+}
+
+int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep) {
+    /* factor_graph::solve, source/factor_graph.hpp:489-615 */
+    zso_report rr;
+    memset(&rr, 0, sizeof(rr));
+    const int K = p->num_poses, L = p->num_landmarks, n = 6 * K;
+    const size_t nall = (size_t)n + 3 * (size_t)L;
+    if (p->num_obs == 0 || (K == 0 && L == 0)) {
+        if (rep) *rep = rr;
+        return 0;
+    }
+    lin s;
+    if (!linearise(p, &s)) return 0;
+    double nu = 2.0;
+    double chi2 = zso_chi2(p);
+    rr.chi2_initial = chi2;
+    double lambda = 1e-5 * max_diag(&s);
+    const int max_failures = 10;
+    const double legacy = 1e-10 * chi2;
+    double* delta = calloc(nall + 1, sizeof(double));
+    double* bk_pose = malloc(((size_t)K * 7 + 1) * sizeof(double));
+    double* bk_lm = malloc(((size_t)L * 3 + 1) * sizeof(double));
+    int success = 0;
+    for (int it = 0; it < iterations; ++it) {
+        rr.iterations = it + 1;
+        const double last = chi2;
+        int failures = 0;
+        while (failures < max_failures) {
+            rr.attempts++;
+            if (!solve_system(p, &s, lambda, NULL, NULL, delta)) {
+                rr.chol_failures++;
+                memset(delta, 0, nall * sizeof(double));
+                lambda *= nu;
+                nu *= 2.0;
+                ++failures;
+                if (!isfinite(lambda)) break;
+                continue;
+            }
+            /* update_states, source/factor_graph.hpp:809-830 */
+            memcpy(bk_pose, p->poses, (size_t)K * 7 * sizeof(double));
+            memcpy(bk_lm, p->landmarks, (size_t)L * 3 * sizeof(double));
+            for (int k = 0; k < K; ++k)
+                if (!p->pose_fixed[k]) zso_pose_plus(p->poses + 7LL * k, delta + 6LL * k);
+            for (int l = 0; l < L; ++l)
+                if (!p->landmark_fixed[l])
+                    for (int c = 0; c < 3; ++c) p->landmarks[3LL * l + c] += delta[n + 3 * l + c];
+            double scale = 0.0;
+            for (size_t i = 0; i < nall; ++i) scale += delta[i] * (lambda * delta[i] + s.b[i]);
+            scale += 1e-3;
+            const double chi_new = zso_chi2(p);
+            const double rho = (chi2 - chi_new) / scale;
+            int good = 0;
+            if (rho > 0 && isfinite(chi_new)) {
+                double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
+                alpha = fmin(alpha, 2.0 / 3.0);
+                lambda *= fmax(1.0 / 3.0, alpha);
+                nu = 2.0;
+                chi2 = chi_new;
+                good = 1;
+                ++success;
+            } else {
+                lambda *= nu;
+                nu *= 2.0;
+            }
+            if (!isfinite(lambda)) break;
+            if (good) {
+                lin_free(&s);
+                if (!linearise(p, &s)) { success = -1; goto out; }
+                break;
+            }
+            /* rollback_states, source/factor_graph.hpp:833-846 */
+            memcpy(p->poses, bk_pose, (size_t)K * 7 * sizeof(double));
+            memcpy(p->landmarks, bk_lm, (size_t)L * 3 * sizeof(double));
+            ++failures;
+        }
+        const double thr = use_relative ? 1e-6 * fmax(last, 1e-12) : legacy;
+        if (failures >= max_failures || (last - chi2) < thr || !isfinite(lambda)) break;
+    }
+    lin_free(&s);
+out:
+    rr.accepted = success;
+    rr.chi2_final = chi2;
+    rr.lambda_final = lambda;
+    if (rep) *rep = rr;
+    free(delta); free(bk_pose); free(bk_lm);
+    return success;
+}

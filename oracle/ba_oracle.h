@@ -1,0 +1,101 @@
+/*
+ * CPU restatement of zeroslam's factor-graph bundle adjustment, in plain C99.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the oracle that the CUDA path is checked
+ * against; the product path never links or calls it. Only tests/, the smoke
+ * check in __graft_entry__.py and bench.py's CPU-baseline leg load it.
+ *
+ * It restates, in double precision and with a fixed summation order:
+ *   source/factor_graph.hpp:489-615  factor_graph::solve (LM driver)
+ *   source/factor_graph.hpp:618-629  get_current_chi
+ *   source/factor_graph.hpp:648-732  make_hessian
+ *   source/factor_graph.hpp:736-806  solve_linear_system
+ *   source/factor_graph.hpp:809-846  update_states / rollback_states
+ *   source/factor_graph.hpp:851-934  loss_trivial / huber / cauchy / tukey
+ *   source/factor_graph.hpp:947-960  vertex_pose::plus
+ *   source/factor_graph.hpp:990-1048 edge_reprojection residual and Jacobians
+ *   source/matrix.hpp:749-774        invert<3>
+ *   source/matrix_decomposition_cholesky.hpp:26-95
+ *   source/lie.hpp:188-204,247-264,284-294,337-362,446-450,521-531
+ *   source/camera.hpp:91-142
+ * The reference stores H_pl in a hash map and sums the Schur products in
+ * hash-iteration order; this restatement sums per landmark in ascending
+ * landmark order, so results agree to rounding, not bit for bit.
+ */
+#ifndef ZS_BA_ORACLE_H
+#define ZS_BA_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct zso_problem {
+    int num_poses;
+    int num_landmarks;
+    long long num_obs;
+    double* poses;                 /* [K*7] tx ty tz qx qy qz qw, updated in place */
+    const unsigned char* pose_fixed;
+    double* landmarks;             /* [L*3], updated in place */
+    const unsigned char* landmark_fixed;
+    const int* obs_pose;           /* [M] */
+    const int* obs_landmark;       /* [M] */
+    const double* obs_uv;          /* [M*2] */
+    const double* obs_info;        /* [M*4] row-major 2x2, or NULL for identity */
+    double intrinsics[4];          /* fx fy cx cy */
+    int loss_kind;                 /* 0 none, 1 huber, 2 cauchy, 3 tukey */
+    double loss_delta;
+} zso_problem;
+
+typedef struct zso_report {
+    int iterations;    /* outer LM iterations run */
+    int accepted;      /* accepted steps: the value solve() returns */
+    int attempts;      /* linear solves attempted */
+    int chol_failures; /* attempts whose reduced Cholesky failed */
+    double chi2_initial;
+    double chi2_final;
+    double lambda_final;
+} zso_report;
+
+/* Per-edge residual and Jacobians (J_p 2x6 row-major, J_l 2x3 row-major).
+ * Returns 1 when the point projects (Z >= 1e-12), 0 for the behind-camera
+ * penalty branch. Jp / Jl may be NULL. */
+int zso_edge(const double pose[7], const double X[3], const double uv[2], const double intr[4],
+             double r[2], double Jp[12], double Jl[6]);
+
+/* rho[0..2] of the robust loss at squared error e2. */
+void zso_loss(int kind, double delta, double e2, double rho[3]);
+
+/* Sum of robust chi2 over all edges at the current state. */
+double zso_chi2(const zso_problem* p);
+
+/* 3x3 inverse with zeroslam's |det| > 1e-12 * max|a|^3 test; out = 0 and
+ * returns 0 when singular. */
+int zso_invert3(const double A[9], double out[9]);
+
+/* Row-major dense Cholesky A = L L^T and the two triangular solves, with
+ * zeroslam's pivot thresholds. Return 1 on success, 0 on failure. */
+int zso_cholesky(const double* A, int n, double* L);
+int zso_cholesky_solve(const double* L, const double* b, int n, double* x);
+
+/* T <- exp(delta) * T on a [tx ty tz qx qy qz qw] pose, delta = (omega, upsilon). */
+void zso_pose_plus(double pose[7], const double delta[6]);
+
+/* Linearise at the current state and solve the damped system once at
+ * `lambda`. Any output pointer may be NULL:
+ *   S [n*n] reduced camera matrix (damped), bs [n], delta [6K+3L],
+ *   b [6K+3L] gradient vector, hpp [K*36], hll [L*9] (undamped).
+ * Returns 1 on success, 0 when the reduced Cholesky failed. */
+int zso_linear_step(const zso_problem* p, double lambda, double* S, double* bs, double* delta,
+                    double* b, double* hpp, double* hll);
+
+/* Initial damping tau * min(5e10, max diagonal) at the current state. */
+double zso_initial_lambda(const zso_problem* p);
+
+/* Full Levenberg-Marquardt solve; returns the accepted-step count. */
+int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,262 @@
+"""ctypes access to the oracle (test infrastructure only).
+
+``Oracle`` wraps the C restatement ``ba_oracle.c``; ``Reference`` wraps the
+reference's own solver compiled by ``build.py`` into ``oracle/_ref``. Both
+take scenes in the structure-of-arrays form of ``zeroslam_gb300.scenes``.
+Only tests/, the smoke check and bench.py's CPU-baseline leg use this module.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_ubyte)
+
+
+def _ptr(a: np.ndarray | None, t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+class _Problem(C.Structure):
+    _fields_ = [("num_poses", C.c_int), ("num_landmarks", C.c_int), ("num_obs", C.c_longlong),
+                ("poses", _dp), ("pose_fixed", _up), ("landmarks", _dp), ("landmark_fixed", _up),
+                ("obs_pose", _ip), ("obs_landmark", _ip), ("obs_uv", _dp), ("obs_info", _dp),
+                ("intrinsics", C.c_double * 4), ("loss_kind", C.c_int), ("loss_delta", C.c_double)]
+
+
+class Report(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("accepted", C.c_int), ("attempts", C.c_int),
+                ("chol_failures", C.c_int), ("chi2_initial", C.c_double), ("chi2_final", C.c_double),
+                ("lambda_final", C.c_double)]
+
+
+class _Arrays:
+    """Contiguous copies of a scene's arrays that stay alive with the struct."""
+
+    def __init__(self, scene):
+        self.poses = np.ascontiguousarray(scene.poses, dtype=np.float64).copy()
+        self.landmarks = np.ascontiguousarray(scene.landmarks, dtype=np.float64).copy()
+        self.pose_fixed = np.ascontiguousarray(scene.pose_fixed, dtype=np.uint8)
+        self.landmark_fixed = np.ascontiguousarray(scene.landmark_fixed, dtype=np.uint8)
+        self.obs_pose = np.ascontiguousarray(scene.obs_pose, dtype=np.int32)
+        self.obs_landmark = np.ascontiguousarray(scene.obs_landmark, dtype=np.int32)
+        self.obs_uv = np.ascontiguousarray(scene.obs_uv, dtype=np.float64)
+        self.obs_info = None if scene.obs_info is None else np.ascontiguousarray(scene.obs_info, dtype=np.float64)
+        self.intrinsics = np.ascontiguousarray(scene.intrinsics, dtype=np.float64)
+        self.loss_kind = int(scene.loss_kind)
+        self.loss_delta = float(scene.loss_delta)
+
+    def struct(self) -> _Problem:
+        p = _Problem()
+        p.num_poses = self.poses.shape[0]
+        p.num_landmarks = self.landmarks.shape[0]
+        p.num_obs = self.obs_pose.shape[0]
+        p.poses = _ptr(self.poses, _dp)
+        p.pose_fixed = _ptr(self.pose_fixed, _up)
+        p.landmarks = _ptr(self.landmarks, _dp)
+        p.landmark_fixed = _ptr(self.landmark_fixed, _up)
+        p.obs_pose = _ptr(self.obs_pose, _ip)
+        p.obs_landmark = _ptr(self.obs_landmark, _ip)
+        p.obs_uv = _ptr(self.obs_uv, _dp)
+        p.obs_info = _ptr(self.obs_info, _dp)
+        for i in range(4):
+            p.intrinsics[i] = self.intrinsics[i]
+        p.loss_kind = self.loss_kind
+        p.loss_delta = self.loss_delta
+        return p
+
+
+class Oracle:
+    def __init__(self):
+        self.lib = C.CDLL(_build.build_oracle())
+        L = self.lib
+        L.zso_chi2.restype = C.c_double
+        L.zso_chi2.argtypes = [C.POINTER(_Problem)]
+        L.zso_solve.restype = C.c_int
+        L.zso_solve.argtypes = [C.POINTER(_Problem), C.c_int, C.c_int, C.POINTER(Report)]
+        L.zso_linear_step.restype = C.c_int
+        L.zso_linear_step.argtypes = [C.POINTER(_Problem), C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.zso_initial_lambda.restype = C.c_double
+        L.zso_initial_lambda.argtypes = [C.POINTER(_Problem)]
+        L.zso_edge.restype = C.c_int
+        L.zso_edge.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.zso_cholesky.restype = C.c_int
+        L.zso_cholesky.argtypes = [_dp, C.c_int, _dp]
+        L.zso_cholesky_solve.restype = C.c_int
+        L.zso_cholesky_solve.argtypes = [_dp, _dp, C.c_int, _dp]
+        L.zso_invert3.restype = C.c_int
+        L.zso_invert3.argtypes = [_dp, _dp]
+        L.zso_pose_plus.restype = None
+        L.zso_pose_plus.argtypes = [_dp, _dp]
+        L.zso_loss.restype = None
+        L.zso_loss.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+
+    def chi2(self, scene) -> float:
+        a = _Arrays(scene)
+        p = a.struct()
+        return self.lib.zso_chi2(C.byref(p))
+
+    def solve(self, scene, iterations: int, use_relative: bool = False):
+        """Returns (poses, landmarks, Report)."""
+        a = _Arrays(scene)
+        p = a.struct()
+        rep = Report()
+        self.lib.zso_solve(C.byref(p), int(iterations), int(bool(use_relative)), C.byref(rep))
+        return a.poses, a.landmarks, rep
+
+    def initial_lambda(self, scene) -> float:
+        a = _Arrays(scene)
+        p = a.struct()
+        return self.lib.zso_initial_lambda(C.byref(p))
+
+    def linear_step(self, scene, lam: float, want_S: bool = True):
+        """One linearisation + damped solve. Returns dict(ok, S, bs, delta, b, hpp, hll)."""
+        a = _Arrays(scene)
+        p = a.struct()
+        K, L = scene.K, scene.L
+        n = 6 * K
+        S = np.zeros((n, n)) if want_S else None
+        bs = np.zeros(n)
+        delta = np.zeros(n + 3 * L)
+        b = np.zeros(n + 3 * L)
+        hpp = np.zeros((K, 6, 6))
+        hll = np.zeros((L, 3, 3))
+        ok = self.lib.zso_linear_step(C.byref(p), float(lam), _ptr(S, _dp), _ptr(bs, _dp), _ptr(delta, _dp),
+                                      _ptr(b, _dp), _ptr(hpp, _dp), _ptr(hll, _dp))
+        return dict(ok=bool(ok), S=S, bs=bs, delta=delta, b=b, hpp=hpp, hll=hll)
+
+    def edge(self, pose7, X3, uv2, intr4):
+        pose7, X3, uv2, intr4 = (np.ascontiguousarray(v, dtype=np.float64) for v in (pose7, X3, uv2, intr4))
+        r = np.zeros(2)
+        Jp = np.zeros((2, 6))
+        Jl = np.zeros((2, 3))
+        front = self.lib.zso_edge(_ptr(pose7, _dp), _ptr(X3, _dp), _ptr(uv2, _dp), _ptr(intr4, _dp),
+                                  _ptr(r, _dp), _ptr(Jp, _dp), _ptr(Jl, _dp))
+        return r, Jp, Jl, bool(front)
+
+    def cholesky(self, A):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        n = A.shape[0]
+        Lm = np.zeros_like(A)
+        ok = self.lib.zso_cholesky(_ptr(A, _dp), n, _ptr(Lm, _dp))
+        return bool(ok), Lm
+
+    def cholesky_solve(self, Lm, b):
+        Lm = np.ascontiguousarray(Lm, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        ok = self.lib.zso_cholesky_solve(_ptr(Lm, _dp), _ptr(b, _dp), Lm.shape[0], _ptr(x, _dp))
+        return bool(ok), x
+
+    def invert3(self, A):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        out = np.zeros((3, 3))
+        ok = self.lib.zso_invert3(_ptr(A, _dp), _ptr(out, _dp))
+        return bool(ok), out
+
+    def pose_plus(self, pose7, d6):
+        pose = np.ascontiguousarray(pose7, dtype=np.float64).copy()
+        d6 = np.ascontiguousarray(d6, dtype=np.float64)
+        self.lib.zso_pose_plus(_ptr(pose, _dp), _ptr(d6, _dp))
+        return pose
+
+    def loss(self, kind, delta, e2):
+        rho = np.zeros(3)
+        self.lib.zso_loss(int(kind), float(delta), float(e2), _ptr(rho, _dp))
+        return rho
+
+
+class Reference:
+    """zeroslam's own factor_graph, compiled from the reference tree."""
+
+    def __init__(self, path: str | None = None):
+        path = path or _build.build_ref()
+        if path is None or not os.path.exists(path):
+            raise FileNotFoundError("the reference solver has not been built (oracle/_ref)")
+        self.lib = C.CDLL(path)
+        L = self.lib
+        args = [C.c_int, C.c_int, C.c_longlong, _dp, _up, _dp, _up, _ip, _ip, _dp, _dp, _dp, C.c_int, C.c_double]
+        L.zsref_solve.restype = C.c_int
+        L.zsref_solve.argtypes = args + [C.c_int, C.c_int, _dp]
+        L.zsref_chi2.restype = C.c_double
+        L.zsref_chi2.argtypes = args
+        L.zsref_edge.restype = None
+        L.zsref_edge.argtypes = [_dp] * 7
+        L.zsref_cholesky.restype = C.c_int
+        L.zsref_cholesky.argtypes = [_dp, C.c_int, _dp]
+        L.zsref_cholesky_solve.restype = C.c_int
+        L.zsref_cholesky_solve.argtypes = [_dp, _dp, C.c_int, _dp]
+        L.zsref_invert3.restype = C.c_int
+        L.zsref_invert3.argtypes = [_dp, _dp]
+        L.zsref_pose_plus.restype = None
+        L.zsref_pose_plus.argtypes = [_dp, _dp]
+        L.zsref_loss.restype = None
+        L.zsref_loss.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+
+    @staticmethod
+    def available() -> bool:
+        return _build.reference_available() or os.path.exists(_build.REF_SO)
+
+    def _args(self, a: _Arrays):
+        return (a.poses.shape[0], a.landmarks.shape[0], a.obs_pose.shape[0], _ptr(a.poses, _dp),
+                _ptr(a.pose_fixed, _up), _ptr(a.landmarks, _dp), _ptr(a.landmark_fixed, _up),
+                _ptr(a.obs_pose, _ip), _ptr(a.obs_landmark, _ip), _ptr(a.obs_uv, _dp), _ptr(a.obs_info, _dp),
+                _ptr(a.intrinsics, _dp), a.loss_kind, a.loss_delta)
+
+    def solve(self, scene, iterations: int, use_relative: bool = False):
+        """Returns (poses, landmarks, accepted, chi2_before, chi2_after, build_s, solve_s)."""
+        a = _Arrays(scene)
+        out = np.zeros(4)
+        acc = self.lib.zsref_solve(*self._args(a), int(iterations), int(bool(use_relative)), _ptr(out, _dp))
+        return a.poses, a.landmarks, acc, out[0], out[1], out[2], out[3]
+
+    def chi2(self, scene) -> float:
+        return self.lib.zsref_chi2(*self._args(_Arrays(scene)))
+
+    def edge(self, pose7, X3, uv2, intr4):
+        pose7, X3, uv2, intr4 = (np.ascontiguousarray(v, dtype=np.float64) for v in (pose7, X3, uv2, intr4))
+        r = np.zeros(2)
+        Jp = np.zeros((2, 6))
+        Jl = np.zeros((2, 3))
+        self.lib.zsref_edge(_ptr(pose7, _dp), _ptr(X3, _dp), _ptr(uv2, _dp), _ptr(intr4, _dp), _ptr(r, _dp),
+                            _ptr(Jp, _dp), _ptr(Jl, _dp))
+        return r, Jp, Jl
+
+    def cholesky(self, A):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        Lm = np.zeros_like(A)
+        ok = self.lib.zsref_cholesky(_ptr(A, _dp), A.shape[0], _ptr(Lm, _dp))
+        return bool(ok), Lm
+
+    def cholesky_solve(self, Lm, b):
+        Lm = np.ascontiguousarray(Lm, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        ok = self.lib.zsref_cholesky_solve(_ptr(Lm, _dp), _ptr(b, _dp), Lm.shape[0], _ptr(x, _dp))
+        return bool(ok), x
+
+    def invert3(self, A):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        out = np.zeros((3, 3))
+        ok = self.lib.zsref_invert3(_ptr(A, _dp), _ptr(out, _dp))
+        return bool(ok), out
+
+    def pose_plus(self, pose7, d6):
+        pose = np.ascontiguousarray(pose7, dtype=np.float64).copy()
+        d6 = np.ascontiguousarray(d6, dtype=np.float64)
+        self.lib.zsref_pose_plus(_ptr(pose, _dp), _ptr(d6, _dp))
+        return pose
+
+    def loss(self, kind, delta, e2):
+        rho = np.zeros(3)
+        self.lib.zsref_loss(int(kind), float(delta), float(e2), _ptr(rho, _dp))
+        return rho

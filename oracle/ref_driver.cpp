@@ -1,0 +1,163 @@
+// C-callable driver around zeroslam's own factor-graph solver.
+//
+// TEST INFRASTRUCTURE ONLY: compiled by oracle/build_ref.py against the
+// unmodified reference headers (source/factor_graph.hpp, camera.hpp, lie.hpp,
+// matrix*.hpp) into oracle/_ref/. It is used to pin the C restatement
+// (ba_oracle.c), to write the golden fixtures under tests/golden/, and as the
+// timed CPU baseline. Only the reference's public API is used.
+#include "factor_graph.hpp"
+#include "camera.hpp"
+
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+namespace {
+
+struct graph_build {
+    std::vector<std::unique_ptr<factor_graph::vertex_base>> poses;
+    std::vector<std::unique_ptr<factor_graph::vertex_base>> landmarks;
+    std::vector<std::unique_ptr<factor_graph::edge_base>> edges;
+    std::unique_ptr<factor_graph::loss_function_base> loss;
+};
+
+// Builds the graph the way source/map.hpp:129-179 does: one vertex_pose per
+// pose, one marginalised vertex_point_xyz per landmark, one
+// edge_reprojection<pinhole> per observation sharing one loss object.
+void build(factor_graph::factor_graph& fg, graph_build& g, int K, int L, long long M, const double* poses,
+           const unsigned char* pose_fixed, const double* lms, const unsigned char* lm_fixed, const int* obs_pose,
+           const int* obs_lm, const double* obs_uv, const double* obs_info, const double* intr, int loss_kind,
+           double loss_delta) {
+    if (loss_kind == 1) g.loss = std::make_unique<factor_graph::loss_huber>(loss_delta);
+    if (loss_kind == 2) g.loss = std::make_unique<factor_graph::loss_cauchy>(loss_delta);
+    if (loss_kind == 3) g.loss = std::make_unique<factor_graph::loss_tukey>(loss_delta);
+    for (int k = 0; k < K; ++k) {
+        auto v = std::make_unique<factor_graph::vertex_pose>();
+        v->set_parameters(matrix::matrix<double, 0, 0>(7, 1, poses + 7LL * k));
+        v->set_fixed(pose_fixed[k] != 0);
+        fg.add_vertex(v.get());
+        g.poses.push_back(std::move(v));
+    }
+    for (int l = 0; l < L; ++l) {
+        auto v = std::make_unique<factor_graph::vertex_point_xyz>();
+        v->set_parameters(matrix::matrix<double, 0, 0>(3, 1, lms + 3LL * l));
+        v->set_fixed(lm_fixed[l] != 0);
+        v->set_marginalised(true);
+        fg.add_vertex(v.get());
+        g.landmarks.push_back(std::move(v));
+    }
+    camera::pinhole cam(intr, 4);
+    g.edges.reserve(static_cast<size_t>(M));
+    for (long long o = 0; o < M; ++o) {
+        auto e = std::make_unique<factor_graph::edge_reprojection<camera::pinhole>>(cam);
+        e->set_observation(matrix::matrix<double, 0, 0>(2, 1, obs_uv + 2 * o));
+        e->add_vertex(g.poses[obs_pose[o]].get());
+        e->add_vertex(g.landmarks[obs_lm[o]].get());
+        if (obs_info) e->set_information(matrix::matrix<double, 0, 0>(2, 2, obs_info + 4 * o));
+        if (g.loss) e->set_loss_function(g.loss.get());
+        fg.add_edge(e.get());
+        g.edges.push_back(std::move(e));
+    }
+}
+
+void read_back(const graph_build& g, double* poses, double* lms) {
+    for (size_t k = 0; k < g.poses.size(); ++k)
+        for (int i = 0; i < 7; ++i) poses[7 * k + i] = g.poses[k]->get_parameters()[i][0];
+    for (size_t l = 0; l < g.landmarks.size(); ++l)
+        for (int i = 0; i < 3; ++i) lms[3 * l + i] = g.landmarks[l]->get_parameters()[i][0];
+}
+
+}  // namespace
+
+extern "C" {
+
+// Runs factor_graph::solve(iterations, use_relative) and writes the solved
+// state back into poses / lms. out[0] = chi2 before, out[1] = chi2 after,
+// out[2] = seconds spent building the graph, out[3] = seconds in solve().
+// Returns solve()'s accepted-step count.
+int zsref_solve(int K, int L, long long M, double* poses, const unsigned char* pose_fixed, double* lms,
+                const unsigned char* lm_fixed, const int* obs_pose, const int* obs_lm, const double* obs_uv,
+                const double* obs_info, const double* intr, int loss_kind, double loss_delta, int iterations,
+                int use_relative, double* out) {
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    factor_graph::factor_graph fg(false);
+    graph_build g;
+    build(fg, g, K, L, M, poses, pose_fixed, lms, lm_fixed, obs_pose, obs_lm, obs_uv, obs_info, intr, loss_kind,
+          loss_delta);
+    const auto t1 = clk::now();
+    out[0] = fg.get_current_chi();
+    const auto t2 = clk::now();
+    const int accepted = fg.solve(iterations, use_relative != 0);
+    const auto t3 = clk::now();
+    out[1] = fg.get_current_chi();
+    out[2] = std::chrono::duration<double>(t1 - t0).count();
+    out[3] = std::chrono::duration<double>(t3 - t2).count();
+    read_back(g, poses, lms);
+    return accepted;
+}
+
+double zsref_chi2(int K, int L, long long M, const double* poses, const unsigned char* pose_fixed, const double* lms,
+                  const unsigned char* lm_fixed, const int* obs_pose, const int* obs_lm, const double* obs_uv,
+                  const double* obs_info, const double* intr, int loss_kind, double loss_delta) {
+    factor_graph::factor_graph fg(false);
+    graph_build g;
+    build(fg, g, K, L, M, poses, pose_fixed, lms, lm_fixed, obs_pose, obs_lm, obs_uv, obs_info, intr, loss_kind,
+          loss_delta);
+    return fg.get_current_chi();
+}
+
+// Residual and analytic Jacobians of one edge_reprojection<pinhole>
+// (J_p 2x6 and J_l 2x3, row-major).
+void zsref_edge(const double* pose7, const double* X3, const double* uv2, const double* intr, double* r2,
+                double* Jp12, double* Jl6) {
+    factor_graph::vertex_pose vp;
+    vp.set_parameters(matrix::matrix<double, 0, 0>(7, 1, pose7));
+    factor_graph::vertex_point_xyz vl;
+    vl.set_parameters(matrix::matrix<double, 0, 0>(3, 1, X3));
+    vl.set_marginalised(true);
+    camera::pinhole cam(intr, 4);
+    factor_graph::edge_reprojection<camera::pinhole> e(cam);
+    e.set_observation(matrix::matrix<double, 0, 0>(2, 1, uv2));
+    e.add_vertex(&vp);
+    e.add_vertex(&vl);
+    e.compute_residual();
+    e.compute_jacobians();
+    for (int i = 0; i < 2; ++i) r2[i] = e.get_residual()[i][0];
+    for (int i = 0; i < 2; ++i)
+        for (int c = 0; c < 6; ++c) Jp12[i * 6 + c] = e.get_jacobians()[0][i][c];
+    for (int i = 0; i < 2; ++i)
+        for (int c = 0; c < 3; ++c) Jl6[i * 3 + c] = e.get_jacobians()[1][i][c];
+}
+
+int zsref_cholesky(const double* A, int n, double* L) { return matrix::decompose_cholesky(A, n, n, L) ? 1 : 0; }
+
+int zsref_cholesky_solve(const double* L, const double* b, int n, double* x) {
+    return matrix::solve_cholesky(L, b, n, n, x) ? 1 : 0;
+}
+
+int zsref_invert3(const double* A, double* out) {
+    matrix::matrix<double, 3, 3> a(A), o;
+    const bool ok = matrix::invert(a, o);
+    std::memcpy(out, o.data(), 9 * sizeof(double));
+    return ok ? 1 : 0;
+}
+
+void zsref_pose_plus(double* pose7, const double* d6) {
+    factor_graph::vertex_pose vp;
+    vp.set_parameters(matrix::matrix<double, 0, 0>(7, 1, pose7));
+    vp.plus(matrix::matrix<double, 0, 0>(6, 1, d6));
+    for (int i = 0; i < 7; ++i) pose7[i] = vp.get_parameters()[i][0];
+}
+
+void zsref_loss(int kind, double delta, double e2, double* rho3) {
+    matrix::matrix<double, 3, 1> rho = matrix::matrix<double, 3, 1>::zero();
+    if (kind == 1) factor_graph::loss_huber(delta).compute(e2, rho);
+    else if (kind == 2) factor_graph::loss_cauchy(delta).compute(e2, rho);
+    else if (kind == 3) factor_graph::loss_tukey(delta).compute(e2, rho);
+    else factor_graph::loss_trivial().compute(e2, rho);
+    for (int i = 0; i < 3; ++i) rho3[i] = rho[i];
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+"""The C restatement (oracle) against zeroslam's own outputs stored in
+tests/golden/ (written by tests/golden/make_golden.py from the reference)."""
+
+import numpy as np
+import pytest
+
+from conftest import SOLVE_FIXTURES, cost_tol, load_npz, rel_err, scene_from_npz, state_tol
+
+
+def test_edge_literals(oracle):
+    # tests/factor_graph.test.cpp:236-276: residual and Jacobians compared with ==
+    r, Jp, Jl, front = oracle.edge([0, 0, 0, 0, 0, 0, 1.0], [0, 0, 1.0], [0.1, -0.2], [1, 1, 0, 0.0])
+    assert front
+    assert r[0] == 0.1 and r[1] == -0.2
+    assert np.array_equal(Jp, [[0.0, -1.0, 0.0, -1.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0, -1.0, 0.0]])
+    assert np.array_equal(Jl, [[-1.0, 0.0, 0.0], [0.0, -1.0, 0.0]])
+
+
+def test_behind_camera_penalty(oracle):
+    # tests/factor_graph.test.cpp:278-323
+    r, Jp, Jl, front = oracle.edge([0, 0, 0, 0, 0, 0, 1.0], [0.1, 0.2, -10.0], [0.1, -0.2], [1, 1, 0, 0.0])
+    assert not front
+    assert np.all(np.isfinite(r)) and np.all(np.abs(r) > 1e-8)
+    assert r @ r > 1.0
+    assert np.all(np.isfinite(Jp)) and np.any(Jp != 0) and np.any(Jl != 0)
+    assert Jl[0, 2] < 0 and Jl[1, 2] < 0
+
+
+def test_edges_match_reference(oracle):
+    g = load_npz("edges.npz")
+    for i in range(g["pose"].shape[0]):
+        r, Jp, Jl, _ = oracle.edge(g["pose"][i], g["X"][i], g["uv"][i], g["intr"][i])
+        assert np.allclose(r, g["r"][i], rtol=1e-14, atol=1e-12), i
+        assert np.allclose(Jp, g["Jp"][i], rtol=1e-13, atol=1e-12), i
+        assert np.allclose(Jl, g["Jl"][i], rtol=1e-13, atol=1e-12), i
+
+
+def test_losses_match_reference(oracle):
+    for kind, delta, e2, r0, r1, r2 in load_npz("losses.npz")["table"]:
+        rho = oracle.loss(int(kind), delta, e2)
+        assert np.allclose(rho, [r0, r1, r2], rtol=1e-15, atol=0), (kind, delta, e2)
+
+
+def test_invert3_matches_reference(oracle):
+    g = load_npz("invert3.npz")
+    for A, inv, ok in zip(g["A"], g["inv"], g["ok"]):
+        o_ok, o_inv = oracle.invert3(A)
+        assert o_ok == bool(ok)
+        assert np.array_equal(o_inv, inv)
+
+
+def test_cholesky_matches_reference(oracle):
+    g = load_npz("cholesky.npz")
+    for i in range(int(g["count"])):
+        A, b, Lr, xr, (ok, okx) = g[f"A{i}"], g[f"b{i}"], g[f"L{i}"], g[f"x{i}"], g[f"ok{i}"]
+        o_ok, Lo = oracle.cholesky(A)
+        assert o_ok == bool(ok), i
+        if ok:
+            assert np.array_equal(Lo, Lr), i
+            s_ok, xo = oracle.cholesky_solve(Lo, b)
+            assert s_ok == bool(okx)
+            if okx:
+                assert np.array_equal(xo, xr), i
+
+
+def test_pose_plus_matches_reference(oracle):
+    g = load_npz("pose_plus.npz")
+    for p, d, out in zip(g["pose"], g["delta"], g["out"]):
+        assert np.allclose(oracle.pose_plus(p, d), out, rtol=1e-15, atol=1e-15)
+
+
+@pytest.mark.parametrize("name", SOLVE_FIXTURES)
+def test_solve_matches_reference(oracle, name):
+    g = load_npz(name)
+    sc = scene_from_npz(g, name)
+    poses, lms, rep = oracle.solve(sc, int(g["iterations"]), bool(g["use_relative"]))
+    assert rep.accepted == int(g["accepted"])
+    c_ref = float(g["chi2_after"])
+    assert abs(rep.chi2_final - c_ref) <= cost_tol(g) * abs(c_ref) + 1e-12
+    assert abs(rep.chi2_initial - float(g["chi2_before"])) <= 1e-12 * abs(float(g["chi2_before"]))
+    tol = state_tol(g)
+    if tol is not None:
+        assert rel_err(poses, g["out_poses"]) < tol
+        assert rel_err(lms, g["out_landmarks"]) < tol
+    if name == "solve_seven_camera.npz":
+        # tests/factor_graph.test.cpp:157-179
+        assert abs(rep.chi2_final) < 1e-5
+        err0 = np.linalg.norm(g["landmarks"] - np.array([[0, 0, 1.0], [0, 1, 1.0], [1, 0, 1.0]]), axis=1).sum()
+        err1 = np.linalg.norm(lms - np.array([[0, 0, 1.0], [0, 1, 1.0], [1, 0, 1.0]]), axis=1).sum()
+        assert err1 < err0
+    if name == "solve_negative_information.npz":
+        assert np.all(np.isfinite(poses))

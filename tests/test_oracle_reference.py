@@ -1,0 +1,56 @@
+"""The oracle against zeroslam's solver run live (only where the reference
+tree has been compiled into oracle/_ref; skipped elsewhere)."""
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from zeroslam_gb300 import scenes
+
+
+def test_chi2_bitwise(oracle, reference):
+    sc = scenes.arc_scene(10, 300, seed=21)
+    assert oracle.chi2(sc) == reference.chi2(sc)
+
+
+@pytest.mark.parametrize("seed,huber", [(31, False), (32, True)])
+def test_single_step_parity(oracle, reference, seed, huber):
+    sc = scenes.arc_scene(15, 800, seed=seed, huber=huber)
+    po, lo, rep = oracle.solve(sc, 1)
+    pr, lr, acc, c0, c1, _, _ = reference.solve(sc, 1)
+    assert rep.accepted == acc
+    assert rel_err(po - sc.poses, pr - sc.poses) < 1e-9
+    assert rel_err(lo - sc.landmarks, lr - sc.landmarks) < 1e-9
+    assert abs(rep.chi2_final - c1) <= 1e-9 * c1
+
+
+def test_full_solve_parity_window(oracle, reference):
+    sc = scenes.arc_scene(12, 1200, seed=41)
+    po, lo, rep = oracle.solve(sc, 10)
+    pr, lr, acc, c0, c1, _, _ = reference.solve(sc, 10)
+    assert rep.accepted == acc
+    assert abs(rep.chi2_final - c1) <= 1e-9 * c1
+    assert rel_err(po, pr) < 1e-8
+
+
+def test_cauchy_tukey_parity(oracle, reference):
+    for kind in (2, 3):
+        sc = scenes.arc_scene(8, 300, seed=50 + kind)
+        sc.loss_kind, sc.loss_delta = kind, 2.0
+        po, lo, rep = oracle.solve(sc, 3)
+        pr, lr, acc, c0, c1, _, _ = reference.solve(sc, 3)
+        assert rep.accepted == acc
+        assert abs(rep.chi2_final - c1) <= 1e-9 * abs(c1)
+
+
+def test_random_cholesky_and_invert(oracle, reference):
+    rng = np.random.default_rng(7)
+    for n in (3, 17, 64):
+        G = rng.normal(size=(n, n))
+        A = G @ G.T + np.eye(n)
+        ok1, L1 = oracle.cholesky(A)
+        ok2, L2 = reference.cholesky(A)
+        assert ok1 and ok2 and np.array_equal(L1, L2)
+    for _ in range(20):
+        A = rng.normal(size=(3, 3))
+        assert np.array_equal(oracle.invert3(A)[1], reference.invert3(A)[1])

@@ -1,0 +1,275 @@
+"""Python access to the C ABI of ``include/zeroslam_ba.h`` (ctypes).
+
+The CUDA library is the only implementation: if ``_lib/libzeroslam_ba.so``
+is missing or no CUDA device is usable, every call that needs one raises
+``ZsError``. There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ZS_OK = 0
+ZS_ERR_INVALID = -1
+ZS_ERR_CUDA = -2
+ZS_ERR_UNSUPPORTED = -3
+ZS_ERR_TIMEOUT = -4
+ZS_ERR_NONFINITE = -5
+ZS_ERR_NO_PROBLEM = -6
+ZS_ERR_OUT_OF_MEMORY = -7
+ZS_ERR_CHOLESKY = -8
+
+FP64 = 0
+MIXED = 1
+
+LOSS_NONE, LOSS_HUBER, LOSS_CAUCHY, LOSS_TUKEY = 0, 1, 2, 3
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_up = C.POINTER(C.c_uint8)
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("max_failures", C.c_int32), ("tau", C.c_double),
+                ("diagonal_clamp", C.c_double), ("legacy_stop", C.c_double), ("relative_tolerance", C.c_double),
+                ("chi2_floor", C.c_double), ("refine_iterations", C.c_int32), ("refine_tolerance", C.c_double),
+                ("device", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32)]
+
+
+class Problem(C.Structure):
+    _fields_ = [("num_poses", C.c_int32), ("num_landmarks", C.c_int32), ("num_obs", C.c_int64),
+                ("poses", _dp), ("pose_fixed", _up), ("landmarks", _dp), ("landmark_fixed", _up),
+                ("obs_pose", _ip), ("obs_landmark", _ip), ("obs_uv", _dp), ("obs_info", _dp),
+                ("intrinsics", C.c_double * 4), ("loss_kind", C.c_int32), ("loss_delta", C.c_double)]
+
+
+class Report(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("accepted", C.c_int32), ("attempts", C.c_int32),
+                ("cholesky_failures", C.c_int32), ("refine_sweeps", C.c_int32), ("chi2_initial", C.c_double),
+                ("chi2_final", C.c_double), ("lambda_final", C.c_double), ("ms_total", C.c_double),
+                ("ms_phase", C.c_double * 8), ("phase_calls", C.c_int32 * 8), ("kernel_launches", C.c_int64)]
+
+    PHASES = ("linearize", "invert", "schur", "factor", "trisolve", "update", "cost", "other")
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("ms_phase", "phase_calls")}
+        d["ms_phase"] = {p: self.ms_phase[i] for i, p in enumerate(self.PHASES)}
+        d["phase_calls"] = {p: self.phase_calls[i] for i, p in enumerate(self.PHASES)}
+        return d
+
+
+class ZsError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = _LIB.zs_ba_status_string(status).decode() if _LIB is not None else str(status)
+        super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
+
+
+_LIB = None
+
+ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
+                 "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
+                 "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string")
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads (building first if needed and nvcc is present) the CUDA library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or library_path()
+    if not os.path.exists(path):
+        path = _build.build()
+    lib = C.CDLL(path)
+    lib.zs_ba_default_options.restype = None
+    lib.zs_ba_default_options.argtypes = [C.POINTER(Options)]
+    lib.zs_ba_create.restype = C.c_int
+    lib.zs_ba_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Options)]
+    lib.zs_ba_destroy.restype = None
+    lib.zs_ba_destroy.argtypes = [C.c_void_p]
+    lib.zs_ba_set_problem.restype = C.c_int
+    lib.zs_ba_set_problem.argtypes = [C.c_void_p, C.POINTER(Problem)]
+    lib.zs_ba_set_state.restype = C.c_int
+    lib.zs_ba_set_state.argtypes = [C.c_void_p, _dp, _dp]
+    lib.zs_ba_get_state.restype = C.c_int
+    lib.zs_ba_get_state.argtypes = [C.c_void_p, _dp, _dp]
+    lib.zs_ba_reset_state.restype = C.c_int
+    lib.zs_ba_reset_state.argtypes = [C.c_void_p]
+    lib.zs_pipe_peaks.restype = C.c_int
+    lib.zs_pipe_peaks.argtypes = [C.c_int, _dp, _dp]
+    lib.zs_ba_solve.restype = C.c_int
+    lib.zs_ba_solve.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(Report)]
+    lib.zs_ba_chi2.restype = C.c_int
+    lib.zs_ba_chi2.argtypes = [C.c_void_p, _dp]
+    lib.zs_ba_linear_step.restype = C.c_int
+    lib.zs_ba_linear_step.argtypes = [C.c_void_p, C.c_double, _dp, _dp, _dp, _dp]
+    lib.zs_ba_initial_lambda.restype = C.c_int
+    lib.zs_ba_initial_lambda.argtypes = [C.c_void_p, _dp]
+    lib.zs_dense_cholesky_solve.restype = C.c_int
+    lib.zs_dense_cholesky_solve.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.c_int]
+    lib.zs_ba_status_string.restype = C.c_char_p
+    lib.zs_ba_status_string.argtypes = [C.c_int]
+    _LIB = lib
+    return lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def default_options(**kw) -> Options:
+    lib = load()
+    o = Options()
+    lib.zs_ba_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class BundleAdjuster:
+    """One device handle (zs_ba_handle): problem upload, LM solve, state access."""
+
+    def __init__(self, precision: int = FP64, **options):
+        self.lib = load()
+        self.options = default_options(precision=precision, **options)
+        h = C.c_void_p()
+        st = self.lib.zs_ba_create(C.byref(h), C.byref(self.options))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_create")
+        self.h = h
+        self.K = self.L = self.M = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.zs_ba_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_problem(self, scene) -> None:
+        self._keep = dict(
+            poses=np.ascontiguousarray(scene.poses, dtype=np.float64),
+            pose_fixed=np.ascontiguousarray(scene.pose_fixed, dtype=np.uint8),
+            landmarks=np.ascontiguousarray(scene.landmarks, dtype=np.float64),
+            landmark_fixed=np.ascontiguousarray(scene.landmark_fixed, dtype=np.uint8),
+            obs_pose=np.ascontiguousarray(scene.obs_pose, dtype=np.int32),
+            obs_landmark=np.ascontiguousarray(scene.obs_landmark, dtype=np.int32),
+            obs_uv=np.ascontiguousarray(scene.obs_uv, dtype=np.float64),
+            obs_info=None if scene.obs_info is None else np.ascontiguousarray(scene.obs_info, dtype=np.float64),
+        )
+        k = self._keep
+        p = Problem()
+        p.num_poses = k["poses"].shape[0]
+        p.num_landmarks = k["landmarks"].shape[0]
+        p.num_obs = k["obs_pose"].shape[0]
+        p.poses = _p(k["poses"], _dp)
+        p.pose_fixed = _p(k["pose_fixed"], _up)
+        p.landmarks = _p(k["landmarks"], _dp)
+        p.landmark_fixed = _p(k["landmark_fixed"], _up)
+        p.obs_pose = _p(k["obs_pose"], _ip)
+        p.obs_landmark = _p(k["obs_landmark"], _ip)
+        p.obs_uv = _p(k["obs_uv"], _dp)
+        p.obs_info = _p(k["obs_info"], _dp)
+        for i in range(4):
+            p.intrinsics[i] = float(scene.intrinsics[i])
+        p.loss_kind = int(scene.loss_kind)
+        p.loss_delta = float(scene.loss_delta)
+        st = self.lib.zs_ba_set_problem(self.h, C.byref(p))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_set_problem")
+        self.K, self.L, self.M = p.num_poses, p.num_landmarks, p.num_obs
+
+    def set_state(self, poses=None, landmarks=None) -> None:
+        P = None if poses is None else np.ascontiguousarray(poses, dtype=np.float64)
+        Lm = None if landmarks is None else np.ascontiguousarray(landmarks, dtype=np.float64)
+        st = self.lib.zs_ba_set_state(self.h, _p(P, _dp), _p(Lm, _dp))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_set_state")
+
+    def get_state(self):
+        P = np.zeros((self.K, 7))
+        Lm = np.zeros((self.L, 3))
+        st = self.lib.zs_ba_get_state(self.h, _p(P, _dp), _p(Lm, _dp))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_get_state")
+        return P, Lm
+
+    def reset_state(self) -> None:
+        st = self.lib.zs_ba_reset_state(self.h)
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_reset_state")
+
+    def solve(self, iterations: int, use_relative: bool = False) -> Report:
+        rep = Report()
+        v = self.lib.zs_ba_solve(self.h, int(iterations), int(bool(use_relative)), C.byref(rep))
+        if v < 0:
+            raise ZsError(v, "zs_ba_solve")
+        return rep
+
+    def chi2(self) -> float:
+        out = C.c_double()
+        st = self.lib.zs_ba_chi2(self.h, C.byref(out))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_chi2")
+        return out.value
+
+    def initial_lambda(self) -> float:
+        out = C.c_double()
+        st = self.lib.zs_ba_initial_lambda(self.h, C.byref(out))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_initial_lambda")
+        return out.value
+
+    def linear_step(self, lam: float, want_S: bool = True) -> dict:
+        n = 6 * self.K
+        S = np.zeros((n, n)) if want_S else None
+        bs = np.zeros(n)
+        delta = np.zeros(n + 3 * self.L)
+        b = np.zeros(n + 3 * self.L)
+        st = self.lib.zs_ba_linear_step(self.h, float(lam), _p(S, _dp), _p(bs, _dp), _p(delta, _dp), _p(b, _dp))
+        if st not in (ZS_OK, ZS_ERR_CHOLESKY):
+            raise ZsError(st, "zs_ba_linear_step")
+        return dict(ok=(st == ZS_OK), S=S, bs=bs, delta=delta, b=b)
+
+
+def dense_cholesky_solve(A, b, precision: int = FP64):
+    """(ok, L, x) of the device Cholesky solve of A x = b."""
+    lib = load()
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = A.shape[0]
+    Lm = np.zeros_like(A)
+    x = np.zeros(n)
+    st = lib.zs_dense_cholesky_solve(_p(A, _dp), n, _p(b, _dp), _p(Lm, _dp), _p(x, _dp), int(precision))
+    if st not in (ZS_OK, ZS_ERR_CHOLESKY):
+        raise ZsError(st, "zs_dense_cholesky_solve")
+    return st == ZS_OK, Lm, x
+
+
+def pipe_peaks(device: int = 0):
+    """(fp64_tflops, fp32_tflops) measured by an FMA-chain microbenchmark."""
+    lib = load()
+    a, b = C.c_double(), C.c_double()
+    st = lib.zs_pipe_peaks(int(device), C.byref(a), C.byref(b))
+    if st != ZS_OK:
+        raise ZsError(st, "zs_pipe_peaks")
+    return a.value, b.value

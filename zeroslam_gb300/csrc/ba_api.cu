@@ -1,0 +1,795 @@
+// C ABI of the sm_103a bundle adjuster (include/zeroslam_ba.h): the handle,
+// the once-per-problem structure analysis and the Levenberg-Marquardt driver
+// whose state lives on the device (one small read-back per attempt).
+//
+// The LM control flow restates factor_graph::solve, source/factor_graph.hpp:489-615
+// (gpdaniels/zeroslam): initial damping (:511-522), up to max_failures attempts
+// per outer iteration (:541), Cholesky failure -> more damping (:542-551),
+// acceptance by the gain ratio (:556-591), rollback of rejected steps
+// (:601-605) and the stop rules (:608-611).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/zeroslam_ba.h"
+#include "ba_internal.h"
+
+using namespace zs;
+
+namespace {
+
+constexpr int kChunk = 32;  // triples per Schur chunk
+
+struct CudaError {
+    cudaError_t err;
+};
+
+#define ZS_CUDA(x)                                  \
+    do {                                            \
+        cudaError_t e_ = (x);                       \
+        if (e_ != cudaSuccess) throw CudaError{e_}; \
+    } while (0)
+
+template <typename T>
+T* dalloc(size_t count, std::vector<void*>& owned) {
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    ZS_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+T* upload(const std::vector<T>& v, std::vector<void*>& owned, cudaStream_t s) {
+    T* d = dalloc<T>(v.size(), owned);
+    if (!v.empty()) ZS_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+}  // namespace
+
+// CUDA-event timing of solve phases (options.profile): event pairs are
+// recorded around each phase and folded into the report at every host sync.
+struct PhaseTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    double ms[8] = {0};
+    int calls[8] = {0};
+    // nullptr when no event could be created (the phase then goes untimed)
+    cudaEvent_t get() noexcept {
+        cudaEvent_t e = nullptr;
+        if (!pool.empty()) {
+            e = pool.back();
+            pool.pop_back();
+        } else if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            e = nullptr;
+        }
+        return e;
+    }
+    void reset() {
+        collect();
+        for (int i = 0; i < 8; ++i) ms[i] = 0.0, calls[i] = 0;
+    }
+    // call only after the stream has been synchronised
+    void collect() {
+        for (auto& p : pending) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, p.second.first, p.second.second);
+            ms[p.first] += t;
+            calls[p.first] += 1;
+            pool.push_back(p.second.first);
+            pool.push_back(p.second.second);
+        }
+        pending.clear();
+    }
+    void destroy() {
+        collect();
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+        pool.clear();
+    }
+};
+
+struct PhaseScope {
+    PhaseTimer& t;
+    int phase;
+    cudaStream_t s;
+    cudaEvent_t e0 = nullptr;
+    PhaseScope(PhaseTimer& t_, int ph, cudaStream_t s_) : t(t_), phase(ph), s(s_) {
+        if (t.on) {
+            e0 = t.get();
+            if (e0) cudaEventRecord(e0, s);
+        }
+    }
+    ~PhaseScope() {
+        if (t.on && e0) {
+            cudaEvent_t e1 = t.get();
+            if (!e1) {
+                t.pool.push_back(e0);
+                return;
+            }
+            cudaEventRecord(e1, s);
+            t.pending.push_back({phase, {e0, e1}});
+        }
+    }
+};
+
+struct zs_ba_handle {
+    zs_ba_options opt{};
+    PhaseTimer timer;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool has_problem = false;
+    DevProblem P;
+    DevWork W;
+    LmState* st = nullptr;       // device
+    LmState* st_host = nullptr;  // pinned mirror
+    std::vector<void*> owned;    // problem-lifetime device allocations
+    std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
+    int tsize = 8;
+
+    void release_problem() {
+        for (void* p : owned) cudaFree(p);
+        owned.clear();
+        P = DevProblem{};
+        W = DevWork{};
+        has_problem = false;
+    }
+};
+
+extern "C" {
+
+void zs_ba_default_options(zs_ba_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = ZS_PRECISION_FP64;
+    o->max_failures = 10;
+    o->tau = 1e-5;
+    o->diagonal_clamp = 5e10;
+    o->legacy_stop = 1e-10;
+    o->relative_tolerance = 1e-6;
+    o->chi2_floor = 1e-12;
+    o->refine_iterations = 8;
+    o->refine_tolerance = 1e-12;
+    o->device = 0;
+    o->verbose = 0;
+}
+
+const char* zs_ba_status_string(int s) {
+    switch (s) {
+        case ZS_OK: return "ok";
+        case ZS_ERR_INVALID: return "invalid argument or problem";
+        case ZS_ERR_CUDA: return "CUDA error or no usable CUDA device";
+        case ZS_ERR_UNSUPPORTED: return "unsupported vertex, edge or loss kind";
+        case ZS_ERR_TIMEOUT: return "a bounded device wait ran out";
+        case ZS_ERR_NONFINITE: return "non-finite input values";
+        case ZS_ERR_NO_PROBLEM: return "no problem has been set";
+        case ZS_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case ZS_ERR_CHOLESKY: return "Cholesky solver failed";
+        default: return "unknown status";
+    }
+}
+
+static int cuda_status(cudaError_t e) {
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? ZS_ERR_OUT_OF_MEMORY : ZS_ERR_CUDA;
+}
+
+int zs_ba_create(zs_ba_handle** out, const zs_ba_options* opt) {
+    if (!out) return ZS_ERR_INVALID;
+    *out = nullptr;
+    zs_ba_handle* h = new (std::nothrow) zs_ba_handle();
+    if (!h) return ZS_ERR_OUT_OF_MEMORY;
+    if (opt) h->opt = *opt;
+    else zs_ba_default_options(&h->opt);
+    if (h->opt.precision != ZS_PRECISION_FP64 && h->opt.precision != ZS_PRECISION_MIXED) {
+        delete h;
+        return ZS_ERR_INVALID;
+    }
+    h->tsize = h->opt.precision == ZS_PRECISION_FP64 ? 8 : 4;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0 || h->opt.device < 0 || h->opt.device >= count) {
+        cudaGetLastError();
+        delete h;
+        return ZS_ERR_CUDA;
+    }
+    h->device = h->opt.device;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        ZS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        ZS_CUDA(cudaEventCreate(&h->ev0));
+        ZS_CUDA(cudaEventCreate(&h->ev1));
+        ZS_CUDA(cudaMalloc(&h->st, sizeof(LmState)));
+        ZS_CUDA(cudaMallocHost(&h->st_host, sizeof(LmState)));
+        ZS_CUDA(cudaMemset(h->st, 0, sizeof(LmState)));
+    } catch (const CudaError& e) {
+        zs_ba_destroy(h);
+        return cuda_status(e.err);
+    }
+    *out = h;
+    return ZS_OK;
+}
+
+void zs_ba_destroy(zs_ba_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->timer.destroy();
+    h->release_problem();
+    if (h->st) cudaFree(h->st);
+    if (h->st_host) cudaFreeHost(h->st_host);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+static int validate(const zs_ba_problem* p) {
+    if (!p) return ZS_ERR_INVALID;
+    if (p->num_poses < 0 || p->num_landmarks < 0 || p->num_obs < 0) return ZS_ERR_INVALID;
+    if (p->num_obs > 0x7fffffffLL) return ZS_ERR_INVALID;
+    if (p->num_poses > 0 && (!p->poses || !p->pose_fixed)) return ZS_ERR_INVALID;
+    if (p->num_landmarks > 0 && (!p->landmarks || !p->landmark_fixed)) return ZS_ERR_INVALID;
+    if (p->num_obs > 0 && (!p->obs_pose || !p->obs_landmark || !p->obs_uv)) return ZS_ERR_INVALID;
+    if (p->loss_kind < ZS_LOSS_NONE || p->loss_kind > ZS_LOSS_TUKEY) return ZS_ERR_UNSUPPORTED;
+    if (p->loss_kind != ZS_LOSS_NONE && !(p->loss_delta > 0.0)) return ZS_ERR_INVALID;
+    if (!(p->intrinsics[0] > 0.0) || !(p->intrinsics[1] > 0.0)) return ZS_ERR_INVALID;
+    for (int i = 0; i < 4; ++i)
+        if (!std::isfinite(p->intrinsics[i])) return ZS_ERR_NONFINITE;
+    for (int64_t o = 0; o < p->num_obs; ++o) {
+        if (p->obs_pose[o] < 0 || p->obs_pose[o] >= p->num_poses) return ZS_ERR_INVALID;
+        if (p->obs_landmark[o] < 0 || p->obs_landmark[o] >= p->num_landmarks) return ZS_ERR_INVALID;
+        if (p->obs_info && p->obs_info[4 * o + 1] != p->obs_info[4 * o + 2]) return ZS_ERR_INVALID;
+    }
+    return ZS_OK;
+}
+
+// Builds the device orderings and the Schur pair/triple lists, uploads the
+// problem and allocates the working arrays of the handle's precision.
+static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
+    cudaStream_t s = h->stream;
+    const int K = p->num_poses, L = p->num_landmarks;
+    const int64_t M = p->num_obs;
+    DevProblem& P = h->P;
+    P.K = K;
+    P.L = L;
+    P.M = M;
+    P.n = 6 * K;
+    P.intr = Intrinsics{p->intrinsics[0], p->intrinsics[1], p->intrinsics[2], p->intrinsics[3]};
+    P.loss = LossParams{p->loss_kind, p->loss_delta};
+
+    // landmark-major order, poses ascending within a landmark (stable)
+    std::vector<int32_t> lm_ptr(L + 1, 0);
+    for (int64_t o = 0; o < M; ++o) lm_ptr[p->obs_landmark[o] + 1]++;
+    for (int l = 0; l < L; ++l) lm_ptr[l + 1] += lm_ptr[l];
+    std::vector<int64_t>& perm = h->perm;
+    perm.assign(M, 0);
+    {
+        std::vector<int32_t> fill(lm_ptr.begin(), lm_ptr.end() - 1);
+        for (int64_t o = 0; o < M; ++o) perm[fill[p->obs_landmark[o]]++] = o;
+    }
+    for (int l = 0; l < L; ++l)
+        std::stable_sort(perm.begin() + lm_ptr[l], perm.begin() + lm_ptr[l + 1],
+                         [&](int64_t a, int64_t b) { return p->obs_pose[a] < p->obs_pose[b]; });
+    std::vector<int32_t> obs_pose(M), obs_lm(M), dup_owner(M);
+    std::vector<double2> uv(M);
+    std::vector<double> info(p->obs_info ? 4 * M : 0);
+    std::vector<uint8_t> blk_valid(M, 0);
+    bool has_dups = false;
+    for (int64_t i = 0; i < M; ++i) {
+        const int64_t o = perm[i];
+        obs_pose[i] = p->obs_pose[o];
+        obs_lm[i] = p->obs_landmark[o];
+        uv[i] = make_double2(p->obs_uv[2 * o], p->obs_uv[2 * o + 1]);
+        if (p->obs_info)
+            for (int k = 0; k < 4; ++k) info[4 * i + k] = p->obs_info[4 * o + k];
+        const bool same = i > 0 && obs_lm[i - 1] == obs_lm[i] && obs_pose[i - 1] == obs_pose[i];
+        dup_owner[i] = same ? dup_owner[i - 1] : (int32_t)i;
+        has_dups = has_dups || same;
+        blk_valid[i] = (!same && !p->pose_fixed[obs_pose[i]] && !p->landmark_fixed[obs_lm[i]]) ? 1 : 0;
+    }
+    // pose-major lists of landmark-major indices, ascending
+    std::vector<int32_t> pose_ptr(K + 1, 0), pose_obs(M);
+    for (int64_t i = 0; i < M; ++i) pose_ptr[obs_pose[i] + 1]++;
+    for (int k = 0; k < K; ++k) pose_ptr[k + 1] += pose_ptr[k];
+    {
+        std::vector<int32_t> fill(pose_ptr.begin(), pose_ptr.end() - 1);
+        for (int64_t i = 0; i < M; ++i) pose_obs[fill[obs_pose[i]]++] = (int32_t)i;
+    }
+    // Schur triples: for each landmark, every (block a, block b) with pose_a >= pose_b,
+    // grouped by pose pair (i, j) = (pose_a, pose_b), landmark order within a pair.
+    std::vector<int64_t> pair_count((size_t)K * K, 0);
+    std::vector<int32_t> vb;
+    for (int l = 0; l < L; ++l) {
+        vb.clear();
+        for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
+            if (blk_valid[i]) vb.push_back(i);
+        for (size_t a = 0; a < vb.size(); ++a)
+            for (size_t b = 0; b <= a; ++b) pair_count[(size_t)obs_pose[vb[a]] * K + obs_pose[vb[b]]]++;
+    }
+    std::vector<int64_t> pair_off((size_t)K * K + 1, 0);
+    int npairs = 0;
+    for (size_t k = 0; k < (size_t)K * K; ++k) {
+        pair_off[k + 1] = pair_off[k] + pair_count[k];
+        if (pair_count[k]) ++npairs;
+    }
+    const int64_t ntriples = pair_off[(size_t)K * K];
+    std::vector<int2> triples(ntriples);
+    {
+        std::vector<int64_t> fill(pair_off.begin(), pair_off.end() - 1);
+        for (int l = 0; l < L; ++l) {
+            vb.clear();
+            for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
+                if (blk_valid[i]) vb.push_back(i);
+            for (size_t a = 0; a < vb.size(); ++a)
+                for (size_t b = 0; b <= a; ++b)
+                    triples[fill[(size_t)obs_pose[vb[a]] * K + obs_pose[vb[b]]]++] = make_int2(vb[a], vb[b]);
+        }
+    }
+    std::vector<int32_t> pair_i, pair_j;
+    std::vector<int64_t> pair_chunk_ptr{0}, chunk_ptr{0};
+    pair_i.reserve(npairs);
+    pair_j.reserve(npairs);
+    for (size_t k = 0; k < (size_t)K * K; ++k) {
+        if (!pair_count[k]) continue;
+        pair_i.push_back((int32_t)(k / K));
+        pair_j.push_back((int32_t)(k % K));
+        for (int64_t t = pair_off[k]; t < pair_off[k + 1]; t += kChunk)
+            chunk_ptr.push_back(std::min<int64_t>(t + kChunk, pair_off[k + 1]));
+        pair_chunk_ptr.push_back((int64_t)chunk_ptr.size() - 1);
+    }
+    P.npairs = npairs;
+    P.ntriples = ntriples;
+    P.nchunks = (int64_t)chunk_ptr.size() - 1;
+
+    // state (padded device layout)
+    std::vector<double> pose8((size_t)K * kPoseStride, 0.0), lm4((size_t)L * kLmStride, 0.0);
+    for (int k = 0; k < K; ++k)
+        for (int i = 0; i < 7; ++i) pose8[(size_t)k * kPoseStride + i] = p->poses[7LL * k + i];
+    for (int l = 0; l < L; ++l)
+        for (int i = 0; i < 3; ++i) lm4[(size_t)l * kLmStride + i] = p->landmarks[3LL * l + i];
+    std::vector<uint8_t> pf(p->pose_fixed, p->pose_fixed + K), lf(p->landmark_fixed, p->landmark_fixed + L);
+
+    auto& own = h->owned;
+    P.pose = upload(pose8, own, s);
+    P.pose_bk = dalloc<double>(pose8.size(), own);
+    P.lm = upload(lm4, own, s);
+    P.lm_bk = dalloc<double>(lm4.size(), own);
+    P.pose_init = upload(pose8, own, s);
+    P.lm_init = upload(lm4, own, s);
+    P.pose_fixed = upload(pf, own, s);
+    P.lm_fixed = upload(lf, own, s);
+    P.obs_pose = upload(obs_pose, own, s);
+    P.obs_lm = upload(obs_lm, own, s);
+    P.obs_uv = upload(uv, own, s);
+    P.obs_info = p->obs_info ? upload(info, own, s) : nullptr;
+    P.lm_ptr = upload(lm_ptr, own, s);
+    P.pose_ptr = upload(pose_ptr, own, s);
+    P.pose_obs = upload(pose_obs, own, s);
+    P.blk_valid = upload(blk_valid, own, s);
+    P.has_dups = has_dups;
+    P.dup_owner = has_dups ? upload(dup_owner, own, s) : nullptr;
+    P.pair_i = upload(pair_i, own, s);
+    P.pair_j = upload(pair_j, own, s);
+    P.pair_chunk_ptr = upload(pair_chunk_ptr, own, s);
+    P.chunk_ptr = upload(chunk_ptr, own, s);
+    P.triples = upload(triples, own, s);
+
+    const size_t ts = (size_t)h->tsize;
+    const int n = P.n;
+    DevWork& W = h->W;
+    W.hpl = dalloc<char>(ts * 18 * M, own);
+    W.W = dalloc<char>(ts * 18 * M, own);
+    W.lm_part = dalloc<char>(ts * 9 * M, own);
+    W.pose_part = dalloc<char>(ts * 27 * M, own);
+    W.hpp = dalloc<double>((size_t)K * 36, own);
+    W.hll = dalloc<double>((size_t)L * 9, own);
+    W.hll_inv = dalloc<double>((size_t)L * 9, own);
+    W.b = dalloc<double>((size_t)n + 3 * (size_t)L, own);
+    W.partial = dalloc<char>(ts * 36 * (size_t)P.nchunks, own);
+    W.S = dalloc<char>(ts * (size_t)n * n, own);
+    W.F = dalloc<char>(ts * (size_t)n * n, own);
+    W.bs = dalloc<double>(n, own);
+    W.y = dalloc<double>(2 * (size_t)n, own);
+    W.r = dalloc<double>(2 * (size_t)n, own);
+    W.delta = dalloc<double>((size_t)n + 3 * (size_t)L, own);
+    W.red = dalloc<double>(kReduceBlocks * 4, own);
+    W.ired = dalloc<int32_t>(kReduceBlocks, own);
+    ZS_CUDA(cudaMemsetAsync(W.hll_inv, 0, sizeof(double) * 9 * (size_t)std::max(L, 1), s));
+    ZS_CUDA(cudaMemsetAsync(W.delta, 0, sizeof(double) * ((size_t)n + 3 * (size_t)L + 1), s));
+    ZS_CUDA(cudaStreamSynchronize(s));
+    ZS_CUDA(cudaGetLastError());
+}
+
+int zs_ba_set_problem(zs_ba_handle* h, const zs_ba_problem* p) {
+    if (!h) return ZS_ERR_INVALID;
+    const int v = validate(p);
+    if (v != ZS_OK) return v;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+        h->release_problem();
+        build_problem(h, p);
+        h->has_problem = true;
+    } catch (const CudaError& e) {
+        h->release_problem();
+        return cuda_status(e.err);
+    } catch (const std::bad_alloc&) {
+        h->release_problem();
+        return ZS_ERR_OUT_OF_MEMORY;
+    }
+    return ZS_OK;
+}
+
+int zs_ba_set_state(zs_ba_handle* h, const double* poses, const double* landmarks) {
+    if (!h) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    const DevProblem& P = h->P;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        if (poses && P.K > 0) {
+            ZS_CUDA(cudaMemcpy2DAsync(P.pose, kPoseStride * sizeof(double), poses, 7 * sizeof(double),
+                                      7 * sizeof(double), P.K, cudaMemcpyHostToDevice, h->stream));
+        }
+        if (landmarks && P.L > 0) {
+            ZS_CUDA(cudaMemcpy2DAsync(P.lm, kLmStride * sizeof(double), landmarks, 3 * sizeof(double),
+                                      3 * sizeof(double), P.L, cudaMemcpyHostToDevice, h->stream));
+        }
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
+}
+
+int zs_ba_get_state(zs_ba_handle* h, double* poses, double* landmarks) {
+    if (!h) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    const DevProblem& P = h->P;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        if (poses && P.K > 0) {
+            ZS_CUDA(cudaMemcpy2DAsync(poses, 7 * sizeof(double), P.pose, kPoseStride * sizeof(double),
+                                      7 * sizeof(double), P.K, cudaMemcpyDeviceToHost, h->stream));
+        }
+        if (landmarks && P.L > 0) {
+            ZS_CUDA(cudaMemcpy2DAsync(landmarks, 3 * sizeof(double), P.lm, kLmStride * sizeof(double),
+                                      3 * sizeof(double), P.L, cudaMemcpyDeviceToHost, h->stream));
+        }
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
+}
+
+int zs_ba_reset_state(zs_ba_handle* h) {
+    if (!h) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    const DevProblem& P = h->P;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        if (P.K > 0)
+            ZS_CUDA(cudaMemcpyAsync(P.pose, P.pose_init, sizeof(double) * kPoseStride * (size_t)P.K,
+                                    cudaMemcpyDeviceToDevice, h->stream));
+        if (P.L > 0)
+            ZS_CUDA(cudaMemcpyAsync(P.lm, P.lm_init, sizeof(double) * kLmStride * (size_t)P.L,
+                                    cudaMemcpyDeviceToDevice, h->stream));
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+void read_state(zs_ba_handle* h) {
+    ZS_CUDA(cudaMemcpyAsync(h->st_host, h->st, sizeof(LmState), cudaMemcpyDeviceToHost, h->stream));
+    ZS_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->timer.on) h->timer.collect();
+}
+
+template <typename T>
+void linearize(zs_ba_handle* h) {
+    PhaseScope ps(h->timer, ZS_PHASE_LINEARIZE, h->stream);
+    launch_linearize<T>(h->P, h->W, h->stream);
+}
+
+// One damped solve at st->lambda: H_ll inverses, Schur complement, reduced
+// Cholesky solve into delta[0..n), landmark back-substitution.
+template <typename T>
+void system_solve(zs_ba_handle* h) {
+    DevProblem& P = h->P;
+    DevWork& W = h->W;
+    cudaStream_t s = h->stream;
+    launch_set_solve_ok(h->st, 1, s);
+    {
+        PhaseScope ps(h->timer, ZS_PHASE_INVERT, s);
+        launch_invert_w<T>(P, W, h->st, s);
+    }
+    {
+        PhaseScope ps(h->timer, ZS_PHASE_SCHUR, s);
+        launch_schur<T>(P, W, h->st, s);
+    }
+    {
+        PhaseScope ps(h->timer, ZS_PHASE_FACTOR, s);
+        launch_factor<T, T>(P.n, (const T*)W.S, (T*)W.F, h->st, s);
+    }
+    {
+        PhaseScope ps(h->timer, ZS_PHASE_TRISOLVE, s);
+        const int refine = (sizeof(T) == 4) ? std::max(0, h->opt.refine_iterations) : 0;
+        launch_solve_refine<T, T>(P.n, (const T*)W.S, (const T*)W.F, W.bs, W.delta, W.y, W.r, h->st, refine, s);
+    }
+    PhaseScope ps(h->timer, ZS_PHASE_UPDATE, s);
+    launch_backsub<T>(P, W, h->st, s);
+}
+
+template <typename T>
+int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report* rep) {
+    DevProblem& P = h->P;
+    DevWork& W = h->W;
+    cudaStream_t s = h->stream;
+    const zs_ba_options& o = h->opt;
+    zs_ba_report r{};
+    const long long launches0 = launch_counter();
+    h->timer.on = o.profile != 0;
+    h->timer.reset();
+    ZS_CUDA(cudaEventRecord(h->ev0, s));
+    linearize<T>(h);
+    {
+        PhaseScope ps(h->timer, ZS_PHASE_COST, s);
+        launch_cost(P, W, h->st, false, s);
+        launch_init_lambda(P, W, h->st, o.tau, o.diagonal_clamp, s);
+    }
+    read_state(h);
+    LmState& hs = *h->st_host;
+    r.chi2_initial = hs.chi2;
+    double chi2 = hs.chi2;
+    double lambda = hs.lambda;
+    if (o.verbose)
+        std::fprintf(stderr,
+                     "[INIT] iter: XXX, attempt XXX, chi = % 7.7f, rho = XXXX.XXXXXXX, base lambda = % 8.7f\n", chi2,
+                     lambda);
+    const double legacy = o.legacy_stop * chi2;
+    int success = 0;
+    for (int it = 0; it < iterations; ++it) {
+        r.iterations = it + 1;
+        const double last = chi2;
+        int failures = 0;
+        while (failures < o.max_failures) {
+            system_solve<T>(h);
+            {
+                PhaseScope ps(h->timer, ZS_PHASE_UPDATE, s);
+                launch_update(P, W, h->st, s);
+                launch_scale(P, W, h->st, s);
+            }
+            {
+                PhaseScope ps(h->timer, ZS_PHASE_COST, s);
+                launch_cost(P, W, h->st, true, s);
+                launch_decide(h->st, s);
+                launch_rollback(P, h->st, s);
+            }
+            read_state(h);
+            r.attempts++;
+            lambda = hs.lambda;
+            if (!hs.solve_ok) {
+                r.cholesky_failures++;
+                if (o.verbose) std::fprintf(stderr, "Cholesky solver failed!\n");
+                ++failures;
+                if (!std::isfinite(lambda)) break;
+                continue;
+            }
+            if (sizeof(T) == 4) r.refine_sweeps += o.refine_iterations;
+            if (hs.good) {
+                chi2 = hs.chi2;
+                ++success;
+                if (o.verbose)
+                    std::fprintf(stderr,
+                                 "[GOOD] iter: % 3d, attempt % 3d, chi2 = % 7.7f, rho = % 7.7f, next lambda = % 8.7f\n",
+                                 it, failures, hs.chi2_new, hs.rho, lambda);
+                if (!std::isfinite(lambda)) break;
+                linearize<T>(h);
+                break;
+            }
+            if (o.verbose)
+                std::fprintf(stderr,
+                             "[ BAD] iter: % 3d, attempt % 3d, chi2 = % 7.7f, rho = % 7.7f, next lambda = % 8.7f\n", it,
+                             failures, hs.chi2_new, hs.rho, lambda);
+            if (!std::isfinite(lambda)) break;
+            ++failures;
+        }
+        const double thr = use_relative ? o.relative_tolerance * std::max(last, o.chi2_floor) : legacy;
+        if (failures >= o.max_failures || (last - chi2) < thr || !std::isfinite(lambda)) break;
+    }
+    ZS_CUDA(cudaEventRecord(h->ev1, s));
+    ZS_CUDA(cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    r.ms_total = ms;
+    r.kernel_launches = launch_counter() - launches0;
+    if (h->timer.on) {
+        h->timer.collect();
+        for (int i = 0; i < 8; ++i) {
+            r.ms_phase[i] = h->timer.ms[i];
+            r.phase_calls[i] = h->timer.calls[i];
+        }
+        h->timer.on = false;
+    }
+    r.accepted = success;
+    r.chi2_final = chi2;
+    r.lambda_final = lambda;
+    r.status = ZS_OK;
+    if (rep) *rep = r;
+    return success;
+}
+
+template <typename T>
+int linear_step_impl(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b) {
+    DevProblem& P = h->P;
+    DevWork& W = h->W;
+    cudaStream_t s = h->stream;
+    linearize<T>(h);
+    LmState init{};
+    init.lambda = lambda;
+    init.nu = 2.0;
+    ZS_CUDA(cudaMemcpyAsync(h->st, &init, sizeof(LmState), cudaMemcpyHostToDevice, s));
+    system_solve<T>(h);
+    read_state(h);
+    const int n = P.n;
+    const size_t nall = (size_t)n + 3 * (size_t)P.L;
+    if (S && n > 0) {
+        std::vector<T> tmp((size_t)n * n);
+        ZS_CUDA(cudaMemcpyAsync(tmp.data(), W.S, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, s));
+        ZS_CUDA(cudaStreamSynchronize(s));
+        for (size_t i = 0; i < tmp.size(); ++i) S[i] = (double)tmp[i];
+    }
+    if (bs && n > 0) ZS_CUDA(cudaMemcpyAsync(bs, W.bs, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (delta && nall > 0) ZS_CUDA(cudaMemcpyAsync(delta, W.delta, nall * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (b && nall > 0) ZS_CUDA(cudaMemcpyAsync(b, W.b, nall * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ZS_CUDA(cudaStreamSynchronize(s));
+    return h->st_host->solve_ok ? ZS_OK : ZS_ERR_CHOLESKY;
+}
+
+}  // namespace
+
+extern "C" {
+
+int zs_ba_solve(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* rep) {
+    if (!h) return ZS_ERR_INVALID;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    // source/factor_graph.hpp:494-499: nothing to do without edges or vertices
+    if (h->P.M == 0 || (h->P.K == 0 && h->P.L == 0)) return 0;
+    if (iterations < 0) return ZS_ERR_INVALID;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        const int v = h->tsize == 8 ? solve_impl<double>(h, iterations, use_relative != 0, rep)
+                                    : solve_impl<float>(h, iterations, use_relative != 0, rep);
+        ZS_CUDA(cudaGetLastError());
+        return v;
+    } catch (const CudaError& e) {
+        const int st = cuda_status(e.err);
+        if (rep) rep->status = st;
+        return st;
+    }
+}
+
+int zs_ba_chi2(zs_ba_handle* h, double* chi2) {
+    if (!h || !chi2) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        if (h->P.M == 0) {
+            *chi2 = 0.0;
+            return ZS_OK;
+        }
+        launch_cost(h->P, h->W, h->st, false, h->stream);
+        read_state(h);
+        *chi2 = h->st_host->chi2_new;
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
+}
+
+int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda) {
+    if (!h || !lambda) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        if (h->tsize == 8) linearize<double>(h);
+        else linearize<float>(h);
+        launch_cost(h->P, h->W, h->st, false, h->stream);
+        launch_init_lambda(h->P, h->W, h->st, h->opt.tau, h->opt.diagonal_clamp, h->stream);
+        read_state(h);
+        *lambda = h->st_host->lambda;
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
+}
+
+int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b) {
+    if (!h) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        return h->tsize == 8 ? linear_step_impl<double>(h, lambda, S, bs, delta, b)
+                             : linear_step_impl<float>(h, lambda, S, bs, delta, b);
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+}
+
+int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lout, double* x, int precision) {
+    if (!A || n <= 0 || !b) return ZS_ERR_INVALID;
+    if (precision != ZS_PRECISION_FP64 && precision != ZS_PRECISION_MIXED) return ZS_ERR_INVALID;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return ZS_ERR_CUDA;
+    }
+    std::vector<void*> owned;
+    cudaStream_t s = nullptr;
+    int status = ZS_OK;
+    try {
+        ZS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        const size_t nn = (size_t)n * n;
+        double* dA = dalloc<double>(nn, owned);
+        double* db = dalloc<double>(n, owned);
+        double* dx = dalloc<double>(n, owned);
+        double* dy = dalloc<double>(2 * (size_t)n, owned);
+        double* dr = dalloc<double>(2 * (size_t)n, owned);
+        LmState* st = dalloc<LmState>(1, owned);
+        LmState init{};
+        init.solve_ok = 1;
+        ZS_CUDA(cudaMemcpyAsync(st, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+        ZS_CUDA(cudaMemcpyAsync(dA, A, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+        ZS_CUDA(cudaMemcpyAsync(db, b, n * sizeof(double), cudaMemcpyHostToDevice, s));
+        std::vector<double> Lh;
+        if (precision == ZS_PRECISION_FP64) {
+            double* dF = dalloc<double>(nn, owned);
+            launch_reduced_solve<double, double>(n, dA, dF, db, dx, dy, dr, st, 0, s);
+            if (Lout) {
+                Lh.resize(nn);
+                ZS_CUDA(cudaMemcpyAsync(Lh.data(), dF, nn * sizeof(double), cudaMemcpyDeviceToHost, s));
+            }
+        } else {
+            float* dF = dalloc<float>(nn, owned);
+            launch_reduced_solve<double, float>(n, dA, dF, db, dx, dy, dr, st, 8, s);
+            if (Lout) {
+                std::vector<float> tmp(nn);
+                ZS_CUDA(cudaMemcpyAsync(tmp.data(), dF, nn * sizeof(float), cudaMemcpyDeviceToHost, s));
+                ZS_CUDA(cudaStreamSynchronize(s));
+                Lh.assign(tmp.begin(), tmp.end());
+            }
+        }
+        LmState out{};
+        ZS_CUDA(cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s));
+        if (x) ZS_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        ZS_CUDA(cudaStreamSynchronize(s));
+        ZS_CUDA(cudaGetLastError());
+        if (Lout) {
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) Lout[(size_t)i * n + j] = (j <= i) ? Lh[(size_t)i * n + j] : 0.0;
+        }
+        status = out.solve_ok ? ZS_OK : ZS_ERR_CHOLESKY;
+    } catch (const CudaError& e) {
+        status = cuda_status(e.err);
+    }
+    if (s) cudaStreamSynchronize(s);
+    for (void* p : owned) cudaFree(p);
+    if (s) cudaStreamDestroy(s);
+    return status;
+}
+
+}  // extern "C"

@@ -1,0 +1,660 @@
+// Bundle-adjustment kernels for sm_103a: per-observation linearisation,
+// deterministic segmented assembly, 3x3 landmark inverses, the Schur
+// complement, landmark back-substitution, the manifold update, the cost and
+// the Levenberg-Marquardt decision. No floating-point atomics anywhere: every
+// sum has one owner thread or a fixed reduction tree, so results repeat bit
+// for bit from run to run.
+//
+// Reference counterparts (gpdaniels/zeroslam):
+//   k_linearize, k_reduce_lm, k_reduce_pose  make_hessian       source/factor_graph.hpp:648-732
+//                                            compute_jacobians  source/factor_graph.hpp:1012-1048
+//                                            robust_info        source/factor_graph.hpp:254-269
+//   k_invert, k_w                            damping + invert<3> source/factor_graph.hpp:738-765,
+//                                                               source/matrix.hpp:749-774
+//   k_schur_chunks, k_schur_assemble, k_bs   W = H_pl H_ll^-1, S = H_pp - W H_lp, b_s = b_p - W b_l
+//                                            source/factor_graph.hpp:768-781,
+//                                            source/matrix_sparse_block.hpp:158-196,
+//                                            source/matrix_sparse_block_diagonal.hpp:107-142
+//   k_backsub                                source/factor_graph.hpp:799-800
+//   k_update, k_rollback                     source/factor_graph.hpp:809-846, 947-960
+//   k_cost_partial                           get_current_chi    source/factor_graph.hpp:618-629
+//   k_scale_partial, k_decide                LM acceptance      source/factor_graph.hpp:555-606
+#include "ba_internal.h"
+
+namespace zs {
+
+// (a, c) with a <= c of a symmetric 6x6 block, row by row.
+__constant__ int8_t kUp6[21][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 5}, {1, 1}, {1, 2}, {1, 3}, {1, 4}, {1, 5},
+                                   {2, 2}, {2, 3}, {2, 4}, {2, 5}, {3, 3}, {3, 4}, {3, 5}, {4, 4}, {4, 5}, {5, 5}};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
+                                                        T* __restrict__ pose_part) {
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= P.M) return;
+    const int pi = P.obs_pose[o], li = P.obs_lm[o];
+    const double* pp = P.pose + (int64_t)pi * kPoseStride;
+    const double* xp = P.lm + (int64_t)li * kLmStride;
+    double p[7], X[3];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) p[i] = __ldg(pp + i);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) X[i] = __ldg(xp + i);
+    const double2 uv = P.obs_uv[o];
+    double Xc[3], r[2];
+    const int front = residual(p, X, uv.x, uv.y, P.intr, Xc, r);
+    const double* om = P.obs_info ? P.obs_info + 4 * o : nullptr;
+
+    // Robust weight W = rho' Omega (+ 2 rho'' (Omega r)(Omega r)^T), and the
+    // gradient's non-robust Omega r scaled by rho'.
+    double Wd[4] = {1.0, 0.0, 0.0, 1.0};
+    if (om) {
+        Wd[0] = om[0]; Wd[1] = om[1]; Wd[2] = om[2]; Wd[3] = om[3];
+    }
+    double orr0 = r[0], orr1 = r[1];
+    if (om) {
+        orr0 = om[0] * r[0] + om[1] * r[1];
+        orr1 = om[2] * r[0] + om[3] * r[1];
+    }
+    double drho = 1.0;
+    if (P.loss.kind) {
+        const double e2 = chi2_of(r, om);
+        double rho[3];
+        loss_rho(P.loss, e2, rho);
+        drho = rho[1];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Wd[i] *= rho[1];
+        if ((rho[1] + 2.0 * rho[2] * e2) > 0.0) {
+            const double k2 = 2.0 * rho[2];
+            Wd[0] += k2 * orr0 * orr0;
+            Wd[1] += k2 * orr0 * orr1;
+            Wd[2] += k2 * orr1 * orr0;
+            Wd[3] += k2 * orr1 * orr1;
+        }
+    }
+
+    // Camera Jacobian (2x3); behind the camera d(residual)/dZ = -0.3.
+    T Jc[6];
+    if (front) {
+        const T iz = (T)(1.0 / Xc[2]);
+        const T iz2 = iz * iz;
+        const T fx = (T)P.intr.fx, fy = (T)P.intr.fy;
+        Jc[0] = fx * iz; Jc[1] = T(0); Jc[2] = -fx * (T)Xc[0] * iz2;
+        Jc[3] = T(0); Jc[4] = fy * iz; Jc[5] = -fy * (T)Xc[1] * iz2;
+    } else {
+        Jc[0] = T(0); Jc[1] = T(0); Jc[2] = (T)kBehindPenalty;
+        Jc[3] = T(0); Jc[4] = T(0); Jc[5] = (T)kBehindPenalty;
+    }
+    const T Xv = (T)Xc[0], Yv = (T)Xc[1], Zv = (T)Xc[2];
+    // J_p = -J_cam [-[Xc]x | I] (omega first), J_l = -J_cam R.
+    T Jp[12], Jl[6];
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+        const T c0 = Jc[rr * 3], c1 = Jc[rr * 3 + 1], c2 = Jc[rr * 3 + 2];
+        Jp[rr * 6 + 0] = -(c2 * Yv - c1 * Zv);
+        Jp[rr * 6 + 1] = -(c0 * Zv - c2 * Xv);
+        Jp[rr * 6 + 2] = -(c1 * Xv - c0 * Yv);
+        Jp[rr * 6 + 3] = -c0;
+        Jp[rr * 6 + 4] = -c1;
+        Jp[rr * 6 + 5] = -c2;
+    }
+    {
+        double q[4] = {p[6], p[3], p[4], p[5]};
+        double R[9];
+        quat_matrix(q, R);
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                Jl[rr * 3 + c] = -(Jc[rr * 3] * (T)R[c] + Jc[rr * 3 + 1] * (T)R[3 + c] + Jc[rr * 3 + 2] * (T)R[6 + c]);
+    }
+    const T W00 = (T)Wd[0], W01 = (T)Wd[1], W10 = (T)Wd[2], W11 = (T)Wd[3];
+    const T g0 = (T)(drho * orr0), g1 = (T)(drho * orr1);
+    const bool pf = P.pose_fixed[pi] != 0, lf = P.lm_fixed[li] != 0;
+
+    T* hb = hpl + o * 18;
+    if (!pf) {
+        T A0[6], A1[6];  // (J_p^T W) columns
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            A0[a] = Jp[a] * W00 + Jp[6 + a] * W10;
+            A1[a] = Jp[a] * W01 + Jp[6 + a] * W11;
+        }
+#pragma unroll
+        for (int k = 0; k < 21; ++k) {
+            const int a = kUp6[k][0], c = kUp6[k][1];
+            pose_part[(int64_t)k * P.M + o] = A0[a] * Jp[c] + A1[a] * Jp[6 + c];
+        }
+#pragma unroll
+        for (int a = 0; a < 6; ++a) pose_part[(int64_t)(21 + a) * P.M + o] = -(Jp[a] * g0 + Jp[6 + a] * g1);
+        if (!lf) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) hb[a * 3 + c] = A0[a] * Jl[c] + A1[a] * Jl[3 + c];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 18; ++k) hb[k] = T(0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 27; ++k) pose_part[(int64_t)k * P.M + o] = T(0);
+#pragma unroll
+        for (int k = 0; k < 18; ++k) hb[k] = T(0);
+    }
+    if (!lf) {
+        T B0[3], B1[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            B0[a] = Jl[a] * W00 + Jl[3 + a] * W10;
+            B1[a] = Jl[a] * W01 + Jl[3 + a] * W11;
+        }
+        lm_part[0 * P.M + o] = B0[0] * Jl[0] + B1[0] * Jl[3];
+        lm_part[1 * P.M + o] = B0[0] * Jl[1] + B1[0] * Jl[4];
+        lm_part[2 * P.M + o] = B0[0] * Jl[2] + B1[0] * Jl[5];
+        lm_part[3 * P.M + o] = B0[1] * Jl[1] + B1[1] * Jl[4];
+        lm_part[4 * P.M + o] = B0[1] * Jl[2] + B1[1] * Jl[5];
+        lm_part[5 * P.M + o] = B0[2] * Jl[2] + B1[2] * Jl[5];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) lm_part[(int64_t)(6 + a) * P.M + o] = -(Jl[a] * g0 + Jl[3 + a] * g1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) lm_part[(int64_t)k * P.M + o] = T(0);
+    }
+}
+
+// Duplicate (pose, landmark) observations: the run's owner gets the sum of
+// the run's H_pl blocks, in order.
+template <typename T>
+__global__ void k_merge_dups(DevProblem P, T* hpl) {
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= P.M) return;
+    if (P.dup_owner[o] != o) return;
+    int64_t e = o + 1;
+    T acc[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) acc[k] = hpl[o * 18 + k];
+    while (e < P.M && P.dup_owner[e] == o) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) acc[k] += hpl[e * 18 + k];
+        ++e;
+    }
+#pragma unroll
+    for (int k = 0; k < 18; ++k) hpl[o * 18 + k] = acc[k];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* __restrict__ lm_part, double* hll,
+                                                        double* b) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= P.L) return;
+    T acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = T(0);
+    const int e = P.lm_ptr[l + 1];
+    for (int o = P.lm_ptr[l]; o < e; ++o) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] += lm_part[(int64_t)k * P.M + o];
+    }
+    double* h = hll + (int64_t)l * 9;
+    h[0] = acc[0]; h[1] = acc[1]; h[2] = acc[2];
+    h[3] = acc[1]; h[4] = acc[3]; h[5] = acc[4];
+    h[6] = acc[2]; h[7] = acc[4]; h[8] = acc[5];
+    double* bl = b + P.n + 3LL * l;
+    bl[0] = acc[6]; bl[1] = acc[7]; bl[2] = acc[8];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T* __restrict__ pose_part, double* hpp,
+                                                          double* b) {
+    __shared__ T sh[kThreads];
+    const int k = blockIdx.x;
+    T acc[27];
+#pragma unroll
+    for (int c = 0; c < 27; ++c) acc[c] = T(0);
+    const int e = P.pose_ptr[k + 1];
+    for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x) {
+        const int64_t o = P.pose_obs[i];
+#pragma unroll
+        for (int c = 0; c < 27; ++c) acc[c] += pose_part[(int64_t)c * P.M + o];
+    }
+    double* H = hpp + (int64_t)k * 36;
+#pragma unroll 1
+    for (int c = 0; c < 21; ++c) {
+        const T v = block_sum(acc[c], sh);
+        if (threadIdx.x == 0) {
+            const int a = kUp6[c][0], d = kUp6[c][1];
+            H[a * 6 + d] = v;
+            H[d * 6 + a] = v;
+        }
+    }
+#pragma unroll 1
+    for (int c = 0; c < 6; ++c) {
+        const T v = block_sum(acc[21 + c], sh);
+        if (threadIdx.x == 0) b[6LL * k + c] = v;
+    }
+}
+
+// matrix::invert<3> on H_ll + lambda I (source/matrix.hpp:749-774); fixed or
+// singular blocks leave a zero inverse, as solve_linear_system ignores the
+// failed inversion (source/factor_graph.hpp:763).
+__global__ void __launch_bounds__(kThreads) k_invert(DevProblem P, const double* __restrict__ hll, double* hinv,
+                                                     const LmState* st) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= P.L) return;
+    double* o = hinv + (int64_t)l * 9;
+    if (P.lm_fixed[l]) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) o[i] = 0.0;
+        return;
+    }
+    const double lam = st->lambda;
+    double a[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) a[i] = hll[(int64_t)l * 9 + i];
+    a[0] += lam; a[4] += lam; a[8] += lam;
+    const double det = +a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                       a[2] * (a[3] * a[7] - a[4] * a[6]);
+    double scale = 0.0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
+    if (!(fabs(det) > scale * scale * scale * 1e-12)) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) o[i] = 0.0;
+        return;
+    }
+    const double id = 1.0 / det;
+    o[0] = (a[4] * a[8] - a[7] * a[5]) * id;
+    o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+    o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+    o[3] = (a[5] * a[6] - a[3] * a[8]) * id;
+    o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+    o[5] = (a[3] * a[2] - a[0] * a[5]) * id;
+    o[6] = (a[3] * a[7] - a[6] * a[4]) * id;
+    o[7] = (a[6] * a[1] - a[0] * a[7]) * id;
+    o[8] = (a[0] * a[4] - a[3] * a[1]) * id;
+}
+
+// W = H_pl H_ll^-1 per block.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_w(DevProblem P, const T* __restrict__ hpl, const double* __restrict__ hinv,
+                                                T* __restrict__ W) {
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= P.M || !P.blk_valid[o]) return;
+    const double* I = hinv + (int64_t)P.obs_lm[o] * 9;
+    T iv[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) iv[i] = (T)I[i];
+    const T* h = hpl + o * 18;
+    T* w = W + o * 18;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+        const T h0 = h[a * 3], h1 = h[a * 3 + 1], h2 = h[a * 3 + 2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) w[a * 3 + c] = h0 * iv[c] + h1 * iv[3 + c] + h2 * iv[6 + c];
+    }
+}
+
+// Partial 6x6 sums W_i H_j^T over one chunk of a pose pair's triples.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_schur_chunks(DevProblem P, const T* __restrict__ W,
+                                                           const T* __restrict__ hpl, T* __restrict__ partial) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= P.nchunks) return;
+    T acc[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = T(0);
+    const int64_t e1 = P.chunk_ptr[c + 1];
+    for (int64_t t = P.chunk_ptr[c]; t < e1; ++t) {
+        const int2 tr = P.triples[t];
+        const T* w = W + (int64_t)tr.x * 18;
+        const T* h = hpl + (int64_t)tr.y * 18;
+        T wv[18], hv[18];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+            wv[k] = w[k];
+            hv[k] = h[k];
+        }
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int d = 0; d < 6; ++d)
+                acc[a * 6 + d] += wv[a * 3] * hv[d * 3] + wv[a * 3 + 1] * hv[d * 3 + 1] + wv[a * 3 + 2] * hv[d * 3 + 2];
+    }
+    T* out = partial + c * 36;
+#pragma unroll
+    for (int e = 0; e < 36; ++e) out[e] = acc[e];
+}
+
+// S = blockdiag(H_pp + lambda I); the pair sums are subtracted next.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_s_init(DevProblem P, const double* __restrict__ hpp, T* S,
+                                                     const LmState* st) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t n = P.n;
+    if (idx >= n * n) return;
+    const int row = (int)(idx / n), col = (int)(idx % n);
+    double v = 0.0;
+    if (row / 6 == col / 6) {
+        v = hpp[(int64_t)(row / 6) * 36 + (row % 6) * 6 + (col % 6)];
+        if (row == col) v += st->lambda;
+    }
+    S[idx] = (T)v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const T* __restrict__ partial, T* S) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)P.npairs * 36) return;
+    const int p = (int)(idx / 36), e = (int)(idx % 36);
+    T sum = T(0);
+    const int64_t c1 = P.pair_chunk_ptr[p + 1];
+    for (int64_t c = P.pair_chunk_ptr[p]; c < c1; ++c) sum += partial[c * 36 + e];
+    const int i = P.pair_i[p], j = P.pair_j[p];
+    const int64_t n = P.n;
+    const int64_t row = 6LL * i + e / 6, col = 6LL * j + e % 6;
+    if (i == j) {
+        S[row * n + col] = S[row * n + col] - sum;
+    } else {
+        S[row * n + col] = -sum;
+        S[col * n + row] = -sum;
+    }
+}
+
+// b_s = b_p - sum over the pose's blocks of W b_l.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bs(DevProblem P, const T* __restrict__ W, const double* __restrict__ b,
+                                                 double* bs) {
+    __shared__ double sh[kThreads];
+    const int k = blockIdx.x;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const int e = P.pose_ptr[k + 1];
+    for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x) {
+        const int64_t o = P.pose_obs[i];
+        if (!P.blk_valid[o]) continue;
+        const T* w = W + o * 18;
+        const double* bl = b + P.n + 3LL * P.obs_lm[o];
+        const T b0 = (T)bl[0], b1 = (T)bl[1], b2 = (T)bl[2];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) acc[a] += (double)(w[a * 3] * b0 + w[a * 3 + 1] * b1 + w[a * 3 + 2] * b2);
+    }
+#pragma unroll 1
+    for (int a = 0; a < 6; ++a) {
+        const double v = block_sum(acc[a], sh);
+        if (threadIdx.x == 0) bs[6LL * k + a] = b[6LL * k + a] - v;
+    }
+}
+
+// delta_l = H_ll^-1 (b_l - H_lp delta_p); delta[0..n) already holds delta_p.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_backsub(DevProblem P, const T* __restrict__ hpl,
+                                                      const double* __restrict__ hinv, const double* __restrict__ b,
+                                                      double* delta, const LmState* st) {
+    if (!st->solve_ok) return;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= P.L) return;
+    const double* bl = b + P.n + 3LL * l;
+    double v0 = bl[0], v1 = bl[1], v2 = bl[2];
+    const int e = P.lm_ptr[l + 1];
+    for (int o = P.lm_ptr[l]; o < e; ++o) {
+        if (!P.blk_valid[o]) continue;
+        const T* h = hpl + (int64_t)o * 18;
+        const double* dp = delta + 6LL * P.obs_pose[o];
+        T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            const T d = (T)dp[a];
+            s0 += h[a * 3] * d;
+            s1 += h[a * 3 + 1] * d;
+            s2 += h[a * 3 + 2] * d;
+        }
+        v0 -= s0; v1 -= s1; v2 -= s2;
+    }
+    const double* I = hinv + (int64_t)l * 9;
+    double* dl = delta + P.n + 3LL * l;
+    dl[0] = I[0] * v0 + I[1] * v1 + I[2] * v2;
+    dl[1] = I[3] * v0 + I[4] * v1 + I[5] * v2;
+    dl[2] = I[6] * v0 + I[7] * v1 + I[8] * v2;
+}
+
+// Backup and apply the step to free vertices.
+__global__ void __launch_bounds__(kThreads) k_update(DevProblem P, const double* __restrict__ delta, const LmState* st) {
+    if (!st->solve_ok) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < P.K) {
+        double* p = P.pose + (int64_t)t * kPoseStride;
+        double* bk = P.pose_bk + (int64_t)t * kPoseStride;
+#pragma unroll
+        for (int i = 0; i < kPoseStride; ++i) bk[i] = p[i];
+        if (P.pose_fixed[t]) return;
+        double d[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) d[i] = delta[6LL * t + i];
+        pose_plus(p, d);
+    } else if (t < P.K + P.L) {
+        const int l = t - P.K;
+        double* x = P.lm + (int64_t)l * kLmStride;
+        double* bk = P.lm_bk + (int64_t)l * kLmStride;
+#pragma unroll
+        for (int i = 0; i < kLmStride; ++i) bk[i] = x[i];
+        if (P.lm_fixed[l]) return;
+        const double* d = delta + P.n + 3LL * l;
+        x[0] += d[0];
+        x[1] += d[1];
+        x[2] += d[2];
+    }
+}
+
+// A rejected step is rolled back only while lambda stays finite: the
+// reference breaks out before rollback_states() otherwise (source/factor_graph.hpp:592-604).
+__global__ void __launch_bounds__(kThreads) k_rollback(DevProblem P, const LmState* st) {
+    if (!st->solve_ok || st->good || !isfinite(st->lambda)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < P.K) {
+#pragma unroll
+        for (int i = 0; i < kPoseStride; ++i)
+            P.pose[(int64_t)t * kPoseStride + i] = P.pose_bk[(int64_t)t * kPoseStride + i];
+    } else if (t < P.K + P.L) {
+        const int l = t - P.K;
+#pragma unroll
+        for (int i = 0; i < kLmStride; ++i) P.lm[(int64_t)l * kLmStride + i] = P.lm_bk[(int64_t)l * kLmStride + i];
+    }
+}
+
+// Fixed-shape two-level sums: kReduceBlocks blocks stride over the items in
+// a fixed order, then one block adds the block results in a fixed tree.
+__global__ void __launch_bounds__(kThreads) k_scale_partial(DevProblem P, const double* __restrict__ delta,
+                                                            const double* __restrict__ b, double* red,
+                                                            const LmState* st) {
+    __shared__ double sh[kThreads];
+    if (!st->solve_ok) return;
+    const double lam = st->lambda;
+    const int64_t N = (int64_t)P.n + 3LL * P.L;
+    double v = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+        v += delta[i] * (lam * delta[i] + b[i]);
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) red[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_cost_partial(DevProblem P, double* red, const LmState* st,
+                                                           int only_if_ok) {
+    __shared__ double sh[kThreads];
+    if (only_if_ok && !st->solve_ok) return;
+    double v = 0.0;
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < P.M; o += (int64_t)gridDim.x * blockDim.x) {
+        const int pi = P.obs_pose[o], li = P.obs_lm[o];
+        const double* pp = P.pose + (int64_t)pi * kPoseStride;
+        const double* xp = P.lm + (int64_t)li * kLmStride;
+        double p[7], X[3];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) p[i] = pp[i];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) X[i] = xp[i];
+        const double2 uv = P.obs_uv[o];
+        double Xc[3], r[2];
+        residual(p, X, uv.x, uv.y, P.intr, Xc, r);
+        const double e2 = chi2_of(r, P.obs_info ? P.obs_info + 4 * o : nullptr);
+        if (P.loss.kind) {
+            double rho[3];
+            loss_rho(P.loss, e2, rho);
+            v += rho[0];
+        } else {
+            v += e2;
+        }
+    }
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) red[blockIdx.x] = v;
+}
+
+// target: 0 = chi2_new, 1 = scale (+1e-3)
+__global__ void __launch_bounds__(kThreads) k_finish_sum(const double* red, LmState* st, int target, int only_if_ok) {
+    __shared__ double sh[kThreads];
+    if (only_if_ok && !st->solve_ok) return;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < kReduceBlocks; i += kThreads) v += red[i];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        if (target == 0) st->chi2_new = v;
+        else st->scale = v + 1e-3;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_max_diag(DevProblem P, const double* __restrict__ hpp,
+                                                       const double* __restrict__ hll, double* red) {
+    __shared__ double sh[kThreads];
+    double m = 0.0;
+    const int64_t N = 6LL * P.K + 3LL * P.L;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double v;
+        if (i < 6LL * P.K) v = hpp[(i / 6) * 36 + (i % 6) * 7];
+        else {
+            const int64_t j = i - 6LL * P.K;
+            v = hll[(j / 3) * 9 + (j % 3) * 4];
+        }
+        m = fmax(fabs(v), m);
+    }
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) red[blockIdx.x] = sh[0];
+}
+
+__global__ void k_init_lambda(const double* red, LmState* st, double tau, double clamp) {
+    if (threadIdx.x != 0) return;
+    double m = 0.0;
+    for (int i = 0; i < kReduceBlocks; ++i) m = fmax(m, red[i]);
+    st->max_diag = m;
+    st->lambda = tau * fmin(clamp, m);
+    st->nu = 2.0;
+    st->chi2 = st->chi2_new;
+}
+
+// source/factor_graph.hpp:542-591
+__global__ void k_decide(LmState* st) {
+    if (threadIdx.x != 0) return;
+    if (!st->solve_ok) {
+        st->lambda *= st->nu;
+        st->nu *= 2.0;
+        st->good = 0;
+        return;
+    }
+    const double rho = (st->chi2 - st->chi2_new) / st->scale;
+    st->rho = rho;
+    if ((rho > 0) && isfinite(st->chi2_new)) {
+        double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
+        alpha = fmin(alpha, 2.0 / 3.0);
+        st->lambda *= fmax(1.0 / 3.0, alpha);
+        st->nu = 2.0;
+        st->chi2 = st->chi2_new;
+        st->good = 1;
+    } else {
+        st->lambda *= st->nu;
+        st->nu *= 2.0;
+        st->good = 0;
+    }
+}
+
+__global__ void k_set_solve_ok(LmState* st, int v) {
+    if (threadIdx.x == 0) st->solve_ok = v;
+}
+
+// ------------------------------------------------------------------ launchers
+
+long long& launch_counter() {
+    static long long count = 0;
+    return count;
+}
+
+template <typename T>
+void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
+    if (P.M > 0) {
+        k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part); note_launch();
+        if (P.has_dups) k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch();
+    }
+    if (P.L > 0) k_reduce_lm<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.lm_part, W.hll, W.b); note_launch();
+    if (P.K > 0) k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b); note_launch();
+}
+
+template <typename T>
+void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
+    if (P.L > 0) k_invert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, st); note_launch();
+    if (P.M > 0) k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch();
+}
+
+template <typename T>
+void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
+    const int64_t nn = (int64_t)P.n * P.n;
+    if (nn > 0) k_s_init<T><<<grid_for(nn), kThreads, 0, s>>>(P, W.hpp, (T*)W.S, st); note_launch();
+    if (P.nchunks > 0) {
+        k_schur_chunks<T><<<grid_for(P.nchunks), kThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial); note_launch();
+        k_schur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, (T*)W.S); note_launch();
+    }
+    if (P.K > 0) k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch();
+}
+
+template <typename T>
+void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
+    if (P.L > 0) k_backsub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st); note_launch();
+}
+
+void launch_update(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
+    k_update<<<grid_for((int64_t)P.K + P.L), kThreads, 0, s>>>(P, W.delta, st); note_launch();
+}
+
+void launch_rollback(const DevProblem& P, const LmState* st, cudaStream_t s) {
+    k_rollback<<<grid_for((int64_t)P.K + P.L), kThreads, 0, s>>>(P, st); note_launch();
+}
+
+void launch_scale(const DevProblem& P, DevWork& W, LmState* st, cudaStream_t s) {
+    k_scale_partial<<<kReduceBlocks, kThreads, 0, s>>>(P, W.delta, W.b, W.red, st); note_launch();
+    k_finish_sum<<<1, kThreads, 0, s>>>(W.red, st, 1, 1); note_launch();
+}
+
+void launch_cost(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, cudaStream_t s) {
+    k_cost_partial<<<kReduceBlocks, kThreads, 0, s>>>(P, W.red, st, only_if_ok ? 1 : 0); note_launch();
+    k_finish_sum<<<1, kThreads, 0, s>>>(W.red, st, 0, only_if_ok ? 1 : 0); note_launch();
+}
+
+void launch_init_lambda(const DevProblem& P, DevWork& W, LmState* st, double tau, double clamp, cudaStream_t s) {
+    k_max_diag<<<kReduceBlocks, kThreads, 0, s>>>(P, W.hpp, W.hll, W.red); note_launch();
+    k_init_lambda<<<1, 32, 0, s>>>(W.red, st, tau, clamp); note_launch();
+}
+
+void launch_decide(LmState* st, cudaStream_t s) { k_decide<<<1, 32, 0, s>>>(st); note_launch(); }
+
+void launch_set_solve_ok(LmState* st, int v, cudaStream_t s) { k_set_solve_ok<<<1, 32, 0, s>>>(st, v); note_launch(); }
+
+template void launch_linearize<double>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_linearize<float>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_invert_w<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_invert_w<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_schur<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_schur<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_backsub<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_backsub<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+
+}  // namespace zs
