@@ -74,7 +74,7 @@ typedef struct zs_ba_options {
     double relative_tolerance;  /* 1e-6: stop when the gain < tol * max(last, floor) */
     double chi2_floor;          /* 1e-12 */
     int32_t refine_iterations;  /* mixed form: FP64 refinement sweeps at most (8) */
-    double refine_tolerance;    /* mixed form: stop refining at ||b - S x|| <= tol ||b|| (1e-12) */
+    double refine_tolerance;    /* mixed form: stop refining at ||b - S x|| <= tol ||b|| (1e-10) */
     int32_t device;             /* CUDA device ordinal (0) */
     int32_t verbose;            /* 1: print [INIT]/[GOOD]/[ BAD] lines to stderr */
     int32_t profile;            /* 1: time each phase with CUDA events into zs_ba_report.ms_phase */
@@ -178,6 +178,10 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, 
 int zs_pipe_peaks(int device, double* fp64_tflops, double* fp32_tflops);
 
 const char* zs_ba_status_string(int status);
+
+/* The CUDA error behind the last ZS_ERR_CUDA / ZS_ERR_OUT_OF_MEMORY returned
+ * on this host thread ("" if none). */
+const char* zs_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -186,3 +186,35 @@ def test_empty_and_degenerate(zs_lib):
         bad.obs_pose[0] = 99
         with pytest.raises(ba.ZsError):
             ba_.set_problem(bad)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 64, 100, 257, 600, 1200])
+def test_dense_cholesky_sizes(zs_lib, n):
+    """Multi-panel factorisations, partial last blocks and every level of the
+    mixed form's recursive L^-1, against numpy on random SPD systems."""
+    from zeroslam_gb300 import ba
+
+    rng = np.random.default_rng(n)
+    G = rng.normal(size=(n, n))
+    A = G @ G.T / n + np.eye(n)
+    b = rng.normal(size=n)
+    ok, Lg, x = ba.dense_cholesky_solve(A, b)
+    assert ok
+    assert rel_err(Lg, np.linalg.cholesky(A)) < 1e-12
+    xr = np.linalg.solve(A, b)
+    assert rel_err(x, xr) < 1e-11
+    ok, _, xm = ba.dense_cholesky_solve(A, b, precision=ba.MIXED)
+    assert ok and rel_err(xm, xr) < 1e-10
+
+
+def test_dense_cholesky_rejects_indefinite(zs_lib):
+    from zeroslam_gb300 import ba
+
+    rng = np.random.default_rng(5)
+    n = 200
+    G = rng.normal(size=(n, n))
+    A = G @ G.T + np.eye(n)
+    A[150, 150] = -5.0  # a negative pivot deep in the factorisation
+    for prec in (ba.FP64, ba.MIXED):
+        ok, _, _ = ba.dense_cholesky_solve(A, rng.normal(size=n), precision=prec)
+        assert not ok

@@ -67,6 +67,10 @@ class ZsError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
         msg = _LIB.zs_ba_status_string(status).decode() if _LIB is not None else str(status)
+        if _LIB is not None and status in (ZS_ERR_CUDA, ZS_ERR_OUT_OF_MEMORY):
+            detail = _LIB.zs_last_error().decode()
+            if detail:
+                msg += f" [{detail}]"
         super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
 
 
@@ -74,7 +78,8 @@ _LIB = None
 
 ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
-                 "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string")
+                 "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
+                 "zs_last_error")
 
 
 def library_path() -> str:
@@ -118,6 +123,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_dense_cholesky_solve.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.c_int]
     lib.zs_ba_status_string.restype = C.c_char_p
     lib.zs_ba_status_string.argtypes = [C.c_int]
+    lib.zs_last_error.restype = C.c_char_p
+    lib.zs_last_error.argtypes = []
     _LIB = lib
     return lib
 

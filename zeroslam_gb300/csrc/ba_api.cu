@@ -156,7 +156,7 @@ void zs_ba_default_options(zs_ba_options* o) {
     o->relative_tolerance = 1e-6;
     o->chi2_floor = 1e-12;
     o->refine_iterations = 8;
-    o->refine_tolerance = 1e-12;
+    o->refine_tolerance = 1e-10;
     o->device = 0;
     o->verbose = 0;
 }
@@ -176,10 +176,15 @@ const char* zs_ba_status_string(int s) {
     }
 }
 
+static thread_local char g_last_error[256] = "";
+
 static int cuda_status(cudaError_t e) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
     cudaGetLastError();
     return e == cudaErrorMemoryAllocation ? ZS_ERR_OUT_OF_MEMORY : ZS_ERR_CUDA;
 }
+
+const char* zs_last_error(void) { return g_last_error; }
 
 int zs_ba_create(zs_ba_handle** out, const zs_ba_options* opt) {
     if (!out) return ZS_ERR_INVALID;
@@ -384,8 +389,10 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
     const size_t ts = (size_t)h->tsize;
     const int n = P.n;
     DevWork& W = h->W;
-    W.hpl = dalloc<char>(ts * 18 * M, own);
-    W.W = dalloc<char>(ts * 18 * M, own);
+    const size_t rs = h->tsize == 4 ? 20 : 18;  // padded H_pl / W record
+    W.hpl = dalloc<char>(ts * rs * M, own);
+    W.W = dalloc<char>(ts * rs * M, own);
+    W.pose_aux = dalloc<double>((size_t)K * 24, own);
     W.lm_part = dalloc<char>(ts * 9 * M, own);
     W.pose_part = dalloc<char>(ts * 27 * M, own);
     W.hpp = dalloc<double>((size_t)K * 36, own);
@@ -393,16 +400,20 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
     W.hll_inv = dalloc<double>((size_t)L * 9, own);
     W.b = dalloc<double>((size_t)n + 3 * (size_t)L, own);
     W.partial = dalloc<char>(ts * 36 * (size_t)P.nchunks, own);
-    W.S = dalloc<char>(ts * (size_t)n * n, own);
+    W.S = dalloc<double>((size_t)n * n, own);
     W.F = dalloc<char>(ts * (size_t)n * n, own);
     W.bs = dalloc<double>(n, own);
-    W.y = dalloc<double>(2 * (size_t)n, own);
-    W.r = dalloc<double>(2 * (size_t)n, own);
+    W.D = dalloc<char>(ts * 1024 * (size_t)((n + 31) / 32), own);
+    W.work = dalloc<double>(4 * (size_t)n + 256, own);
+    if (h->tsize == 4) {
+        W.X = dalloc<char>(ts * (size_t)n * n, own);
+        W.XT = dalloc<char>(ts * (size_t)n * n, own);
+    }
     W.delta = dalloc<double>((size_t)n + 3 * (size_t)L, own);
     W.red = dalloc<double>(kReduceBlocks * 4, own);
     W.ired = dalloc<int32_t>(kReduceBlocks, own);
     ZS_CUDA(cudaMemsetAsync(W.hll_inv, 0, sizeof(double) * 9 * (size_t)std::max(L, 1), s));
-    ZS_CUDA(cudaMemsetAsync(W.delta, 0, sizeof(double) * ((size_t)n + 3 * (size_t)L + 1), s));
+    ZS_CUDA(cudaMemsetAsync(W.delta, 0, sizeof(double) * std::max<size_t>(1, (size_t)n + 3 * (size_t)L), s));
     ZS_CUDA(cudaStreamSynchronize(s));
     ZS_CUDA(cudaGetLastError());
 }
@@ -522,12 +533,21 @@ void system_solve(zs_ba_handle* h) {
     }
     {
         PhaseScope ps(h->timer, ZS_PHASE_FACTOR, s);
-        launch_factor<T, T>(P.n, (const T*)W.S, (T*)W.F, h->st, s);
+        ZS_CUDA((launch_factor<double, T>(P.n, W.S, (T*)W.F, (T*)W.D, h->st, s)));
     }
     {
         PhaseScope ps(h->timer, ZS_PHASE_TRISOLVE, s);
-        const int refine = (sizeof(T) == 4) ? std::max(0, h->opt.refine_iterations) : 0;
-        launch_solve_refine<T, T>(P.n, (const T*)W.S, (const T*)W.F, W.bs, W.delta, W.y, W.r, h->st, refine, s);
+        if (sizeof(T) == 4) {
+            // mixed form: explicit L^-1, then FP64 refinement by GEMVs
+            ZS_CUDA((launch_tri_inverse<float>(P.n, (const float*)W.F, (const float*)W.D, (float*)W.X,
+                                               (float*)W.XT, h->st, s)));
+            ZS_CUDA((launch_refine<double, float>(P.n, W.S, (const float*)W.X, (const float*)W.XT, W.bs, W.delta,
+                                                  W.work, h->st, std::max(0, h->opt.refine_iterations),
+                                                  h->opt.refine_tolerance, s)));
+        } else {
+            ZS_CUDA((launch_solve_refine<double, double>(P.n, W.S, (const double*)W.F, (const double*)W.D, W.bs,
+                                                         W.delta, W.work, h->st, 0, 0.0, s)));
+        }
     }
     PhaseScope ps(h->timer, ZS_PHASE_UPDATE, s);
     launch_backsub<T>(P, W, h->st, s);
@@ -588,7 +608,7 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
                 if (!std::isfinite(lambda)) break;
                 continue;
             }
-            if (sizeof(T) == 4) r.refine_sweeps += o.refine_iterations;
+            if (sizeof(T) == 4) r.refine_sweeps += hs.refine_sweeps;
             if (hs.good) {
                 chi2 = hs.chi2;
                 ++success;
@@ -646,12 +666,7 @@ int linear_step_impl(zs_ba_handle* h, double lambda, double* S, double* bs, doub
     read_state(h);
     const int n = P.n;
     const size_t nall = (size_t)n + 3 * (size_t)P.L;
-    if (S && n > 0) {
-        std::vector<T> tmp((size_t)n * n);
-        ZS_CUDA(cudaMemcpyAsync(tmp.data(), W.S, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, s));
-        ZS_CUDA(cudaStreamSynchronize(s));
-        for (size_t i = 0; i < tmp.size(); ++i) S[i] = (double)tmp[i];
-    }
+    if (S && n > 0) ZS_CUDA(cudaMemcpyAsync(S, W.S, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (bs && n > 0) ZS_CUDA(cudaMemcpyAsync(bs, W.bs, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (delta && nall > 0) ZS_CUDA(cudaMemcpyAsync(delta, W.delta, nall * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (b && nall > 0) ZS_CUDA(cudaMemcpyAsync(b, W.b, nall * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -747,8 +762,7 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
         double* dA = dalloc<double>(nn, owned);
         double* db = dalloc<double>(n, owned);
         double* dx = dalloc<double>(n, owned);
-        double* dy = dalloc<double>(2 * (size_t)n, owned);
-        double* dr = dalloc<double>(2 * (size_t)n, owned);
+        double* dwork = dalloc<double>(4 * (size_t)n + 256, owned);
         LmState* st = dalloc<LmState>(1, owned);
         LmState init{};
         init.solve_ok = 1;
@@ -758,14 +772,20 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
         std::vector<double> Lh;
         if (precision == ZS_PRECISION_FP64) {
             double* dF = dalloc<double>(nn, owned);
-            launch_reduced_solve<double, double>(n, dA, dF, db, dx, dy, dr, st, 0, s);
+            double* dD = dalloc<double>(1024 * (size_t)((n + 31) / 32), owned);
+            ZS_CUDA((launch_reduced_solve<double, double>(n, dA, dF, dD, db, dx, dwork, st, 0, 0.0, s)));
             if (Lout) {
                 Lh.resize(nn);
                 ZS_CUDA(cudaMemcpyAsync(Lh.data(), dF, nn * sizeof(double), cudaMemcpyDeviceToHost, s));
             }
         } else {
             float* dF = dalloc<float>(nn, owned);
-            launch_reduced_solve<double, float>(n, dA, dF, db, dx, dy, dr, st, 8, s);
+            float* dD = dalloc<float>(1024 * (size_t)((n + 31) / 32), owned);
+            float* dX = dalloc<float>(nn, owned);
+            float* dXT = dalloc<float>(nn, owned);
+            ZS_CUDA((launch_factor<double, float>(n, dA, dF, dD, st, s)));
+            ZS_CUDA((launch_tri_inverse<float>(n, dF, dD, dX, dXT, st, s)));
+            ZS_CUDA((launch_refine<double, float>(n, dA, dX, dXT, db, dx, dwork, st, 10, 1e-14, s)));
             if (Lout) {
                 std::vector<float> tmp(nn);
                 ZS_CUDA(cudaMemcpyAsync(tmp.data(), dF, nn * sizeof(float), cudaMemcpyDeviceToHost, s));

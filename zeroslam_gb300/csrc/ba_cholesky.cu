@@ -1,18 +1,38 @@
 // Dense reduced-camera-system solve S x = b_s on the device (sm_103a).
 //
-// Blocked right-looking Cholesky S = L L^T on the row-major lower triangle:
-// per 32-wide panel, one CTA factors the diagonal block (k_chol_diag), the
-// panel below is solved against it (k_chol_trsm) and the trailing lower
-// triangle is updated (k_chol_syrk). The pivot and solve tests are zeroslam's
-// (source/matrix_decomposition_cholesky.hpp:40,53 and :74,80,89): a pivot
-// must exceed 1e-14 * max|S_ii| and every |L_ii| must exceed
-// 1e-7 * max|L_ii|. The triangular solves run block by block. The mixed form
-// factors in FP32 and refines x in FP64 against S.
+// Factorisation: one cooperative persistent kernel over every SM performs a
+// blocked right-looking Cholesky S = L L^T on the row-major lower triangle,
+// 32-wide panels, two grid barriers per panel:
+//   phase B  L_ik = A_ik D_k^T for the rows below the panel (D_k = L_kk^-1),
+//   phase C  A_ij -= L_ik L_jk^T over the trailing lower 32 x 32 tiles; the
+//            CTA that updates the next diagonal tile first factors it and
+//            inverts its factor (look-ahead), so the next panel can start.
+// Triangular solves: one thread-block cluster (16 CTAs, or 8 where 16 is not
+// allowed) walks the 32-row blocks with cluster barriers, each block step a
+// small GEMV with D_k; the mixed form's FP64 refinement sweeps
+// x += (L L^T)^-1 (b - S x) run inside the same launch and stop once the
+// residual has converged.
+//
+// The pivot and solve tests are zeroslam's (gpdaniels/zeroslam
+// source/matrix_decomposition_cholesky.hpp:40,53 and :74,80,89): a pivot must
+// exceed 1e-14 * max|S_ii| and every |L_ii| must exceed 1e-7 * max|L_ii|.
+#include <cooperative_groups.h>
+
 #include "ba_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace zs {
 
 constexpr int kNB = 32;
+
+// Loads of data that another CTA of the same launch wrote (persistent and
+// cluster kernels) go through L2, never a possibly stale L1 line.
+template <typename T>
+__device__ __forceinline__ T ldg2(const T* p) {
+    return __ldcg(p);
+}
+__device__ __forceinline__ int ld_ok(const LmState* st) { return __ldcg(&st->solve_ok); }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_diag_max(int n, const T* __restrict__ A, LmState* st, double factor,
@@ -27,246 +47,8 @@ __global__ void __launch_bounds__(kThreads) k_diag_max(int n, const T* __restric
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        if (which == 0) {
-            st->eps_factor = sh[0] * factor;
-        } else {
-            st->eps_solve = sh[0] * factor;
-        }
-    }
-}
-
-// Every |L_ii| must exceed eps_solve.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_check_solve_eps(int n, const T* __restrict__ F, LmState* st) {
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    if (!st->solve_ok) return;
-    const double eps = st->eps_solve;
-    for (int i = threadIdx.x; i < n; i += kThreads)
-        if (!(fabs((double)F[(int64_t)i * n + i]) > eps)) bad = 1;
-    __syncthreads();
-    if (threadIdx.x == 0 && bad) st->solve_ok = 0;
-}
-
-// Unblocked right-looking factor of the b x b diagonal block at j0.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_chol_diag(int n, T* F, int j0, LmState* st) {
-    __shared__ T a[kNB][kNB + 1];
-    __shared__ int fail;
-    if (!st->solve_ok) return;
-    const int b = min(kNB, n - j0);
-    const double eps = st->eps_factor;
-    for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
-        const int i = e / b, m = e % b;
-        a[i][m] = F[(int64_t)(j0 + i) * n + j0 + m];
-    }
-    if (threadIdx.x == 0) fail = 0;
-    __syncthreads();
-    for (int k = 0; k < b; ++k) {
-        if (threadIdx.x == 0) {
-            const T v = a[k][k];
-            if (!((double)v > eps)) fail = 1;
-            else a[k][k] = sqrt(v);
-        }
-        __syncthreads();
-        if (fail) break;
-        for (int i = k + 1 + threadIdx.x; i < b; i += blockDim.x) a[i][k] = a[i][k] / a[k][k];
-        __syncthreads();
-        const int rem = b - k - 1;
-        for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
-            const int i = k + 1 + e / rem, m = k + 1 + e % rem;
-            if (m <= i) a[i][m] = a[i][m] - a[i][k] * a[m][k];
-        }
-        __syncthreads();
-    }
-    if (fail) {
-        if (threadIdx.x == 0) st->solve_ok = 0;
-        return;
-    }
-    for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
-        const int i = e / b, m = e % b;
-        F[(int64_t)(j0 + i) * n + j0 + m] = (m <= i) ? a[i][m] : T(0);
-    }
-}
-
-// L21 = A21 L11^-T, one thread per row below the panel.
-template <typename T>
-__global__ void __launch_bounds__(64) k_chol_trsm(int n, T* F, int j0, const LmState* st) {
-    __shared__ T l11[kNB][kNB + 1];
-    if (!st->solve_ok) return;
-    const int b = min(kNB, n - j0);
-    for (int e = threadIdx.x; e < b * b; e += blockDim.x) l11[e / b][e % b] = F[(int64_t)(j0 + e / b) * n + j0 + e % b];
-    __syncthreads();
-    const int i = j0 + b + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    T x[kNB];
-    T* row = F + (int64_t)i * n + j0;
-#pragma unroll
-    for (int k = 0; k < kNB; ++k) {
-        if (k < b) {
-            T v = row[k];
-            for (int m = 0; m < k; ++m) v -= x[m] * l11[k][m];
-            x[k] = v / l11[k][k];
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kNB; ++k)
-        if (k < b) row[k] = x[k];
-}
-
-// Trailing lower-triangle update A22 -= L21 L21^T over 32 x 32 tiles.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_chol_syrk(int n, T* F, int j0, const LmState* st) {
-    __shared__ T pa[32][kNB + 1];
-    __shared__ T pm[32][kNB + 1];
-    if (!st->solve_ok) return;
-    const int b = min(kNB, n - j0);
-    const int c0 = j0 + b;
-    // blockIdx.x -> (ti, tm), tm <= ti
-    const int t = blockIdx.x;
-    int ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
-    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-    while (ti * (ti + 1) / 2 > t) --ti;
-    const int tm = t - ti * (ti + 1) / 2;
-    const int r0 = c0 + ti * 32, m0 = c0 + tm * 32;
-    for (int e = threadIdx.x; e < 32 * kNB; e += blockDim.x) {
-        const int r = e / kNB, k = e % kNB;
-        const bool ok = k < b;
-        pa[r][k] = (ok && r0 + r < n) ? F[(int64_t)(r0 + r) * n + j0 + k] : T(0);
-        pm[r][k] = (ok && m0 + r < n) ? F[(int64_t)(m0 + r) * n + j0 + k] : T(0);
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
-        const int r = e / 32, c = e % 32;
-        const int row = r0 + r, col = m0 + c;
-        if (row >= n || col >= n || col > row) continue;
-        T acc = T(0);
-#pragma unroll 8
-        for (int k = 0; k < kNB; ++k) acc += pa[r][k] * pm[c][k];
-        F[(int64_t)row * n + col] -= acc;
-    }
-}
-
-__device__ inline double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Forward block step: solve L_JJ y_J = w_J (J = [j0, j0+b)), write y_J (block
-// 0 only), and update w_i -= L_iJ y_J for the rows below, a warp per row.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_trsv_fwd(int n, const T* __restrict__ F, int j0, double* w, double* y,
-                                                       const LmState* st) {
-    __shared__ double xs[kNB];
-    if (!st->solve_ok) return;
-    const int b = min(kNB, n - j0);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        double xv = 0.0;
-        for (int k = 0; k < b; ++k) {
-            double part = (lane < k) ? (double)F[(int64_t)(j0 + k) * n + j0 + lane] * xv : 0.0;
-            part = warp_sum(part);
-            const double v = (w[j0 + k] - part) / (double)F[(int64_t)(j0 + k) * n + j0 + k];
-            if (lane == k) xv = v;
-        }
-        if (lane < b) xs[lane] = xv;
-    }
-    __syncthreads();
-    if (blockIdx.x == 0)
-        for (int k = threadIdx.x; k < b; k += blockDim.x) y[j0 + k] = xs[k];
-    const int i = j0 + b + blockIdx.x * (kThreads / 32) + warp;
-    if (i >= n) return;
-    double part = (lane < b) ? (double)F[(int64_t)i * n + j0 + lane] * xs[lane] : 0.0;
-    part = warp_sum(part);
-    if (lane == 0) w[i] -= part;
-}
-
-// Backward block step: solve L_JJ^T x_J = z_J, write x_J (block 0 only), and
-// update z_i -= sum_m L_{j0+m, i} x_m for i < j0, a thread per i.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_trsv_bwd(int n, const T* __restrict__ F, int j0, double* z, double* x,
-                                                       const LmState* st) {
-    __shared__ double xs[kNB];
-    if (!st->solve_ok) return;
-    const int b = min(kNB, n - j0);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        double xv = 0.0;
-        for (int k = b - 1; k >= 0; --k) {
-            double part = (lane > k && lane < b) ? (double)F[(int64_t)(j0 + lane) * n + j0 + k] * xv : 0.0;
-            part = warp_sum(part);
-            const double v = (z[j0 + k] - part) / (double)F[(int64_t)(j0 + k) * n + j0 + k];
-            if (lane == k) xv = v;
-        }
-        if (lane < b) xs[lane] = xv;
-    }
-    __syncthreads();
-    if (blockIdx.x == 0)
-        for (int k = threadIdx.x; k < b; k += blockDim.x) x[j0 + k] = xs[k];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= j0) return;
-    double acc = 0.0;
-    for (int m = 0; m < b; ++m) acc += (double)F[(int64_t)(j0 + m) * n + i] * xs[m];
-    z[i] -= acc;
-}
-
-// r = bs - S x (FP64 accumulation), a warp per row; also |r|^2 and |bs|^2
-// partial sums per block for the report.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_residual(int n, const T* __restrict__ S, const double* __restrict__ x,
-                                                       const double* __restrict__ bs, double* r, const LmState* st) {
-    if (!st->solve_ok) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i = blockIdx.x * (kThreads / 32) + warp;
-    if (i >= n) return;
-    double acc = 0.0;
-    for (int c = lane; c < n; c += 32) acc += (double)S[(int64_t)i * n + c] * x[c];
-    acc = warp_sum(acc);
-    if (lane == 0) r[i] = bs[i] - acc;
-}
-
-__global__ void __launch_bounds__(kThreads) k_axpy_copy(int n, const double* __restrict__ a, double* __restrict__ x,
-                                                        int accumulate, const LmState* st) {
-    if (!st->solve_ok) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    x[i] = accumulate ? x[i] + a[i] : a[i];
-}
-
-__global__ void __launch_bounds__(kThreads) k_norms(int n, const double* __restrict__ r, const double* __restrict__ b,
-                                                    LmState* st) {
-    __shared__ double sh[kThreads];
-    double a = 0.0, c = 0.0;
-    for (int i = threadIdx.x; i < n; i += kThreads) {
-        a += r[i] * r[i];
-        c += b[i] * b[i];
-    }
-    a = block_sum(a, sh);
-    c = block_sum(c, sh);
-    if (threadIdx.x == 0) {
-        st->resid_norm = sqrt(a);
-        st->rhs_norm = sqrt(c);
-    }
-}
-
-// x = L^-T L^-1 rhs using scratch w (forward work), y (forward result).
-template <typename T>
-static void tri_solve(int n, const T* F, const double* rhs, double* w, double* y, double* x, const LmState* st,
-                      cudaStream_t s) {
-    k_axpy_copy<<<grid_for(n), kThreads, 0, s>>>(n, rhs, w, 0, st); note_launch();
-    for (int j0 = 0; j0 < n; j0 += kNB) {
-        const int rows = n - j0 - min(kNB, n - j0);
-        const int g = rows > 0 ? (rows + kThreads / 32 - 1) / (kThreads / 32) : 1;
-        k_trsv_fwd<T><<<g, kThreads, 0, s>>>(n, F, j0, w, y, st); note_launch();
-    }
-    // backward: z starts as y (reuse w as z)
-    k_axpy_copy<<<grid_for(n), kThreads, 0, s>>>(n, y, w, 0, st); note_launch();
-    const int last = ((n - 1) / kNB) * kNB;
-    for (int j0 = last; j0 >= 0; j0 -= kNB) {
-        const int g = j0 > 0 ? grid_for(j0) : 1;
-        k_trsv_bwd<T><<<g, kThreads, 0, s>>>(n, F, j0, w, x, st); note_launch();
+        if (which == 0) st->eps_factor = sh[0] * factor;
+        else st->eps_solve = sh[0] * factor;
     }
 }
 
@@ -276,67 +58,494 @@ __global__ void __launch_bounds__(kThreads) k_convert(int64_t N, const TS* __res
     if (i < N) dst[i] = (TF)src[i];
 }
 
+// The CTA factors the b x b diagonal block at j0 (b <= 32) in shared memory,
+// right-looking, two barriers per column; pivots go to dg[] and the
+// multipliers are formed with one reciprocal per column. Writes L_jj (zero
+// above the diagonal) into F. Returns false, uniformly across the CTA, when a
+// pivot fails zeroslam's test (the block is then left unwritten).
+template <typename T>
+__device__ bool factor_diag(int n, T* F, int j0, double eps, T (*a)[kNB + 1], T* dg) {
+    const int b = min(kNB, n - j0);
+    T v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int i = e >> 5, m = e & 31;
+        v[q] = (i < b && m < b) ? ldg2(F + (int64_t)(j0 + i) * n + j0 + m) : (i == m ? T(1) : T(0));
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        a[e >> 5][e & 31] = v[q];
+    }
+    __syncthreads();
+    bool ok = true;
+    for (int k = 0; k < b; ++k) {
+        const T akk = a[k][k];
+        if (!((double)akk > eps)) {
+            ok = false;
+            break;
+        }
+        const T piv = sqrt(akk);
+        const T inv = T(1) / piv;
+        if (threadIdx.x > k && threadIdx.x < b) a[threadIdx.x][k] *= inv;
+        if (threadIdx.x == 0) dg[k] = piv;
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * kThreads;
+            const int i = e >> 5, m = e & 31;
+            if (m > k && m <= i && i < b) a[i][m] -= a[i][k] * a[m][k];
+        }
+        __syncthreads();
+    }
+    if (!ok) return false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int i = e >> 5, m = e & 31;
+        if (i < b && m < b) F[(int64_t)(j0 + i) * n + j0 + m] = (m < i) ? a[i][m] : (m == i ? dg[i] : T(0));
+    }
+    __syncthreads();
+    return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1) k_chol_coop(int n, T* F, LmState* st) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ T sa[kNB][kNB + 1];
+    __shared__ T sb[kNB][kNB + 1];
+    __shared__ T dg[kNB];
+    const int nblk = (n + kNB - 1) / kNB;
+    const double eps = ldg2(&st->eps_factor);
+    const int G = gridDim.x;
+    if (blockIdx.x == 0) {
+        if (!factor_diag<T>(n, F, 0, eps, sa, dg) && threadIdx.x == 0) st->solve_ok = 0;
+    }
+    grid.sync();
+    for (int k = 0; k < nblk; ++k) {
+        if (!ld_ok(st)) return;  // read after a grid barrier: every CTA sees the same value
+        const int k0 = k * kNB;
+        const int kb = min(kNB, n - k0);
+        const int r0 = k0 + kb;
+        if (r0 >= n) break;
+        // Phase B: rows below the panel solve x L_kk^T = a by substitution
+        // (a thread per row) against L_kk in shared memory.
+        {
+            T v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * kThreads;
+                const int i = e >> 5, m = e & 31;
+                v[q] = (i < kb && m < kb) ? ldg2(F + (int64_t)(k0 + i) * n + k0 + m) : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * kThreads;
+                sb[e >> 5][e & 31] = v[q];
+            }
+            __syncthreads();
+            if (threadIdx.x < kNB) dg[threadIdx.x] = threadIdx.x < kb ? T(1) / sb[threadIdx.x][threadIdx.x] : T(0);
+            __syncthreads();
+            const int rows = n - r0;
+            const int per = (rows + G - 1) / G;
+            const int rbeg = r0 + blockIdx.x * per, rend = min(n, rbeg + per);
+            for (int row = rbeg + threadIdx.x; row < rend; row += blockDim.x) {
+                T x[kNB];
+                T* rp = F + (int64_t)row * n + k0;
+#pragma unroll
+                for (int c = 0; c < kNB; ++c) x[c] = (c < kb) ? ldg2(rp + c) : T(0);
+#pragma unroll
+                for (int c = 0; c < kNB; ++c) {
+                    T acc = x[c];
+#pragma unroll
+                    for (int m = 0; m < c; ++m) acc -= x[m] * sb[c][m];
+                    x[c] = acc * dg[c];
+                }
+#pragma unroll
+                for (int c = 0; c < kNB; ++c)
+                    if (c < kb) rp[c] = x[c];
+            }
+        }
+        grid.sync();
+        // Phase C: trailing tiles (ti, tj), tj <= ti, relative to block k+1.
+        // CTA 0 updates only tile 0, the next diagonal block, and factors it
+        // (look-ahead); the other CTAs share the remaining tiles.
+        const int tn = nblk - k - 1;
+        const int ntiles = tn * (tn + 1) / 2;
+        const int first = (G == 1) ? 0 : (blockIdx.x == 0 ? 0 : blockIdx.x);
+        const int stride = (G == 1) ? 1 : (blockIdx.x == 0 ? ntiles : G - 1);
+        for (int t = first; t < ntiles; t += stride) {
+            int ti = 0;
+            while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+            const int tj = t - ti * (ti + 1) / 2;
+            const int i0 = r0 + ti * kNB, j0 = r0 + tj * kNB;
+            const int r = threadIdx.x / 8, c4 = (threadIdx.x % 8) * 4;
+            T va[4], vb[4], vf[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * kThreads;
+                const int rr = e >> 5, m = e & 31;
+                va[q] = (i0 + rr < n && m < kb) ? ldg2(F + (int64_t)(i0 + rr) * n + k0 + m) : T(0);
+                vb[q] = (j0 + rr < n && m < kb) ? ldg2(F + (int64_t)(j0 + rr) * n + k0 + m) : T(0);
+            }
+            const int row = i0 + r;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int col = j0 + c4 + q;
+                vf[q] = (row < n && col < n) ? ldg2(F + (int64_t)row * n + col) : T(0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * kThreads;
+                sa[e >> 5][e & 31] = va[q];
+                sb[e >> 5][e & 31] = vb[q];
+            }
+            __syncthreads();
+            T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
+#pragma unroll 8
+            for (int m = 0; m < kNB; ++m) {
+                const T av = sa[r][m];
+                acc0 += av * sb[c4][m];
+                acc1 += av * sb[c4 + 1][m];
+                acc2 += av * sb[c4 + 2][m];
+                acc3 += av * sb[c4 + 3][m];
+            }
+            const T accs[4] = {acc0, acc1, acc2, acc3};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int col = j0 + c4 + q;
+                if (row < n && col < n && (ti != tj || col <= row)) F[(int64_t)row * n + col] = vf[q] - accs[q];
+            }
+            __syncthreads();
+            if (t == 0) {
+                if (!factor_diag<T>(n, F, r0, eps, sa, dg) && threadIdx.x == 0) st->solve_ok = 0;
+            }
+        }
+        grid.sync();
+    }
+}
+
+// D_k = L_kk^-1 for every 32 x 32 diagonal block, a CTA per block:
+// X = I, then per column k  X[k,:] /= L_kk and X[i,:] -= L_ik X[k,:] (i > k).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_diag_inverses(int n, const T* __restrict__ F, T* D,
+                                                            const LmState* st) {
+    __shared__ T l[kNB][kNB + 1];
+    __shared__ T x[kNB][kNB + 1];
+    if (!st->solve_ok) return;
+    const int k0 = blockIdx.x * kNB, b = min(kNB, n - k0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int i = e >> 5, m = e & 31;
+        l[i][m] = (i < b && m < b) ? F[(int64_t)(k0 + i) * n + k0 + m] : (i == m ? T(1) : T(0));
+        x[i][m] = (i == m) ? T(1) : T(0);
+    }
+    __syncthreads();
+    for (int k = 0; k < kNB; ++k) {
+        const T inv = T(1) / l[k][k];
+        if (threadIdx.x < kNB) x[k][threadIdx.x] *= inv;
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * kThreads;
+            const int i = e >> 5, c = e & 31;
+            if (i > k) x[i][c] -= l[i][k] * x[k][c];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int i = e >> 5, c = e & 31;
+        D[(int64_t)blockIdx.x * kNB * kNB + e] = (i < b && c < b) ? x[i][c] : T(0);
+    }
+}
+
+// Every |L_ii| must exceed 1e-7 max |L_ii|.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_check_solve_eps(int n, const T* __restrict__ F, LmState* st) {
+    __shared__ double sh[kThreads];
+    __shared__ int bad;
+    if (!st->solve_ok) return;
+    double m = 0.0;
+    for (int i = threadIdx.x; i < n; i += kThreads) m = fmax(m, fabs((double)F[(int64_t)i * n + i]));
+    sh[threadIdx.x] = m;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double eps = sh[0] * 1e-7;
+    for (int i = threadIdx.x; i < n; i += kThreads)
+        if (!(fabs((double)F[(int64_t)i * n + i]) > eps)) bad = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->eps_solve = eps;
+        if (bad) st->solve_ok = 0;
+    }
+}
+
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Cluster-wide deterministic sum: each CTA publishes its partial in global
+// scratch, then every CTA adds them in rank order.
+__device__ inline double cluster_sum(cg::cluster_group& cl, double v, double* scratch) {
+    if (threadIdx.x == 0) scratch[cl.block_rank()] = v;
+    cl.sync();
+    double s = 0.0;
+    for (unsigned r = 0; r < cl.num_blocks(); ++r) s += ldg2(scratch + r);
+    cl.sync();
+    return s;
+}
+
+// Stages D_k (32 x 32, as double) and the kb entries of w_k in shared memory
+// with independent loads (w_k may come from another CTA of the cluster).
+template <typename T>
+__device__ void stage_block(const T* Dk, const double* wk, int kb, double (*ds)[kNB + 1], double* ws) {
+    T v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = Dk[threadIdx.x + q * kThreads];
+    const double wv = (threadIdx.x < kb) ? ldg2(wk + threadIdx.x) : 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        ds[e >> 5][e & 31] = (double)v[q];
+    }
+    if (threadIdx.x < kNB) ws[threadIdx.x] = wv;
+    __syncthreads();
+}
+
+// x = (L L^T)^-1 rhs by blocked forward and backward substitution; w is the
+// running right-hand side, y the forward result. Block b (32 rows) belongs to
+// cluster CTA b % C. Ends with a cluster barrier.
+template <typename T>
+__device__ void cluster_trisolve(cg::cluster_group& cl, int n, const T* __restrict__ F, const T* __restrict__ D,
+                                 const double* rhs, double* w, double* y, double* x, double* xs,
+                                 double (*ds)[kNB + 1], double* ws) {
+    const unsigned C = cl.num_blocks(), me = cl.block_rank();
+    const int nblk = (n + kNB - 1) / kNB;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if ((unsigned)((i / kNB) % C) == me) w[i] = rhs[i];
+    cl.sync();
+    for (int k = 0; k < nblk; ++k) {
+        const int k0 = k * kNB, kb = min(kNB, n - k0);
+        // y_k = D_k w_k (every CTA, redundantly; w_k and D_k staged in shared memory)
+        stage_block<T>(D + (int64_t)k * kNB * kNB, w + k0, kb, ds, ws);
+        if (threadIdx.x < kNB) {
+            const int c = threadIdx.x;
+            double v = 0.0;
+#pragma unroll 8
+            for (int m = 0; m < kNB; ++m) v += (m <= c) ? ds[c][m] * ws[m] : 0.0;
+            xs[c] = (c < kb) ? v : 0.0;
+        }
+        __syncthreads();
+        if ((unsigned)(k % C) == me)
+            for (int c = threadIdx.x; c < kb; c += blockDim.x) y[k0 + c] = xs[c];
+        // w_i -= L_i,k y_k for the rows of later blocks this CTA owns, a warp per row
+        for (int b = k + 1; b < nblk; ++b) {
+            if ((unsigned)(b % C) != me) continue;
+            const int b0 = b * kNB, bb = min(kNB, n - b0);
+            for (int r = warp; r < bb; r += nw) {
+                const int i = b0 + r;
+                double part = (lane < kb) ? (double)F[(int64_t)i * n + k0 + lane] * xs[lane] : 0.0;
+                part = warp_sum(part);
+                if (lane == 0) w[i] -= part;
+            }
+        }
+        cl.sync();
+    }
+    // backward: w = y, then x_k = D_k^T w_k and w_i -= sum_m L_{k0+m, i} x_m for i < k0
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if ((unsigned)((i / kNB) % C) == me) w[i] = y[i];
+    cl.sync();
+    for (int k = nblk - 1; k >= 0; --k) {
+        const int k0 = k * kNB, kb = min(kNB, n - k0);
+        stage_block<T>(D + (int64_t)k * kNB * kNB, w + k0, kb, ds, ws);
+        if (threadIdx.x < kNB) {
+            const int c = threadIdx.x;
+            double v = 0.0;
+#pragma unroll 8
+            for (int m = 0; m < kNB; ++m) v += (m >= c) ? ds[m][c] * ws[m] : 0.0;
+            xs[c] = (c < kb) ? v : 0.0;
+        }
+        __syncthreads();
+        if ((unsigned)(k % C) == me)
+            for (int c = threadIdx.x; c < kb; c += blockDim.x) x[k0 + c] = xs[c];
+        for (int b = 0; b < k; ++b) {
+            if ((unsigned)(b % C) != me) continue;
+            const int b0 = b * kNB;
+            for (int r = threadIdx.x; r < kNB; r += blockDim.x) {
+                const int i = b0 + r;
+                double acc = 0.0;
+                for (int m = 0; m < kb; ++m) acc += (double)F[(int64_t)(k0 + m) * n + i] * xs[m];
+                w[i] -= acc;
+            }
+        }
+        cl.sync();
+    }
+}
+
+// Solve, then (refine > 0) FP64 refinement sweeps against S until
+// ||bs - S x|| <= tol ||bs||. Vectors w, y, d, r: n doubles each; scratch
+// holds at least 16 doubles for the cluster sums.
 template <typename TS, typename TF>
-void launch_factor(int n, const TS* S, TF* F, LmState* st, cudaStream_t s) {
-    if (n <= 0) return;
+__global__ void __launch_bounds__(kThreads) k_solve_cluster(int n, const TS* __restrict__ S, const TF* __restrict__ F,
+                                                            const TF* __restrict__ D, const double* __restrict__ bs,
+                                                            double* x, double* w, double* y, double* d, double* r,
+                                                            double* scratch, int refine, double tol, LmState* st) {
+    __shared__ double xs[kNB];
+    __shared__ double red[kThreads];
+    __shared__ double ds[kNB][kNB + 1];
+    __shared__ double ws[kNB];
+    cg::cluster_group cl = cg::this_cluster();
+    if (!ld_ok(st)) return;  // uniform across the cluster
+    const unsigned C = cl.num_blocks(), me = cl.block_rank();
+    cluster_trisolve<TF>(cl, n, F, D, bs, w, y, x, xs, ds, ws);
+    if (refine <= 0) return;
+    double bb = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if ((unsigned)((i / kNB) % C) == me) bb += bs[i] * bs[i];
+    bb = block_sum(bb, red);
+    const double bnorm2 = cluster_sum(cl, bb, scratch);
+    int sweeps = 0;
+    double rn2 = 0.0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int it = 0; it <= refine; ++it) {
+        // r = bs - S x for this CTA's rows, a warp per row
+        double part2 = 0.0;
+        for (int blk = (int)me; blk * kNB < n; blk += (int)C) {
+            const int b0 = blk * kNB, bnum = min(kNB, n - b0);
+            for (int rr = warp; rr < bnum; rr += nw) {
+                const int i = b0 + rr;
+                double acc = 0.0;
+                for (int c = lane; c < n; c += 32) acc += (double)S[(int64_t)i * n + c] * ldg2(x + c);
+                acc = warp_sum(acc);
+                const double ri = bs[i] - acc;
+                if (lane == 0) {
+                    r[i] = ri;
+                    part2 += ri * ri;
+                }
+            }
+        }
+        part2 = block_sum(part2, red);
+        rn2 = cluster_sum(cl, part2, scratch);
+        if (it == refine || !(rn2 > tol * tol * bnorm2)) break;
+        cluster_trisolve<TF>(cl, n, F, D, r, w, y, d, xs, ds, ws);
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            if ((unsigned)((i / kNB) % C) == me) x[i] += d[i];
+        cl.sync();
+        ++sweeps;
+    }
+    if (me == 0 && threadIdx.x == 0) {
+        st->resid_norm = sqrt(rn2);
+        st->rhs_norm = sqrt(bnorm2);
+        st->refine_sweeps = sweeps;
+    }
+}
+
+template <typename TS, typename TF>
+static int cluster_size() {
+    static int cached = 0;
+    if (cached) return cached;
+    int c = 8;
+    if (cudaFuncSetAttribute(k_solve_cluster<TS, TF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+        cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(kThreads);
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = 16;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_solve_cluster<TS, TF>, &cfg) == cudaSuccess && clusters > 0)
+            c = 16;
+    }
+    cudaGetLastError();
+    cached = c;
+    return c;
+}
+
+template <typename TS, typename TF>
+cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
     const int64_t nn = (int64_t)n * n;
     k_diag_max<TS><<<1, kThreads, 0, s>>>(n, S, st, 1e-14, 0); note_launch();
     k_convert<TS, TF><<<grid_for(nn), kThreads, 0, s>>>(nn, S, F); note_launch();
-    for (int j0 = 0; j0 < n; j0 += kNB) {
-        const int b = min(kNB, n - j0);
-        k_chol_diag<TF><<<1, kThreads, 0, s>>>(n, F, j0, st); note_launch();
-        const int rows = n - j0 - b;
-        if (rows > 0) {
-            k_chol_trsm<TF><<<(rows + 63) / 64, 64, 0, s>>>(n, F, j0, st); note_launch();
-            const int nt = (rows + 31) / 32;
-            k_chol_syrk<TF><<<nt * (nt + 1) / 2, kThreads, 0, s>>>(n, F, j0, st); note_launch();
-        }
-    }
-    k_diag_max<TF><<<1, kThreads, 0, s>>>(n, F, st, 1e-7, 1); note_launch();
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int nblk = (n + kNB - 1) / kNB;
+    int blocks = sms;  // one CTA per SM, all co-resident
+    if (blocks > nblk * (nblk + 1) / 2 + 1) blocks = nblk * (nblk + 1) / 2 + 1;
+    if (blocks < 1) blocks = 1;
+    int nn_i = n;
+    void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<TF>, dim3(blocks), dim3(kThreads), args, 0, s);
+    if (e != cudaSuccess) return e;
+    note_launch();
     k_check_solve_eps<TF><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
+    k_diag_inverses<TF><<<nblk, kThreads, 0, s>>>(n, F, D, st); note_launch();
+    return cudaGetLastError();
 }
 
 template <typename TS, typename TF>
-void launch_solve_refine(int n, const TS* S, const TF* F, const double* bs, double* x, double* y, double* r,
-                         LmState* st, int refine_iters, cudaStream_t s) {
-    if (n <= 0) return;
-    // r[0..n) is the forward work vector, y[0..n) the forward result.
-    tri_solve<TF>(n, F, bs, r, y, x, st, s);
-    if (refine_iters <= 0) return;
-    // Refinement: x += solve(bs - S x), residual in FP64 against S.
-    double* d = y + n;   // y holds 2n
-    double* res = r + n; // r holds 2n
-    const int rg = (n + kThreads / 32 - 1) / (kThreads / 32);
-    for (int it = 0; it < refine_iters; ++it) {
-        k_residual<TS><<<rg, kThreads, 0, s>>>(n, S, x, bs, res, st); note_launch();
-        tri_solve<TF>(n, F, res, r, y, d, st, s);
-        k_axpy_copy<<<grid_for(n), kThreads, 0, s>>>(n, d, x, 1, st); note_launch();
-    }
-    k_residual<TS><<<rg, kThreads, 0, s>>>(n, S, x, bs, res, st); note_launch();
-    k_norms<<<1, kThreads, 0, s>>>(n, res, bs, st); note_launch();
+cudaError_t launch_solve_refine(int n, const TS* S, const TF* F, const TF* D, const double* bs, double* x,
+                                double* work, LmState* st, int refine_iters, double tol, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int C = cluster_size<TS, TF>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = C;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    double* w = work;
+    double* y = work + n;
+    double* d = work + 2 * (int64_t)n;
+    double* r = work + 3 * (int64_t)n;
+    double* scratch = work + 4 * (int64_t)n;
+    cudaError_t e =
+        cudaLaunchKernelEx(&cfg, k_solve_cluster<TS, TF>, n, S, F, D, bs, x, w, y, d, r, scratch, refine_iters, tol, st);
+    if (e != cudaSuccess) return e;
+    note_launch();
+    return cudaSuccess;
 }
 
 template <typename TS, typename TF>
-void launch_reduced_solve(int n, const TS* S, TF* F, const double* bs, double* x, double* y, double* r, LmState* st,
-                          int refine_iters, cudaStream_t s) {
-    launch_factor<TS, TF>(n, S, F, st, s);
-    launch_solve_refine<TS, TF>(n, S, F, bs, x, y, r, st, refine_iters, s);
+cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double* bs, double* x, double* work,
+                                 LmState* st, int refine_iters, double tol, cudaStream_t s) {
+    cudaError_t e = launch_factor<TS, TF>(n, S, F, D, st, s);
+    if (e != cudaSuccess) return e;
+    return launch_solve_refine<TS, TF>(n, S, F, D, bs, x, work, st, refine_iters, tol, s);
 }
 
-#define ZS_INST(TS, TF)                                                                                          \
-    template void launch_factor<TS, TF>(int, const TS*, TF*, LmState*, cudaStream_t);                             \
-    template void launch_solve_refine<TS, TF>(int, const TS*, const TF*, const double*, double*, double*, double*, \
-                                              LmState*, int, cudaStream_t);
+#define ZS_INST(TS, TF)                                                                                        \
+    template cudaError_t launch_factor<TS, TF>(int, const TS*, TF*, TF*, LmState*, cudaStream_t);               \
+    template cudaError_t launch_solve_refine<TS, TF>(int, const TS*, const TF*, const TF*, const double*, double*, \
+                                                     double*, LmState*, int, double, cudaStream_t);             \
+    template cudaError_t launch_reduced_solve<TS, TF>(int, const TS*, TF*, TF*, const double*, double*, double*, \
+                                                      LmState*, int, double, cudaStream_t);
 ZS_INST(double, double)
 ZS_INST(float, float)
 ZS_INST(double, float)
 #undef ZS_INST
-
-template void launch_reduced_solve<double, double>(int, const double*, double*, const double*, double*, double*,
-                                                   double*, LmState*, int, cudaStream_t);
-template void launch_reduced_solve<float, float>(int, const float*, float*, const double*, double*, double*, double*,
-                                                 LmState*, int, cudaStream_t);
-template void launch_reduced_solve<double, float>(int, const double*, float*, const double*, double*, double*,
-                                                  double*, LmState*, int, cudaStream_t);
 
 }  // namespace zs

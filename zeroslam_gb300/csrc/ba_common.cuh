@@ -127,25 +127,45 @@ __device__ inline void pose_plus(double* p, const double d[6]) {
     p[6] = nq[0];
 }
 
+// Separately rounded IEEE operations (never fused into an FMA). The
+// residual and the squared error go through these so that every edge's
+// residual rounds exactly as the reference's double arithmetic does: the
+// reference's robust-weight branch (source/factor_graph.hpp:265) is decided
+// by rounding for Huber outliers, and reproducing it needs identical inputs.
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+
+__device__ inline void quat_mul_rn(const double a[4], const double b[4], double o[4]) {
+    o[0] = rsub(rsub(rsub(rmul(a[0], b[0]), rmul(a[1], b[1])), rmul(a[2], b[2])), rmul(a[3], b[3]));
+    o[1] = rsub(radd(radd(rmul(a[0], b[1]), rmul(a[1], b[0])), rmul(a[2], b[3])), rmul(a[3], b[2]));
+    o[2] = radd(radd(rsub(rmul(a[0], b[2]), rmul(a[1], b[3])), rmul(a[2], b[0])), rmul(a[3], b[1]));
+    o[3] = radd(rsub(radd(rmul(a[0], b[3]), rmul(a[1], b[2])), rmul(a[2], b[1])), rmul(a[3], b[0]));
+}
+
 // Camera-frame point of landmark X under pose p; returns 1 when it projects
 // (Z >= 1e-12) and writes the residual uv - pi(Xc), else the penalty
-// (-0.3 Z, -0.3 Z).
+// (-0.3 Z, -0.3 Z). Rounded operation by operation as the reference.
 __device__ inline int residual(const double* p, const double* X, double u_obs, double v_obs, const Intrinsics& in,
                                double Xc[3], double r[2]) {
     const double q[4] = {p[6], p[3], p[4], p[5]};
-    quat_rotate(q, X, Xc);
-    Xc[0] += p[0];
-    Xc[1] += p[1];
-    Xc[2] += p[2];
+    const double pq[4] = {0.0, X[0], X[1], X[2]};
+    const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
+    double t[4], o[4];
+    quat_mul_rn(q, pq, t);
+    quat_mul_rn(t, qc, o);
+    Xc[0] = radd(o[1], p[0]);
+    Xc[1] = radd(o[2], p[1]);
+    Xc[2] = radd(o[3], p[2]);
     if (Xc[2] < 1.0e-12) {
-        const double pen = -kBehindPenalty * Xc[2];
+        const double pen = rmul(-kBehindPenalty, Xc[2]);
         r[0] = pen;
         r[1] = pen;
         return 0;
     }
     const double iz = 1.0 / Xc[2];
-    r[0] = u_obs - (in.fx * (Xc[0] * iz) + in.cx);
-    r[1] = v_obs - (in.fy * (Xc[1] * iz) + in.cy);
+    r[0] = rsub(u_obs, radd(rmul(in.fx, rmul(Xc[0], iz)), in.cx));
+    r[1] = rsub(v_obs, radd(rmul(in.fy, rmul(Xc[1], iz)), in.cy));
     return 1;
 }
 
@@ -184,12 +204,13 @@ __device__ inline void loss_rho(const LossParams& L, double e2, double rho[3]) {
     }
 }
 
-// r^T Omega r with Omega row-major (identity when om == nullptr).
+// r^T Omega r with Omega row-major (identity when om == nullptr), rounded
+// as the reference's (r^T Omega) r.
 __device__ inline double chi2_of(const double r[2], const double* om) {
-    if (!om) return r[0] * r[0] + r[1] * r[1];
-    const double a = r[0] * om[0] + r[1] * om[2];
-    const double b = r[0] * om[1] + r[1] * om[3];
-    return a * r[0] + b * r[1];
+    if (!om) return radd(rmul(r[0], r[0]), rmul(r[1], r[1]));
+    const double a = radd(rmul(r[0], om[0]), rmul(r[1], om[2]));
+    const double b = radd(rmul(r[0], om[1]), rmul(r[1], om[3]));
+    return radd(rmul(a, r[0]), rmul(b, r[1]));
 }
 
 // Deterministic block sum of one value per thread (fixed tree over

@@ -52,8 +52,9 @@ struct DevProblem {
 // Working arrays of one precision (T = double for the plain form, float for
 // the mixed form).
 struct DevWork {
-    void* hpl = nullptr;       // [M*18] T
-    void* W = nullptr;         // [M*18] T
+    void* hpl = nullptr;       // [M*RS] T, RS = 18 (double) or 20 (float, padded)
+    void* W = nullptr;         // [M*RS] T
+    double* pose_aux = nullptr; // [K*24] mixed form: per-pose sandwich matrix, translation, rotation
     void* lm_part = nullptr;   // [9*M] T, component-major
     void* pose_part = nullptr; // [27*M] T, component-major
     double* hpp = nullptr;     // [K*36]
@@ -61,11 +62,13 @@ struct DevWork {
     double* hll_inv = nullptr; // [L*9]
     double* b = nullptr;       // [n + 3L] gradient vector (poses then landmarks)
     void* partial = nullptr;   // [nchunks*36] T
-    void* S = nullptr;         // [n*n] T
-    void* F = nullptr;         // [n*n] T, Cholesky factor (lower)
+    double* S = nullptr;       // [n*n] reduced camera matrix, FP64 in both forms
+    void* F = nullptr;         // [n*n] Cholesky factor (lower): double (plain form) or float (mixed)
+    void* D = nullptr;         // [ceil(n/32)*1024] T, inverses of F's diagonal blocks
     double* bs = nullptr;      // [n]
-    double* y = nullptr;       // [2n] scratch for triangular solves
-    double* r = nullptr;       // [2n] scratch: forward work vector, refinement residual
+    double* work = nullptr;    // [4n + 256] triangular-solve and refinement vectors
+    void* X = nullptr;         // mixed form: [n*n] L^-1 (lower)
+    void* XT = nullptr;        // mixed form: [n*n] (L^-1)^T (upper; lower used as scratch)
     double* delta = nullptr;   // [n + 3L]
     double* red = nullptr;     // [kReduceBlocks * 4] reduction partials
     int32_t* ired = nullptr;   // [kReduceBlocks]
@@ -87,7 +90,7 @@ struct LmState {
     int32_t solve_ok;  // reduced Cholesky factor and solve passed
     int32_t good;      // trial step accepted
     int32_t nonfinite;
-    int32_t pad;
+    int32_t refine_sweeps;  // refinement sweeps of the last reduced solve
 };
 
 // ---- kernels (ba_kernels.cu) ----
@@ -109,17 +112,29 @@ void launch_decide(LmState* st, cudaStream_t s);
 void launch_set_solve_ok(LmState* st, int v, cudaStream_t s);
 
 // ---- dense reduced system (ba_cholesky.cu) ----
-// Factor S (n x n row-major, type TS) in type TF into F and solve for x
-// given bs; sets st->solve_ok. With refine_iters > 0, that many FP64
-// refinement sweeps x += F^-1 (bs - S x). y and r need 2n doubles.
+// launch_factor: S (n x n row-major, type TS) -> F = L (lower, type TF) and
+// D = the inverses of L's 32 x 32 diagonal blocks ([ceil(n/32) * 1024] TF);
+// sets st->solve_ok = 0 on a failed pivot or solve test.
+// launch_solve_refine: x = (L L^T)^-1 bs, then up to refine_iters FP64
+// refinement sweeps against S until ||bs - S x|| <= tol ||bs||. work needs
+// 4n + 16 doubles. Both return the launch error, if any.
 template <typename TS, typename TF>
-void launch_reduced_solve(int n, const TS* S, TF* F, const double* bs, double* x, double* y, double* r, LmState* st,
-                          int refine_iters, cudaStream_t s);
-// The two halves of launch_reduced_solve.
+cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStream_t s);
 template <typename TS, typename TF>
-void launch_factor(int n, const TS* S, TF* F, LmState* st, cudaStream_t s);
+cudaError_t launch_solve_refine(int n, const TS* S, const TF* F, const TF* D, const double* bs, double* x,
+                                double* work, LmState* st, int refine_iters, double tol, cudaStream_t s);
 template <typename TS, typename TF>
-void launch_solve_refine(int n, const TS* S, const TF* F, const double* bs, double* x, double* y, double* r,
-                         LmState* st, int refine_iters, cudaStream_t s);
+cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double* bs, double* x, double* work,
+                                 LmState* st, int refine_iters, double tol, cudaStream_t s);
+
+// ---- mixed form (ba_inverse.cu) ----
+// X = L^-1 and XT = X^T from the factor F and its diagonal-block inverses D.
+template <typename TX>
+cudaError_t launch_tri_inverse(int n, const TX* F, const TX* D, TX* X, TX* XT, LmState* st, cudaStream_t s);
+// x = X^T X bs, then FP64 refinement x += X^T X (bs - S x) until
+// ||bs - S x|| <= tol ||bs|| or refine_iters sweeps; work: 4n + 256 doubles.
+template <typename TS, typename TX>
+cudaError_t launch_refine(int n, const TS* S, const TX* X, const TX* XT, const double* bs, double* x, double* work,
+                          LmState* st, int refine_iters, double tol, cudaStream_t s);
 
 }  // namespace zs

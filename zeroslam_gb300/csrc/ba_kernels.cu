@@ -23,27 +23,105 @@
 
 namespace zs {
 
+// H_pl / W records per observation: 18 values, padded to a multiple of 16
+// bytes so the Schur kernel can load them as vectors.
+template <typename T>
+struct RecStride {
+    static constexpr int value = sizeof(T) == 4 ? 20 : 18;
+};
+
 // (a, c) with a <= c of a symmetric 6x6 block, row by row.
 __constant__ int8_t kUp6[21][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 5}, {1, 1}, {1, 2}, {1, 3}, {1, 4}, {1, 5},
                                    {2, 2}, {2, 3}, {2, 4}, {2, 5}, {3, 3}, {3, 4}, {3, 5}, {4, 4}, {4, 5}, {5, 5}};
 
+// Per-pose data for the mixed form's linearisation: the quaternion-sandwich
+// matrix M with M X = q (0, X) q* (valid for unnormalised q),
+// M = (w^2 - |v|^2) I + 2 v v^T + 2 w [v]x, the translation, and the rotation
+// matrix of source/lie.hpp:188-204 used by the landmark Jacobian.
+// Layout per pose: M (9), t (3), R (9), pad (3).
+constexpr int kAux = 24;
+
+__global__ void __launch_bounds__(kThreads) k_pose_aux(DevProblem P, double* aux) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.K) return;
+    const double* p = P.pose + (int64_t)k * kPoseStride;
+    const double w = p[6], x = p[3], y = p[4], z = p[5];
+    const double s = w * w - (x * x + y * y + z * z);
+    double* a = aux + (int64_t)k * kAux;
+    a[0] = s + 2.0 * x * x;      a[1] = 2.0 * (x * y - w * z); a[2] = 2.0 * (x * z + w * y);
+    a[3] = 2.0 * (x * y + w * z); a[4] = s + 2.0 * y * y;      a[5] = 2.0 * (y * z - w * x);
+    a[6] = 2.0 * (x * z - w * y); a[7] = 2.0 * (y * z + w * x); a[8] = s + 2.0 * z * z;
+    a[9] = p[0];
+    a[10] = p[1];
+    a[11] = p[2];
+    const double q[4] = {w, x, y, z};
+    quat_matrix(q, a + 12);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
-                                                        T* __restrict__ pose_part) {
+                                                        T* __restrict__ pose_part, const double* __restrict__ aux) {
+    constexpr int RS = RecStride<T>::value;
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= P.M) return;
     const int pi = P.obs_pose[o], li = P.obs_lm[o];
-    const double* pp = P.pose + (int64_t)pi * kPoseStride;
     const double* xp = P.lm + (int64_t)li * kLmStride;
-    double p[7], X[3];
-#pragma unroll
-    for (int i = 0; i < 7; ++i) p[i] = __ldg(pp + i);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) X[i] = __ldg(xp + i);
     const double2 uv = P.obs_uv[o];
-    double Xc[3], r[2];
-    const int front = residual(p, X, uv.x, uv.y, P.intr, Xc, r);
     const double* om = P.obs_info ? P.obs_info + 4 * o : nullptr;
+    T Jc[6], Xv, Yv, Zv, Rm[9];
+    double r[2];
+    if (sizeof(T) == 8) {
+        // plain form: residual rounded exactly as the reference's
+        const double* pp = P.pose + (int64_t)pi * kPoseStride;
+        double p[7], X[3], Xc[3];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) p[i] = __ldg(pp + i);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) X[i] = __ldg(xp + i);
+        const int front = residual(p, X, uv.x, uv.y, P.intr, Xc, r);
+        if (front) {
+            const T iz = (T)(1.0 / Xc[2]);
+            const T iz2 = iz * iz;
+            const T fx = (T)P.intr.fx, fy = (T)P.intr.fy;
+            Jc[0] = fx * iz; Jc[1] = T(0); Jc[2] = -fx * (T)Xc[0] * iz2;
+            Jc[3] = T(0); Jc[4] = fy * iz; Jc[5] = -fy * (T)Xc[1] * iz2;
+        } else {
+            Jc[0] = T(0); Jc[1] = T(0); Jc[2] = (T)kBehindPenalty;
+            Jc[3] = T(0); Jc[4] = T(0); Jc[5] = (T)kBehindPenalty;
+        }
+        Xv = (T)Xc[0]; Yv = (T)Xc[1]; Zv = (T)Xc[2];
+        double q[4] = {p[6], p[3], p[4], p[5]};
+        double R[9];
+        quat_matrix(q, R);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rm[i] = (T)R[i];
+    } else {
+        // mixed form: camera-frame point in FP64 through the per-pose
+        // sandwich matrix, everything after it in FP32
+        const double* a = aux + (int64_t)pi * kAux;
+        const double X0 = __ldg(xp), X1 = __ldg(xp + 1), X2 = __ldg(xp + 2);
+        const double xc = fma(a[0], X0, fma(a[1], X1, fma(a[2], X2, a[9])));
+        const double yc = fma(a[3], X0, fma(a[4], X1, fma(a[5], X2, a[10])));
+        const double zc = fma(a[6], X0, fma(a[7], X1, fma(a[8], X2, a[11])));
+        Xv = (T)xc; Yv = (T)yc; Zv = (T)zc;
+        if (zc < 1.0e-12) {
+            const double pen = -kBehindPenalty * zc;
+            r[0] = pen; r[1] = pen;
+            Jc[0] = T(0); Jc[1] = T(0); Jc[2] = (T)kBehindPenalty;
+            Jc[3] = T(0); Jc[4] = T(0); Jc[5] = (T)kBehindPenalty;
+        } else {
+            const T iz = T(1) / Zv;
+            const T fx = (T)P.intr.fx, fy = (T)P.intr.fy;
+            const T u0 = (T)(uv.x - P.intr.cx), v0 = (T)(uv.y - P.intr.cy);
+            r[0] = (double)(u0 - fx * (Xv * iz));
+            r[1] = (double)(v0 - fy * (Yv * iz));
+            const T iz2 = iz * iz;
+            Jc[0] = fx * iz; Jc[1] = T(0); Jc[2] = -fx * Xv * iz2;
+            Jc[3] = T(0); Jc[4] = fy * iz; Jc[5] = -fy * Yv * iz2;
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rm[i] = (T)a[12 + i];
+    }
 
     // Robust weight W = rho' Omega (+ 2 rho'' (Omega r)(Omega r)^T), and the
     // gradient's non-robust Omega r scaled by rho'.
@@ -64,7 +142,10 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         drho = rho[1];
 #pragma unroll
         for (int i = 0; i < 4; ++i) Wd[i] *= rho[1];
-        if ((rho[1] + 2.0 * rho[2] * e2) > 0.0) {
+        // For Huber outliers rho' + 2 rho'' e2 is zero in exact arithmetic, so
+        // the sign comes from rounding: evaluate it as separately rounded
+        // multiply and add (no FMA), as the reference does.
+        if (__dadd_rn(rho[1], __dmul_rn(2.0 * rho[2], e2)) > 0.0) {
             const double k2 = 2.0 * rho[2];
             Wd[0] += k2 * orr0 * orr0;
             Wd[1] += k2 * orr0 * orr1;
@@ -72,20 +153,6 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
             Wd[3] += k2 * orr1 * orr1;
         }
     }
-
-    // Camera Jacobian (2x3); behind the camera d(residual)/dZ = -0.3.
-    T Jc[6];
-    if (front) {
-        const T iz = (T)(1.0 / Xc[2]);
-        const T iz2 = iz * iz;
-        const T fx = (T)P.intr.fx, fy = (T)P.intr.fy;
-        Jc[0] = fx * iz; Jc[1] = T(0); Jc[2] = -fx * (T)Xc[0] * iz2;
-        Jc[3] = T(0); Jc[4] = fy * iz; Jc[5] = -fy * (T)Xc[1] * iz2;
-    } else {
-        Jc[0] = T(0); Jc[1] = T(0); Jc[2] = (T)kBehindPenalty;
-        Jc[3] = T(0); Jc[4] = T(0); Jc[5] = (T)kBehindPenalty;
-    }
-    const T Xv = (T)Xc[0], Yv = (T)Xc[1], Zv = (T)Xc[2];
     // J_p = -J_cam [-[Xc]x | I] (omega first), J_l = -J_cam R.
     T Jp[12], Jl[6];
 #pragma unroll
@@ -97,22 +164,14 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         Jp[rr * 6 + 3] = -c0;
         Jp[rr * 6 + 4] = -c1;
         Jp[rr * 6 + 5] = -c2;
-    }
-    {
-        double q[4] = {p[6], p[3], p[4], p[5]};
-        double R[9];
-        quat_matrix(q, R);
 #pragma unroll
-        for (int rr = 0; rr < 2; ++rr)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                Jl[rr * 3 + c] = -(Jc[rr * 3] * (T)R[c] + Jc[rr * 3 + 1] * (T)R[3 + c] + Jc[rr * 3 + 2] * (T)R[6 + c]);
+        for (int c = 0; c < 3; ++c) Jl[rr * 3 + c] = -(c0 * Rm[c] + c1 * Rm[3 + c] + c2 * Rm[6 + c]);
     }
     const T W00 = (T)Wd[0], W01 = (T)Wd[1], W10 = (T)Wd[2], W11 = (T)Wd[3];
     const T g0 = (T)(drho * orr0), g1 = (T)(drho * orr1);
     const bool pf = P.pose_fixed[pi] != 0, lf = P.lm_fixed[li] != 0;
 
-    T* hb = hpl + o * 18;
+    T* hb = hpl + o * RS;
     if (!pf) {
         T A0[6], A1[6];  // (J_p^T W) columns
 #pragma unroll
@@ -167,20 +226,21 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
 // the run's H_pl blocks, in order.
 template <typename T>
 __global__ void k_merge_dups(DevProblem P, T* hpl) {
+    constexpr int RS = RecStride<T>::value;
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= P.M) return;
     if (P.dup_owner[o] != o) return;
     int64_t e = o + 1;
     T acc[18];
 #pragma unroll
-    for (int k = 0; k < 18; ++k) acc[k] = hpl[o * 18 + k];
+    for (int k = 0; k < 18; ++k) acc[k] = hpl[o * RS + k];
     while (e < P.M && P.dup_owner[e] == o) {
 #pragma unroll
-        for (int k = 0; k < 18; ++k) acc[k] += hpl[e * 18 + k];
+        for (int k = 0; k < 18; ++k) acc[k] += hpl[e * RS + k];
         ++e;
     }
 #pragma unroll
-    for (int k = 0; k < 18; ++k) hpl[o * 18 + k] = acc[k];
+    for (int k = 0; k < 18; ++k) hpl[o * RS + k] = acc[k];
 }
 
 template <typename T>
@@ -204,10 +264,12 @@ __global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* _
     bl[0] = acc[6]; bl[1] = acc[7]; bl[2] = acc[8];
 }
 
+// Per pose: each thread sums its strided share of the pose's observations
+// in T, the thread partials meet in a fixed FP64 tree.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T* __restrict__ pose_part, double* hpp,
                                                           double* b) {
-    __shared__ T sh[kThreads];
+    __shared__ double sh[kThreads];
     const int k = blockIdx.x;
     T acc[27];
 #pragma unroll
@@ -221,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T*
     double* H = hpp + (int64_t)k * 36;
 #pragma unroll 1
     for (int c = 0; c < 21; ++c) {
-        const T v = block_sum(acc[c], sh);
+        const double v = block_sum((double)acc[c], sh);
         if (threadIdx.x == 0) {
             const int a = kUp6[c][0], d = kUp6[c][1];
             H[a * 6 + d] = v;
@@ -230,7 +292,7 @@ __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T*
     }
 #pragma unroll 1
     for (int c = 0; c < 6; ++c) {
-        const T v = block_sum(acc[21 + c], sh);
+        const double v = block_sum((double)acc[21 + c], sh);
         if (threadIdx.x == 0) b[6LL * k + c] = v;
     }
 }
@@ -279,14 +341,15 @@ __global__ void __launch_bounds__(kThreads) k_invert(DevProblem P, const double*
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_w(DevProblem P, const T* __restrict__ hpl, const double* __restrict__ hinv,
                                                 T* __restrict__ W) {
+    constexpr int RS = RecStride<T>::value;
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= P.M || !P.blk_valid[o]) return;
     const double* I = hinv + (int64_t)P.obs_lm[o] * 9;
     T iv[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) iv[i] = (T)I[i];
-    const T* h = hpl + o * 18;
-    T* w = W + o * 18;
+    const T* h = hpl + o * RS;
+    T* w = W + o * RS;
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
         const T h0 = h[a * 3], h1 = h[a * 3 + 1], h2 = h[a * 3 + 2];
@@ -295,10 +358,29 @@ __global__ void __launch_bounds__(kThreads) k_w(DevProblem P, const T* __restric
     }
 }
 
+// Loads one 18-value record (padded stride) with 16-byte vector loads.
+__device__ __forceinline__ void load_rec(const float* p, float v[20]) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const float4 t = __ldg(q + i);
+        v[4 * i] = t.x; v[4 * i + 1] = t.y; v[4 * i + 2] = t.z; v[4 * i + 3] = t.w;
+    }
+}
+__device__ __forceinline__ void load_rec(const double* p, double v[20]) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const double2 t = __ldg(q + i);
+        v[2 * i] = t.x; v[2 * i + 1] = t.y;
+    }
+}
+
 // Partial 6x6 sums W_i H_j^T over one chunk of a pose pair's triples.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_schur_chunks(DevProblem P, const T* __restrict__ W,
                                                            const T* __restrict__ hpl, T* __restrict__ partial) {
+    constexpr int RS = RecStride<T>::value;
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= P.nchunks) return;
     T acc[36];
@@ -307,14 +389,9 @@ __global__ void __launch_bounds__(kThreads) k_schur_chunks(DevProblem P, const T
     const int64_t e1 = P.chunk_ptr[c + 1];
     for (int64_t t = P.chunk_ptr[c]; t < e1; ++t) {
         const int2 tr = P.triples[t];
-        const T* w = W + (int64_t)tr.x * 18;
-        const T* h = hpl + (int64_t)tr.y * 18;
-        T wv[18], hv[18];
-#pragma unroll
-        for (int k = 0; k < 18; ++k) {
-            wv[k] = w[k];
-            hv[k] = h[k];
-        }
+        T wv[20], hv[20];
+        load_rec(W + (int64_t)tr.x * RS, wv);
+        load_rec(hpl + (int64_t)tr.y * RS, hv);
 #pragma unroll
         for (int a = 0; a < 6; ++a)
 #pragma unroll
@@ -327,8 +404,7 @@ __global__ void __launch_bounds__(kThreads) k_schur_chunks(DevProblem P, const T
 }
 
 // S = blockdiag(H_pp + lambda I); the pair sums are subtracted next.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_s_init(DevProblem P, const double* __restrict__ hpp, T* S,
+__global__ void __launch_bounds__(kThreads) k_s_init(DevProblem P, const double* __restrict__ hpp, double* S,
                                                      const LmState* st) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t n = P.n;
@@ -339,17 +415,18 @@ __global__ void __launch_bounds__(kThreads) k_s_init(DevProblem P, const double*
         v = hpp[(int64_t)(row / 6) * 36 + (row % 6) * 6 + (col % 6)];
         if (row == col) v += st->lambda;
     }
-    S[idx] = (T)v;
+    S[idx] = v;
 }
 
+// S (FP64) -= the pair's chunk partials, summed in FP64 in chunk order.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const T* __restrict__ partial, T* S) {
+__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const T* __restrict__ partial, double* S) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= (int64_t)P.npairs * 36) return;
     const int p = (int)(idx / 36), e = (int)(idx % 36);
-    T sum = T(0);
+    double sum = 0.0;
     const int64_t c1 = P.pair_chunk_ptr[p + 1];
-    for (int64_t c = P.pair_chunk_ptr[p]; c < c1; ++c) sum += partial[c * 36 + e];
+    for (int64_t c = P.pair_chunk_ptr[p]; c < c1; ++c) sum += (double)partial[c * 36 + e];
     const int i = P.pair_i[p], j = P.pair_j[p];
     const int64_t n = P.n;
     const int64_t row = 6LL * i + e / 6, col = 6LL * j + e % 6;
@@ -365,6 +442,7 @@ __global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bs(DevProblem P, const T* __restrict__ W, const double* __restrict__ b,
                                                  double* bs) {
+    constexpr int RS = RecStride<T>::value;
     __shared__ double sh[kThreads];
     const int k = blockIdx.x;
     double acc[6] = {0, 0, 0, 0, 0, 0};
@@ -372,7 +450,7 @@ __global__ void __launch_bounds__(kThreads) k_bs(DevProblem P, const T* __restri
     for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x) {
         const int64_t o = P.pose_obs[i];
         if (!P.blk_valid[o]) continue;
-        const T* w = W + o * 18;
+        const T* w = W + o * RS;
         const double* bl = b + P.n + 3LL * P.obs_lm[o];
         const T b0 = (T)bl[0], b1 = (T)bl[1], b2 = (T)bl[2];
 #pragma unroll
@@ -390,6 +468,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_backsub(DevProblem P, const T* __restrict__ hpl,
                                                       const double* __restrict__ hinv, const double* __restrict__ b,
                                                       double* delta, const LmState* st) {
+    constexpr int RS = RecStride<T>::value;
     if (!st->solve_ok) return;
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= P.L) return;
@@ -398,7 +477,7 @@ __global__ void __launch_bounds__(kThreads) k_backsub(DevProblem P, const T* __r
     const int e = P.lm_ptr[l + 1];
     for (int o = P.lm_ptr[l]; o < e; ++o) {
         if (!P.blk_valid[o]) continue;
-        const T* h = hpl + (int64_t)o * 18;
+        const T* h = hpl + (int64_t)o * RS;
         const double* dp = delta + 6LL * P.obs_pose[o];
         T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
@@ -591,34 +670,37 @@ long long& launch_counter() {
 
 template <typename T>
 void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
-    if (P.M > 0) {
-        k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part); note_launch();
-        if (P.has_dups) k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch();
+    if (sizeof(T) == 4 && P.K > 0) {
+        k_pose_aux<<<grid_for(P.K), kThreads, 0, s>>>(P, W.pose_aux); note_launch();
     }
-    if (P.L > 0) k_reduce_lm<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.lm_part, W.hll, W.b); note_launch();
-    if (P.K > 0) k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b); note_launch();
+    if (P.M > 0) {
+        k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part, W.pose_aux); note_launch();
+        if (P.has_dups) { k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch(); }
+    }
+    if (P.L > 0) { k_reduce_lm<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.lm_part, W.hll, W.b); note_launch(); }
+    if (P.K > 0) { k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b); note_launch(); }
 }
 
 template <typename T>
 void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
-    if (P.L > 0) k_invert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, st); note_launch();
-    if (P.M > 0) k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch();
+    if (P.L > 0) { k_invert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, st); note_launch(); }
+    if (P.M > 0) { k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch(); }
 }
 
 template <typename T>
 void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
     const int64_t nn = (int64_t)P.n * P.n;
-    if (nn > 0) k_s_init<T><<<grid_for(nn), kThreads, 0, s>>>(P, W.hpp, (T*)W.S, st); note_launch();
+    if (nn > 0) { k_s_init<<<grid_for(nn), kThreads, 0, s>>>(P, W.hpp, (double*)W.S, st); note_launch(); }
     if (P.nchunks > 0) {
         k_schur_chunks<T><<<grid_for(P.nchunks), kThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial); note_launch();
-        k_schur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, (T*)W.S); note_launch();
+        k_schur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, (double*)W.S); note_launch();
     }
-    if (P.K > 0) k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch();
+    if (P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
 }
 
 template <typename T>
 void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
-    if (P.L > 0) k_backsub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st); note_launch();
+    if (P.L > 0) { k_backsub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st); note_launch(); }
 }
 
 void launch_update(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {

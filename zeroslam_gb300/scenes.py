@@ -303,6 +303,19 @@ def _finish(name, q_gt, t_gt, X_gt, obs_pose, obs_lm, obs_uv, q0, t0, X0, iterat
     )
 
 
+def _depth_relative_noise(X, centre, obs_pose, obs_lm, rng, rel):
+    """Isotropic Gaussian landmark noise with sigma = rel x the distance from
+    the landmark to the first camera that observes it."""
+    L = X.shape[0]
+    first = np.full(L, -1, dtype=np.int64)
+    order = np.argsort(obs_lm, kind="stable")
+    lm_sorted = obs_lm[order]
+    starts = np.searchsorted(lm_sorted, np.arange(L))
+    first = obs_pose[order][np.minimum(starts, len(order) - 1)]
+    dist = np.linalg.norm(X - centre[first], axis=1)
+    return rel * dist[:, None] * rng.normal(3 * L).reshape(L, 3)
+
+
 def _perturb_poses(q, t, rng, sig_rot, sig_trans, drift=None):
     """Left-multiplicative perturbation exp(xi) * T for every pose but pose 0."""
     K = q.shape[0]
@@ -343,7 +356,7 @@ WALK_DMAX = 7.0
 
 
 def walk_scene(K: int = 200, L: int = 50000, seed: int = 1, iterations: int = 20,
-               dmax: float = WALK_DMAX, sigma_px: float = 1.0) -> Scene:
+               dmax: float = WALK_DMAX, sigma_px: float = 1.0, landmark_rel_noise: float = 0.02) -> Scene:
     """20 m random walk (0.1 m steps, yaw jitter N(0, 3 deg) per step) through
     a 30 x 10 x 30 m box of landmarks; observations with depth in [0.5, dmax]."""
     rng = Pcg32Streams(seed)
@@ -356,8 +369,9 @@ def walk_scene(K: int = 200, L: int = 50000, seed: int = 1, iterations: int = 20
     kept, obs_pose, obs_lm, obs_uv = _observe(q_gt, t_gt, X, rng, sigma_px, 0.5, dmax, L, 2)
     X = X[kept]
     q0, t0 = _perturb_poses(q_gt, t_gt, rng, 0.01, 0.03)
-    X0 = X * (1.0 + 0.05 * rng.normal(3 * L).reshape(L, 3))
-    meta = dict(generator="walk", K=K, L_requested=L, seed=seed, dmax=dmax, sigma_px=sigma_px)
+    X0 = X + _depth_relative_noise(X, centre, obs_pose, obs_lm, rng, landmark_rel_noise)
+    meta = dict(generator="walk", K=K, L_requested=L, seed=seed, dmax=dmax, sigma_px=sigma_px,
+                landmark_rel_noise=landmark_rel_noise)
     return _finish(f"walk_K{K}_L{L}_s{seed}", q_gt, t_gt, X, obs_pose, obs_lm, obs_uv,
                    q0, t0, X0, iterations, meta)
 
@@ -366,7 +380,7 @@ LOOP_DMAX = 5.6
 
 
 def loop_scene(K: int = 1000, L: int = 200000, seed: int = 4, iterations: int = 30,
-               dmax: float = LOOP_DMAX, sigma_px: float = 0.5) -> Scene:
+               dmax: float = LOOP_DMAX, sigma_px: float = 0.5, landmark_rel_noise: float = 0.02) -> Scene:
     """K keyframes on a 100 m circular loop looking along the direction of
     travel, landmarks in a 60 x 15 x 60 m box; initial drift grows linearly to
     0.5 m / 2 degrees at the end of the loop."""
@@ -399,8 +413,9 @@ def loop_scene(K: int = 1000, L: int = 200000, seed: int = 4, iterations: int = 
     s = (np.arange(K) / max(1, K - 1))[:, None]
     drift = np.concatenate([s * math.radians(2.0) * axis[None], s * 0.5 * tdir[None]], axis=1)
     q0, t0 = _perturb_poses(q_gt, t_gt, rng, 0.001, 0.003, drift=drift)
-    X0 = X * (1.0 + 0.05 * rng.normal(3 * L).reshape(L, 3))
-    meta = dict(generator="loop", K=K, L_requested=L, seed=seed, dmax=dmax, sigma_px=sigma_px)
+    X0 = X + _depth_relative_noise(X, centre, obs_pose, obs_lm, rng, landmark_rel_noise)
+    meta = dict(generator="loop", K=K, L_requested=L, seed=seed, dmax=dmax, sigma_px=sigma_px,
+                landmark_rel_noise=landmark_rel_noise)
     return _finish(f"loop_K{K}_L{L}_s{seed}", q_gt, t_gt, X, obs_pose, obs_lm, obs_uv,
                    q0, t0, X0, iterations, meta)
 
