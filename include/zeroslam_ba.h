@@ -172,6 +172,26 @@ int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda);
  * Returns ZS_OK or ZS_ERR_CHOLESKY. */
 int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, double* x, int precision);
 
+/* Largest n accepted by zs_dense_cholesky_solve_noalloc. */
+#define ZS_NOALLOC_MAX_N 384
+
+/* zs_dense_cholesky_solve (FP64) for callers that must not allocate device
+ * memory while they run: a real-time tracking thread that cannot block in
+ * the allocator or risk an out-of-memory failure mid-sequence, or a host
+ * application whose device memory belongs to another allocator. This entry
+ * point has no counterpart in the reference; it calls no cudaMalloc, cudaFree
+ * or other allocating routine. Its device workspace is one fixed array of
+ * about 2.5 MB inside this library (sized for n <= ZS_NOALLOC_MAX_N) that
+ * every device loading the library keeps until the process exits; larger n
+ * returns ZS_ERR_INVALID. A, b, L and x are host pointers as in
+ * zs_dense_cholesky_solve; L and x may be NULL. Runs on the current device's
+ * legacy default stream and returns after the result is copied back. The
+ * first call on each device looks the workspace address up, so make that
+ * first call before any stream capture. All calls share the one workspace:
+ * calls that overlap on the GPU (other host threads, other streams) race.
+ * Returns ZS_OK or ZS_ERR_CHOLESKY. */
+int zs_dense_cholesky_solve_noalloc(const double* A, int n, const double* b, double* L, double* x);
+
 /* Measures the FP64 and FP32 fused multiply-add pipe peaks of `device` with
  * a register-resident FMA chain on every SM (TFLOP/s, 2 flops per FMA). A
  * measurement utility for roofline reports; no reference counterpart. */

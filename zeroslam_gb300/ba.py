@@ -79,7 +79,7 @@ _LIB = None
 ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
-                 "zs_last_error")
+                 "zs_last_error", "zs_dense_cholesky_solve_noalloc")
 
 
 def library_path() -> str:
@@ -125,6 +125,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_ba_status_string.argtypes = [C.c_int]
     lib.zs_last_error.restype = C.c_char_p
     lib.zs_last_error.argtypes = []
+    lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
+    lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
     _LIB = lib
     return lib
 
