@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--single", choices=["mixed", "fp64"], default=None,
+                    help="run one solve of --iterations (default 2) on the workload and exit; for profilers")
     return ap.parse_args()
 
 
@@ -387,8 +389,25 @@ def ours_arm(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def single_solve(args):
+    """One solve on the workload, nothing else: the unit a profiler captures."""
+    from zeroslam_gb300 import ba
+
+    sc = make_scene(args.workload)
+    prec = ba.MIXED if args.single == "mixed" else ba.FP64
+    with ba.BundleAdjuster(precision=prec) as h:
+        h.set_problem(sc)
+        rep = h.solve(args.iterations or 2)
+    print(json.dumps({"single": args.single, "workload": args.workload, "iterations": rep.iterations,
+                      "attempts": rep.attempts, "chi2_final": rep.chi2_final,
+                      "kernel_launches": rep.kernel_launches}), flush=True)
+
+
 def main():
     args = parse()
+    if args.single:
+        single_solve(args)
+        return
     dist = Dist()
     if args.impl == "reference":
         reference_arm(args, dist)
