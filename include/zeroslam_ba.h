@@ -162,6 +162,31 @@ int zs_ba_chi2(zs_ba_handle* h, double* chi2);
  * vector. Returns ZS_OK or ZS_ERR_CHOLESKY. */
 int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b);
 
+/* What an adjoint solve did. */
+typedef struct zs_ba_adjoint_report {
+    int32_t status;
+    int32_t iterations;      /* preconditioned conjugate-gradient iterations */
+    double rel_residual;     /* ||a - H v|| / ||a|| at exit */
+    double ms_total;
+} zs_ba_adjoint_report;
+
+/* Gradient of a scalar loss of the solved state with respect to the observed
+ * pixels and the intrinsics, by the implicit-function theorem at the current
+ * state (call after zs_ba_solve has converged). Inputs: a = dL/dx in the
+ * solver's local coordinates, dloss_dpose [K*6] (left perturbation
+ * exp(d) T, omega then upsilon) and dloss_dlandmark [L*3] (either may be
+ * NULL = zero); fixed vertices are ignored. Outputs (each may be NULL):
+ * dloss_duv [M*2] in the problem's observation order, dloss_dintrinsics [4]
+ * (fx, fy, cx, cy) and adjoint_state [6K+3L], the solution v of H v = a.
+ * H is the exact Hessian of the cost in local coordinates (Gauss-Newton term
+ * plus residual curvature); H v = a is solved by conjugate gradients
+ * preconditioned with the solver's Schur / reduced-Cholesky factorisation.
+ * With a = the gradient vector b of zs_ba_linear_step, v is the exact Newton
+ * step. FP64 handles and ZS_LOSS_NONE only (ZS_ERR_UNSUPPORTED otherwise).
+ * No counterpart in the reference. */
+int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dloss_dlandmark, double* dloss_duv,
+                  double* dloss_dintrinsics, double* adjoint_state, zs_ba_adjoint_report* rep);
+
 /* Initial damping tau * min(clamp, max diagonal of H) at the current state. */
 int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda);
 

@@ -63,6 +63,11 @@ class Report(C.Structure):
         return d
 
 
+class AdjointReport(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_residual", C.c_double),
+                ("ms_total", C.c_double)]
+
+
 class ZsError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
@@ -79,7 +84,7 @@ _LIB = None
 ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
-                 "zs_last_error", "zs_dense_cholesky_solve_noalloc")
+                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint")
 
 
 def library_path() -> str:
@@ -125,6 +130,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_ba_status_string.argtypes = [C.c_int]
     lib.zs_last_error.restype = C.c_char_p
     lib.zs_last_error.argtypes = []
+    lib.zs_ba_adjoint.restype = C.c_int
+    lib.zs_ba_adjoint.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, C.POINTER(AdjointReport)]
     lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
     lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
     _LIB = lib
@@ -247,6 +254,20 @@ class BundleAdjuster:
         if st != ZS_OK:
             raise ZsError(st, "zs_ba_initial_lambda")
         return out.value
+
+    def adjoint(self, dloss_dpose=None, dloss_dlandmark=None, want_state=False):
+        """(dL/duv [M,2], dL/d(fx,fy,cx,cy) [4], AdjointReport[, v [6K+3L]]) at the current state."""
+        dp = None if dloss_dpose is None else np.ascontiguousarray(dloss_dpose, dtype=np.float64)
+        dl = None if dloss_dlandmark is None else np.ascontiguousarray(dloss_dlandmark, dtype=np.float64)
+        duv = np.zeros((self.M, 2))
+        dint = np.zeros(4)
+        v = np.zeros(6 * self.K + 3 * self.L) if want_state else None
+        rep = AdjointReport()
+        st = self.lib.zs_ba_adjoint(self.h, _p(dp, _dp), _p(dl, _dp), _p(duv, _dp), _p(dint, _dp), _p(v, _dp),
+                                    C.byref(rep))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_adjoint")
+        return (duv, dint, rep, v) if want_state else (duv, dint, rep)
 
     def linear_step(self, lam: float, want_S: bool = True) -> dict:
         n = 6 * self.K

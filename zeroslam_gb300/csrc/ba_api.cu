@@ -131,6 +131,9 @@ struct zs_ba_handle {
     LmState* st = nullptr;       // device
     LmState* st_host = nullptr;  // pinned mirror
     std::vector<void*> owned;    // problem-lifetime device allocations
+    double* adj_rec = nullptr;   // adjoint buffers, allocated on first use (owned)
+    double* adj_part = nullptr;
+    double* adj_vec = nullptr;   // a, v, r, z, p, q, zero: 7 x (n + 3L)
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
 
@@ -139,6 +142,7 @@ struct zs_ba_handle {
         owned.clear();
         P = DevProblem{};
         W = DevWork{};
+        adj_rec = adj_part = adj_vec = nullptr;
         has_problem = false;
     }
 };
@@ -743,6 +747,156 @@ int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, dou
     } catch (const CudaError& e) {
         return cuda_status(e.err);
     }
+}
+
+int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dloss_dlandmark, double* dloss_duv,
+                  double* dloss_dintrinsics, double* adjoint_state, zs_ba_adjoint_report* rep) {
+    if (!h) return ZS_ERR_INVALID;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (h->tsize != 8 || h->P.loss.kind != ZS_LOSS_NONE) return ZS_ERR_UNSUPPORTED;
+    DevProblem& P = h->P;
+    DevWork& W = h->W;
+    cudaStream_t s = h->stream;
+    const int n = P.n;
+    const int64_t N = (int64_t)n + 3LL * P.L;
+    int status = ZS_OK;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        ZS_CUDA(cudaEventRecord(h->ev0, s));
+        if (!h->adj_rec) {
+            h->adj_rec = dalloc<double>((size_t)std::max<int64_t>(P.M, 1) * kAdjRecord, h->owned);
+            h->adj_part = dalloc<double>((size_t)std::max<int64_t>(P.M, 1) * 9, h->owned);
+            h->adj_vec = dalloc<double>((size_t)std::max<int64_t>(N, 1) * 7, h->owned);
+        }
+        double* a = h->adj_vec;
+        double* v = a + N;
+        double* r = v + N;
+        double* z = r + N;
+        double* pv = z + N;
+        double* q = pv + N;
+        double* zero = q + N;
+        // a = dL/dx (local coordinates)
+        std::vector<double> ah((size_t)N, 0.0);
+        for (int k = 0; k < P.K && dloss_dpose; ++k)
+            for (int i = 0; i < 6; ++i) ah[6 * (size_t)k + i] = dloss_dpose[6 * (size_t)k + i];
+        for (int l = 0; l < P.L && dloss_dlandmark; ++l)
+            for (int i = 0; i < 3; ++i) ah[(size_t)n + 3 * (size_t)l + i] = dloss_dlandmark[3 * (size_t)l + i];
+        if (N > 0) ZS_CUDA(cudaMemcpyAsync(a, ah.data(), N * sizeof(double), cudaMemcpyHostToDevice, s));
+        ZS_CUDA(cudaMemsetAsync(v, 0, std::max<int64_t>(N, 1) * sizeof(double), s));
+        ZS_CUDA(cudaMemsetAsync(zero, 0, std::max<int64_t>(N, 1) * sizeof(double), s));
+        // Gauss-Newton linearisation and its lightly damped factorisation:
+        // the preconditioner M = H_GN + lambda I.
+        linearize<double>(h);
+        launch_adj_prep(P, h->adj_rec, s);
+        launch_cost(P, W, h->st, false, s);
+        launch_init_lambda(P, W, h->st, h->opt.tau, h->opt.diagonal_clamp, s);
+        read_state(h);
+        LmState init{};
+        init.lambda = 1e-9 * std::max(h->st_host->max_diag, 1e-300);
+        init.nu = 2.0;
+        init.solve_ok = 1;
+        ZS_CUDA(cudaMemcpyAsync(h->st, &init, sizeof(LmState), cudaMemcpyHostToDevice, s));
+        launch_invert_w<double>(P, W, h->st, s);
+        launch_schur<double>(P, W, h->st, s);
+        ZS_CUDA((launch_factor<double, double>(n, W.S, (double*)W.F, (double*)W.D, h->st, s)));
+        read_state(h);
+        if (!h->st_host->solve_ok) {
+            status = ZS_ERR_CHOLESKY;
+        } else {
+            std::vector<double> red(kReduceBlocks * 4);
+            auto dot = [&](const double* x, const double* y) {
+                launch_adj_dot(N, x, y, W.red, s);
+                ZS_CUDA(cudaMemcpyAsync(red.data(), W.red, kReduceBlocks * sizeof(double), cudaMemcpyDeviceToHost, s));
+                ZS_CUDA(cudaStreamSynchronize(s));
+                double t = 0.0;
+                for (int i = 0; i < kReduceBlocks; ++i) t += red[i];
+                return t;
+            };
+            // z = M^-1 x through the Schur complement and the reduced factor
+            auto precondition = [&](const double* x, double* out) {
+                launch_adj_copy(N, x, W.b, s);
+                launch_bs<double>(P, W, s);
+                ZS_CUDA((launch_solve_refine<double, double>(n, W.S, (const double*)W.F, (const double*)W.D, W.bs,
+                                                             W.delta, W.work, h->st, 0, 0.0, s)));
+                launch_backsub<double>(P, W, h->st, s);
+                launch_adj_copy(N, W.delta, out, s);
+            };
+            launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, r, s);  // r = a, fixed entries zeroed
+            const double anorm = std::sqrt(dot(r, r));
+            double rn = anorm;
+            int it = 0;
+            const int max_it = 200;
+            if (anorm > 0.0) {
+                precondition(r, z);
+                launch_adj_copy(N, z, pv, s);
+                double rz = dot(r, z);
+                if (h->opt.verbose)
+                    std::fprintf(stderr, "zs adjoint: |a| %.6e  r.Mr %.6e  |M^-1 a| %.6e\n", anorm, rz,
+                                 std::sqrt(dot(z, z)));
+                while (it < max_it) {
+                    launch_adj_residual(P, h->adj_rec, pv, zero, h->adj_part, q, s);  // q = -H p
+                    const double pAp = -dot(pv, q);
+                    if (h->opt.verbose) std::fprintf(stderr, "zs adjoint: it %3d  p.Hp %.6e", it, pAp);
+                    if (!(pAp > 0.0)) {  // H not positive definite along p
+                        if (h->opt.verbose) std::fprintf(stderr, "\n");
+                        break;
+                    }
+                    const double alpha = rz / pAp;
+                    launch_adj_axpby(N, alpha, pv, 1.0, v, s);  // v += alpha p
+                    launch_adj_axpby(N, alpha, q, 1.0, r, s);   // r -= alpha H p
+                    ++it;
+                    rn = std::sqrt(dot(r, r));
+                    if (h->opt.verbose) std::fprintf(stderr, "  |r|/|a| %.6e\n", rn / anorm);
+                    if (rn <= 1e-13 * anorm) break;
+                    precondition(r, z);
+                    const double rz_new = dot(r, z);
+                    launch_adj_axpby(N, 1.0, z, rz_new / rz, pv, s);  // p = z + beta p
+                    rz = rz_new;
+                }
+                // the true residual of the returned v
+                launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, r, s);
+                rn = std::sqrt(dot(r, r));
+            }
+            // outputs from v
+            double* duv_dev = h->adj_part;  // 2M doubles of scratch
+            launch_adj_out(P, h->adj_rec, v, duv_dev, W.red, s);
+            std::vector<double> duv((size_t)std::max<int64_t>(P.M, 1) * 2);
+            if (P.M > 0)
+                ZS_CUDA(cudaMemcpyAsync(duv.data(), duv_dev, 2 * P.M * sizeof(double), cudaMemcpyDeviceToHost, s));
+            ZS_CUDA(cudaMemcpyAsync(red.data(), W.red, kReduceBlocks * 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            ZS_CUDA(cudaStreamSynchronize(s));
+            if (dloss_duv)
+                for (int64_t i = 0; i < P.M; ++i) {
+                    dloss_duv[2 * h->perm[i]] = duv[2 * i];
+                    dloss_duv[2 * h->perm[i] + 1] = duv[2 * i + 1];
+                }
+            if (dloss_dintrinsics)
+                for (int c = 0; c < 4; ++c) {
+                    double t = 0.0;
+                    for (int b = 0; b < kReduceBlocks; ++b) t += red[4 * b + c];
+                    dloss_dintrinsics[c] = t;
+                }
+            if (adjoint_state && N > 0)
+                ZS_CUDA(cudaMemcpy(adjoint_state, v, N * sizeof(double), cudaMemcpyDeviceToHost));
+            if (rep) {
+                rep->iterations = it;
+                rep->rel_residual = anorm > 0 ? rn / anorm : 0.0;
+            }
+        }
+        ZS_CUDA(cudaEventRecord(h->ev1, s));
+        ZS_CUDA(cudaEventSynchronize(h->ev1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        if (rep) {
+            rep->ms_total = ms;
+            rep->status = status;
+        }
+    } catch (const CudaError& e) {
+        status = cuda_status(e.err);
+        if (rep) rep->status = status;
+    }
+    return status;
 }
 
 int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lout, double* x, int precision) {

@@ -102,6 +102,9 @@ template <typename T>
 void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s);
 template <typename T>
 void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s);
+// b_s = b_p - W b_l from the current W.b (no other Schur work).
+template <typename T>
+void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s);
 void launch_update(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s);
 void launch_rollback(const DevProblem& P, const LmState* st, cudaStream_t s);
 void launch_scale(const DevProblem& P, DevWork& W, LmState* st, cudaStream_t s);
@@ -110,6 +113,16 @@ void launch_cost(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, 
 void launch_init_lambda(const DevProblem& P, DevWork& W, LmState* st, double tau, double clamp, cudaStream_t s);
 void launch_decide(LmState* st, cudaStream_t s);
 void launch_set_solve_ok(LmState* st, int v, cudaStream_t s);
+
+// ---- adjoint (ba_adjoint.cu) ----
+constexpr int kAdjRecord = 64;  // doubles per observation in the adjoint record
+void launch_adj_prep(const DevProblem& P, double* rec, cudaStream_t s);
+void launch_adj_residual(const DevProblem& P, const double* rec, const double* v, const double* a, double* part,
+                         double* out, cudaStream_t s);
+void launch_adj_axpby(int64_t N, double alpha, const double* x, double beta, double* y, cudaStream_t s);
+void launch_adj_dot(int64_t N, const double* x, const double* y, double* red, cudaStream_t s);
+void launch_adj_copy(int64_t N, const double* src, double* dst, cudaStream_t s);
+void launch_adj_out(const DevProblem& P, const double* rec, const double* v, double* duv, double* red, cudaStream_t s);
 
 // ---- dense reduced system (ba_cholesky.cu) ----
 // launch_factor: S (n x n row-major, type TS) -> F = L (lower, type TF) and

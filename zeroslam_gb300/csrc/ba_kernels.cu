@@ -699,6 +699,11 @@ void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream
 }
 
 template <typename T>
+void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s) {
+    if (P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
+}
+
+template <typename T>
 void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
     if (P.L > 0) { k_backsub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st); note_launch(); }
 }
@@ -737,6 +742,7 @@ template void launch_invert_w<float>(const DevProblem&, DevWork&, const LmState*
 template void launch_schur<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 template void launch_schur<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 template void launch_backsub<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_bs<double>(const DevProblem&, DevWork&, cudaStream_t);
 template void launch_backsub<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 
 }  // namespace zs

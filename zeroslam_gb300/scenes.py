@@ -332,7 +332,8 @@ def _perturb_poses(q, t, rng, sig_rot, sig_trans, drift=None):
 
 def arc_scene(K: int = 10, L: int = 500, seed: int = 0, iterations: int = 10,
               sigma_px: float = 1.0, rot_sigma: float = 0.02, trans_sigma: float = 0.05,
-              landmark_rel_noise: float = 0.05, huber: bool = False, name: str | None = None) -> Scene:
+              landmark_rel_noise: float = 0.05, huber: bool = False, name: str | None = None,
+              min_obs: int = 1) -> Scene:
     """K keyframes on a 1 m radius arc (36 degree span) in the x-z plane, each
     optical axis through the origin; L landmarks uniform in [-2,2]^2 x [1,7]."""
     rng = Pcg32Streams(seed)
@@ -341,7 +342,7 @@ def arc_scene(K: int = 10, L: int = 500, seed: int = 0, iterations: int = 10,
     q_gt, t_gt = yaw_pose(centre, -theta)
     C = 2 * L + 64  # candidates; the first L that some camera sees are kept
     X = np.stack([rng.uniform(C, -2.0, 2.0), rng.uniform(C, -2.0, 2.0), rng.uniform(C, 1.0, 7.0)], 1)
-    kept, obs_pose, obs_lm, obs_uv = _observe(q_gt, t_gt, X, rng, sigma_px, 1e-12, np.inf, L, 1)
+    kept, obs_pose, obs_lm, obs_uv = _observe(q_gt, t_gt, X, rng, sigma_px, 1e-12, np.inf, L, min_obs)
     X = X[kept]
     q0, t0 = _perturb_poses(q_gt, t_gt, rng, rot_sigma, trans_sigma)
     X0 = X * (1.0 + landmark_rel_noise * rng.normal(3 * L).reshape(L, 3))
@@ -441,8 +442,23 @@ def large_scene(seed: int = 1) -> Scene:
     return walk_scene(seed=seed)
 
 
-def adjoint_scene(seed: int = 3) -> Scene:
-    return arc_scene(50, 10000, seed=seed, iterations=50)
+ADJOINT_INIT_NOISE = dict(rot_sigma=0.002, trans_sigma=0.005, landmark_rel_noise=0.005)
+
+
+def adjoint_scene(K: int = 50, L: int = 10000, seed: int = 3) -> Scene:
+    """The differentiable-BA scene: the arc generator at 50 keyframes and
+    10,000 landmarks, every landmark seen at least twice, and poses 0 and 1
+    fixed (zeroslam's own gauge for windows of more than two frames,
+    source/map.hpp:134), so the converged solution is an isolated point.
+    The initial guess is close to the truth (0.1 degree, 5 mm, 0.5% of the
+    landmark coordinates), as for a tracked estimate that is refined: from
+    the generator's default 5% landmark noise a few landmarks settle in poor
+    local minima (behind a camera, or on a near-degenerate ray) and the
+    Hessian at the solution is singular to working precision."""
+    sc = arc_scene(K, L, seed=seed, iterations=50, min_obs=2, name=f"adjoint_K{K}_L{L}_s{seed}",
+                   **ADJOINT_INIT_NOISE)
+    sc.pose_fixed[1] = 1
+    return sc
 
 
 def loop_large_scene(seed: int = 4) -> Scene:
