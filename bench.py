@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-windows measurement")
+    ap.add_argument("--batch-windows", type=int, default=256)
     ap.add_argument("--single", choices=["mixed", "fp64"], default=None,
                     help="run one solve of --iterations (default 2) on the workload and exit; for profilers")
     return ap.parse_args()
@@ -217,6 +219,61 @@ def run_solves(sc, precision: int, steps: int, warmup: int, iters: int, device: 
     return dict(ms=ms, iterations=it, launches=launches, chi2=final_chi2, rep=reps[-1].as_dict())
 
 
+def batch_run(wins, precision: int, steps: int, warmup: int, iters: int, device: int, dist: Dist) -> dict:
+    """The batched windows: each step restores the initial states on the
+    device (outside the timed region) and runs zs_ba_solve_batch, one graph
+    launch timed with CUDA events on the handle's stream."""
+    from zeroslam_gb300 import ba
+
+    with ba.BundleAdjuster(precision=precision, device=device) as h:
+        h.set_batch(wins)
+        for _ in range(warmup):
+            h.reset_state()
+            h.solve_batch(iters)
+        dist.barrier()
+        ms = 0.0
+        it = 0
+        obs_att = 0
+        launches = 0
+        for _ in range(steps):
+            h.reset_state()
+            _, reps, brep = h.solve_batch(iters)
+            ms += brep.ms_total
+            it += sum(r.iterations for r in reps)
+            obs_att += sum(r.attempts * w.M for r, w in zip(reps, wins))
+            launches += brep.kernel_launches
+        dist.barrier()
+        return dict(ms=ms, iterations=it, obs_attempts=obs_att, launches=launches,
+                    chi2=np.array([r.chi2_final for r in reps]), brep=brep.as_dict())
+
+
+def batch_section(args, dist: Dist) -> dict:
+    """256 independent windows (K in [5, 30], L in [200, 3000]), 10 LM
+    iterations each, mixed and FP64, each a single graph launch."""
+    from zeroslam_gb300 import scenes
+
+    wins = scenes.window_batch(args.batch_windows)
+    iters = 10
+    m = batch_run(wins, 1, args.steps, args.warmup, iters, dist.local, dist)
+    d = batch_run(wins, 0, args.steps, args.warmup, iters, dist.local, dist)
+    M = sum(w.M for w in wins)
+    out = {"workload": f"{len(wins)} windows, K in [5, 30] (sum {sum(w.K for w in wins)}), L in [200, 3000] "
+                       f"(sum {sum(w.L for w in wins)}), M = {M} observations, {iters} LM iterations each",
+           "windows": len(wins), "observations": M}
+    for key, r in (("mixed", m), ("fp64", d)):
+        sec = dist.max(r["ms"]) * 1e-3
+        out[key] = {"windows_per_s": dist.sum(len(wins) * args.steps) / sec,
+                    "lm_iters_per_s": dist.sum(r["iterations"]) / sec,
+                    "obs_per_s": dist.sum(r["obs_attempts"]) / sec,
+                    "ms_per_batch": dist.max(r["ms"]) / args.steps,
+                    "rounds": r["brep"]["rounds"], "graph_launches_per_batch": r["brep"]["graph_launches"],
+                    "kernel_launches_per_batch": r["launches"] / args.steps,
+                    "bucket_windows": r["brep"]["bucket_windows"], "bucket_threads": r["brep"]["bucket_threads"]}
+    out["mixed_over_fp64"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
+    out["max_rel_cost_mixed_vs_fp64"] = float(np.max(np.abs(m["chi2"] - d["chi2"]) / d["chi2"]))
+    return out
+
+
 def profile_solve(sc, precision: int, iters: int, device: int) -> dict:
     from zeroslam_gb300 import ba
 
@@ -333,6 +390,8 @@ def ours_arm(args, dist: Dist):
     fp64 = run_solves(sc, ba.FP64, args.steps, args.warmup, iters, device, dist)
     clk = clocks.stop()
 
+    batch = None if args.no_batch else batch_section(args, dist)
+
     prof_m = profile_solve(sc, ba.MIXED, iters, device)
     prof_d = profile_solve(sc, ba.FP64, iters, device)
     roof_m = phase_roofline(sc, prof_m, 1, peaks, hbm)
@@ -385,6 +444,7 @@ def ours_arm(args, dist: Dist):
         "e2e": e2e,
         "clocks": clk,
         "gpu_launches": int(dist.sum(mixed["launches"])),
+        "batched_windows": batch,
     }
     print(json.dumps(line), flush=True)
 

@@ -78,6 +78,10 @@ typedef struct zs_ba_options {
     int32_t device;             /* CUDA device ordinal (0) */
     int32_t verbose;            /* 1: print [INIT]/[GOOD]/[ BAD] lines to stderr */
     int32_t profile;            /* 1: time each phase with CUDA events into zs_ba_report.ms_phase */
+    int32_t batch_graph;        /* batched solve: 1 = one CUDA graph launch (conditional WHILE
+                                   node over attempt rounds), 0 = host loop over rounds (1) */
+    const char* autotune_cache; /* batched solve: file of autotuned block sizes (read, and written
+                                   after tuning), or NULL for a per-process cache only */
 } zs_ba_options;
 
 /* A bundle-adjustment problem as structure of arrays (host pointers).
@@ -169,6 +173,44 @@ typedef struct zs_ba_adjoint_report {
     double rel_residual;     /* ||a - H v|| / ||a|| at exit */
     double ms_total;
 } zs_ba_adjoint_report;
+
+/* ---- Batched local windows ----
+ * Many independent windows (each a complete problem as for zs_ba_set_problem)
+ * solved together on one device: the reference runs one factor_graph per
+ * window (map::optimise, source/map.hpp:65-267, calling
+ * factor_graph::solve, source/factor_graph.hpp:489-615); here every window
+ * runs the same LM control flow with its own damping, acceptance and stop
+ * decisions, in one CUDA graph launch. All windows share the intrinsics, the
+ * loss and the presence of obs_info; each window has at most
+ * ZS_BATCH_MAX_POSES poses. */
+#define ZS_BATCH_MAX_POSES 32
+#define ZS_BATCH_BUCKETS 5
+
+typedef struct zs_ba_batch_report {
+    int32_t status;
+    int32_t windows;
+    int32_t rounds;                           /* attempt rounds run (each: one attempt per active window) */
+    int32_t graph_launches;                   /* 1 when the solve ran as one graph launch, else 0 */
+    int64_t kernel_launches;                  /* kernels executed: prologue + rounds x round body */
+    int64_t attempts;                         /* summed over windows */
+    int64_t accepted;                         /* summed over windows */
+    double ms_total;                          /* device time of the batched solve (CUDA events) */
+    int32_t bucket_windows[ZS_BATCH_BUCKETS]; /* windows per reduced-system size bucket (n <= 64, 96, 128, 160, 192) */
+    int32_t bucket_threads[ZS_BATCH_BUCKETS]; /* autotuned block size of each bucket's reduced solve */
+    float bucket_tune_us[ZS_BATCH_BUCKETS];   /* autotuner's best time (synthetic 2 x SMs windows), 0 if cached */
+} zs_ba_batch_report;
+
+/* Uploads num_windows windows (an array of problems) as one batch; replaces
+ * any problem of the handle. */
+int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windows);
+/* Solves every window of the batch as zs_ba_solve would (same iterations /
+ * use_relative semantics per window). window_reports (may be NULL): one
+ * report per window; rep (may be NULL): the batch summary. Returns the
+ * accepted steps summed over windows, or a negative status. */
+int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* window_reports,
+                      zs_ba_batch_report* rep);
+/* Current state of one window ([K_w*7], [L_w*3]; either may be NULL). */
+int zs_ba_get_window_state(zs_ba_handle* h, int window, double* poses, double* landmarks);
 
 /* Gradient of a scalar loss of the solved state with respect to the observed
  * pixels and the intrinsics, by the implicit-function theorem at the current

@@ -38,7 +38,8 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_failures", C.c_int32), ("tau", C.c_double),
                 ("diagonal_clamp", C.c_double), ("legacy_stop", C.c_double), ("relative_tolerance", C.c_double),
                 ("chi2_floor", C.c_double), ("refine_iterations", C.c_int32), ("refine_tolerance", C.c_double),
-                ("device", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32)]
+                ("device", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32),
+                ("batch_graph", C.c_int32), ("autotune_cache", C.c_char_p)]
 
 
 class Problem(C.Structure):
@@ -63,6 +64,19 @@ class Report(C.Structure):
         return d
 
 
+class BatchReport(C.Structure):
+    _fields_ = [("status", C.c_int32), ("windows", C.c_int32), ("rounds", C.c_int32), ("graph_launches", C.c_int32),
+                ("kernel_launches", C.c_int64), ("attempts", C.c_int64), ("accepted", C.c_int64),
+                ("ms_total", C.c_double), ("bucket_windows", C.c_int32 * 5), ("bucket_threads", C.c_int32 * 5),
+                ("bucket_tune_us", C.c_float * 5)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("bucket_")}
+        for k in ("bucket_windows", "bucket_threads", "bucket_tune_us"):
+            d[k] = list(getattr(self, k))
+        return d
+
+
 class AdjointReport(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_residual", C.c_double),
                 ("ms_total", C.c_double)]
@@ -84,7 +98,8 @@ _LIB = None
 ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
-                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint")
+                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
+                 "zs_ba_solve_batch", "zs_ba_get_window_state")
 
 
 def library_path() -> str:
@@ -132,6 +147,12 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_last_error.argtypes = []
     lib.zs_ba_adjoint.restype = C.c_int
     lib.zs_ba_adjoint.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, C.POINTER(AdjointReport)]
+    lib.zs_ba_set_batch.restype = C.c_int
+    lib.zs_ba_set_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(Problem)]
+    lib.zs_ba_solve_batch.restype = C.c_int
+    lib.zs_ba_solve_batch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(Report), C.POINTER(BatchReport)]
+    lib.zs_ba_get_window_state.restype = C.c_int
+    lib.zs_ba_get_window_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
     lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
     _LIB = lib
@@ -181,8 +202,10 @@ class BundleAdjuster:
     def __exit__(self, *a):
         self.close()
 
-    def set_problem(self, scene) -> None:
-        self._keep = dict(
+    @staticmethod
+    def _problem(scene, p=None):
+        """Fills a Problem from a scene; returns (problem, arrays that must stay alive)."""
+        k = dict(
             poses=np.ascontiguousarray(scene.poses, dtype=np.float64),
             pose_fixed=np.ascontiguousarray(scene.pose_fixed, dtype=np.uint8),
             landmarks=np.ascontiguousarray(scene.landmarks, dtype=np.float64),
@@ -192,8 +215,7 @@ class BundleAdjuster:
             obs_uv=np.ascontiguousarray(scene.obs_uv, dtype=np.float64),
             obs_info=None if scene.obs_info is None else np.ascontiguousarray(scene.obs_info, dtype=np.float64),
         )
-        k = self._keep
-        p = Problem()
+        p = Problem() if p is None else p
         p.num_poses = k["poses"].shape[0]
         p.num_landmarks = k["landmarks"].shape[0]
         p.num_obs = k["obs_pose"].shape[0]
@@ -209,6 +231,43 @@ class BundleAdjuster:
             p.intrinsics[i] = float(scene.intrinsics[i])
         p.loss_kind = int(scene.loss_kind)
         p.loss_delta = float(scene.loss_delta)
+        return p, k
+
+    def set_batch(self, scenes) -> None:
+        """Uploads independent windows (zs_ba_set_batch)."""
+        arr = (Problem * len(scenes))()
+        keep = []
+        for i, sc in enumerate(scenes):
+            keep.append(self._problem(sc, arr[i])[1])
+        st = self.lib.zs_ba_set_batch(self.h, len(scenes), arr)
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_set_batch")
+        self._keep = keep
+        self.windows = [(a["poses"].shape[0], a["landmarks"].shape[0]) for a in keep]
+        self.K = sum(k for k, _ in self.windows)
+        self.L = sum(l for _, l in self.windows)
+        self.M = sum(a["obs_pose"].shape[0] for a in keep)
+
+    def solve_batch(self, iterations: int, use_relative: bool = False):
+        """(accepted summed over windows, [Report per window], BatchReport)."""
+        reps = (Report * len(self.windows))()
+        brep = BatchReport()
+        v = self.lib.zs_ba_solve_batch(self.h, int(iterations), int(bool(use_relative)), reps, C.byref(brep))
+        if v < 0:
+            raise ZsError(v, "zs_ba_solve_batch")
+        return v, list(reps), brep
+
+    def get_window_state(self, w: int):
+        K, L = self.windows[w]
+        P = np.zeros((K, 7))
+        Lm = np.zeros((L, 3))
+        st = self.lib.zs_ba_get_window_state(self.h, int(w), _p(P, _dp), _p(Lm, _dp))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_get_window_state")
+        return P, Lm
+
+    def set_problem(self, scene) -> None:
+        p, self._keep = self._problem(scene)
         st = self.lib.zs_ba_set_problem(self.h, C.byref(p))
         if st != ZS_OK:
             raise ZsError(st, "zs_ba_set_problem")

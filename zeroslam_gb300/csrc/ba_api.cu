@@ -12,7 +12,12 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <set>
+#include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/zeroslam_ba.h"
@@ -136,13 +141,35 @@ struct zs_ba_handle {
     double* adj_vec = nullptr;   // a, v, r, z, p, q, zero: 7 x (n + 3L)
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
+    // batched windows
+    bool batch = false;
+    BatchDev B;
+    std::vector<int32_t> wpose0, wlm0;  // first pose / landmark of each window, plus the end
+    cudaGraph_t bgraph = nullptr;
+    cudaGraphExec_t bexec = nullptr;
+    int bgraph_iters = -1, bgraph_rel = -1;
+    long long bbody_launches = 0, bpro_launches = 0;
+    float tune_us[kBatchBuckets] = {0};
+
+    void release_graph() {
+        if (bexec) cudaGraphExecDestroy(bexec);
+        if (bgraph) cudaGraphDestroy(bgraph);
+        bexec = nullptr;
+        bgraph = nullptr;
+        bgraph_iters = bgraph_rel = -1;
+    }
 
     void release_problem() {
+        release_graph();
         for (void* p : owned) cudaFree(p);
         owned.clear();
         P = DevProblem{};
         W = DevWork{};
         adj_rec = adj_part = adj_vec = nullptr;
+        batch = false;
+        B = BatchDev{};
+        wpose0.clear();
+        wlm0.clear();
         has_problem = false;
     }
 };
@@ -163,6 +190,8 @@ void zs_ba_default_options(zs_ba_options* o) {
     o->refine_tolerance = 1e-10;
     o->device = 0;
     o->verbose = 0;
+    o->batch_graph = 1;
+    o->autotune_cache = nullptr;
 }
 
 const char* zs_ba_status_string(int s) {
@@ -260,11 +289,20 @@ static int validate(const zs_ba_problem* p) {
 }
 
 // Builds the device orderings and the Schur pair/triple lists, uploads the
-// problem and allocates the working arrays of the handle's precision.
-static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
+// problem and allocates the working arrays of the handle's precision. With
+// windows (wpose0 / wlm0: first pose / landmark of each window, plus the
+// end), the problem is a batch of independent windows: pairs stay inside a
+// window and S is block diagonal; without, it is one problem.
+static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::vector<int32_t>* wpose0 = nullptr,
+                          const std::vector<int32_t>* wlm0 = nullptr) {
     cudaStream_t s = h->stream;
     const int K = p->num_poses, L = p->num_landmarks;
     const int64_t M = p->num_obs;
+    const bool batched = wpose0 != nullptr;
+    const std::vector<int32_t> one_p{0, K}, one_l{0, L};
+    const std::vector<int32_t>& wp = batched ? *wpose0 : one_p;
+    const std::vector<int32_t>& wl = batched ? *wlm0 : one_l;
+    const int nwin = (int)wp.size() - 1;
     DevProblem& P = h->P;
     P.K = K;
     P.L = L;
@@ -313,22 +351,37 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
     }
     // Schur triples: for each landmark, every (block a, block b) with pose_a >= pose_b,
     // grouped by pose pair (i, j) = (pose_a, pose_b), landmark order within a pair.
-    std::vector<int64_t> pair_count((size_t)K * K, 0);
+    // Pair keys are window-local: key = base_w + (i - p0_w) K_w + (j - p0_w).
+    std::vector<int32_t> pose_win(K, 0), lm_win(L, 0);
+    std::vector<int64_t> key_base(nwin + 1, 0);
+    for (int w = 0; w < nwin; ++w) {
+        const int64_t kw = wp[w + 1] - wp[w];
+        key_base[w + 1] = key_base[w] + kw * kw;
+        for (int k = wp[w]; k < wp[w + 1]; ++k) pose_win[k] = w;
+        for (int l = wl[w]; l < wl[w + 1]; ++l) lm_win[l] = w;
+    }
+    auto pair_key = [&](int i, int j) {
+        const int w = pose_win[i];
+        const int64_t kw = wp[w + 1] - wp[w];
+        return (size_t)(key_base[w] + (int64_t)(i - wp[w]) * kw + (j - wp[w]));
+    };
+    const size_t nkeys = (size_t)key_base[nwin];
+    std::vector<int64_t> pair_count(nkeys, 0);
     std::vector<int32_t> vb;
     for (int l = 0; l < L; ++l) {
         vb.clear();
         for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
             if (blk_valid[i]) vb.push_back(i);
         for (size_t a = 0; a < vb.size(); ++a)
-            for (size_t b = 0; b <= a; ++b) pair_count[(size_t)obs_pose[vb[a]] * K + obs_pose[vb[b]]]++;
+            for (size_t b = 0; b <= a; ++b) pair_count[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++;
     }
-    std::vector<int64_t> pair_off((size_t)K * K + 1, 0);
+    std::vector<int64_t> pair_off(nkeys + 1, 0);
     int npairs = 0;
-    for (size_t k = 0; k < (size_t)K * K; ++k) {
+    for (size_t k = 0; k < nkeys; ++k) {
         pair_off[k + 1] = pair_off[k] + pair_count[k];
         if (pair_count[k]) ++npairs;
     }
-    const int64_t ntriples = pair_off[(size_t)K * K];
+    const int64_t ntriples = pair_off[nkeys];
     std::vector<int2> triples(ntriples);
     {
         std::vector<int64_t> fill(pair_off.begin(), pair_off.end() - 1);
@@ -338,20 +391,23 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
                 if (blk_valid[i]) vb.push_back(i);
             for (size_t a = 0; a < vb.size(); ++a)
                 for (size_t b = 0; b <= a; ++b)
-                    triples[fill[(size_t)obs_pose[vb[a]] * K + obs_pose[vb[b]]]++] = make_int2(vb[a], vb[b]);
+                    triples[fill[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++] = make_int2(vb[a], vb[b]);
         }
     }
     std::vector<int32_t> pair_i, pair_j;
     std::vector<int64_t> pair_chunk_ptr{0}, chunk_ptr{0};
     pair_i.reserve(npairs);
     pair_j.reserve(npairs);
-    for (size_t k = 0; k < (size_t)K * K; ++k) {
-        if (!pair_count[k]) continue;
-        pair_i.push_back((int32_t)(k / K));
-        pair_j.push_back((int32_t)(k % K));
-        for (int64_t t = pair_off[k]; t < pair_off[k + 1]; t += kChunk)
-            chunk_ptr.push_back(std::min<int64_t>(t + kChunk, pair_off[k + 1]));
-        pair_chunk_ptr.push_back((int64_t)chunk_ptr.size() - 1);
+    for (int w = 0; w < nwin; ++w) {
+        const int64_t kw = wp[w + 1] - wp[w];
+        for (int64_t k = key_base[w]; k < key_base[w + 1]; ++k) {
+            if (!pair_count[k]) continue;
+            pair_i.push_back((int32_t)(wp[w] + (k - key_base[w]) / kw));
+            pair_j.push_back((int32_t)(wp[w] + (k - key_base[w]) % kw));
+            for (int64_t t = pair_off[k]; t < pair_off[k + 1]; t += kChunk)
+                chunk_ptr.push_back(std::min<int64_t>(t + kChunk, pair_off[k + 1]));
+            pair_chunk_ptr.push_back((int64_t)chunk_ptr.size() - 1);
+        }
     }
     P.npairs = npairs;
     P.ntriples = ntriples;
@@ -389,6 +445,36 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
     P.pair_chunk_ptr = upload(pair_chunk_ptr, own, s);
     P.chunk_ptr = upload(chunk_ptr, own, s);
     P.triples = upload(triples, own, s);
+    P.nwin = nwin;
+    std::vector<int64_t> win_s_off(nwin, 0);
+    int64_t s_total = 0;
+    for (int w = 0; w < nwin; ++w) {
+        win_s_off[w] = s_total;
+        const int64_t nw = 6LL * (wp[w + 1] - wp[w]);
+        s_total += nw * nw;
+    }
+    if (batched) {
+        // observation chunks for per-window cost sums, never across windows
+        std::vector<int64_t> ochunk_ptr{0};
+        std::vector<int32_t> ochunk_win, win_ochunk{0};
+        for (int w = 0; w < nwin; ++w) {
+            const int64_t o0 = lm_ptr[wl[w]], o1 = lm_ptr[wl[w + 1]];
+            for (int64_t o = o0; o < o1; o += kBatchObsChunk) {
+                ochunk_ptr.push_back(std::min<int64_t>(o + kBatchObsChunk, o1));
+                ochunk_win.push_back(w);
+            }
+            win_ochunk.push_back((int32_t)ochunk_win.size());
+        }
+        P.nochunks = (int64_t)ochunk_win.size();
+        P.pose_win = upload(pose_win, own, s);
+        P.lm_win = upload(lm_win, own, s);
+        P.win_pose0 = upload(wp, own, s);
+        P.win_lm0 = upload(wl, own, s);
+        P.win_s_off = upload(win_s_off, own, s);
+        P.ochunk_ptr = upload(ochunk_ptr, own, s);
+        P.ochunk_win = upload(ochunk_win, own, s);
+        P.win_ochunk = upload(win_ochunk, own, s);
+    }
 
     const size_t ts = (size_t)h->tsize;
     const int n = P.n;
@@ -404,17 +490,19 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p) {
     W.hll_inv = dalloc<double>((size_t)L * 9, own);
     W.b = dalloc<double>((size_t)n + 3 * (size_t)L, own);
     W.partial = dalloc<char>(ts * 36 * (size_t)P.nchunks, own);
-    W.S = dalloc<double>((size_t)n * n, own);
-    W.F = dalloc<char>(ts * (size_t)n * n, own);
+    W.S = dalloc<double>((size_t)s_total, own);
     W.bs = dalloc<double>(n, own);
-    W.D = dalloc<char>(ts * 1024 * (size_t)((n + 31) / 32), own);
-    W.work = dalloc<double>(4 * (size_t)n + 256, own);
-    if (h->tsize == 4) {
-        W.X = dalloc<char>(ts * (size_t)n * n, own);
-        W.XT = dalloc<char>(ts * (size_t)n * n, own);
+    if (!batched) {
+        W.F = dalloc<char>(ts * (size_t)n * n, own);
+        W.D = dalloc<char>(ts * 1024 * (size_t)((n + 31) / 32), own);
+        W.work = dalloc<double>(4 * (size_t)n + 256, own);
+        if (h->tsize == 4) {
+            W.X = dalloc<char>(ts * (size_t)n * n, own);
+            W.XT = dalloc<char>(ts * (size_t)n * n, own);
+        }
     }
     W.delta = dalloc<double>((size_t)n + 3 * (size_t)L, own);
-    W.red = dalloc<double>(kReduceBlocks * 4, own);
+    W.red = dalloc<double>(std::max<size_t>(kReduceBlocks * 4, (size_t)P.nochunks), own);
     W.ired = dalloc<int32_t>(kReduceBlocks, own);
     ZS_CUDA(cudaMemsetAsync(W.hll_inv, 0, sizeof(double) * 9 * (size_t)std::max(L, 1), s));
     ZS_CUDA(cudaMemsetAsync(W.delta, 0, sizeof(double) * std::max<size_t>(1, (size_t)n + 3 * (size_t)L), s));
@@ -686,6 +774,7 @@ int zs_ba_solve(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report*
     if (!h) return ZS_ERR_INVALID;
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (h->batch) return ZS_ERR_UNSUPPORTED;  // zs_ba_solve_batch
     // source/factor_graph.hpp:494-499: nothing to do without edges or vertices
     if (h->P.M == 0 || (h->P.K == 0 && h->P.L == 0)) return 0;
     if (iterations < 0) return ZS_ERR_INVALID;
@@ -740,6 +829,7 @@ int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda) {
 int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b) {
     if (!h) return ZS_ERR_INVALID;
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (h->batch) return ZS_ERR_UNSUPPORTED;
     try {
         ZS_CUDA(cudaSetDevice(h->device));
         return h->tsize == 8 ? linear_step_impl<double>(h, lambda, S, bs, delta, b)
@@ -754,7 +844,7 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
     if (!h) return ZS_ERR_INVALID;
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
-    if (h->tsize != 8 || h->P.loss.kind != ZS_LOSS_NONE) return ZS_ERR_UNSUPPORTED;
+    if (h->tsize != 8 || h->P.loss.kind != ZS_LOSS_NONE || h->batch) return ZS_ERR_UNSUPPORTED;
     DevProblem& P = h->P;
     DevWork& W = h->W;
     cudaStream_t s = h->stream;
@@ -964,6 +1054,386 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
     for (void* p : owned) cudaFree(p);
     if (s) cudaStreamDestroy(s);
     return status;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ batched windows
+
+namespace {
+
+// Autotuned reduced-solve block sizes per (device name, precision, bucket),
+// shared by all handles of the process and optionally kept in a file:
+// one JSON object per line inside {"entries": [ ... ]}.
+struct TuneCache {
+    std::mutex mu;
+    std::map<std::tuple<std::string, int, int>, int> threads;
+    std::set<std::string> loaded;
+};
+
+TuneCache& tune_cache() {
+    static TuneCache c;
+    return c;
+}
+
+void tune_load_locked(TuneCache& c, const char* path) {
+    if (!path || c.loaded.count(path)) return;
+    c.loaded.insert(path);
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    char line[512];
+    while (std::fgets(line, sizeof(line), f)) {
+        char dev[256] = {0}, prec[16] = {0};
+        int bucket = -1, threads = 0;
+        if (std::sscanf(line, " {\"device\": \"%255[^\"]\", \"precision\": \"%15[^\"]\", \"bucket\": %d, \"threads\": %d",
+                        dev, prec, &bucket, &threads) == 4 &&
+            bucket >= 0 && bucket < kBatchBuckets && (threads == 128 || threads == 256 || threads == 512 || threads == 1024)) {
+            const int ts = std::strcmp(prec, "fp64") == 0 ? 8 : 4;
+            c.threads[std::make_tuple(std::string(dev), ts, bucket)] = threads;
+        }
+    }
+    std::fclose(f);
+}
+
+void tune_save_locked(TuneCache& c, const char* path) {
+    if (!path) return;
+    FILE* f = std::fopen(path, "w");
+    if (!f) return;
+    std::fprintf(f, "{\"entries\": [\n");
+    size_t i = 0;
+    for (const auto& e : c.threads) {
+        std::fprintf(f, "  {\"device\": \"%s\", \"precision\": \"%s\", \"bucket\": %d, \"threads\": %d}%s\n",
+                     std::get<0>(e.first).c_str(), std::get<1>(e.first) == 8 ? "fp64" : "mixed", std::get<2>(e.first),
+                     e.second, ++i < c.threads.size() ? "," : "");
+    }
+    std::fprintf(f, "]}\n");
+    std::fclose(f);
+}
+
+// Block size of each present bucket: from the cache, else timed now.
+template <typename T>
+void batch_tune(zs_ba_handle* h) {
+    BatchDev& B = h->B;
+    int sms = 0;
+    ZS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    cudaDeviceProp prop;
+    ZS_CUDA(cudaGetDeviceProperties(&prop, h->device));
+    TuneCache& c = tune_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    tune_load_locked(c, h->opt.autotune_cache);
+    bool tuned = false;
+    for (int b = 0; b < kBatchBuckets; ++b) {
+        const int cnt = B.bucket_off[b + 1] - B.bucket_off[b];
+        if (cnt == 0 || B.threads[b] > 0) continue;
+        const auto key = std::make_tuple(std::string(prop.name), (int)sizeof(T), b);
+        auto it = c.threads.find(key);
+        int t = 0;
+        if (it != c.threads.end()) {
+            t = it->second;
+            h->tune_us[b] = 0.f;
+        } else {
+            int bps = 0;
+            float us = 0.f;
+            ZS_CUDA(bsolve_autotune<T>(b, sms, h->stream, &t, &bps, &us));
+            c.threads[key] = t;
+            h->tune_us[b] = us;
+            tuned = true;
+        }
+        const int per_sm = bsolve_max_blocks_per_sm<T>(b, t);  // also sets the kernel's shared-memory limit
+        if (per_sm <= 0) throw CudaError{cudaErrorInvalidConfiguration};
+        B.threads[b] = t;
+        B.blocks[b] = std::min(cnt, per_sm * sms);
+    }
+    if (tuned) tune_save_locked(c, h->opt.autotune_cache);
+}
+
+BatchParams batch_params(const zs_ba_handle* h, int iterations, bool use_relative) {
+    const zs_ba_options& o = h->opt;
+    BatchParams prm{};
+    prm.iterations = iterations;
+    prm.use_relative = use_relative ? 1 : 0;
+    prm.max_failures = o.max_failures;
+    prm.refine_iters = std::max(0, o.refine_iterations);
+    prm.max_rounds = std::max(1, iterations) * std::max(1, o.max_failures) + 1;
+    prm.use_cond = 0;
+    prm.relative_tolerance = o.relative_tolerance;
+    prm.chi2_floor = o.chi2_floor;
+    prm.legacy_stop = o.legacy_stop;
+    prm.tau = o.tau;
+    prm.clamp = o.diagonal_clamp;
+    prm.refine_tol = o.refine_tolerance;
+    prm.cond = 0;
+    return prm;
+}
+
+// The batched solve as one graph: prologue (child graph), then a
+// conditional WHILE node whose body is one attempt round; the round's last
+// kernel sets the condition to "any window still active".
+template <typename T>
+void build_batch_graph(zs_ba_handle* h, BatchParams prm) {
+    cudaStream_t s = h->stream;
+    ZS_CUDA(cudaGraphCreate(&h->bgraph, 0));
+    cudaGraph_t pro = nullptr;
+    long long c0 = launch_counter();
+    ZS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launch_batch_prologue<T>(h->P, h->W, h->B, prm, s);
+    ZS_CUDA(cudaStreamEndCapture(s, &pro));
+    h->bpro_launches = launch_counter() - c0;
+    cudaGraphNode_t npro = nullptr;
+    const cudaError_t ea = cudaGraphAddChildGraphNode(&npro, h->bgraph, nullptr, 0, pro);
+    cudaGraphDestroy(pro);
+    ZS_CUDA(ea);
+    cudaGraphConditionalHandle cond = 0;
+    ZS_CUDA(cudaGraphConditionalHandleCreate(&cond, h->bgraph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t nloop = nullptr;
+    ZS_CUDA(cudaGraphAddNode(&nloop, h->bgraph, &npro, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    prm.use_cond = 1;
+    prm.cond = cond;
+    c0 = launch_counter();
+    ZS_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t el = launch_batch_round<T>(h->P, h->W, h->B, prm, s);
+    cudaGraph_t body_out = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(s, &body_out);
+    ZS_CUDA(el);
+    ZS_CUDA(ee);
+    h->bbody_launches = launch_counter() - c0;
+    ZS_CUDA(cudaGraphInstantiate(&h->bexec, h->bgraph, 0));
+}
+
+template <typename T>
+int solve_batch_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report* wr, zs_ba_batch_report* rep) {
+    const DevProblem& P = h->P;
+    BatchDev& B = h->B;
+    cudaStream_t s = h->stream;
+    zs_ba_batch_report r{};
+    r.windows = P.nwin;
+    batch_tune<T>(h);
+    for (int b = 0; b < kBatchBuckets; ++b) {
+        r.bucket_windows[b] = B.bucket_off[b + 1] - B.bucket_off[b];
+        r.bucket_threads[b] = B.threads[b];
+        r.bucket_tune_us[b] = h->tune_us[b];
+    }
+    BatchParams prm = batch_params(h, iterations, use_relative);
+    const long long launches0 = launch_counter();
+    if (h->opt.batch_graph) {
+        if (!h->bexec || h->bgraph_iters != iterations || h->bgraph_rel != (int)use_relative) {
+            h->release_graph();
+            build_batch_graph<T>(h, prm);
+            h->bgraph_iters = iterations;
+            h->bgraph_rel = use_relative ? 1 : 0;
+        }
+        ZS_CUDA(cudaEventRecord(h->ev0, s));
+        ZS_CUDA(cudaGraphLaunch(h->bexec, s));
+        ZS_CUDA(cudaEventRecord(h->ev1, s));
+        r.graph_launches = 1;
+    } else {
+        ZS_CUDA(cudaEventRecord(h->ev0, s));
+        launch_batch_prologue<T>(h->P, h->W, B, prm, s);
+        int any = 1;
+        while (any) {
+            ZS_CUDA(launch_batch_round<T>(h->P, h->W, B, prm, s));
+            ZS_CUDA(cudaMemcpyAsync(&any, B.any_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+            ZS_CUDA(cudaStreamSynchronize(s));
+        }
+        ZS_CUDA(cudaEventRecord(h->ev1, s));
+    }
+    ZS_CUDA(cudaEventSynchronize(h->ev1));
+    ZS_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    ZS_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    std::vector<LmState> st(P.nwin);
+    std::vector<WinCtl> ctl(P.nwin);
+    int rounds = 0;
+    ZS_CUDA(cudaMemcpyAsync(st.data(), B.st, sizeof(LmState) * P.nwin, cudaMemcpyDeviceToHost, s));
+    ZS_CUDA(cudaMemcpyAsync(ctl.data(), B.ctl, sizeof(WinCtl) * P.nwin, cudaMemcpyDeviceToHost, s));
+    ZS_CUDA(cudaMemcpyAsync(&rounds, B.rounds, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ZS_CUDA(cudaStreamSynchronize(s));
+    r.rounds = rounds;
+    r.ms_total = ms;
+    r.kernel_launches = r.graph_launches ? h->bpro_launches + (long long)rounds * h->bbody_launches
+                                         : launch_counter() - launches0;
+    int64_t accepted = 0;
+    for (int w = 0; w < P.nwin; ++w) {
+        accepted += ctl[w].accepted;
+        r.attempts += ctl[w].attempts;
+        if (!wr) continue;
+        zs_ba_report& o = wr[w];
+        std::memset(&o, 0, sizeof(o));
+        o.status = ZS_OK;
+        o.iterations = ctl[w].iterations;
+        o.accepted = ctl[w].accepted;
+        o.attempts = ctl[w].attempts;
+        o.cholesky_failures = ctl[w].chol_failures;
+        o.refine_sweeps = ctl[w].refine_sweeps;
+        o.chi2_initial = ctl[w].chi2_initial;
+        o.chi2_final = st[w].chi2;
+        o.lambda_final = st[w].lambda;
+        o.ms_total = ms;
+    }
+    r.accepted = accepted;
+    r.status = ZS_OK;
+    if (rep) *rep = r;
+    return (int)std::min<int64_t>(accepted, 0x7fffffff);
+}
+
+}  // namespace
+
+extern "C" {
+
+int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windows) {
+    if (!h || !windows || num_windows <= 0 || num_windows > 65535) return ZS_ERR_INVALID;
+    int64_t K = 0, L = 0, M = 0;
+    for (int w = 0; w < num_windows; ++w) {
+        const zs_ba_problem& p = windows[w];
+        const int v = validate(&p);
+        if (v != ZS_OK) return v;
+        if (p.num_poses > ZS_BATCH_MAX_POSES) return ZS_ERR_UNSUPPORTED;
+        if (w > 0) {
+            const zs_ba_problem& q = windows[0];
+            for (int i = 0; i < 4; ++i)
+                if (p.intrinsics[i] != q.intrinsics[i]) return ZS_ERR_UNSUPPORTED;
+            if (p.loss_kind != q.loss_kind || p.loss_delta != q.loss_delta) return ZS_ERR_UNSUPPORTED;
+            if ((p.obs_info != nullptr) != (q.obs_info != nullptr)) return ZS_ERR_UNSUPPORTED;
+        }
+        K += p.num_poses;
+        L += p.num_landmarks;
+        M += p.num_obs;
+    }
+    if (K > 0x7fffffffLL / 6 || L > 0x7fffffffLL / 3 || M > 0x7fffffffLL) return ZS_ERR_INVALID;
+    try {
+        // the windows concatenated: poses, landmarks and observations in window order
+        std::vector<double> poses(7 * K), lms(3 * L), uv(2 * M);
+        std::vector<uint8_t> pf(K), lf(L);
+        std::vector<int32_t> op(M), ol(M);
+        const bool has_info = windows[0].obs_info != nullptr;
+        std::vector<double> info(has_info ? 4 * M : 0);
+        std::vector<int32_t> wp{0}, wl{0};
+        int64_t k0 = 0, l0 = 0, o0 = 0;
+        for (int w = 0; w < num_windows; ++w) {
+            const zs_ba_problem& p = windows[w];
+            if (p.num_poses) {
+                std::memcpy(&poses[7 * k0], p.poses, sizeof(double) * 7 * p.num_poses);
+                std::memcpy(&pf[k0], p.pose_fixed, p.num_poses);
+            }
+            if (p.num_landmarks) {
+                std::memcpy(&lms[3 * l0], p.landmarks, sizeof(double) * 3 * p.num_landmarks);
+                std::memcpy(&lf[l0], p.landmark_fixed, p.num_landmarks);
+            }
+            for (int64_t o = 0; o < p.num_obs; ++o) {
+                op[o0 + o] = (int32_t)(k0 + p.obs_pose[o]);
+                ol[o0 + o] = (int32_t)(l0 + p.obs_landmark[o]);
+                uv[2 * (o0 + o)] = p.obs_uv[2 * o];
+                uv[2 * (o0 + o) + 1] = p.obs_uv[2 * o + 1];
+                if (has_info)
+                    for (int i = 0; i < 4; ++i) info[4 * (o0 + o) + i] = p.obs_info[4 * o + i];
+            }
+            k0 += p.num_poses;
+            l0 += p.num_landmarks;
+            o0 += p.num_obs;
+            wp.push_back((int32_t)k0);
+            wl.push_back((int32_t)l0);
+        }
+        zs_ba_problem cat = windows[0];
+        cat.num_poses = (int32_t)K;
+        cat.num_landmarks = (int32_t)L;
+        cat.num_obs = M;
+        cat.poses = poses.data();
+        cat.pose_fixed = pf.data();
+        cat.landmarks = lms.data();
+        cat.landmark_fixed = lf.data();
+        cat.obs_pose = op.data();
+        cat.obs_landmark = ol.data();
+        cat.obs_uv = uv.data();
+        cat.obs_info = has_info ? info.data() : nullptr;
+
+        ZS_CUDA(cudaSetDevice(h->device));
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+        h->release_problem();
+        build_problem(h, &cat, &wp, &wl);
+        // windows by reduced-system size bucket, largest first within a bucket
+        BatchDev& B = h->B;
+        std::vector<std::vector<int32_t>> byb(kBatchBuckets);
+        for (int w = 0; w < num_windows; ++w) byb[batch_bucket(6 * (wp[w + 1] - wp[w]))].push_back(w);
+        std::vector<int32_t> lists;
+        B.bucket_off[0] = 0;
+        for (int b = 0; b < kBatchBuckets; ++b) {
+            std::stable_sort(byb[b].begin(), byb[b].end(),
+                             [&](int32_t a, int32_t c) { return wp[a + 1] - wp[a] > wp[c + 1] - wp[c]; });
+            lists.insert(lists.end(), byb[b].begin(), byb[b].end());
+            B.bucket_off[b + 1] = (int)lists.size();
+        }
+        auto& own = h->owned;
+        B.lists = upload(lists, own, h->stream);
+        B.st = dalloc<LmState>(num_windows, own);
+        B.ctl = dalloc<WinCtl>(num_windows, own);
+        B.counters = dalloc<int>(kBatchBuckets, own);
+        B.any_active = dalloc<int>(1, own);
+        B.rounds = dalloc<int>(1, own);
+        ZS_CUDA(cudaMemsetAsync(B.st, 0, sizeof(LmState) * num_windows, h->stream));
+        ZS_CUDA(cudaMemsetAsync(B.ctl, 0, sizeof(WinCtl) * num_windows, h->stream));
+        ZS_CUDA(cudaMemsetAsync(B.rounds, 0, sizeof(int), h->stream));
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+        h->wpose0 = wp;
+        h->wlm0 = wl;
+        h->batch = true;
+        h->has_problem = true;
+    } catch (const CudaError& e) {
+        h->release_problem();
+        return cuda_status(e.err);
+    } catch (const std::bad_alloc&) {
+        h->release_problem();
+        return ZS_ERR_OUT_OF_MEMORY;
+    }
+    return ZS_OK;
+}
+
+int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* window_reports,
+                      zs_ba_batch_report* rep) {
+    if (!h) return ZS_ERR_INVALID;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (!h->batch) return ZS_ERR_INVALID;
+    if (iterations < 0) return ZS_ERR_INVALID;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        return h->tsize == 8 ? solve_batch_impl<double>(h, iterations, use_relative != 0, window_reports, rep)
+                             : solve_batch_impl<float>(h, iterations, use_relative != 0, window_reports, rep);
+    } catch (const CudaError& e) {
+        const int st = cuda_status(e.err);
+        if (rep) rep->status = st;
+        return st;
+    }
+}
+
+int zs_ba_get_window_state(zs_ba_handle* h, int window, double* poses, double* landmarks) {
+    if (!h) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (!h->batch || window < 0 || window >= h->P.nwin) return ZS_ERR_INVALID;
+    const DevProblem& P = h->P;
+    const int k0 = h->wpose0[window], nk = h->wpose0[window + 1] - k0;
+    const int l0 = h->wlm0[window], nl = h->wlm0[window + 1] - l0;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        if (poses && nk > 0) {
+            ZS_CUDA(cudaMemcpy2DAsync(poses, 7 * sizeof(double), P.pose + (size_t)k0 * kPoseStride,
+                                      kPoseStride * sizeof(double), 7 * sizeof(double), nk, cudaMemcpyDeviceToHost,
+                                      h->stream));
+        }
+        if (landmarks && nl > 0) {
+            ZS_CUDA(cudaMemcpy2DAsync(landmarks, 3 * sizeof(double), P.lm + (size_t)l0 * kLmStride,
+                                      kLmStride * sizeof(double), 3 * sizeof(double), nl, cudaMemcpyDeviceToHost,
+                                      h->stream));
+        }
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
 }
 
 }  // extern "C"

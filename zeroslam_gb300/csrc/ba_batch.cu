@@ -1,0 +1,822 @@
+// Batched local windows: many independent bundle-adjustment problems solved
+// together. The windows are concatenated into one problem whose reduced
+// camera system is block diagonal; the per-observation and per-landmark
+// kernels of the single-problem path run unchanged over all windows at
+// once, and the kernels here add what is per window:
+//   * the LM state machine (source/factor_graph.hpp:511-611) per window,
+//     advanced once per attempt round on the device (k_bdecide), with the
+//     same acceptance, damping, rollback and stop rules as zs_ba_solve;
+//   * the damped H_ll inverses, S block initialisation and Schur assembly
+//     at each window's own lambda, into the window's S block;
+//   * the reduced solve: a persistent kernel per size bucket whose CTAs
+//     take windows from a device work queue (largest first), factor the
+//     window's S in shared memory (packed lower triangle, right-looking
+//     Cholesky with the reference's pivot and solve thresholds,
+//     source/matrix_decomposition_cholesky.hpp:26-95), solve with one warp,
+//     and in the mixed form refine against the FP64 S;
+//   * per-window cost and model-decrease sums in a fixed order.
+// A round's kernels are captured once into a CUDA graph body that a
+// conditional WHILE node repeats until no window is active, so a batched
+// solve is one graph launch.
+#include <algorithm>
+
+#include "ba_internal.h"
+
+namespace zs {
+
+namespace {
+
+__device__ inline double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ inline double warp_max_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide deterministic sum / max for any blockDim.x that is a multiple
+// of 32 (<= 1024); result valid in every thread.
+__device__ inline double cta_sum(double v, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum_d(v);
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = lane < nw ? sh[lane] : 0.0;
+    t = warp_sum_d(t);
+    return t;
+}
+
+__device__ inline double cta_max(double v, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_max_d(v);
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = lane < nw ? sh[lane] : 0.0;
+    t = warp_max_d(t);
+    return t;
+}
+
+__device__ inline int64_t tri(int i) { return (int64_t)i * (i + 1) / 2; }
+
+}  // namespace
+
+// ------------------------------------------------------------ per-window kernels
+
+// matrix::invert<3> on H_ll + lambda_w I, as k_invert (source/matrix.hpp:749-774).
+__global__ void __launch_bounds__(kThreads) k_binvert(DevProblem P, const double* __restrict__ hll, double* hinv,
+                                                      const LmState* __restrict__ st, const WinCtl* __restrict__ ctl) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= P.L) return;
+    const int w = P.lm_win[l];
+    if (!ctl[w].active) return;
+    double* o = hinv + (int64_t)l * 9;
+    if (P.lm_fixed[l]) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) o[i] = 0.0;
+        return;
+    }
+    const double lam = st[w].lambda;
+    double a[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) a[i] = hll[(int64_t)l * 9 + i];
+    a[0] += lam; a[4] += lam; a[8] += lam;
+    const double det = +a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                       a[2] * (a[3] * a[7] - a[4] * a[6]);
+    double scale = 0.0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
+    if (!(fabs(det) > scale * scale * scale * 1e-12)) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) o[i] = 0.0;
+        return;
+    }
+    const double id = 1.0 / det;
+    o[0] = (a[4] * a[8] - a[7] * a[5]) * id;
+    o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+    o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+    o[3] = (a[5] * a[6] - a[3] * a[8]) * id;
+    o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+    o[5] = (a[3] * a[2] - a[0] * a[5]) * id;
+    o[6] = (a[3] * a[7] - a[6] * a[4]) * id;
+    o[7] = (a[6] * a[1] - a[0] * a[7]) * id;
+    o[8] = (a[0] * a[4] - a[3] * a[1]) * id;
+}
+
+// S_w = blockdiag(H_pp) + lambda_w I; blockIdx.y = window.
+__global__ void __launch_bounds__(kThreads) k_bs_init(DevProblem P, const double* __restrict__ hpp, double* S,
+                                                      const LmState* __restrict__ st, const WinCtl* __restrict__ ctl) {
+    const int w = blockIdx.y;
+    if (!ctl[w].active) return;
+    const int p0 = P.win_pose0[w];
+    const int n = 6 * (P.win_pose0[w + 1] - p0);
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const int row = (int)(idx / n), col = (int)(idx % n);
+    double v = 0.0;
+    if (row / 6 == col / 6) {
+        v = hpp[(int64_t)(p0 + row / 6) * 36 + (row % 6) * 6 + (col % 6)];
+        if (row == col) v += st[w].lambda;
+    }
+    S[P.win_s_off[w] + idx] = v;
+}
+
+// S_w -= the pair's chunk partials (FP64, chunk order), as k_schur_assemble.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bschur_assemble(DevProblem P, const T* __restrict__ partial, double* S,
+                                                              const WinCtl* __restrict__ ctl) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)P.npairs * 36) return;
+    const int p = (int)(idx / 36), e = (int)(idx % 36);
+    const int i = P.pair_i[p], j = P.pair_j[p];
+    const int w = P.pose_win[i];
+    if (!ctl[w].active) return;
+    double sum = 0.0;
+    const int64_t c1 = P.pair_chunk_ptr[p + 1];
+    for (int64_t c = P.pair_chunk_ptr[p]; c < c1; ++c) sum += (double)partial[c * 36 + e];
+    const int p0 = P.win_pose0[w];
+    const int64_t n = 6LL * (P.win_pose0[w + 1] - p0);
+    double* Sw = S + P.win_s_off[w];
+    const int64_t row = 6LL * (i - p0) + e / 6, col = 6LL * (j - p0) + e % 6;
+    if (i == j) {
+        Sw[row * n + col] = Sw[row * n + col] - sum;
+    } else {
+        Sw[row * n + col] = -sum;
+        Sw[col * n + row] = -sum;
+    }
+}
+
+// delta_l = H_ll^-1 (b_l - H_lp delta_p), as k_backsub.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bbacksub(DevProblem P, const T* __restrict__ hpl,
+                                                       const double* __restrict__ hinv, const double* __restrict__ b,
+                                                       double* delta, const LmState* __restrict__ st,
+                                                       const WinCtl* __restrict__ ctl) {
+    constexpr int RS = sizeof(T) == 4 ? 20 : 18;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= P.L) return;
+    const int w = P.lm_win[l];
+    if (!ctl[w].active || !st[w].solve_ok) return;
+    const double* bl = b + P.n + 3LL * l;
+    double v0 = bl[0], v1 = bl[1], v2 = bl[2];
+    const int e = P.lm_ptr[l + 1];
+    for (int o = P.lm_ptr[l]; o < e; ++o) {
+        if (!P.blk_valid[o]) continue;
+        const T* h = hpl + (int64_t)o * RS;
+        const double* dp = delta + 6LL * P.obs_pose[o];
+        T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            const T d = (T)dp[a];
+            s0 += h[a * 3] * d;
+            s1 += h[a * 3 + 1] * d;
+            s2 += h[a * 3 + 2] * d;
+        }
+        v0 -= s0; v1 -= s1; v2 -= s2;
+    }
+    const double* I = hinv + (int64_t)l * 9;
+    double* dl = delta + P.n + 3LL * l;
+    dl[0] = I[0] * v0 + I[1] * v1 + I[2] * v2;
+    dl[1] = I[3] * v0 + I[4] * v1 + I[5] * v2;
+    dl[2] = I[6] * v0 + I[7] * v1 + I[8] * v2;
+}
+
+// Backup and apply the step to the free vertices of windows whose solve passed.
+__global__ void __launch_bounds__(kThreads) k_bupdate(DevProblem P, const double* __restrict__ delta,
+                                                      const LmState* __restrict__ st, const WinCtl* __restrict__ ctl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < P.K) {
+        const int w = P.pose_win[t];
+        if (!ctl[w].active || !st[w].solve_ok) return;
+        double* p = P.pose + (int64_t)t * kPoseStride;
+        double* bk = P.pose_bk + (int64_t)t * kPoseStride;
+#pragma unroll
+        for (int i = 0; i < kPoseStride; ++i) bk[i] = p[i];
+        if (P.pose_fixed[t]) return;
+        double d[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) d[i] = delta[6LL * t + i];
+        pose_plus(p, d);
+    } else if (t < P.K + P.L) {
+        const int l = t - P.K;
+        const int w = P.lm_win[l];
+        if (!ctl[w].active || !st[w].solve_ok) return;
+        double* x = P.lm + (int64_t)l * kLmStride;
+        double* bk = P.lm_bk + (int64_t)l * kLmStride;
+#pragma unroll
+        for (int i = 0; i < kLmStride; ++i) bk[i] = x[i];
+        if (P.lm_fixed[l]) return;
+        const double* d = delta + P.n + 3LL * l;
+        x[0] += d[0];
+        x[1] += d[1];
+        x[2] += d[2];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_brollback(DevProblem P, const WinCtl* __restrict__ ctl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < P.K) {
+        if (!ctl[P.pose_win[t]].rollback) return;
+#pragma unroll
+        for (int i = 0; i < kPoseStride; ++i)
+            P.pose[(int64_t)t * kPoseStride + i] = P.pose_bk[(int64_t)t * kPoseStride + i];
+    } else if (t < P.K + P.L) {
+        const int l = t - P.K;
+        if (!ctl[P.lm_win[l]].rollback) return;
+#pragma unroll
+        for (int i = 0; i < kLmStride; ++i) P.lm[(int64_t)l * kLmStride + i] = P.lm_bk[(int64_t)l * kLmStride + i];
+    }
+}
+
+// Model decrease sum delta (lambda delta + b) + 1e-3 per window (one CTA per window).
+__global__ void __launch_bounds__(kThreads) k_bscale(DevProblem P, const double* __restrict__ delta,
+                                                     const double* __restrict__ b, LmState* st,
+                                                     const WinCtl* __restrict__ ctl) {
+    __shared__ double sh[kThreads];
+    const int w = blockIdx.x;
+    if (!ctl[w].active || !st[w].solve_ok) return;
+    const double lam = st[w].lambda;
+    double v = 0.0;
+    const int64_t a0 = 6LL * P.win_pose0[w], a1 = 6LL * P.win_pose0[w + 1];
+    for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) v += delta[i] * (lam * delta[i] + b[i]);
+    const int64_t c0 = P.n + 3LL * P.win_lm0[w], c1 = P.n + 3LL * P.win_lm0[w + 1];
+    for (int64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) v += delta[i] * (lam * delta[i] + b[i]);
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) st[w].scale = v + 1e-3;
+}
+
+// Cost partial per observation chunk (a CTA per chunk).
+__global__ void __launch_bounds__(kThreads) k_bcost_partial(DevProblem P, double* red, const LmState* __restrict__ st,
+                                                            const WinCtl* __restrict__ ctl, int initial) {
+    __shared__ double sh[kThreads];
+    const int c = blockIdx.x;
+    const int w = P.ochunk_win[c];
+    if (!initial && (!ctl[w].active || !st[w].solve_ok)) return;
+    double v = 0.0;
+    const int64_t o1 = P.ochunk_ptr[c + 1];
+    for (int64_t o = P.ochunk_ptr[c] + threadIdx.x; o < o1; o += blockDim.x) {
+        const int pi = P.obs_pose[o], li = P.obs_lm[o];
+        const double* pp = P.pose + (int64_t)pi * kPoseStride;
+        const double* xp = P.lm + (int64_t)li * kLmStride;
+        double p[7], X[3];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) p[i] = pp[i];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) X[i] = xp[i];
+        const double2 uv = P.obs_uv[o];
+        double Xc[3], r[2];
+        residual(p, X, uv.x, uv.y, P.intr, Xc, r);
+        const double e2 = chi2_of(r, P.obs_info ? P.obs_info + 4 * o : nullptr);
+        if (P.loss.kind) {
+            double rho[3];
+            loss_rho(P.loss, e2, rho);
+            v += rho[0];
+        } else {
+            v += e2;
+        }
+    }
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) red[c] = v;
+}
+
+// chi2_new per window: its chunk partials added in chunk order.
+__global__ void k_bcost_finish(DevProblem P, const double* __restrict__ red, LmState* st,
+                               const WinCtl* __restrict__ ctl, int initial) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= P.nwin) return;
+    if (!initial && (!ctl[w].active || !st[w].solve_ok)) return;
+    double v = 0.0;
+    for (int c = P.win_ochunk[w]; c < P.win_ochunk[w + 1]; ++c) v += red[c];
+    st[w].chi2_new = v;
+}
+
+// Initial damping per window (source/factor_graph.hpp:511-522) and the
+// window's LM control state (one CTA per window).
+__global__ void __launch_bounds__(kThreads) k_binit(DevProblem P, const double* __restrict__ hpp,
+                                                    const double* __restrict__ hll, LmState* st, WinCtl* ctl,
+                                                    BatchParams prm) {
+    __shared__ double sh[kThreads];
+    const int w = blockIdx.x;
+    const int p0 = P.win_pose0[w], p1 = P.win_pose0[w + 1];
+    const int l0 = P.win_lm0[w], l1 = P.win_lm0[w + 1];
+    double m = 0.0;
+    for (int i = threadIdx.x; i < 6 * (p1 - p0); i += blockDim.x)
+        m = fmax(m, fabs(hpp[(int64_t)(p0 + i / 6) * 36 + (i % 6) * 7]));
+    for (int i = threadIdx.x; i < 3 * (l1 - l0); i += blockDim.x)
+        m = fmax(m, fabs(hll[(int64_t)(l0 + i / 3) * 9 + (i % 3) * 4]));
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    LmState& s = st[w];
+    const double chi2 = s.chi2_new;
+    s.max_diag = sh[0];
+    s.lambda = prm.tau * fmin(prm.clamp, sh[0]);
+    s.nu = 2.0;
+    s.chi2 = chi2;
+    s.solve_ok = 0;
+    s.good = 0;
+    s.rho = 0.0;
+    s.refine_sweeps = 0;
+    WinCtl& c = ctl[w];
+    const bool has_obs = P.win_ochunk[w + 1] > P.win_ochunk[w];
+    c.active = (prm.iterations > 0 && prm.max_failures > 0 && has_obs && (p1 > p0 || l1 > l0)) ? 1 : 0;
+    c.it = 0;
+    c.iterations = 0;
+    c.failures = 0;
+    c.accepted = 0;
+    c.attempts = 0;
+    c.chol_failures = 0;
+    c.refine_sweeps = 0;
+    c.rollback = 0;
+    c.last = chi2;
+    c.legacy = prm.legacy_stop * chi2;
+    c.chi2_initial = chi2;
+}
+
+// One attempt's decision per window (source/factor_graph.hpp:542-611), then
+// the loop condition: repeat the round while any window is active.
+__global__ void __launch_bounds__(kThreads) k_bdecide(int nwin, LmState* st, WinCtl* ctl, BatchParams prm,
+                                                      int* counters, int* any_active, int* rounds) {
+    __shared__ int sh_any;
+    if (threadIdx.x == 0) sh_any = 0;
+    __syncthreads();
+    const int round = *rounds + 1;
+    const bool last_round = round >= prm.max_rounds;
+    int any = 0;
+    for (int w = threadIdx.x; w < nwin; w += blockDim.x) {
+        WinCtl& c = ctl[w];
+        LmState& s = st[w];
+        c.rollback = 0;
+        if (!c.active) continue;
+        c.attempts++;
+        bool end_inner = false;
+        if (!s.solve_ok) {
+            c.chol_failures++;
+            s.lambda *= s.nu;
+            s.nu *= 2.0;
+            s.good = 0;
+            c.failures++;
+            end_inner = !isfinite(s.lambda) || c.failures >= prm.max_failures;
+        } else {
+            c.refine_sweeps += s.refine_sweeps;
+            const double rho = (s.chi2 - s.chi2_new) / s.scale;
+            s.rho = rho;
+            if ((rho > 0) && isfinite(s.chi2_new)) {
+                double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
+                alpha = fmin(alpha, 2.0 / 3.0);
+                s.lambda *= fmax(1.0 / 3.0, alpha);
+                s.nu = 2.0;
+                s.chi2 = s.chi2_new;
+                s.good = 1;
+                c.accepted++;
+                end_inner = true;
+            } else {
+                s.lambda *= s.nu;
+                s.nu *= 2.0;
+                s.good = 0;
+                // rollback only while lambda stays finite (source/factor_graph.hpp:592-604)
+                if (isfinite(s.lambda)) {
+                    c.rollback = 1;
+                    c.failures++;
+                    end_inner = c.failures >= prm.max_failures;
+                } else {
+                    end_inner = true;
+                }
+            }
+        }
+        if (end_inner) {
+            const double thr =
+                prm.use_relative ? prm.relative_tolerance * fmax(c.last, prm.chi2_floor) : c.legacy;
+            if (c.failures >= prm.max_failures || (c.last - s.chi2) < thr || !isfinite(s.lambda)) {
+                c.active = 0;
+                c.iterations = c.it + 1;
+            } else {
+                c.it++;
+                if (c.it >= prm.iterations) {
+                    c.active = 0;
+                    c.iterations = c.it;
+                } else {
+                    c.failures = 0;
+                    c.last = s.chi2;
+                }
+            }
+        }
+        if (c.active && last_round) {
+            c.active = 0;  // bounded number of rounds: report what was done
+            c.iterations = c.it + 1;
+        }
+        any |= c.active;
+    }
+    if (any) atomicOr(&sh_any, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *rounds = round;
+        *any_active = sh_any;
+        for (int b = 0; b < kBatchBuckets; ++b) counters[b] = 0;
+        if (prm.use_cond) cudaGraphSetConditional(prm.cond, sh_any ? 1u : 0u);
+    }
+}
+
+__global__ void k_breset(int* counters, int* any_active, int* rounds) {
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < kBatchBuckets; ++b) counters[b] = 0;
+        *any_active = 1;
+        *rounds = 0;
+    }
+}
+
+// ------------------------------------------------------------ reduced solve
+
+// In-place triangular solves L L^T v = v by one warp, FP64 accumulation;
+// lane l keeps rows l, l + 32, ... in registers. dinv = 1 / L_kk.
+template <typename TF, int NS>
+__device__ void warp_chol_solve(const TF* __restrict__ A, const double* __restrict__ dinv, int n, double* v) {
+    const int lane = threadIdx.x & 31;
+    double y[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const int i = lane + 32 * s;
+        y[s] = i < n ? v[i] : 0.0;
+    }
+    for (int k = 0; k < n; ++k) {
+        const int owner = k & 31, slot = k >> 5;
+        double yk = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s == slot) yk = y[s];
+        yk = __shfl_sync(0xffffffffu, yk * dinv[k], owner);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const int i = lane + 32 * s;
+            if (i == k) y[s] = yk;
+            else if (i > k && i < n) y[s] -= (double)A[tri(i) + k] * yk;
+        }
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const int owner = k & 31, slot = k >> 5;
+        double xk = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s == slot) xk = y[s];
+        xk = __shfl_sync(0xffffffffu, xk * dinv[k], owner);
+        const TF* row = A + tri(k);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const int i = lane + 32 * s;
+            if (i == k) y[s] = xk;
+            else if (i < k) y[s] -= (double)row[i] * xk;
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const int i = lane + 32 * s;
+        if (i < n) v[i] = y[s];
+    }
+}
+
+// Shared memory of one CTA of k_bsolve for windows with n <= 32 NS.
+template <typename TF, int NS>
+constexpr size_t bsolve_smem() {
+    return 4 * sizeof(double) * 32 * NS + sizeof(TF) * 32 * NS +
+           sizeof(TF) * ((size_t)32 * NS * (32 * NS + 1) / 2);
+}
+
+// Persistent reduced solve of one size bucket: CTAs take windows from the
+// bucket's queue (list, largest first). Per window: S_w (FP64, global) ->
+// packed lower triangle in shared memory (TF), right-looking Cholesky with
+// pivot test d > 1e-14 max|S_ii|, solve test |L_ii| > 1e-7 max|L_ii|
+// (source/matrix_decomposition_cholesky.hpp:40,53,74,80,89), warp
+// triangular solves; with refine_iters > 0, FP64 refinement
+// x += (L L^T)^-1 (b - S x) until ||b - S x|| <= tol ||b||.
+template <typename TF, int NS>
+__global__ void k_bsolve(BatchView V, const int32_t* __restrict__ list, int count, int* counter, int refine_iters,
+                         double refine_tol) {
+    constexpr int NMAX = 32 * NS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* xs = reinterpret_cast<double*>(smem_raw);  // [NMAX] solution
+    double* rs = xs + NMAX;                            // [NMAX] residual / correction
+    double* bv = rs + NMAX;                            // [NMAX] right-hand side
+    double* dinv = bv + NMAX;                          // [NMAX] 1 / L_kk
+    TF* col = reinterpret_cast<TF*>(dinv + NMAX);      // [NMAX] scaled column k
+    TF* A = col + NMAX;                                // packed lower triangle
+    __shared__ int s_idx;
+    __shared__ double s_red[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_idx = atomicAdd(counter, 1);
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= count) return;
+        const int w = list[idx];
+        if (!V.ctl[w].active) continue;
+        const int p0 = V.win_pose0[w];
+        const int n = 6 * (V.win_pose0[w + 1] - p0);
+        const double* S = V.S + V.win_s_off[w];
+        for (int i = warp; i < n; i += nwarps) {
+            const double* srow = S + (int64_t)i * n;
+            TF* arow = A + tri(i);
+            for (int j = lane; j <= i; j += 32) arow[j] = (TF)srow[j];
+        }
+        double m = 0.0;
+        for (int i = tid; i < n; i += blockDim.x) {
+            bv[i] = V.bs[6LL * p0 + i];
+            m = fmax(m, fabs(S[(int64_t)i * n + i]));
+        }
+        m = cta_max(m, s_red);
+        const double eps_f = 1e-14 * m;
+        __syncthreads();
+        int ok = 1;
+        for (int k = 0; k < n; ++k) {
+            const TF d = A[tri(k) + k];
+            if (!((double)d > eps_f)) {
+                ok = 0;
+                break;
+            }
+            const TF lkk = sqrt(d);
+            for (int i = k + 1 + tid; i < n; i += blockDim.x) {
+                const TF v = A[tri(i) + k] / lkk;
+                col[i] = v;
+                A[tri(i) + k] = v;
+            }
+            __syncthreads();
+            if (tid == 0) A[tri(k) + k] = lkk;
+            for (int i = k + 1 + warp; i < n; i += nwarps) {
+                const TF ci = col[i];
+                TF* arow = A + tri(i);
+                for (int j = k + 1 + lane; j <= i; j += 32) arow[j] -= ci * col[j];
+            }
+            __syncthreads();
+        }
+        int sweeps = 0;
+        if (ok) {
+            double lm = 0.0;
+            for (int i = tid; i < n; i += blockDim.x) {
+                const double lii = (double)A[tri(i) + i];
+                lm = fmax(lm, fabs(lii));
+                dinv[i] = 1.0 / lii;
+            }
+            lm = cta_max(lm, s_red);
+            int bad = 0;
+            for (int i = tid; i < n; i += blockDim.x)
+                if (!(fabs((double)A[tri(i) + i]) > 1e-7 * lm)) bad = 1;
+            ok = __syncthreads_or(bad) ? 0 : 1;
+        }
+        if (ok) {
+            for (int i = tid; i < n; i += blockDim.x) xs[i] = bv[i];
+            __syncthreads();
+            if (warp == 0) warp_chol_solve<TF, NS>(A, dinv, n, xs);
+            __syncthreads();
+            if (refine_iters > 0) {
+                double b2 = 0.0;
+                for (int i = tid; i < n; i += blockDim.x) b2 += bv[i] * bv[i];
+                b2 = cta_sum(b2, s_red);
+                for (;;) {
+                    for (int i = warp; i < n; i += nwarps) {
+                        const double* srow = S + (int64_t)i * n;
+                        double acc = 0.0;
+                        for (int j = lane; j < n; j += 32) acc += srow[j] * xs[j];
+                        acc = warp_sum_d(acc);
+                        if (lane == 0) rs[i] = bv[i] - acc;
+                    }
+                    __syncthreads();
+                    double r2 = 0.0;
+                    for (int i = tid; i < n; i += blockDim.x) r2 += rs[i] * rs[i];
+                    r2 = cta_sum(r2, s_red);
+                    if (!(r2 > refine_tol * refine_tol * b2) || sweeps >= refine_iters) break;
+                    if (warp == 0) warp_chol_solve<TF, NS>(A, dinv, n, rs);
+                    __syncthreads();
+                    for (int i = tid; i < n; i += blockDim.x) xs[i] += rs[i];
+                    __syncthreads();
+                    ++sweeps;
+                }
+            }
+            for (int i = tid; i < n; i += blockDim.x) V.delta[6LL * p0 + i] = xs[i];
+        }
+        if (tid == 0) {
+            V.st[w].solve_ok = ok;
+            V.st[w].refine_sweeps = sweeps;
+        }
+    }
+}
+
+// ------------------------------------------------------------ launchers
+
+template <typename TF, int NS>
+static cudaError_t launch_bsolve_ns(const BatchView& V, const int32_t* list, int count, int* counter, int threads,
+                                    int blocks, int refine_iters, double refine_tol, cudaStream_t s) {
+    // the kernel's shared-memory limit is raised by bsolve_max_blocks_per_sm,
+    // outside any stream capture
+    const size_t smem = bsolve_smem<TF, NS>();
+    k_bsolve<TF, NS><<<blocks, threads, smem, s>>>(V, list, count, counter, refine_iters, refine_tol);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename TF>
+cudaError_t launch_bsolve(int bucket, const BatchView& V, const int32_t* list, int count, int* counter, int threads,
+                          int blocks, int refine_iters, double refine_tol, cudaStream_t s) {
+    switch (bucket) {
+        case 0: return launch_bsolve_ns<TF, 2>(V, list, count, counter, threads, blocks, refine_iters, refine_tol, s);
+        case 1: return launch_bsolve_ns<TF, 3>(V, list, count, counter, threads, blocks, refine_iters, refine_tol, s);
+        case 2: return launch_bsolve_ns<TF, 4>(V, list, count, counter, threads, blocks, refine_iters, refine_tol, s);
+        case 3: return launch_bsolve_ns<TF, 5>(V, list, count, counter, threads, blocks, refine_iters, refine_tol, s);
+        default: return launch_bsolve_ns<TF, 6>(V, list, count, counter, threads, blocks, refine_iters, refine_tol, s);
+    }
+}
+
+template <typename TF>
+size_t bsolve_smem_bytes(int bucket) {
+    switch (bucket) {
+        case 0: return bsolve_smem<TF, 2>();
+        case 1: return bsolve_smem<TF, 3>();
+        case 2: return bsolve_smem<TF, 4>();
+        case 3: return bsolve_smem<TF, 5>();
+        default: return bsolve_smem<TF, 6>();
+    }
+}
+
+template <typename TF>
+int bsolve_max_blocks_per_sm(int bucket, int threads) {
+    int nb = 0;
+    const size_t smem = bsolve_smem_bytes<TF>(bucket);
+    cudaError_t e = cudaSuccess;
+    switch (bucket) {
+        case 0: e = cudaFuncSetAttribute(k_bsolve<TF, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bsolve<TF, 2>, threads, smem); break;
+        case 1: e = cudaFuncSetAttribute(k_bsolve<TF, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bsolve<TF, 3>, threads, smem); break;
+        case 2: e = cudaFuncSetAttribute(k_bsolve<TF, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bsolve<TF, 4>, threads, smem); break;
+        case 3: e = cudaFuncSetAttribute(k_bsolve<TF, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bsolve<TF, 5>, threads, smem); break;
+        default: e = cudaFuncSetAttribute(k_bsolve<TF, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                 if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bsolve<TF, 6>, threads, smem); break;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
+}
+
+template <typename T>
+void launch_batch_prologue(const DevProblem& P, DevWork& W, BatchDev& B, const BatchParams& prm, cudaStream_t s) {
+    k_breset<<<1, 32, 0, s>>>(B.counters, B.any_active, B.rounds); note_launch();
+    launch_linearize<T>(P, W, s);
+    if (P.nochunks > 0) { k_bcost_partial<<<(int)P.nochunks, kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 1); note_launch(); }
+    k_bcost_finish<<<grid_for(P.nwin), kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 1); note_launch();
+    k_binit<<<P.nwin, kThreads, 0, s>>>(P, W.hpp, W.hll, B.st, B.ctl, prm); note_launch();
+}
+
+template <typename T>
+cudaError_t launch_batch_round(const DevProblem& P, DevWork& W, BatchDev& B, const BatchParams& prm,
+                               cudaStream_t s) {
+    launch_linearize<T>(P, W, s);
+    if (P.L > 0) { k_binvert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, B.st, B.ctl); note_launch(); }
+    launch_w<T>(P, W, s);
+    {
+        const dim3 g(grid_for(36LL * kBatchMaxK * kBatchMaxK), P.nwin);
+        k_bs_init<<<g, kThreads, 0, s>>>(P, W.hpp, W.S, B.st, B.ctl); note_launch();
+    }
+    launch_schur_chunks<T>(P, W, s);
+    if (P.npairs > 0) {
+        k_bschur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, W.S, B.ctl);
+        note_launch();
+    }
+    launch_bs<T>(P, W, s);
+    BatchView V{W.S, W.bs, W.delta, B.st, B.ctl, P.win_pose0, P.win_s_off};
+    const int refine = sizeof(T) == 4 ? prm.refine_iters : 0;
+    for (int b = 0; b < kBatchBuckets; ++b) {
+        const int cnt = B.bucket_off[b + 1] - B.bucket_off[b];
+        if (cnt == 0) continue;
+        cudaError_t e = launch_bsolve<T>(b, V, B.lists + B.bucket_off[b], cnt, B.counters + b, B.threads[b],
+                                         B.blocks[b], refine, prm.refine_tol, s);
+        if (e != cudaSuccess) return e;
+    }
+    if (P.L > 0) {
+        k_bbacksub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, B.st, B.ctl);
+        note_launch();
+    }
+    k_bupdate<<<grid_for((int64_t)P.K + P.L), kThreads, 0, s>>>(P, W.delta, B.st, B.ctl); note_launch();
+    k_bscale<<<P.nwin, kThreads, 0, s>>>(P, W.delta, W.b, B.st, B.ctl); note_launch();
+    if (P.nochunks > 0) { k_bcost_partial<<<(int)P.nochunks, kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 0); note_launch(); }
+    k_bcost_finish<<<grid_for(P.nwin), kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 0); note_launch();
+    k_bdecide<<<1, kThreads, 0, s>>>(P.nwin, B.st, B.ctl, prm, B.counters, B.any_active, B.rounds); note_launch();
+    k_brollback<<<grid_for((int64_t)P.K + P.L), kThreads, 0, s>>>(P, B.ctl); note_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ autotuning
+
+// Synthetic SPD blocks for timing: S = (n + 1) I + 1 / (1 + |i - j|).
+__global__ void k_tune_fill(int n, int nwin, double* S, double* bs, LmState* st, WinCtl* ctl, int32_t* pose0,
+                            int64_t* soff, int32_t* list) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nn = (int64_t)n * n;
+    if (idx < nn * nwin) {
+        const int64_t e = idx % nn;
+        const int i = (int)(e / n), j = (int)(e % n);
+        S[idx] = (i == j ? n + 1.0 : 0.0) + 1.0 / (1.0 + abs(i - j));
+    }
+    if (idx < (int64_t)n * nwin) bs[idx] = 1.0 + (double)(idx % 7);
+    if (idx < nwin) {
+        ctl[idx] = WinCtl{};
+        ctl[idx].active = 1;
+        st[idx] = LmState{};
+        pose0[idx] = (int32_t)(idx * (n / 6));
+        soff[idx] = idx * nn;
+        list[idx] = (int32_t)idx;
+    }
+    if (idx == nwin) pose0[nwin] = (int32_t)(nwin * (n / 6));
+}
+
+template <typename TF>
+cudaError_t bsolve_autotune(int bucket, int sms, cudaStream_t s, int* threads_out, int* blocks_out, float* us_out) {
+    const int nmax = 32 * (bucket + 2);
+    const int n = 6 * (nmax / 6);
+    const int nwin = 2 * sms;
+    const int64_t nn = (int64_t)n * n;
+    double *S = nullptr, *bs = nullptr, *delta = nullptr;
+    LmState* st = nullptr;
+    WinCtl* ctl = nullptr;
+    int32_t *pose0 = nullptr, *list = nullptr;
+    int64_t* soff = nullptr;
+    int* counter = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaSuccess;
+    auto chk = [&](cudaError_t e) {
+        if (err == cudaSuccess && e != cudaSuccess) err = e;
+        return err == cudaSuccess;
+    };
+    chk(cudaMalloc(&S, nn * nwin * sizeof(double)));
+    chk(cudaMalloc(&bs, (size_t)n * nwin * sizeof(double)));
+    chk(cudaMalloc(&delta, (size_t)n * nwin * sizeof(double)));
+    chk(cudaMalloc(&st, nwin * sizeof(LmState)));
+    chk(cudaMalloc(&ctl, nwin * sizeof(WinCtl)));
+    chk(cudaMalloc(&pose0, (nwin + 1) * sizeof(int32_t)));
+    chk(cudaMalloc(&list, nwin * sizeof(int32_t)));
+    chk(cudaMalloc(&soff, nwin * sizeof(int64_t)));
+    chk(cudaMalloc(&counter, sizeof(int)));
+    chk(cudaEventCreate(&e0));
+    chk(cudaEventCreate(&e1));
+    int best_t = 256, best_b = sms;
+    float best_us = 0.f;
+    if (err == cudaSuccess) {
+        k_tune_fill<<<grid_for(nn * nwin), kThreads, 0, s>>>(n, nwin, S, bs, st, ctl, pose0, soff, list);
+        chk(cudaGetLastError());
+        BatchView V{S, bs, delta, st, ctl, pose0, soff};
+        const int cand[4] = {128, 256, 512, 1024};
+        for (int c = 0; c < 4 && err == cudaSuccess; ++c) {
+            const int t = cand[c];
+            const int per_sm = bsolve_max_blocks_per_sm<TF>(bucket, t);
+            if (per_sm <= 0) continue;
+            const int blocks = std::min(nwin, per_sm * sms);
+            float best_rep = 1e30f;
+            for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+                chk(cudaMemsetAsync(counter, 0, sizeof(int), s));
+                chk(cudaEventRecord(e0, s));
+                chk(launch_bsolve<TF>(bucket, V, list, nwin, counter, t, blocks, sizeof(TF) == 4 ? 8 : 0, 1e-10, s));
+                chk(cudaEventRecord(e1, s));
+                chk(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                chk(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep > 0) best_rep = std::min(best_rep, ms);
+            }
+            if (err == cudaSuccess && (best_us == 0.f || best_rep * 1000.f < best_us)) {
+                best_us = best_rep * 1000.f;
+                best_t = t;
+                best_b = per_sm;
+            }
+        }
+    }
+    cudaStreamSynchronize(s);
+    cudaFree(S); cudaFree(bs); cudaFree(delta); cudaFree(st); cudaFree(ctl);
+    cudaFree(pose0); cudaFree(list); cudaFree(soff); cudaFree(counter);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    *threads_out = best_t;
+    *blocks_out = best_b;  // resident CTAs per SM at that size
+    *us_out = best_us;
+    return err;
+}
+
+template void launch_batch_prologue<double>(const DevProblem&, DevWork&, BatchDev&, const BatchParams&, cudaStream_t);
+template void launch_batch_prologue<float>(const DevProblem&, DevWork&, BatchDev&, const BatchParams&, cudaStream_t);
+template cudaError_t launch_batch_round<double>(const DevProblem&, DevWork&, BatchDev&, const BatchParams&, cudaStream_t);
+template cudaError_t launch_batch_round<float>(const DevProblem&, DevWork&, BatchDev&, const BatchParams&, cudaStream_t);
+template cudaError_t bsolve_autotune<double>(int, int, cudaStream_t, int*, int*, float*);
+template cudaError_t bsolve_autotune<float>(int, int, cudaStream_t, int*, int*, float*);
+template int bsolve_max_blocks_per_sm<double>(int, int);
+template int bsolve_max_blocks_per_sm<float>(int, int);
+
+}  // namespace zs

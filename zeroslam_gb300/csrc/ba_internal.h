@@ -47,6 +47,19 @@ struct DevProblem {
     int2* triples = nullptr;           // [ntriples] (obs of pose i, obs of pose j)
     Intrinsics intr{};
     LossParams loss{};
+    // Batched windows (null / 1 for a single problem): poses, landmarks and
+    // observations of window w are contiguous; S is block diagonal, window
+    // w's n_w x n_w block (n_w = 6 K_w) at S + win_s_off[w].
+    int nwin = 1;
+    int32_t* pose_win = nullptr;   // [K] window of each pose
+    int32_t* lm_win = nullptr;     // [L] window of each landmark
+    int32_t* win_pose0 = nullptr;  // [nwin+1] first pose of each window
+    int32_t* win_lm0 = nullptr;    // [nwin+1] first landmark of each window
+    int64_t* win_s_off = nullptr;  // [nwin] offset of the window's S block
+    int64_t nochunks = 0;          // observation chunks for per-window sums
+    int64_t* ochunk_ptr = nullptr; // [nochunks+1] observation ranges (never across windows)
+    int32_t* ochunk_win = nullptr; // [nochunks] window of each chunk
+    int32_t* win_ochunk = nullptr; // [nwin+1] chunk ranges per window
 };
 
 // Working arrays of one precision (T = double for the plain form, float for
@@ -93,6 +106,24 @@ struct LmState {
     int32_t refine_sweeps;  // refinement sweeps of the last reduced solve
 };
 
+// Per-window LM control of a batched solve (source/factor_graph.hpp:538-611
+// restated as a state machine advanced once per attempt round).
+struct WinCtl {
+    int32_t active;        // still iterating
+    int32_t it;            // completed outer iterations
+    int32_t iterations;    // outer iterations reported (factor_graph::solve's loop count)
+    int32_t failures;      // failed attempts in the current outer iteration
+    int32_t accepted;      // accepted steps (the reference's return value)
+    int32_t attempts;
+    int32_t chol_failures;
+    int32_t refine_sweeps;
+    int32_t rollback;      // the last attempt was rejected and must be undone
+    int32_t pad;
+    double last;           // cost at the start of the current outer iteration
+    double legacy;         // legacy stop threshold (legacy_stop * initial cost)
+    double chi2_initial;
+};
+
 // ---- kernels (ba_kernels.cu) ----
 template <typename T>
 void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s);
@@ -105,6 +136,12 @@ void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStre
 // b_s = b_p - W b_l from the current W.b (no other Schur work).
 template <typename T>
 void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s);
+// W = H_pl H_ll^-1 from the current inverses (no inversion).
+template <typename T>
+void launch_w(const DevProblem& P, DevWork& W, cudaStream_t s);
+// Per-chunk Schur pair partials (no assembly).
+template <typename T>
+void launch_schur_chunks(const DevProblem& P, DevWork& W, cudaStream_t s);
 void launch_update(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s);
 void launch_rollback(const DevProblem& P, const LmState* st, cudaStream_t s);
 void launch_scale(const DevProblem& P, DevWork& W, LmState* st, cudaStream_t s);
@@ -113,6 +150,68 @@ void launch_cost(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, 
 void launch_init_lambda(const DevProblem& P, DevWork& W, LmState* st, double tau, double clamp, cudaStream_t s);
 void launch_decide(LmState* st, cudaStream_t s);
 void launch_set_solve_ok(LmState* st, int v, cudaStream_t s);
+
+// ---- batched windows (ba_batch.cu) ----
+constexpr int kBatchBuckets = 5;     // reduced-solve size buckets: n <= 64, 96, 128, 160, 192
+constexpr int kBatchMaxK = 32;       // poses per window (n <= 192)
+constexpr int kBatchObsChunk = 2048; // observations per cost chunk
+
+inline int batch_bucket(int n) {
+    const int ns = (n + 31) / 32;
+    return ns <= 2 ? 0 : ns - 2;
+}
+
+struct BatchParams {
+    int iterations;
+    int use_relative;
+    int max_failures;
+    int refine_iters;
+    int max_rounds;
+    int use_cond;
+    double relative_tolerance;
+    double chi2_floor;
+    double legacy_stop;
+    double tau;
+    double clamp;
+    double refine_tol;
+    cudaGraphConditionalHandle cond;
+};
+
+// What the reduced-solve kernel needs of a batch.
+struct BatchView {
+    double* S;
+    const double* bs;
+    double* delta;
+    LmState* st;
+    WinCtl* ctl;
+    const int32_t* win_pose0;
+    const int64_t* win_s_off;
+};
+
+struct BatchDev {
+    LmState* st = nullptr;       // [nwin]
+    WinCtl* ctl = nullptr;       // [nwin]
+    int* counters = nullptr;     // [kBatchBuckets] work-queue heads
+    int* any_active = nullptr;   // [1]
+    int* rounds = nullptr;       // [1] attempt rounds run
+    int32_t* lists = nullptr;    // [nwin] windows by bucket, largest first within a bucket
+    int bucket_off[kBatchBuckets + 1] = {0};
+    int threads[kBatchBuckets] = {0};
+    int blocks[kBatchBuckets] = {0};
+};
+
+template <typename T>
+void launch_batch_prologue(const DevProblem& P, DevWork& W, BatchDev& B, const BatchParams& prm, cudaStream_t s);
+template <typename T>
+cudaError_t launch_batch_round(const DevProblem& P, DevWork& W, BatchDev& B, const BatchParams& prm, cudaStream_t s);
+// Times the reduced-solve kernel of one bucket on synthetic SPD blocks for
+// each candidate block size; returns the fastest block size and the number
+// of its CTAs resident per SM.
+template <typename TF>
+cudaError_t bsolve_autotune(int bucket, int sms, cudaStream_t s, int* threads_out, int* blocks_per_sm_out,
+                            float* us_out);
+template <typename TF>
+int bsolve_max_blocks_per_sm(int bucket, int threads);
 
 // ---- adjoint (ba_adjoint.cu) ----
 constexpr int kAdjRecord = 64;  // doubles per observation in the adjoint record

@@ -704,6 +704,18 @@ void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s) {
 }
 
 template <typename T>
+void launch_w(const DevProblem& P, DevWork& W, cudaStream_t s) {
+    if (P.M > 0) { k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch(); }
+}
+
+template <typename T>
+void launch_schur_chunks(const DevProblem& P, DevWork& W, cudaStream_t s) {
+    if (P.nchunks > 0) {
+        k_schur_chunks<T><<<grid_for(P.nchunks), kThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial); note_launch();
+    }
+}
+
+template <typename T>
 void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
     if (P.L > 0) { k_backsub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st); note_launch(); }
 }
@@ -744,5 +756,10 @@ template void launch_schur<float>(const DevProblem&, DevWork&, const LmState*, c
 template void launch_backsub<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 template void launch_bs<double>(const DevProblem&, DevWork&, cudaStream_t);
 template void launch_backsub<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
+template void launch_bs<float>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_w<double>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_w<float>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_schur_chunks<double>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_schur_chunks<float>(const DevProblem&, DevWork&, cudaStream_t);
 
 }  // namespace zs
