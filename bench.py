@@ -46,7 +46,10 @@ def parse():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-windows measurement")
     ap.add_argument("--batch-windows", type=int, default=256)
-    ap.add_argument("--single", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
+                    help="1: one graph launch per batched solve; 0: host loop over rounds (same kernels; "
+                         "for profilers that cannot see kernels inside conditional graph nodes)")
+    ap.add_argument("--single", choices=["mixed", "fp64", "batch-mixed", "batch-fp64"], default=None,
                     help="run one solve of --iterations (default 2) on the workload and exit; for profilers")
     return ap.parse_args()
 
@@ -241,9 +244,12 @@ def batch_run(wins, precision: int, steps: int, warmup: int, iters: int, device:
             ms += brep.ms_total
             it += sum(r.iterations for r in reps)
             obs_att += sum(r.attempts * w.M for r, w in zip(reps, wins))
+            sweeps = sum(r.refine_sweeps for r in reps)
+            attempts = sum(r.attempts for r in reps)
             launches += brep.kernel_launches
         dist.barrier()
         return dict(ms=ms, iterations=it, obs_attempts=obs_att, launches=launches,
+                    refine_sweeps_per_attempt=sweeps / max(attempts, 1),
                     chi2=np.array([r.chi2_final for r in reps]), brep=brep.as_dict())
 
 
@@ -267,6 +273,7 @@ def batch_section(args, dist: Dist) -> dict:
                     "obs_per_s": dist.sum(r["obs_attempts"]) / sec,
                     "ms_per_batch": dist.max(r["ms"]) / args.steps,
                     "rounds": r["brep"]["rounds"], "graph_launches_per_batch": r["brep"]["graph_launches"],
+                    "refine_sweeps_per_attempt": r["refine_sweeps_per_attempt"],
                     "kernel_launches_per_batch": r["launches"] / args.steps,
                     "bucket_windows": r["brep"]["bucket_windows"], "bucket_threads": r["brep"]["bucket_threads"]}
     out["mixed_over_fp64"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
@@ -453,8 +460,20 @@ def single_solve(args):
     """One solve on the workload, nothing else: the unit a profiler captures."""
     from zeroslam_gb300 import ba
 
+    prec = ba.MIXED if args.single.endswith("mixed") else ba.FP64
+    if args.single.startswith("batch"):
+        from zeroslam_gb300 import scenes
+
+        wins = scenes.window_batch(args.batch_windows)
+        with ba.BundleAdjuster(precision=prec, batch_graph=args.batch_graph) as h:
+            h.set_batch(wins)
+            h.solve_batch(10)  # tunes and captures the graph
+            h.reset_state()
+            _, reps, brep = h.solve_batch(args.iterations or 10)
+        print(json.dumps({"single": args.single, "windows": len(wins), "rounds": brep.rounds,
+                          "ms_total": brep.ms_total, "kernel_launches": brep.kernel_launches}), flush=True)
+        return
     sc = make_scene(args.workload)
-    prec = ba.MIXED if args.single == "mixed" else ba.FP64
     with ba.BundleAdjuster(precision=prec) as h:
         h.set_problem(sc)
         rep = h.solve(args.iterations or 2)

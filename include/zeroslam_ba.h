@@ -209,6 +209,11 @@ int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windo
  * accepted steps summed over windows, or a negative status. */
 int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* window_reports,
                       zs_ba_batch_report* rep);
+/* With options.profile: per window, the SM cycles the last zs_ba_solve_batch
+ * spent in each phase of its reduced solves (load, factor, first solve,
+ * refinement; summed over attempts) and its refinement sweeps:
+ * out[window * 5 + phase]. */
+int zs_ba_batch_solve_profile(zs_ba_handle* h, long long* out);
 /* Current state of one window ([K_w*7], [L_w*3]; either may be NULL). */
 int zs_ba_get_window_state(zs_ba_handle* h, int window, double* poses, double* landmarks);
 

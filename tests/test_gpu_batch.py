@@ -104,7 +104,7 @@ def test_batch_mixed_final_cost(zs_lib):
     for w in range(len(wins)):
         assert abs(r32[w].chi2_final - r64[w].chi2_final) <= MIXED_COST_TOL * r64[w].chi2_final, w
     assert sum(brep.bucket_windows) == len(wins)
-    assert all(t in (128, 256, 512, 1024) for t, c in zip(brep.bucket_threads, brep.bucket_windows) if c)
+    assert all(t in (64, 128, 256, 512, 1024) for t, c in zip(brep.bucket_threads, brep.bucket_windows) if c)
 
 
 def test_batch_uneven_and_degenerate_windows(zs_lib, oracle):
@@ -140,3 +140,18 @@ def test_batch_rejects_oversized_and_mixed_cameras(zs_lib):
         h.set_batch([a])
         with pytest.raises(ba.ZsError):
             h.solve(3)  # single-problem entry points refuse a batch
+
+
+def test_batch_autotune_cache_file(zs_lib, tmp_path):
+    import json
+
+    path = tmp_path / "tune.json"
+    wins = _small_batch(4, seed=21)
+    with _ba(1, autotune_cache=str(path).encode()) as h:
+        h.set_batch(wins)
+        _, _, brep = h.solve_batch(3)
+    d = json.loads(path.read_text())
+    used = [b for b, c in enumerate(brep.bucket_windows) if c]
+    got = {(e["precision"], e["bucket"]): e["threads"] for e in d["entries"]}
+    for b in used:
+        assert got[("mixed", b)] == brep.bucket_threads[b]

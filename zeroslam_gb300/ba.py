@@ -99,7 +99,7 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
-                 "zs_ba_solve_batch", "zs_ba_get_window_state")
+                 "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile")
 
 
 def library_path() -> str:
@@ -151,6 +151,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_ba_set_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(Problem)]
     lib.zs_ba_solve_batch.restype = C.c_int
     lib.zs_ba_solve_batch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(Report), C.POINTER(BatchReport)]
+    lib.zs_ba_batch_solve_profile.restype = C.c_int
+    lib.zs_ba_batch_solve_profile.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     lib.zs_ba_get_window_state.restype = C.c_int
     lib.zs_ba_get_window_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
@@ -256,6 +258,16 @@ class BundleAdjuster:
         if v < 0:
             raise ZsError(v, "zs_ba_solve_batch")
         return v, list(reps), brep
+
+    def batch_solve_profile(self) -> np.ndarray:
+        """[windows, 5]: SM cycles per reduced-solve phase (load, factor, first
+        solve, refinement) and refinement sweeps of the last batched solve
+        (needs profile=1)."""
+        out = np.zeros((len(self.windows), 5), dtype=np.int64)
+        st = self.lib.zs_ba_batch_solve_profile(self.h, out.ctypes.data_as(C.POINTER(C.c_longlong)))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_batch_solve_profile")
+        return out
 
     def get_window_state(self, w: int):
         K, L = self.windows[w]

@@ -159,8 +159,17 @@ struct zs_ba_handle {
         bgraph_iters = bgraph_rel = -1;
     }
 
+    void release_batch_streams() {
+        for (int b = 0; b < kBatchBuckets; ++b) {
+            if (B.streams[b]) cudaStreamDestroy(B.streams[b]);
+            if (B.ev_join[b]) cudaEventDestroy(B.ev_join[b]);
+        }
+        if (B.ev_fork) cudaEventDestroy(B.ev_fork);
+    }
+
     void release_problem() {
         release_graph();
+        release_batch_streams();
         for (void* p : owned) cudaFree(p);
         owned.clear();
         P = DevProblem{};
@@ -1062,6 +1071,9 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
 
 namespace {
 
+// Version of the window-solve kernel the tuning results belong to.
+constexpr const char* kTuneKernel = "bsolve-tiles32-v2";
+
 // Autotuned reduced-solve block sizes per (device name, precision, bucket),
 // shared by all handles of the process and optionally kept in a file:
 // one JSON object per line inside {"entries": [ ... ]}.
@@ -1076,23 +1088,33 @@ TuneCache& tune_cache() {
     return c;
 }
 
-void tune_load_locked(TuneCache& c, const char* path) {
-    if (!path || c.loaded.count(path)) return;
-    c.loaded.insert(path);
+// Returns false when a path is given but no cache file exists there yet.
+bool tune_load_locked(TuneCache& c, const char* path) {
+    if (!path) return true;
     FILE* f = std::fopen(path, "r");
-    if (!f) return;
+    if (!f) return false;
+    if (c.loaded.count(path)) {
+        std::fclose(f);
+        return true;
+    }
+    c.loaded.insert(path);
     char line[512];
     while (std::fgets(line, sizeof(line), f)) {
         char dev[256] = {0}, prec[16] = {0};
         int bucket = -1, threads = 0;
-        if (std::sscanf(line, " {\"device\": \"%255[^\"]\", \"precision\": \"%15[^\"]\", \"bucket\": %d, \"threads\": %d",
-                        dev, prec, &bucket, &threads) == 4 &&
-            bucket >= 0 && bucket < kBatchBuckets && (threads == 128 || threads == 256 || threads == 512 || threads == 1024)) {
+        char kern[64] = {0};
+        if (std::sscanf(line, " {\"kernel\": \"%63[^\"]\", \"device\": \"%255[^\"]\", \"precision\": \"%15[^\"]\", "
+                              "\"bucket\": %d, \"threads\": %d",
+                        kern, dev, prec, &bucket, &threads) == 5 &&
+            std::strcmp(kern, kTuneKernel) == 0 &&
+            bucket >= 0 && bucket < kBatchBuckets &&
+            (threads == 64 || threads == 128 || threads == 256 || threads == 512 || threads == 1024)) {
             const int ts = std::strcmp(prec, "fp64") == 0 ? 8 : 4;
             c.threads[std::make_tuple(std::string(dev), ts, bucket)] = threads;
         }
     }
     std::fclose(f);
+    return true;
 }
 
 void tune_save_locked(TuneCache& c, const char* path) {
@@ -1102,8 +1124,8 @@ void tune_save_locked(TuneCache& c, const char* path) {
     std::fprintf(f, "{\"entries\": [\n");
     size_t i = 0;
     for (const auto& e : c.threads) {
-        std::fprintf(f, "  {\"device\": \"%s\", \"precision\": \"%s\", \"bucket\": %d, \"threads\": %d}%s\n",
-                     std::get<0>(e.first).c_str(), std::get<1>(e.first) == 8 ? "fp64" : "mixed", std::get<2>(e.first),
+        std::fprintf(f, "  {\"kernel\": \"%s\", \"device\": \"%s\", \"precision\": \"%s\", \"bucket\": %d, \"threads\": %d}%s\n",
+                     kTuneKernel, std::get<0>(e.first).c_str(), std::get<1>(e.first) == 8 ? "fp64" : "mixed", std::get<2>(e.first),
                      e.second, ++i < c.threads.size() ? "," : "");
     }
     std::fprintf(f, "]}\n");
@@ -1120,8 +1142,7 @@ void batch_tune(zs_ba_handle* h) {
     ZS_CUDA(cudaGetDeviceProperties(&prop, h->device));
     TuneCache& c = tune_cache();
     std::lock_guard<std::mutex> lock(c.mu);
-    tune_load_locked(c, h->opt.autotune_cache);
-    bool tuned = false;
+    bool tuned = !tune_load_locked(c, h->opt.autotune_cache);
     for (int b = 0; b < kBatchBuckets; ++b) {
         const int cnt = B.bucket_off[b + 1] - B.bucket_off[b];
         if (cnt == 0 || B.threads[b] > 0) continue;
@@ -1219,6 +1240,11 @@ int solve_batch_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_r
         r.bucket_tune_us[b] = h->tune_us[b];
     }
     BatchParams prm = batch_params(h, iterations, use_relative);
+    if (h->opt.profile && !B.prof) {
+        B.prof = dalloc<long long>((size_t)P.nwin * kBatchProfSlots, h->owned);
+        h->release_graph();  // the captured kernels must see the profile buffer
+    }
+    if (B.prof) ZS_CUDA(cudaMemsetAsync(B.prof, 0, sizeof(long long) * P.nwin * kBatchProfSlots, s));
     const long long launches0 = launch_counter();
     if (h->opt.batch_graph) {
         if (!h->bexec || h->bgraph_iters != iterations || h->bgraph_rel != (int)use_relative) {
@@ -1368,6 +1394,11 @@ int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windo
             B.bucket_off[b + 1] = (int)lists.size();
         }
         auto& own = h->owned;
+        ZS_CUDA(cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming));
+        for (int b = 0; b < kBatchBuckets; ++b) {
+            ZS_CUDA(cudaStreamCreateWithFlags(&B.streams[b], cudaStreamNonBlocking));
+            ZS_CUDA(cudaEventCreateWithFlags(&B.ev_join[b], cudaEventDisableTiming));
+        }
         B.lists = upload(lists, own, h->stream);
         B.st = dalloc<LmState>(num_windows, own);
         B.ctl = dalloc<WinCtl>(num_windows, own);
@@ -1408,6 +1439,21 @@ int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_r
         if (rep) rep->status = st;
         return st;
     }
+}
+
+int zs_ba_batch_solve_profile(zs_ba_handle* h, long long* out) {
+    if (!h || !out) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (!h->batch || !h->B.prof) return ZS_ERR_INVALID;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        ZS_CUDA(cudaMemcpyAsync(out, h->B.prof, sizeof(long long) * h->P.nwin * kBatchProfSlots,
+                                cudaMemcpyDeviceToHost, h->stream));
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
 }
 
 int zs_ba_get_window_state(zs_ba_handle* h, int window, double* poses, double* landmarks) {

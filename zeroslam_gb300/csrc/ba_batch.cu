@@ -436,79 +436,238 @@ __global__ void k_breset(int* counters, int* any_active, int* rounds) {
 
 // ------------------------------------------------------------ reduced solve
 
-// In-place triangular solves L L^T v = v by one warp, FP64 accumulation;
-// lane l keeps rows l, l + 32, ... in registers. dinv = 1 / L_kk.
-template <typename TF, int NS>
-__device__ void warp_chol_solve(const TF* __restrict__ A, const double* __restrict__ dinv, int n, double* v) {
-    const int lane = threadIdx.x & 31;
-    double y[NS];
+// A window's S lives in shared memory as the lower triangle of 32 x 32
+// tiles, tile (ib, jb) (jb <= ib) at tile index ib (ib + 1) / 2 + jb, rows
+// padded to kLd elements so that row- and column-wise warp accesses hit
+// distinct banks. Rows and columns from n up to the next multiple of 32 are
+// an identity block (zero right-hand side), so every loop runs on whole tiles.
+constexpr int kLd = 33;
+constexpr int kTile = 32 * kLd;
+
+template <typename TF>
+__device__ __forceinline__ TF* tile_at(TF* A, int ib, int jb) {
+    return A + (ib * (ib + 1) / 2 + jb) * kTile;
+}
+
+// Blocked right-looking Cholesky of the nbw x nbw tile lower triangle.
+// Per diagonal tile: warp 0 factors it (a row per lane in registers) and
+// inverts it (a column of L_kk^-1 per lane, right-looking so that the 32
+// accumulators are independent), storing L_kk^-1 transposed in the tile's
+// unused upper triangle (tile[j][i] = (L_kk^-1)[i][j], j < i) and 1 / L_ii in
+// dinv; the panel below is then the product A(ib, kb) L_kk^-T (a row per
+// thread, no division chain), and the trailing tiles get a rank-32 update.
+// Pivot test d > eps_i over the real rows (i < n): eps_i = 1e-14 max|S_ii| sc_i^2
+// is the reference's test on the unscaled pivot
+// (source/matrix_decomposition_cholesky.hpp:40,53).
+// Returns 1 on success (uniform over the CTA).
+template <typename TF>
+__device__ int cta_cholesky(TF* A, int nbw, int n, const TF* eps, TF* dinv, int* s_flag) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int kb = 0; kb < nbw; ++kb) {
+        TF* D = tile_at(A, kb, kb);
+        // 1. diagonal tile by warp 0
+        if (warp == 0) {
+            TF row[32];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const int i = lane + 32 * s;
-        y[s] = i < n ? v[i] : 0.0;
-    }
-    for (int k = 0; k < n; ++k) {
-        const int owner = k & 31, slot = k >> 5;
-        double yk = 0.0;
+            for (int j = 0; j < 32; ++j) row[j] = D[lane * kLd + j];
+            int fail = 0;
 #pragma unroll
-        for (int s = 0; s < NS; ++s)
-            if (s == slot) yk = y[s];
-        yk = __shfl_sync(0xffffffffu, yk * dinv[k], owner);
+            for (int c = 0; c < 32; ++c) {
+                const TF d = __shfl_sync(0xffffffffu, row[c], c);
+                if (32 * kb + c < n && !(d > eps[32 * kb + c])) fail = 1;
+                const TF lcc = sqrt(d);
+                if (lane == c) row[c] = lcc;
+                if (lane > c) row[c] = row[c] / lcc;
+                const TF lic = row[c];
 #pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            const int i = lane + 32 * s;
-            if (i == k) y[s] = yk;
-            else if (i > k && i < n) y[s] -= (double)A[tri(i) + k] * yk;
+                for (int j = 0; j < 32; ++j) {
+                    if (j > c) {
+                        const TF ljc = __shfl_sync(0xffffffffu, lic, j);
+                        if (lane >= j) row[j] -= lic * ljc;
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j <= 31; ++j)
+                if (j <= lane) D[lane * kLd + j] = row[j];
+            // 1 / L_ii of this tile
+            TF lii = TF(0);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (j == lane) lii = row[j];
+            dinv[32 * kb + lane] = TF(1) / lii;
+            __syncwarp();
+            // column `lane` of L_kk^-1, right-looking
+            TF acc[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) acc[i] = TF(0);
+#pragma unroll
+            for (int m = 0; m < 32; ++m) {
+                const TF dm = TF(1) / D[m * kLd + m];
+                const TF ym = (m < lane) ? TF(0) : ((m == lane) ? dm : -acc[m] * dm);
+                acc[m] = ym;  // acc[m] now holds y_m
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                    if (i > m) acc[i] += D[i * kLd + m] * ym;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < 32; ++i)
+                if (i > lane) D[lane * kLd + i] = acc[i];
+            if (lane == 0) *s_flag = fail;
         }
-    }
-    for (int k = n - 1; k >= 0; --k) {
-        const int owner = k & 31, slot = k >> 5;
-        double xk = 0.0;
+        __syncthreads();
+        if (*s_flag) return 0;
+        // 2. panel: L(ib, kb) = A(ib, kb) L_kk^-T, a row per thread:
+        //    out_j = a_j / L_jj + sum_{m < j} a_m (L_kk^-1)[j][m]
+        const int rows = 32 * (nbw - kb - 1);
+        for (int t = tid; t < rows; t += blockDim.x) {
+            const int ib = kb + 1 + (t >> 5), r = t & 31;
+            TF* Ar = tile_at(A, ib, kb) + r * kLd;
+            TF a[32], o[32];
 #pragma unroll
-        for (int s = 0; s < NS; ++s)
-            if (s == slot) xk = y[s];
-        xk = __shfl_sync(0xffffffffu, xk * dinv[k], owner);
-        const TF* row = A + tri(k);
+            for (int j = 0; j < 32; ++j) a[j] = Ar[j];
 #pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            const int i = lane + 32 * s;
-            if (i == k) y[s] = xk;
-            else if (i < k) y[s] -= (double)row[i] * xk;
+            for (int j = 0; j < 32; ++j) o[j] = a[j] * dinv[32 * kb + j];
+#pragma unroll
+            for (int m = 0; m < 32; ++m)
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (j > m) o[j] += a[m] * D[m * kLd + j];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) Ar[j] = o[j];
         }
-    }
+        __syncthreads();
+        // 3. trailing update A(ib, jb) -= L(ib, kb) L(jb, kb)^T, 4 x 4 outputs per item
+        const int m = nbw - kb - 1;
+        const int items = (m * (m + 1) / 2) * 64;
+        for (int it = tid; it < items; it += blockDim.x) {
+            const int t = it >> 6, u = it & 63;
+            int ta = 0;
+            while ((ta + 1) * (ta + 2) / 2 <= t) ++ta;
+            const int tb = t - ta * (ta + 1) / 2;
+            const int ib = kb + 1 + ta, jb = kb + 1 + tb;
+            const int ur = (u >> 3) * 4, uc = (u & 7) * 4;
+            if (ib == jb && uc > ur) continue;
+            const TF* Li = tile_at(A, ib, kb) + ur * kLd;
+            const TF* Lj = tile_at(A, jb, kb) + uc * kLd;
+            TF acc[4][4];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const int i = lane + 32 * s;
-        if (i < n) v[i] = y[s];
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 4; ++y) acc[x][y] = TF(0);
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                TF av[4], bv[4];
+#pragma unroll
+                for (int x = 0; x < 4; ++x) av[x] = Li[x * kLd + k];
+#pragma unroll
+                for (int y = 0; y < 4; ++y) bv[y] = Lj[y * kLd + k];
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) acc[x][y] += av[x] * bv[y];
+            }
+            TF* O = tile_at(A, ib, jb) + ur * kLd + uc;
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 4; ++y) O[x * kLd + y] -= acc[x][y];
+        }
+        __syncthreads();
+    }
+    return 1;
+}
+
+// v <- (L L^T)^-1 v over the tiles with the diagonal-tile inverses, in the
+// factor's precision (the mixed form's accuracy comes from the FP64
+// residual of the refinement): per tile a 32-wide product by warp 0, then
+// the off-diagonal update by the whole CTA (a row per thread).
+template <typename TF>
+__device__ void cta_chol_solve(const TF* A, const TF* dinv, int nbw, TF* v) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int kb = 0; kb < nbw; ++kb) {
+        const TF* D = tile_at(const_cast<TF*>(A), kb, kb);
+        if (warp == 0) {
+            const TF* vb = v + 32 * kb;
+            TF y = dinv[32 * kb + lane] * vb[lane];
+#pragma unroll 8
+            for (int j = 0; j < 32; ++j)
+                if (j < lane) y += D[j * kLd + lane] * vb[j];
+            __syncwarp();
+            v[32 * kb + lane] = y;
+        }
+        __syncthreads();
+        const int rows = 32 * (nbw - kb - 1);
+        for (int t = tid; t < rows; t += blockDim.x) {
+            const int ib = kb + 1 + (t >> 5), r = t & 31;
+            const TF* Lr = tile_at(const_cast<TF*>(A), ib, kb) + r * kLd;
+            TF acc0 = TF(0), acc1 = TF(0);
+#pragma unroll
+            for (int c = 0; c < 32; c += 2) {
+                acc0 += Lr[c] * v[32 * kb + c];
+                acc1 += Lr[c + 1] * v[32 * kb + c + 1];
+            }
+            v[32 * ib + r] -= acc0 + acc1;
+        }
+        __syncthreads();
+    }
+    for (int kb = nbw - 1; kb >= 0; --kb) {
+        const TF* D = tile_at(const_cast<TF*>(A), kb, kb);
+        if (warp == 0) {
+            const TF* vb = v + 32 * kb;
+            TF x = dinv[32 * kb + lane] * vb[lane];
+#pragma unroll 8
+            for (int i = 0; i < 32; ++i)
+                if (i > lane) x += D[lane * kLd + i] * vb[i];
+            __syncwarp();
+            v[32 * kb + lane] = x;
+        }
+        __syncthreads();
+        const int cols = 32 * kb;
+        for (int t = tid; t < cols; t += blockDim.x) {
+            const int jb = t >> 5, cidx = t & 31;
+            const TF* Lc = tile_at(const_cast<TF*>(A), kb, jb) + cidx;
+            TF acc0 = TF(0), acc1 = TF(0);
+#pragma unroll
+            for (int c = 0; c < 32; c += 2) {
+                acc0 += Lc[c * kLd] * v[32 * kb + c];
+                acc1 += Lc[(c + 1) * kLd] * v[32 * kb + c + 1];
+            }
+            v[32 * jb + cidx] -= acc0 + acc1;
+        }
+        __syncthreads();
     }
 }
 
-// Shared memory of one CTA of k_bsolve for windows with n <= 32 NS.
-template <typename TF, int NS>
+// Shared memory of one CTA of k_bsolve for windows with n <= 32 NB.
+template <typename TF, int NB>
 constexpr size_t bsolve_smem() {
-    return 4 * sizeof(double) * 32 * NS + sizeof(TF) * 32 * NS +
-           sizeof(TF) * ((size_t)32 * NS * (32 * NS + 1) / 2);
+    return 4 * sizeof(double) * 32 * NB + 3 * sizeof(TF) * 32 * NB +
+           sizeof(TF) * (size_t)(NB * (NB + 1) / 2) * kTile;
 }
 
 // Persistent reduced solve of one size bucket: CTAs take windows from the
 // bucket's queue (list, largest first). Per window: S_w (FP64, global) ->
-// packed lower triangle in shared memory (TF), right-looking Cholesky with
-// pivot test d > 1e-14 max|S_ii|, solve test |L_ii| > 1e-7 max|L_ii|
-// (source/matrix_decomposition_cholesky.hpp:40,53,74,80,89), warp
+// tiles in shared memory (TF), blocked Cholesky with pivot test
+// d > 1e-14 max|S_ii| and solve test |L_ii| > 1e-7 max|L_ii|
+// (source/matrix_decomposition_cholesky.hpp:40,53,74,80,89), blocked
 // triangular solves; with refine_iters > 0, FP64 refinement
 // x += (L L^T)^-1 (b - S x) until ||b - S x|| <= tol ||b||.
-template <typename TF, int NS>
+template <typename TF, int NB>
 __global__ void k_bsolve(BatchView V, const int32_t* __restrict__ list, int count, int* counter, int refine_iters,
                          double refine_tol) {
-    constexpr int NMAX = 32 * NS;
+    constexpr int NMAX = 32 * NB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* xs = reinterpret_cast<double*>(smem_raw);  // [NMAX] solution
     double* rs = xs + NMAX;                            // [NMAX] residual / correction
     double* bv = rs + NMAX;                            // [NMAX] right-hand side
-    double* dinv = bv + NMAX;                          // [NMAX] 1 / L_kk
-    TF* col = reinterpret_cast<TF*>(dinv + NMAX);      // [NMAX] scaled column k
-    TF* A = col + NMAX;                                // packed lower triangle
-    __shared__ int s_idx;
+    double* sc = bv + NMAX;                            // [NMAX] Jacobi scale (mixed form), else 1
+    TF* dinv = reinterpret_cast<TF*>(sc + NMAX);       // [NMAX] 1 / L_ii
+    TF* vt = dinv + NMAX;                              // [NMAX] solve vector in TF
+    TF* eps = vt + NMAX;                               // [NMAX] per-row pivot threshold
+    TF* A = eps + NMAX;                                // tiles
+    __shared__ int s_idx, s_flag;
     __shared__ double s_red[32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     for (;;) {
@@ -519,89 +678,140 @@ __global__ void k_bsolve(BatchView V, const int32_t* __restrict__ list, int coun
         if (idx >= count) return;
         const int w = list[idx];
         if (!V.ctl[w].active) continue;
+        long long t0 = V.prof ? clock64() : 0;
         const int p0 = V.win_pose0[w];
         const int n = 6 * (V.win_pose0[w + 1] - p0);
+        const int nbw = (n + 31) >> 5;
+        const int np = 32 * nbw;
         const double* S = V.S + V.win_s_off[w];
-        for (int i = warp; i < n; i += nwarps) {
-            const double* srow = S + (int64_t)i * n;
-            TF* arow = A + tri(i);
-            for (int j = lane; j <= i; j += 32) arow[j] = (TF)srow[j];
-        }
+        // The mixed form factors D S D, D = diag(S_ii)^-1/2 (Jacobi scaling
+        // keeps the FP32 factor accurate enough for refinement to converge in
+        // few sweeps); the plain form factors S itself.
+        constexpr bool kScale = sizeof(TF) == 4;
         double m = 0.0;
-        for (int i = tid; i < n; i += blockDim.x) {
-            bv[i] = V.bs[6LL * p0 + i];
-            m = fmax(m, fabs(S[(int64_t)i * n + i]));
+        for (int i = tid; i < np; i += blockDim.x) {
+            const double sii = i < n ? S[(int64_t)i * n + i] : 1.0;
+            if (i < n) m = fmax(m, fabs(sii));
+            sc[i] = (kScale && sii > 0.0) ? 1.0 / sqrt(sii) : 1.0;
+            const double b = i < n ? V.bs[6LL * p0 + i] : 0.0;
+            bv[i] = b;
+            xs[i] = b;
         }
         m = cta_max(m, s_red);
-        const double eps_f = 1e-14 * m;
+        for (int i = tid; i < np; i += blockDim.x) eps[i] = (TF)(1e-14 * m * sc[i] * sc[i]);
         __syncthreads();
-        int ok = 1;
-        for (int k = 0; k < n; ++k) {
-            const TF d = A[tri(k) + k];
-            if (!((double)d > eps_f)) {
-                ok = 0;
-                break;
+        // tiles of the lower triangle; identity beyond n. S rows are 16-byte
+        // aligned (n and the block offsets are even): a warp reads 4 rows at
+        // a time as double2, up to 3 x 4 loads in flight per lane.
+        for (int i0 = 4 * warp; i0 < np; i0 += 4 * nwarps) {
+            double2 v[4][NB / 2 + 1];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int i = i0 + q;
+#pragma unroll
+                for (int c = 0; c < NB / 2 + 1; ++c) {
+                    const int j = 2 * (lane + 32 * c);
+                    v[q][c] = (i < n && j < n && j <= i) ? *reinterpret_cast<const double2*>(S + (int64_t)i * n + j)
+                                                         : make_double2(0.0, 0.0);
+                }
             }
-            const TF lkk = sqrt(d);
-            for (int i = k + 1 + tid; i < n; i += blockDim.x) {
-                const TF v = A[tri(i) + k] / lkk;
-                col[i] = v;
-                A[tri(i) + k] = v;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int i = i0 + q;
+                if (i >= np) break;
+                const int ib = i >> 5, r = i & 31;
+                const double si = sc[i];
+#pragma unroll
+                for (int c = 0; c < NB / 2 + 1; ++c) {
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int j = 2 * (lane + 32 * c) + e;
+                        if (j > i) continue;
+                        double x = e ? v[q][c].y : v[q][c].x;
+                        x = (i < n && j < n) ? x * (si * sc[j]) : (i == j ? 1.0 : 0.0);
+                        tile_at(A, ib, j >> 5)[r * kLd + (j & 31)] = (TF)x;
+                    }
+                }
             }
-            __syncthreads();
-            if (tid == 0) A[tri(k) + k] = lkk;
-            for (int i = k + 1 + warp; i < n; i += nwarps) {
-                const TF ci = col[i];
-                TF* arow = A + tri(i);
-                for (int j = k + 1 + lane; j <= i; j += 32) arow[j] -= ci * col[j];
-            }
-            __syncthreads();
         }
+        __syncthreads();
+        auto mark = [&](int slot) {
+            if (V.prof && tid == 0) {
+                const long long t1 = clock64();
+                V.prof[(int64_t)w * kBatchProfSlots + slot] += t1 - t0;
+                t0 = t1;
+            }
+        };
+        mark(0);
+        int ok = cta_cholesky<TF>(A, nbw, n, eps, dinv, &s_flag);
         int sweeps = 0;
         if (ok) {
+            // solve test on the unscaled diagonal L_ii = Ltilde_ii / sc_i
             double lm = 0.0;
             for (int i = tid; i < n; i += blockDim.x) {
-                const double lii = (double)A[tri(i) + i];
-                lm = fmax(lm, fabs(lii));
-                dinv[i] = 1.0 / lii;
+                const double lii = (double)tile_at(A, i >> 5, i >> 5)[(i & 31) * (kLd + 1)];
+                lm = fmax(lm, fabs(lii / sc[i]));
             }
             lm = cta_max(lm, s_red);
             int bad = 0;
             for (int i = tid; i < n; i += blockDim.x)
-                if (!(fabs((double)A[tri(i) + i]) > 1e-7 * lm)) bad = 1;
+                if (!(fabs((double)tile_at(A, i >> 5, i >> 5)[(i & 31) * (kLd + 1)] / sc[i]) > 1e-7 * lm)) bad = 1;
             ok = __syncthreads_or(bad) ? 0 : 1;
         }
+        mark(1);
         if (ok) {
-            for (int i = tid; i < n; i += blockDim.x) xs[i] = bv[i];
+            // x = D (D S D)^-1 D b
+            for (int i = tid; i < np; i += blockDim.x) vt[i] = (TF)(xs[i] * sc[i]);
             __syncthreads();
-            if (warp == 0) warp_chol_solve<TF, NS>(A, dinv, n, xs);
+            cta_chol_solve<TF>(A, dinv, nbw, vt);
+            for (int i = tid; i < np; i += blockDim.x) xs[i] = sc[i] * (double)vt[i];
             __syncthreads();
+            mark(2);
             if (refine_iters > 0) {
                 double b2 = 0.0;
                 for (int i = tid; i < n; i += blockDim.x) b2 += bv[i] * bv[i];
                 b2 = cta_sum(b2, s_red);
                 for (;;) {
-                    for (int i = warp; i < n; i += nwarps) {
-                        const double* srow = S + (int64_t)i * n;
-                        double acc = 0.0;
-                        for (int j = lane; j < n; j += 32) acc += srow[j] * xs[j];
-                        acc = warp_sum_d(acc);
-                        if (lane == 0) rs[i] = bv[i] - acc;
+                    // r = b - S x, 4 rows per warp step, double2 loads
+                    for (int i0 = 4 * warp; i0 < np; i0 += 4 * nwarps) {
+                        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+                        for (int c = 0; c < NB / 2 + 1; ++c) {
+                            const int j = 2 * (lane + 32 * c);
+                            if (j >= n) continue;
+                            const double x0 = xs[j], x1 = xs[j + 1];
+                            double2 v[4];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q)
+                                v[q] = (i0 + q < n) ? *reinterpret_cast<const double2*>(S + (int64_t)(i0 + q) * n + j)
+                                                    : make_double2(0.0, 0.0);
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) acc[q] += v[q].x * x0 + v[q].y * x1;
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const double t = warp_sum_d(acc[q]);
+                            const int i = i0 + q;
+                            if (lane == 0 && i < np) rs[i] = i < n ? bv[i] - t : 0.0;
+                        }
                     }
                     __syncthreads();
                     double r2 = 0.0;
                     for (int i = tid; i < n; i += blockDim.x) r2 += rs[i] * rs[i];
                     r2 = cta_sum(r2, s_red);
                     if (!(r2 > refine_tol * refine_tol * b2) || sweeps >= refine_iters) break;
-                    if (warp == 0) warp_chol_solve<TF, NS>(A, dinv, n, rs);
+                    for (int i = tid; i < np; i += blockDim.x) vt[i] = (TF)(rs[i] * sc[i]);
                     __syncthreads();
-                    for (int i = tid; i < n; i += blockDim.x) xs[i] += rs[i];
+                    cta_chol_solve<TF>(A, dinv, nbw, vt);
+                    for (int i = tid; i < np; i += blockDim.x) xs[i] += sc[i] * (double)vt[i];
                     __syncthreads();
                     ++sweeps;
                 }
             }
+            mark(3);
             for (int i = tid; i < n; i += blockDim.x) V.delta[6LL * p0 + i] = xs[i];
         }
+        if (V.prof && tid == 0) V.prof[(int64_t)w * kBatchProfSlots + 4] += sweeps;
         if (tid == 0) {
             V.st[w].solve_ok = ok;
             V.st[w].refine_sweeps = sweeps;
@@ -611,13 +821,13 @@ __global__ void k_bsolve(BatchView V, const int32_t* __restrict__ list, int coun
 
 // ------------------------------------------------------------ launchers
 
-template <typename TF, int NS>
+template <typename TF, int NB>
 static cudaError_t launch_bsolve_ns(const BatchView& V, const int32_t* list, int count, int* counter, int threads,
                                     int blocks, int refine_iters, double refine_tol, cudaStream_t s) {
     // the kernel's shared-memory limit is raised by bsolve_max_blocks_per_sm,
     // outside any stream capture
-    const size_t smem = bsolve_smem<TF, NS>();
-    k_bsolve<TF, NS><<<blocks, threads, smem, s>>>(V, list, count, counter, refine_iters, refine_tol);
+    const size_t smem = bsolve_smem<TF, NB>();
+    k_bsolve<TF, NB><<<blocks, threads, smem, s>>>(V, list, count, counter, refine_iters, refine_tol);
     note_launch();
     return cudaGetLastError();
 }
@@ -694,14 +904,20 @@ cudaError_t launch_batch_round(const DevProblem& P, DevWork& W, BatchDev& B, con
         note_launch();
     }
     launch_bs<T>(P, W, s);
-    BatchView V{W.S, W.bs, W.delta, B.st, B.ctl, P.win_pose0, P.win_s_off};
+    BatchView V{W.S, W.bs, W.delta, B.st, B.ctl, P.win_pose0, P.win_s_off, B.prof};
     const int refine = sizeof(T) == 4 ? prm.refine_iters : 0;
+    cudaError_t e = cudaEventRecord(B.ev_fork, s);
+    if (e != cudaSuccess) return e;
     for (int b = 0; b < kBatchBuckets; ++b) {
         const int cnt = B.bucket_off[b + 1] - B.bucket_off[b];
         if (cnt == 0) continue;
-        cudaError_t e = launch_bsolve<T>(b, V, B.lists + B.bucket_off[b], cnt, B.counters + b, B.threads[b],
-                                         B.blocks[b], refine, prm.refine_tol, s);
+        cudaStream_t sb = B.streams[b];
+        if ((e = cudaStreamWaitEvent(sb, B.ev_fork, 0)) != cudaSuccess) return e;
+        e = launch_bsolve<T>(b, V, B.lists + B.bucket_off[b], cnt, B.counters + b, B.threads[b], B.blocks[b], refine,
+                             prm.refine_tol, sb);
         if (e != cudaSuccess) return e;
+        if ((e = cudaEventRecord(B.ev_join[b], sb)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s, B.ev_join[b], 0)) != cudaSuccess) return e;
     }
     if (P.L > 0) {
         k_bbacksub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, B.st, B.ctl);
@@ -774,9 +990,9 @@ cudaError_t bsolve_autotune(int bucket, int sms, cudaStream_t s, int* threads_ou
     if (err == cudaSuccess) {
         k_tune_fill<<<grid_for(nn * nwin), kThreads, 0, s>>>(n, nwin, S, bs, st, ctl, pose0, soff, list);
         chk(cudaGetLastError());
-        BatchView V{S, bs, delta, st, ctl, pose0, soff};
-        const int cand[4] = {128, 256, 512, 1024};
-        for (int c = 0; c < 4 && err == cudaSuccess; ++c) {
+        BatchView V{S, bs, delta, st, ctl, pose0, soff, nullptr};
+        const int cand[5] = {64, 128, 256, 512, 1024};
+        for (int c = 0; c < 5 && err == cudaSuccess; ++c) {
             const int t = cand[c];
             const int per_sm = bsolve_max_blocks_per_sm<TF>(bucket, t);
             if (per_sm <= 0) continue;

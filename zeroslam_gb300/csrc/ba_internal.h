@@ -186,7 +186,10 @@ struct BatchView {
     WinCtl* ctl;
     const int32_t* win_pose0;
     const int64_t* win_s_off;
+    long long* prof;  // with options.profile: [nwin][kBatchProfSlots] SM cycles per phase, else null
 };
+// load, factor, first solve, refinement, refinement sweeps
+constexpr int kBatchProfSlots = 5;
 
 struct BatchDev {
     LmState* st = nullptr;       // [nwin]
@@ -194,10 +197,16 @@ struct BatchDev {
     int* counters = nullptr;     // [kBatchBuckets] work-queue heads
     int* any_active = nullptr;   // [1]
     int* rounds = nullptr;       // [1] attempt rounds run
+    long long* prof = nullptr;   // [nwin * kBatchProfSlots] (options.profile)
     int32_t* lists = nullptr;    // [nwin] windows by bucket, largest first within a bucket
     int bucket_off[kBatchBuckets + 1] = {0};
     int threads[kBatchBuckets] = {0};
     int blocks[kBatchBuckets] = {0};
+    // the buckets' reduced solves run concurrently: forked from the main
+    // stream by ev_fork, joined back by ev_join
+    cudaStream_t streams[kBatchBuckets] = {nullptr};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kBatchBuckets] = {nullptr};
 };
 
 template <typename T>
