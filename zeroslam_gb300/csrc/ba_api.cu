@@ -492,8 +492,8 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     W.hpl = dalloc<char>(ts * rs * M, own);
     W.W = dalloc<char>(ts * rs * M, own);
     W.pose_aux = dalloc<double>((size_t)K * 24, own);
-    W.lm_part = dalloc<char>(ts * 9 * M, own);
-    W.pose_part = dalloc<char>(ts * 27 * M, own);
+    W.lm_part = dalloc<char>(ts * 12 * M, own);    // record-major, 9 values padded to 12
+    W.pose_part = dalloc<char>(ts * 28 * M, own);  // record-major, 27 values padded to 28
     W.hpp = dalloc<double>((size_t)K * 36, own);
     W.hll = dalloc<double>((size_t)L * 9, own);
     W.hll_inv = dalloc<double>((size_t)L * 9, own);
@@ -668,7 +668,8 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
     linearize<T>(h);
     {
         PhaseScope ps(h->timer, ZS_PHASE_COST, s);
-        launch_cost(P, W, h->st, false, s);
+        if (sizeof(T) == 4) launch_cost_fast(P, W, h->st, false, s);
+        else launch_cost(P, W, h->st, false, s);
         launch_init_lambda(P, W, h->st, o.tau, o.diagonal_clamp, s);
     }
     read_state(h);
@@ -695,7 +696,8 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
             }
             {
                 PhaseScope ps(h->timer, ZS_PHASE_COST, s);
-                launch_cost(P, W, h->st, true, s);
+                if (sizeof(T) == 4) launch_cost_fast(P, W, h->st, true, s);
+                else launch_cost(P, W, h->st, true, s);
                 launch_decide(h->st, s);
                 launch_rollback(P, h->st, s);
             }

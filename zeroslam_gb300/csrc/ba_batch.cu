@@ -251,7 +251,10 @@ __global__ void __launch_bounds__(kThreads) k_bscale(DevProblem P, const double*
 }
 
 // Cost partial per observation chunk (a CTA per chunk).
-__global__ void __launch_bounds__(kThreads) k_bcost_partial(DevProblem P, double* red, const LmState* __restrict__ st,
+// aux (the mixed form's per-pose sandwich matrices of the current poses):
+// FP64 cost with contracted multiply-adds; null: the reference's rounding.
+__global__ void __launch_bounds__(kThreads) k_bcost_partial(DevProblem P, const double* __restrict__ aux, double* red,
+                                                            const LmState* __restrict__ st,
                                                             const WinCtl* __restrict__ ctl, int initial) {
     __shared__ double sh[kThreads];
     const int c = blockIdx.x;
@@ -261,6 +264,14 @@ __global__ void __launch_bounds__(kThreads) k_bcost_partial(DevProblem P, double
     const int64_t o1 = P.ochunk_ptr[c + 1];
     for (int64_t o = P.ochunk_ptr[c] + threadIdx.x; o < o1; o += blockDim.x) {
         const int pi = P.obs_pose[o], li = P.obs_lm[o];
+        if (aux) {
+            const double* xq = P.lm + (int64_t)li * kLmStride;
+            const double X[3] = {xq[0], xq[1], xq[2]};
+            const double2 uq = P.obs_uv[o];
+            v += cost_fast(aux + (int64_t)pi * kPoseAux, X, uq.x, uq.y, P.intr, P.obs_info ? P.obs_info + 4 * o : nullptr,
+                           P.loss);
+            continue;
+        }
         const double* pp = P.pose + (int64_t)pi * kPoseStride;
         const double* xp = P.lm + (int64_t)li * kLmStride;
         double p[7], X[3];
@@ -882,8 +893,9 @@ int bsolve_max_blocks_per_sm(int bucket, int threads) {
 template <typename T>
 void launch_batch_prologue(const DevProblem& P, DevWork& W, BatchDev& B, const BatchParams& prm, cudaStream_t s) {
     k_breset<<<1, 32, 0, s>>>(B.counters, B.any_active, B.rounds); note_launch();
-    launch_linearize<T>(P, W, s);
-    if (P.nochunks > 0) { k_bcost_partial<<<(int)P.nochunks, kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 1); note_launch(); }
+    launch_linearize<T>(P, W, s);  // (mixed form: also the per-pose sandwich matrices)
+    const double* aux = sizeof(T) == 4 ? W.pose_aux : nullptr;
+    if (P.nochunks > 0) { k_bcost_partial<<<(int)P.nochunks, kThreads, 0, s>>>(P, aux, W.red, B.st, B.ctl, 1); note_launch(); }
     k_bcost_finish<<<grid_for(P.nwin), kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 1); note_launch();
     k_binit<<<P.nwin, kThreads, 0, s>>>(P, W.hpp, W.hll, B.st, B.ctl, prm); note_launch();
 }
@@ -925,7 +937,12 @@ cudaError_t launch_batch_round(const DevProblem& P, DevWork& W, BatchDev& B, con
     }
     k_bupdate<<<grid_for((int64_t)P.K + P.L), kThreads, 0, s>>>(P, W.delta, B.st, B.ctl); note_launch();
     k_bscale<<<P.nwin, kThreads, 0, s>>>(P, W.delta, W.b, B.st, B.ctl); note_launch();
-    if (P.nochunks > 0) { k_bcost_partial<<<(int)P.nochunks, kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 0); note_launch(); }
+    const double* aux = nullptr;
+    if (sizeof(T) == 4) {
+        launch_pose_aux(P, W, s);
+        aux = W.pose_aux;
+    }
+    if (P.nochunks > 0) { k_bcost_partial<<<(int)P.nochunks, kThreads, 0, s>>>(P, aux, W.red, B.st, B.ctl, 0); note_launch(); }
     k_bcost_finish<<<grid_for(P.nwin), kThreads, 0, s>>>(P, W.red, B.st, B.ctl, 0); note_launch();
     k_bdecide<<<1, kThreads, 0, s>>>(P.nwin, B.st, B.ctl, prm, B.counters, B.any_active, B.rounds); note_launch();
     k_brollback<<<grid_for((int64_t)P.K + P.L), kThreads, 0, s>>>(P, B.ctl); note_launch();

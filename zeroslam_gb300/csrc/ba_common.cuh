@@ -213,6 +213,18 @@ __device__ inline double chi2_of(const double r[2], const double* om) {
     return radd(rmul(a, r[0]), rmul(b, r[1]));
 }
 
+// Per-pose data of the mixed form (k_pose_aux): the quaternion-sandwich
+// matrix M (M X = q (0, X) q*, valid for unnormalised q), the translation,
+// the rotation matrix of source/lie.hpp:188-204, pad.
+constexpr int kPoseAux = 24;
+
+// Squared error (or robust cost) of one observation from the per-pose data,
+// in FP64 with contracted multiply-adds: the mixed form's cost. Same
+// quantities as residual() + chi2_of(), without the reference's operation
+// order.
+__device__ inline double cost_fast(const double* __restrict__ a, const double* __restrict__ X, double u_obs,
+                                   double v_obs, const Intrinsics& in, const double* om, const LossParams& loss);
+
 // Deterministic block sum of one value per thread (fixed tree over
 // blockDim.x = kThreads threads). Result valid in thread 0.
 template <typename V>
@@ -239,6 +251,33 @@ inline int grid_for(long long n, int threads = kThreads) {
     long long g = (n + threads - 1) / threads;
     if (g < 1) g = 1;
     return static_cast<int>(g);
+}
+
+__device__ inline double cost_fast(const double* __restrict__ a, const double* __restrict__ X, double u_obs,
+                                   double v_obs, const Intrinsics& in, const double* om, const LossParams& loss) {
+    const double xc = fma(a[0], X[0], fma(a[1], X[1], fma(a[2], X[2], a[9])));
+    const double yc = fma(a[3], X[0], fma(a[4], X[1], fma(a[5], X[2], a[10])));
+    const double zc = fma(a[6], X[0], fma(a[7], X[1], fma(a[8], X[2], a[11])));
+    double r[2];
+    if (zc < 1.0e-12) {
+        r[0] = r[1] = -kBehindPenalty * zc;
+    } else {
+        const double iz = 1.0 / zc;
+        r[0] = u_obs - fma(in.fx, xc * iz, in.cx);
+        r[1] = v_obs - fma(in.fy, yc * iz, in.cy);
+    }
+    double e2;
+    if (!om) {
+        e2 = fma(r[0], r[0], r[1] * r[1]);
+    } else {
+        const double p = fma(r[0], om[0], r[1] * om[2]);
+        const double q = fma(r[0], om[1], r[1] * om[3]);
+        e2 = fma(p, r[0], q * r[1]);
+    }
+    if (!loss.kind) return e2;
+    double rho[3];
+    loss_rho(loss, e2, rho);
+    return rho[0];
 }
 
 }  // namespace zs

@@ -68,8 +68,8 @@ struct DevWork {
     void* hpl = nullptr;       // [M*RS] T, RS = 18 (double) or 20 (float, padded)
     void* W = nullptr;         // [M*RS] T
     double* pose_aux = nullptr; // [K*24] mixed form: per-pose sandwich matrix, translation, rotation
-    void* lm_part = nullptr;   // [9*M] T, component-major
-    void* pose_part = nullptr; // [27*M] T, component-major
+    void* lm_part = nullptr;   // [M*12] T, per-observation landmark records (9 used)
+    void* pose_part = nullptr; // [M*28] T, per-observation pose records (27 used)
     double* hpp = nullptr;     // [K*36]
     double* hll = nullptr;     // [L*9]
     double* hll_inv = nullptr; // [L*9]
@@ -147,6 +147,9 @@ void launch_rollback(const DevProblem& P, const LmState* st, cudaStream_t s);
 void launch_scale(const DevProblem& P, DevWork& W, LmState* st, cudaStream_t s);
 // cost of the current state into st->chi2_new (when only_if_ok, skipped if !st->solve_ok)
 void launch_cost(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, cudaStream_t s);
+// the mixed form's cost (per-pose sandwich matrices of the current poses, then FP64 residuals)
+void launch_cost_fast(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, cudaStream_t s);
+void launch_pose_aux(const DevProblem& P, DevWork& W, cudaStream_t s);
 void launch_init_lambda(const DevProblem& P, DevWork& W, LmState* st, double tau, double clamp, cudaStream_t s);
 void launch_decide(LmState* st, cudaStream_t s);
 void launch_set_solve_ok(LmState* st, int v, cudaStream_t s);

@@ -34,12 +34,49 @@ struct RecStride {
 __constant__ int8_t kUp6[21][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 5}, {1, 1}, {1, 2}, {1, 3}, {1, 4}, {1, 5},
                                    {2, 2}, {2, 3}, {2, 4}, {2, 5}, {3, 3}, {3, 4}, {3, 5}, {4, 4}, {4, 5}, {5, 5}};
 
+// Per-observation partial records: the pose's 21 H_pp entries (upper
+// triangle) and 6 b_p entries, padded to 28; the landmark's 6 H_ll entries
+// and 3 b_l entries, padded to 12. Record-major, written and read as 16-byte
+// vectors.
+constexpr int kPoseRec = 28;
+constexpr int kLmRec = 12;
+
+template <int N>
+__device__ __forceinline__ void store_rec(float* dst, const float (&v)[N]) {
+    static_assert(N % 4 == 0, "record of whole float4");
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i)
+        reinterpret_cast<float4*>(dst)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <int N>
+__device__ __forceinline__ void store_rec(double* dst, const double (&v)[N]) {
+    static_assert(N % 2 == 0, "record of whole double2");
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) reinterpret_cast<double2*>(dst)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+}
+template <int N>
+__device__ __forceinline__ void add_rec(const float* src, float (&acc)[N]) {
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(src) + i);
+        acc[4 * i] += t.x; acc[4 * i + 1] += t.y; acc[4 * i + 2] += t.z; acc[4 * i + 3] += t.w;
+    }
+}
+template <int N>
+__device__ __forceinline__ void add_rec(const double* src, double (&acc)[N]) {
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+        const double2 t = __ldg(reinterpret_cast<const double2*>(src) + i);
+        acc[2 * i] += t.x; acc[2 * i + 1] += t.y;
+    }
+}
+
 // Per-pose data for the mixed form's linearisation: the quaternion-sandwich
 // matrix M with M X = q (0, X) q* (valid for unnormalised q),
 // M = (w^2 - |v|^2) I + 2 v v^T + 2 w [v]x, the translation, and the rotation
 // matrix of source/lie.hpp:188-204 used by the landmark Jacobian.
 // Layout per pose: M (9), t (3), R (9), pad (3).
-constexpr int kAux = 24;
+constexpr int kAux = kPoseAux;
 
 __global__ void __launch_bounds__(kThreads) k_pose_aux(DevProblem P, double* aux) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -172,6 +209,9 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
     const bool pf = P.pose_fixed[pi] != 0, lf = P.lm_fixed[li] != 0;
 
     T* hb = hpl + o * RS;
+    T prec[kPoseRec];
+#pragma unroll
+    for (int k = 0; k < kPoseRec; ++k) prec[k] = T(0);
     if (!pf) {
         T A0[6], A1[6];  // (J_p^T W) columns
 #pragma unroll
@@ -182,10 +222,10 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
 #pragma unroll
         for (int k = 0; k < 21; ++k) {
             const int a = kUp6[k][0], c = kUp6[k][1];
-            pose_part[(int64_t)k * P.M + o] = A0[a] * Jp[c] + A1[a] * Jp[6 + c];
+            prec[k] = A0[a] * Jp[c] + A1[a] * Jp[6 + c];
         }
 #pragma unroll
-        for (int a = 0; a < 6; ++a) pose_part[(int64_t)(21 + a) * P.M + o] = -(Jp[a] * g0 + Jp[6 + a] * g1);
+        for (int a = 0; a < 6; ++a) prec[21 + a] = -(Jp[a] * g0 + Jp[6 + a] * g1);
         if (!lf) {
 #pragma unroll
             for (int a = 0; a < 6; ++a)
@@ -197,10 +237,12 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < 27; ++k) pose_part[(int64_t)k * P.M + o] = T(0);
-#pragma unroll
         for (int k = 0; k < 18; ++k) hb[k] = T(0);
     }
+    store_rec(pose_part + o * kPoseRec, prec);
+    T lrec[kLmRec];
+#pragma unroll
+    for (int k = 0; k < kLmRec; ++k) lrec[k] = T(0);
     if (!lf) {
         T B0[3], B1[3];
 #pragma unroll
@@ -208,18 +250,16 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
             B0[a] = Jl[a] * W00 + Jl[3 + a] * W10;
             B1[a] = Jl[a] * W01 + Jl[3 + a] * W11;
         }
-        lm_part[0 * P.M + o] = B0[0] * Jl[0] + B1[0] * Jl[3];
-        lm_part[1 * P.M + o] = B0[0] * Jl[1] + B1[0] * Jl[4];
-        lm_part[2 * P.M + o] = B0[0] * Jl[2] + B1[0] * Jl[5];
-        lm_part[3 * P.M + o] = B0[1] * Jl[1] + B1[1] * Jl[4];
-        lm_part[4 * P.M + o] = B0[1] * Jl[2] + B1[1] * Jl[5];
-        lm_part[5 * P.M + o] = B0[2] * Jl[2] + B1[2] * Jl[5];
+        lrec[0] = B0[0] * Jl[0] + B1[0] * Jl[3];
+        lrec[1] = B0[0] * Jl[1] + B1[0] * Jl[4];
+        lrec[2] = B0[0] * Jl[2] + B1[0] * Jl[5];
+        lrec[3] = B0[1] * Jl[1] + B1[1] * Jl[4];
+        lrec[4] = B0[1] * Jl[2] + B1[1] * Jl[5];
+        lrec[5] = B0[2] * Jl[2] + B1[2] * Jl[5];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) lm_part[(int64_t)(6 + a) * P.M + o] = -(Jl[a] * g0 + Jl[3 + a] * g1);
-    } else {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) lm_part[(int64_t)k * P.M + o] = T(0);
+        for (int a = 0; a < 3; ++a) lrec[6 + a] = -(Jl[a] * g0 + Jl[3 + a] * g1);
     }
+    store_rec(lm_part + o * kLmRec, lrec);
 }
 
 // Duplicate (pose, landmark) observations: the run's owner gets the sum of
@@ -248,14 +288,11 @@ __global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* _
                                                         double* b) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= P.L) return;
-    T acc[9];
+    T acc[kLmRec];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) acc[k] = T(0);
+    for (int k = 0; k < kLmRec; ++k) acc[k] = T(0);
     const int e = P.lm_ptr[l + 1];
-    for (int o = P.lm_ptr[l]; o < e; ++o) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) acc[k] += lm_part[(int64_t)k * P.M + o];
-    }
+    for (int o = P.lm_ptr[l]; o < e; ++o) add_rec(lm_part + (int64_t)o * kLmRec, acc);
     double* h = hll + (int64_t)l * 9;
     h[0] = acc[0]; h[1] = acc[1]; h[2] = acc[2];
     h[3] = acc[1]; h[4] = acc[3]; h[5] = acc[4];
@@ -264,36 +301,42 @@ __global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* _
     bl[0] = acc[6]; bl[1] = acc[7]; bl[2] = acc[8];
 }
 
-// Per pose: each thread sums its strided share of the pose's observations
-// in T, the thread partials meet in a fixed FP64 tree.
+// Per pose (a CTA): each thread sums its strided share of the pose's
+// observation records in T; the thread partials meet in FP64 through a
+// fixed tree (warp shuffles, then the warps' results in warp order).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T* __restrict__ pose_part, double* hpp,
                                                           double* b) {
-    __shared__ double sh[kThreads];
+    constexpr int NW = kThreads / 32;
+    __shared__ double sh[NW][28];
     const int k = blockIdx.x;
-    T acc[27];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T acc[kPoseRec];
 #pragma unroll
-    for (int c = 0; c < 27; ++c) acc[c] = T(0);
+    for (int c = 0; c < kPoseRec; ++c) acc[c] = T(0);
     const int e = P.pose_ptr[k + 1];
-    for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x) {
-        const int64_t o = P.pose_obs[i];
+    for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x)
+        add_rec(pose_part + (int64_t)P.pose_obs[i] * kPoseRec, acc);
 #pragma unroll
-        for (int c = 0; c < 27; ++c) acc[c] += pose_part[(int64_t)c * P.M + o];
+    for (int c = 0; c < 27; ++c) {
+        double v = (double)acc[c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) sh[warp][c] = v;
     }
-    double* H = hpp + (int64_t)k * 36;
-#pragma unroll 1
-    for (int c = 0; c < 21; ++c) {
-        const double v = block_sum((double)acc[c], sh);
-        if (threadIdx.x == 0) {
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        const int c = threadIdx.x;
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) v += sh[w][c];
+        if (c < 21) {
             const int a = kUp6[c][0], d = kUp6[c][1];
-            H[a * 6 + d] = v;
-            H[d * 6 + a] = v;
+            hpp[(int64_t)k * 36 + a * 6 + d] = v;
+            hpp[(int64_t)k * 36 + d * 6 + a] = v;
+        } else {
+            b[6LL * k + (c - 21)] = v;
         }
-    }
-#pragma unroll 1
-    for (int c = 0; c < 6; ++c) {
-        const double v = block_sum((double)acc[21 + c], sh);
-        if (threadIdx.x == 0) b[6LL * k + c] = v;
     }
 }
 
@@ -586,6 +629,24 @@ __global__ void __launch_bounds__(kThreads) k_cost_partial(DevProblem P, double*
     if (threadIdx.x == 0) red[blockIdx.x] = v;
 }
 
+// The mixed form's cost: FP64 through the per-pose sandwich matrices
+// (k_pose_aux of the current poses), contracted multiply-adds.
+__global__ void __launch_bounds__(kThreads) k_cost_partial_fast(DevProblem P, const double* __restrict__ aux,
+                                                                double* red, const LmState* st, int only_if_ok) {
+    __shared__ double sh[kThreads];
+    if (only_if_ok && !st->solve_ok) return;
+    double v = 0.0;
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < P.M; o += (int64_t)gridDim.x * blockDim.x) {
+        const double* xp = P.lm + (int64_t)P.obs_lm[o] * kLmStride;
+        const double X[3] = {xp[0], xp[1], xp[2]};
+        const double2 uv = P.obs_uv[o];
+        v += cost_fast(aux + (int64_t)P.obs_pose[o] * kAux, X, uv.x, uv.y, P.intr,
+                       P.obs_info ? P.obs_info + 4 * o : nullptr, P.loss);
+    }
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) red[blockIdx.x] = v;
+}
+
 // target: 0 = chi2_new, 1 = scale (+1e-3)
 __global__ void __launch_bounds__(kThreads) k_finish_sum(const double* red, LmState* st, int target, int only_if_ok) {
     __shared__ double sh[kThreads];
@@ -735,6 +796,16 @@ void launch_scale(const DevProblem& P, DevWork& W, LmState* st, cudaStream_t s) 
 
 void launch_cost(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, cudaStream_t s) {
     k_cost_partial<<<kReduceBlocks, kThreads, 0, s>>>(P, W.red, st, only_if_ok ? 1 : 0); note_launch();
+    k_finish_sum<<<1, kThreads, 0, s>>>(W.red, st, 0, only_if_ok ? 1 : 0); note_launch();
+}
+
+void launch_pose_aux(const DevProblem& P, DevWork& W, cudaStream_t s) {
+    if (P.K > 0) { k_pose_aux<<<grid_for(P.K), kThreads, 0, s>>>(P, W.pose_aux); note_launch(); }
+}
+
+void launch_cost_fast(const DevProblem& P, DevWork& W, LmState* st, bool only_if_ok, cudaStream_t s) {
+    launch_pose_aux(P, W, s);
+    k_cost_partial_fast<<<kReduceBlocks, kThreads, 0, s>>>(P, W.pose_aux, W.red, st, only_if_ok ? 1 : 0); note_launch();
     k_finish_sum<<<1, kThreads, 0, s>>>(W.red, st, 0, only_if_ok ? 1 : 0); note_launch();
 }
 
