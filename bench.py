@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-windows measurement")
     ap.add_argument("--batch-windows", type=int, default=256)
+    ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
                     help="1: one graph launch per batched solve; 0: host loop over rounds (same kernels; "
                          "for profilers that cannot see kernels inside conditional graph nodes)")
@@ -281,6 +282,28 @@ def batch_section(args, dist: Dist) -> dict:
     return out
 
 
+def loop_section(args, dist: Dist) -> dict:
+    """The 1000-keyframe loop (200,000 landmarks, ~4M observations, dense
+    6000 x 6000 reduced system), 30 LM iterations, mixed and FP64: one timed
+    solve each after one warm-up solve."""
+    from zeroslam_gb300 import scenes
+
+    sc = scenes.loop_large_scene()
+    iters = sc.iterations
+    m = run_solves(sc, 1, 1, 1, iters, dist.local, dist)
+    d = run_solves(sc, 0, 1, 1, iters, dist.local, dist)
+    out = {"workload": f"loop: K={sc.K} poses, L={sc.L} landmarks, M={sc.M} observations, n={6 * sc.K}, "
+                       f"{iters} LM iterations", "observations": sc.M}
+    for key, r in (("mixed", m), ("fp64", d)):
+        sec = dist.max(r["ms"]) * 1e-3
+        out[key] = {"lm_iters_per_s": dist.sum(r["iterations"]) / sec, "ms_per_solve": dist.max(r["ms"]),
+                    "attempts": r["rep"]["attempts"], "final_chi2": r["chi2"],
+                    "obs_per_s": dist.sum(r["rep"]["attempts"] * sc.M) / sec}
+    out["mixed_over_fp64"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
+    out["mixed_rel_cost_vs_fp64"] = abs(m["chi2"] - d["chi2"]) / d["chi2"]
+    return out
+
+
 def profile_solve(sc, precision: int, iters: int, device: int) -> dict:
     from zeroslam_gb300 import ba
 
@@ -398,6 +421,7 @@ def ours_arm(args, dist: Dist):
     clk = clocks.stop()
 
     batch = None if args.no_batch else batch_section(args, dist)
+    loop = None if args.no_loop else loop_section(args, dist)
 
     prof_m = profile_solve(sc, ba.MIXED, iters, device)
     prof_d = profile_solve(sc, ba.FP64, iters, device)
@@ -452,6 +476,7 @@ def ours_arm(args, dist: Dist):
         "clocks": clk,
         "gpu_launches": int(dist.sum(mixed["launches"])),
         "batched_windows": batch,
+        "loop_4m": loop,
     }
     print(json.dumps(line), flush=True)
 
