@@ -1,0 +1,321 @@
+// Blocked Cholesky S = L L^T of the mixed form's FP32 reduced camera system
+// (n >= 128): one cooperative persistent kernel, 64-wide panels.
+//
+// Per panel k (columns k0 .. k0 + 64):
+//   stage B  (all CTAs) panel rows below: L21 = A21 L11^-T, a 64 x 64 product
+//            per 64-row block with the explicit inverse of L11;
+//   stage C  (all CTAs) trailing lower 64 x 64 tiles: A22 -= L21 L21^T, a
+//            rank-64 update per tile; CTA 0 updates only the next diagonal
+//            tile and then factors it in shared memory (32 x 32 tiles,
+//            ba_tiles.cuh) and forms its inverse (look-ahead), so the next
+//            panel's stage B can start after one grid barrier.
+// Two grid barriers per panel (19 panels at n = 1200, 94 at n = 6000,
+// against 38 / 188 with 32-wide panels). The pivot test is zeroslam's
+// (source/matrix_decomposition_cholesky.hpp:40,53): a pivot must exceed
+// 1e-14 max|S_ii| (st->eps_factor). The output layout is the one the solves
+// read: L in F's lower triangle, zeros above the diagonal inside each
+// diagonal 32 x 32 block (k_diag_inverses then forms the 32 x 32 inverses).
+#include <cooperative_groups.h>
+
+#include "ba_internal.h"
+#include "ba_tiles.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace zs {
+
+namespace {
+
+constexpr int kP = 64;          // panel width and tile size
+constexpr int kPL = kP + 4;     // row of a shared-memory operand: 16-byte rows, conflict-free 128-bit reads
+constexpr int kBlkThreads = 256;
+
+// Dynamic shared memory: two 64 x 64 operands, the diagonal block as three
+// 32 x 32 tiles, the 64 x 64 inverse, per-row pivot thresholds and 1 / L_ii.
+constexpr size_t kBlkSmem = sizeof(float) * (2 * kP * kPL + 3 * kTile + kP * kPL + 2 * kP) + 64;
+
+__device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
+
+// acc[i][j] = sum_m A[ty + 16 i][m] B[tx + 16 j][m] over m < kk rounded up to
+// 4 (operands zero beyond kk). Thread (ty, tx) of a 16 x 16 grid owns rows
+// ty + 16 i and columns tx + 16 j; operands are read as float4 along m: the B
+// reads of 8 consecutive lanes hit distinct 16-byte bank groups (row stride
+// 68 floats), the A reads are broadcasts.
+__device__ __forceinline__ void tile_nt(const float* A, const float* B, int kk, float acc[4][4]) {
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    const int k4 = (kk + 3) >> 2;
+#pragma unroll 1
+    for (int q = 0; q < k4; ++q) {
+        float4 a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = *reinterpret_cast<const float4*>(A + (ty + 16 * i) * kPL + 4 * q);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = *reinterpret_cast<const float4*>(B + (tx + 16 * j) * kPL + 4 * q);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                acc[i][j] = fmaf(a[i].x, b[j].x, acc[i][j]);
+                acc[i][j] = fmaf(a[i].y, b[j].y, acc[i][j]);
+                acc[i][j] = fmaf(a[i].z, b[j].z, acc[i][j]);
+                acc[i][j] = fmaf(a[i].w, b[j].w, acc[i][j]);
+            }
+    }
+}
+
+// 16-byte asynchronous global -> shared copy; src_bytes < 16 zero-fills the rest.
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, int src_bytes) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Rows r0 .. r0 + 64 (clipped to n), columns c0 .. c0 + kk of F into
+// S[row][m] (zero outside). With n % 4 == 0 (16-byte rows) and c0 % 4 == 0:
+// 16-byte asynchronous copies, four per thread, all in flight together.
+// The caller waits (cp_async_wait_all) and synchronises before reading S.
+__device__ __forceinline__ void load_block(const float* F, int n, int r0, int c0, int kk, float* S) {
+    if ((n & 3) == 0) {
+#pragma unroll
+        for (int q = 0; q < (kP * kP / 4) / kBlkThreads; ++q) {
+            const int e = threadIdx.x + q * kBlkThreads;
+            const int r = e >> 4, c4 = (e & 15) * 4;
+            const int row = r0 + r;
+            int bytes = (row < n) ? 4 * min(4, kk - c4) : 0;
+            if (bytes < 0) bytes = 0;
+            const float* src = bytes > 0 ? F + (int64_t)row * n + c0 + c4 : F;
+            cp_async16(S + r * kPL + c4, src, bytes);
+        }
+    } else {
+        float v[(kP * kP) / kBlkThreads];
+#pragma unroll
+        for (int q = 0; q < (kP * kP) / kBlkThreads; ++q) {
+            const int e = threadIdx.x + q * kBlkThreads;
+            const int r = e >> 6, m = e & 63;
+            v[q] = (r0 + r < n && m < kk) ? ldcg(F + (int64_t)(r0 + r) * n + c0 + m) : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < (kP * kP) / kBlkThreads; ++q) {
+            const int e = threadIdx.x + q * kBlkThreads;
+            S[(e >> 6) * kPL + (e & 63)] = v[q];
+        }
+    }
+}
+
+// Factors the diagonal block at (k0, k0) of width kb (<= 64) in shared
+// memory; on success writes L (zeros above the diagonal) into F and the
+// block's inverse L^-1 (64 x 64, zero-padded) into Li. Returns 1 on success
+// (uniform over the CTA).
+__device__ int factor_diag64(float* F, int n, int k0, int kb, float eps, float* T, float* dinv, float* epsr, float* Inv,
+                             float* Li, int* s_flag) {
+    const int nbw = (kb + 31) >> 5;
+    // tiles (identity padding beyond kb)
+    {
+        float v[(kP * kP) / kBlkThreads];
+#pragma unroll
+        for (int q = 0; q < (kP * kP) / kBlkThreads; ++q) {
+            const int e = threadIdx.x + q * kBlkThreads;
+            const int i = e >> 6, j = e & 63;
+            v[q] = (i < kb && j < kb && j <= i) ? ldcg(F + (int64_t)(k0 + i) * n + k0 + j) : (i == j ? 1.f : 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < (kP * kP) / kBlkThreads; ++q) {
+            const int e = threadIdx.x + q * kBlkThreads;
+            const int i = e >> 6, j = e & 63;
+            if (j <= i && (i >> 5) < nbw) tile_at(T, i >> 5, j >> 5)[(i & 31) * kLd + (j & 31)] = v[q];
+        }
+    }
+    if (threadIdx.x < 64) epsr[threadIdx.x] = eps;
+    __syncthreads();
+    if (!cta_cholesky<float>(T, nbw, kb, epsr, dinv, s_flag)) return 0;
+    // full inverse: [Xa 0; -Xc Lb Xa  Xc] from the tile inverses
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+        const int r = e >> 6, c = e & 63;
+        float v = 0.f;
+        if ((r >> 5) == (c >> 5) && (r >> 5) < nbw) {
+            const int b = r >> 5, rr = r & 31, cc = c & 31;
+            v = rr == cc ? dinv[r] : (cc < rr ? tile_at(T, b, b)[cc * kLd + rr] : 0.f);
+        }
+        Inv[r * kPL + c] = v;
+    }
+    __syncthreads();
+    if (nbw == 2) {
+        // W = Lb Xa (32 x 32) into the lower-left quadrant of Inv, then Xc W
+        float w[4];
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * blockDim.x;
+            const int r = e >> 5, c = e & 31;
+            const float* Lb = tile_at(T, 1, 0) + r * kLd;
+            float s = 0.f;
+            for (int m = c; m < 32; ++m) s = fmaf(Lb[m], Inv[m * kPL + c], s);
+            w[q] = s;
+        }
+        __syncthreads();
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * blockDim.x;
+            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = w[q];
+        }
+        __syncthreads();
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * blockDim.x;
+            const int r = e >> 5, c = e & 31;
+            float s = 0.f;
+            for (int m = 0; m <= r; ++m) s = fmaf(Inv[(32 + r) * kPL + 32 + m], Inv[(32 + m) * kPL + c], s);
+            w[q] = -s;
+        }
+        __syncthreads();
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * blockDim.x;
+            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = w[q];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+        const int i = e >> 6, j = e & 63;
+        Li[e] = Inv[i * kPL + j];
+        if (i < kb && j < kb) {
+            float v = 0.f;
+            if (j < i) v = tile_at(T, i >> 5, j >> 5)[(i & 31) * kLd + (j & 31)];
+            else if (j == i) v = tile_at(T, i >> 5, i >> 5)[(i & 31) * (kLd + 1)];
+            else if ((j >> 5) != (i >> 5)) continue;  // upper blocks outside the diagonal 32-blocks keep S
+            F[(int64_t)(k0 + i) * n + k0 + j] = v;
+        }
+    }
+    __syncthreads();
+    return 1;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kBlkThreads) k_chol_blk(int n, float* F, float* Li, LmState* st) {
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sA = reinterpret_cast<float*>(smem_raw);
+    float* sB = sA + kP * kPL;
+    float* T = sB + kP * kPL;
+    float* Inv = T + 3 * kTile;
+    float* dinv = Inv + kP * kPL;
+    float* epsr = dinv + kP;
+    __shared__ int s_flag;
+    const float eps = (float)__ldcg(&st->eps_factor);
+    const int G = gridDim.x;
+    const int nblk = (n + kP - 1) / kP;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    if (blockIdx.x == 0) {
+        if (!factor_diag64(F, n, 0, min(kP, n), eps, T, dinv, epsr, Inv, Li, &s_flag) && threadIdx.x == 0)
+            st->solve_ok = 0;
+    }
+    grid.sync();
+    for (int k = 0; k < nblk; ++k) {
+        if (!__ldcg(&st->solve_ok)) return;
+        const int k0 = k * kP;
+        const int kb = min(kP, n - k0);
+        const int r0 = k0 + kb;
+        if (r0 >= n) break;
+        const int tn = (n - r0 + kP - 1) / kP;  // trailing block rows
+        // stage B: L21 = A21 L11^-T
+        {
+            bool have_li = false;
+            for (int rb = blockIdx.x; rb < tn; rb += G) {
+                if (!have_li) {
+                    float v[(kP * kP) / kBlkThreads];
+#pragma unroll
+                    for (int q = 0; q < (kP * kP) / kBlkThreads; ++q) v[q] = ldcg(Li + threadIdx.x + q * kBlkThreads);
+#pragma unroll
+                    for (int q = 0; q < (kP * kP) / kBlkThreads; ++q) {
+                        const int e = threadIdx.x + q * kBlkThreads;
+                        sB[(e >> 6) * kPL + (e & 63)] = v[q];
+                    }
+                    have_li = true;
+                }
+                const int rr = r0 + rb * kP;
+                load_block(F, n, rr, k0, kb, sA);
+                cp_async_wait_all();
+                __syncthreads();
+                float acc[4][4];
+                tile_nt(sA, sB, kb, acc);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int row = rr + ty + 16 * i, col = tx + 16 * j;
+                        if (row < n && col < kb) F[(int64_t)row * n + k0 + col] = acc[i][j];
+                    }
+                __syncthreads();
+            }
+        }
+        grid.sync();
+        // stage C: trailing tiles (ti, tj), tj <= ti; CTA 0 takes tile (0, 0)
+        // and then factors it (look-ahead)
+        {
+            const int ntiles = tn * (tn + 1) / 2;
+            const int first = (G == 1) ? 0 : (blockIdx.x == 0 ? 0 : blockIdx.x);
+            const int stride = (G == 1) ? 1 : (blockIdx.x == 0 ? ntiles : G - 1);
+            for (int t = first; t < ntiles; t += stride) {
+                int ti = 0;
+                while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+                const int tj = t - ti * (ti + 1) / 2;
+                const int i0 = r0 + ti * kP, j0 = r0 + tj * kP;
+                load_block(F, n, i0, k0, kb, sA);
+                if (ti != tj) load_block(F, n, j0, k0, kb, sB);
+                cp_async_wait_all();
+                __syncthreads();
+                float acc[4][4];
+                tile_nt(sA, ti != tj ? sB : sA, kb, acc);
+                float c[4][4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int row = i0 + ty + 16 * i, col = j0 + tx + 16 * j;
+                        c[i][j] = (row < n && col < n) ? ldcg(F + (int64_t)row * n + col) : 0.f;
+                    }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int row = i0 + ty + 16 * i, col = j0 + tx + 16 * j;
+                        if (row < n && col < n && (ti != tj || col <= row))
+                            F[(int64_t)row * n + col] = c[i][j] - acc[i][j];
+                    }
+                __syncthreads();
+                if (t == 0) {
+                    __threadfence_block();
+                    if (!factor_diag64(F, n, r0, min(kP, n - r0), eps, T, dinv, epsr, Inv, Li, &s_flag) &&
+                        threadIdx.x == 0)
+                        st->solve_ok = 0;
+                }
+            }
+        }
+        grid.sync();
+    }
+}
+
+cudaError_t launch_chol_blk(int n, float* F, float* Li, LmState* st, cudaStream_t s) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaFuncSetAttribute(k_chol_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBlkSmem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_blk, kBlkThreads, kBlkSmem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int nblk = (n + kP - 1) / kP;
+    int blocks = sms * per_sm;  // all co-resident
+    if (blocks > nblk * (nblk + 1) / 2 + 1) blocks = nblk * (nblk + 1) / 2 + 1;
+    if (blocks < 1) blocks = 1;
+    int nn = n;
+    void* args[] = {(void*)&nn, (void*)&F, (void*)&Li, (void*)&st};
+    e = cudaLaunchCooperativeKernel((const void*)k_chol_blk, dim3(blocks), dim3(kBlkThreads), args, kBlkSmem, s);
+    if (e != cudaSuccess) return e;
+    note_launch();
+    return cudaSuccess;
+}
+
+}  // namespace zs

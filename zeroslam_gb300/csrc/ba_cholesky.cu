@@ -478,6 +478,11 @@ static int cluster_size() {
     return c;
 }
 
+// The mixed form's 64-wide-panel factorisation (ba_chol_blk.cu) for n >= 128;
+// D serves as its 64 x 64 scratch before k_diag_inverses fills it.
+cudaError_t launch_chol_blk(int n, float* F, float* Li, LmState* st, cudaStream_t s);
+constexpr int kBlkMinN = 128;
+
 template <typename TS, typename TF>
 cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
@@ -491,11 +496,17 @@ cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStr
     int blocks = sms;  // one CTA per SM, all co-resident
     if (blocks > nblk * (nblk + 1) / 2 + 1) blocks = nblk * (nblk + 1) / 2 + 1;
     if (blocks < 1) blocks = 1;
-    int nn_i = n;
-    void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<TF>, dim3(blocks), dim3(kThreads), args, 0, s);
-    if (e != cudaSuccess) return e;
-    note_launch();
+    cudaError_t e;
+    if (sizeof(TF) == 4 && n >= kBlkMinN) {
+        e = launch_chol_blk(n, reinterpret_cast<float*>(F), reinterpret_cast<float*>(D), st, s);
+        if (e != cudaSuccess) return e;
+    } else {
+        int nn_i = n;
+        void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
+        e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<TF>, dim3(blocks), dim3(kThreads), args, 0, s);
+        if (e != cudaSuccess) return e;
+        note_launch();
+    }
     k_check_solve_eps<TF><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
     k_diag_inverses<TF><<<nblk, kThreads, 0, s>>>(n, F, D, st); note_launch();
     return cudaGetLastError();
