@@ -188,7 +188,7 @@ def test_empty_and_degenerate(zs_lib):
             ba_.set_problem(bad)
 
 
-@pytest.mark.parametrize("n", [1, 31, 33, 64, 100, 257, 600, 1200])
+@pytest.mark.parametrize("n", [1, 31, 33, 64, 100, 130, 257, 600, 1200, 2050])
 def test_dense_cholesky_sizes(zs_lib, n):
     """Multi-panel factorisations, partial last blocks and every level of the
     mixed form's recursive L^-1, against numpy on random SPD systems."""

@@ -41,12 +41,8 @@ __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 // ty + 16 i and columns tx + 16 j; operands are read as float4 along m: the B
 // reads of 8 consecutive lanes hit distinct 16-byte bank groups (row stride
 // 68 floats), the A reads are broadcasts.
-__device__ __forceinline__ void tile_nt(const float* A, const float* B, int kk, float acc[4][4]) {
+__device__ __forceinline__ void tile_nt_acc(const float* A, const float* B, int kk, float acc[4][4]) {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
     const int k4 = (kk + 3) >> 2;
 #pragma unroll 1
     for (int q = 0; q < k4; ++q) {
@@ -67,6 +63,14 @@ __device__ __forceinline__ void tile_nt(const float* A, const float* B, int kk, 
     }
 }
 
+__device__ __forceinline__ void tile_nt(const float* A, const float* B, int kk, float acc[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    tile_nt_acc(A, B, kk, acc);
+}
+
 // 16-byte asynchronous global -> shared copy; src_bytes < 16 zero-fills the rest.
 __device__ __forceinline__ void cp_async16(float* dst, const float* src, int src_bytes) {
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
@@ -75,6 +79,9 @@ __device__ __forceinline__ void cp_async16(float* dst, const float* src, int src
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_none() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Rows r0 .. r0 + 64 (clipped to n), columns c0 .. c0 + kk of F into
 // S[row][m] (zero outside). With n % 4 == 0 (16-byte rows) and c0 % 4 == 0:
@@ -295,6 +302,172 @@ __global__ void __launch_bounds__(kBlkThreads) k_chol_blk(int n, float* F, float
         }
         grid.sync();
     }
+}
+
+namespace {
+
+constexpr size_t kInvSmem = sizeof(float) * 4 * kP * kPL;
+
+// acc = sum over 64-wide K chunks m in [m0, m1) of A[ra rows][m] B[rb rows][m]^T
+// (both row-major with row length n), two-stage asynchronous pipeline.
+__device__ void tile_nt_chunks(const float* A, int ra, const float* B, int rb, int n, int m0, int m1, float* buf,
+                               float acc[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    if (m0 >= m1) return;
+    float* sa[2] = {buf, buf + 2 * kP * kPL};
+    float* sb[2] = {buf + kP * kPL, buf + 3 * kP * kPL};
+    load_block(A, n, ra, kP * m0, min(kP, n - kP * m0), sa[0]);
+    load_block(B, n, rb, kP * m0, min(kP, n - kP * m0), sb[0]);
+    cp_async_commit();
+    for (int m = m0; m < m1; ++m) {
+        const int cur = (m - m0) & 1;
+        if (m + 1 < m1) {
+            load_block(A, n, ra, kP * (m + 1), min(kP, n - kP * (m + 1)), sa[cur ^ 1]);
+            load_block(B, n, rb, kP * (m + 1), min(kP, n - kP * (m + 1)), sb[cur ^ 1]);
+            cp_async_commit();
+            cp_async_wait_one();
+        } else {
+            cp_async_wait_none();
+        }
+        __syncthreads();
+        tile_nt_acc(sa[cur], sb[cur], min(kP, n - kP * m), acc);
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// X = L^-1 (and X^T) of the mixed form's factor, by recursive 2 x 2 block
+// inversion over 64-wide blocks,
+//     inv([A 0; B C]) = [A^-1 0; -C^-1 (B A^-1)  C^-1],
+// level 0 from the 32 x 32 diagonal inverses D_k (k_diag_inverses), then
+// log2(n/64) levels of 64 x 64 output tiles, two grid barriers per level.
+// Every product reads K-contiguous rows: (B A^-1)^T is kept in X's upper
+// triangle (free: the refinement reads X's lower and X^T's upper triangle).
+__global__ void __launch_bounds__(kBlkThreads) k_tri_inverse64(int n, const float* F, const float* D, float* X, float* XT,
+                                                               const LmState* st) {
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* buf = reinterpret_cast<float*>(smem_raw);
+    if (!__ldcg(&st->solve_ok)) return;  // written by an earlier launch: uniform
+    const int nb = (n + kP - 1) / kP;
+    const int nb32 = (n + 31) / 32;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    // level 0: X_bb = [D0 0; -D1 Lb D0  D1] for each 64-block b
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        float* d0 = buf;               // 32 x 33
+        float* d1 = d0 + 32 * 33;
+        float* lb = d1 + 32 * 33;
+        float* w = lb + 32 * 33;
+        float* y = w + 32 * 33;
+        const bool two = 2 * b + 1 < nb32;
+        for (int e = threadIdx.x; e < 1024; e += blockDim.x) {
+            const int r = e >> 5, c = e & 31;
+            d0[r * 33 + c] = ldcg(D + (int64_t)(2 * b) * 1024 + e);
+            d1[r * 33 + c] = two ? ldcg(D + (int64_t)(2 * b + 1) * 1024 + e) : 0.f;
+            const int gr = 64 * b + 32 + r, gc = 64 * b + c;
+            lb[r * 33 + c] = (two && gr < n) ? ldcg(F + (int64_t)gr * n + gc) : 0.f;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 1024; e += blockDim.x) {
+            const int r = e >> 5, c = e & 31;
+            float s = 0.f;
+            for (int m = c; m < 32; ++m) s = fmaf(lb[r * 33 + m], d0[m * 33 + c], s);
+            w[r * 33 + c] = s;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 1024; e += blockDim.x) {
+            const int r = e >> 5, c = e & 31;
+            float s = 0.f;
+            for (int m = 0; m <= r; ++m) s = fmaf(d1[r * 33 + m], w[m * 33 + c], s);
+            y[r * 33 + c] = -s;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 4096; e += blockDim.x) {
+            const int r = e >> 6, c = e & 63;
+            const int gr = 64 * b + r, gc = 64 * b + c;
+            if (gr >= n || gc >= n) continue;
+            float v = 0.f;
+            if (r < 32 && c < 32) v = c <= r ? d0[r * 33 + c] : 0.f;
+            else if (r >= 32 && c >= 32) v = (c <= r) ? d1[(r - 32) * 33 + (c - 32)] : 0.f;
+            else if (r >= 32) v = y[(r - 32) * 33 + c];
+            X[(int64_t)gr * n + gc] = v;
+            XT[(int64_t)gc * n + gr] = v;
+        }
+        __syncthreads();
+    }
+    grid.sync();
+    float* stage = buf;  // 64 x 65 staging for the transposed store
+    for (int s = 1; s < nb; s *= 2) {
+        const int npairs = (nb + 2 * s - 1) / (2 * s);
+        const int ntask = npairs * s * s;
+        // step 1: (T_ij)^T = sum_{m=j}^{c0-1} X^T[j][m] L[i][m]^T -> X rows of j, columns of i
+        for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
+            const int p = t / (s * s), w = t % (s * s);
+            const int a0 = p * 2 * s, c0 = a0 + s;
+            const int i = c0 + w / s, j = a0 + w % s;
+            if (i >= nb) continue;
+            float acc[4][4];
+            tile_nt_chunks(XT, kP * j, F, kP * i, n, j, c0, buf, acc);
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int row = kP * j + ty + 16 * a, col = kP * i + tx + 16 * q;
+                    if (row < n && col < n) X[(int64_t)row * n + col] = acc[a][q];
+                }
+        }
+        grid.sync();
+        // step 2: X_ij = - sum_{m=c0}^{i} X[i][m] (T^T)[j][m]
+        for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
+            const int p = t / (s * s), w = t % (s * s);
+            const int a0 = p * 2 * s, c0 = a0 + s;
+            const int i = c0 + w / s, j = a0 + w % s;
+            if (i >= nb) continue;
+            float acc[4][4];
+            tile_nt_chunks(X, kP * i, X, kP * j, n, c0, i + 1, buf, acc);
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int r = ty + 16 * a, c = tx + 16 * q;
+                    stage[r * 65 + c] = -acc[a][q];
+                    const int row = kP * i + r, col = kP * j + c;
+                    if (row < n && col < n) X[(int64_t)row * n + col] = -acc[a][q];
+                }
+            __syncthreads();
+            for (int e = threadIdx.x; e < 4096; e += blockDim.x) {
+                const int c = e >> 6, r = e & 63;  // XT[col][row], rows of XT along j, coalesced over r
+                const int row = kP * i + r, col = kP * j + c;
+                if (row < n && col < n) XT[(int64_t)col * n + row] = stage[r * 65 + c];
+            }
+            __syncthreads();
+        }
+        grid.sync();
+    }
+}
+
+cudaError_t launch_tri_inverse64(int n, const float* F, const float* D, float* X, float* XT, LmState* st,
+                                 cudaStream_t s) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_tri_inverse64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInvSmem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tri_inverse64, kBlkThreads, kInvSmem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int nn = n;
+    void* args[] = {(void*)&nn, (void*)&F, (void*)&D, (void*)&X, (void*)&XT, (void*)&st};
+    e = cudaLaunchCooperativeKernel((const void*)k_tri_inverse64, dim3(sms * per_sm), dim3(kBlkThreads), args,
+                                    kInvSmem, s);
+    if (e != cudaSuccess) return e;
+    note_launch();
+    return cudaSuccess;
 }
 
 cudaError_t launch_chol_blk(int n, float* F, float* Li, LmState* st, cudaStream_t s) {

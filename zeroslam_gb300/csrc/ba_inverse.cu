@@ -21,6 +21,9 @@ namespace zs {
 
 constexpr int kB = 32;
 
+cudaError_t launch_tri_inverse64(int n, const float* F, const float* D, float* X, float* XT, LmState* st,
+                                 cudaStream_t s);
+
 template <typename T>
 __device__ __forceinline__ T ldc(const T* p) {
     return __ldcg(p);
@@ -233,6 +236,9 @@ static int sm_count() {
 template <typename TX>
 cudaError_t launch_tri_inverse(int n, const TX* F, const TX* D, TX* X, TX* XT, LmState* st, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (sizeof(TX) == 4 && n >= 128)  // 64-wide blocks, asynchronous tile loads (ba_chol_blk.cu)
+        return launch_tri_inverse64(n, reinterpret_cast<const float*>(F), reinterpret_cast<const float*>(D),
+                                    reinterpret_cast<float*>(X), reinterpret_cast<float*>(XT), st, s);
     int nn = n;
     void* args[] = {(void*)&nn, (void*)&F, (void*)&D, (void*)&X, (void*)&XT, (void*)&st};
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_tri_inverse<TX>, dim3(sm_count()), dim3(kThreads), args,
