@@ -17,6 +17,7 @@
 #include <new>
 #include <set>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -38,6 +39,97 @@ struct CudaError {
         cudaError_t e_ = (x);                       \
         if (e_ != cudaSuccess) throw CudaError{e_}; \
     } while (0)
+
+// Device memory of one problem, allocated in a fixed order. A new problem
+// of the same kind reuses the previous problem's buffer at the same position
+// when it is large enough (setting a problem of the same shape again, as a
+// tracking loop does every frame, then allocates nothing).
+struct DevPool {
+    std::vector<std::pair<void*, size_t>> slots;  // this problem's buffers, in allocation order
+    std::vector<std::pair<void*, size_t>> spare;  // the previous problem's, reusable by position
+
+    void* get(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        const size_t i = slots.size();
+        if (i < spare.size() && spare[i].first) {
+            if (spare[i].second >= bytes) {
+                slots.push_back(spare[i]);
+                spare[i].first = nullptr;
+                return slots.back().first;
+            }
+            cudaFree(spare[i].first);
+            spare[i].first = nullptr;
+        }
+        void* p = nullptr;
+        ZS_CUDA(cudaMalloc(&p, bytes));
+        slots.push_back({p, bytes});
+        return p;
+    }
+    // The problem is released; its buffers stay for the next one.
+    void recycle() {
+        trim();
+        spare = std::move(slots);
+        slots.clear();
+    }
+    // Frees the spare buffers no allocation reused.
+    void trim() {
+        for (auto& e : spare)
+            if (e.first) cudaFree(e.first);
+        spare.clear();
+    }
+    void release_all() {
+        trim();
+        for (auto& e : slots) cudaFree(e.first);
+        slots.clear();
+    }
+};
+
+template <typename T>
+T* dalloc(size_t count, DevPool& pool) {
+    return static_cast<T*>(pool.get(count * sizeof(T)));
+}
+
+template <typename T>
+T* upload(const std::vector<T>& v, DevPool& pool, cudaStream_t s) {
+    T* d = dalloc<T>(v.size(), pool);
+    if (!v.empty()) ZS_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+// Host threads for the structure analysis.
+int host_threads() {
+    static const int n = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+    return n;
+}
+
+// f(t, begin, end) on nt threads over [cuts[t], cuts[t + 1]).
+template <typename F>
+void parallel_ranges(const std::vector<int64_t>& cuts, F f) {
+    const int nt = (int)cuts.size() - 1;
+    if (nt <= 1) {
+        if (nt == 1) f(0, cuts[0], cuts[1]);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) th.emplace_back(f, t, cuts[t], cuts[t + 1]);
+    f(0, cuts[0], cuts[1]);
+    for (auto& x : th) x.join();
+}
+
+// Cuts [0, n) into nt ranges of about equal weight (prefix[i] = weight of [0, i)).
+std::vector<int64_t> balanced_cuts(const std::vector<int64_t>& prefix, int nt) {
+    const int64_t n = (int64_t)prefix.size() - 1;
+    std::vector<int64_t> cuts{0};
+    const int64_t total = prefix[n];
+    for (int t = 1; t < nt; ++t) {
+        const int64_t target = total * t / nt;
+        const int64_t c = std::lower_bound(prefix.begin(), prefix.end(), target) - prefix.begin();
+        cuts.push_back(std::max(cuts.back(), std::min(c, n)));
+    }
+    cuts.push_back(n);
+    return cuts;
+}
 
 template <typename T>
 T* dalloc(size_t count, std::vector<void*>& owned) {
@@ -135,7 +227,7 @@ struct zs_ba_handle {
     DevWork W;
     LmState* st = nullptr;       // device
     LmState* st_host = nullptr;  // pinned mirror
-    std::vector<void*> owned;    // problem-lifetime device allocations
+    DevPool owned;               // problem-lifetime device allocations
     double* adj_rec = nullptr;   // adjoint buffers, allocated on first use (owned)
     double* adj_part = nullptr;
     double* adj_vec = nullptr;   // a, v, r, z, p, q, zero: 7 x (n + 3L)
@@ -167,11 +259,12 @@ struct zs_ba_handle {
         if (B.ev_fork) cudaEventDestroy(B.ev_fork);
     }
 
-    void release_problem() {
+    // keep_memory: the buffers stay for reuse by the next problem
+    void release_problem(bool keep_memory = false) {
         release_graph();
         release_batch_streams();
-        for (void* p : owned) cudaFree(p);
-        owned.clear();
+        if (keep_memory) owned.recycle();
+        else owned.release_all();
         P = DevProblem{};
         W = DevWork{};
         adj_rec = adj_part = adj_vec = nullptr;
@@ -330,26 +423,37 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         std::vector<int32_t> fill(lm_ptr.begin(), lm_ptr.end() - 1);
         for (int64_t o = 0; o < M; ++o) perm[fill[p->obs_landmark[o]]++] = o;
     }
-    for (int l = 0; l < L; ++l)
-        std::stable_sort(perm.begin() + lm_ptr[l], perm.begin() + lm_ptr[l + 1],
-                         [&](int64_t a, int64_t b) { return p->obs_pose[a] < p->obs_pose[b]; });
+    const int nt = host_threads();
+    // landmark ranges of about equal observation counts
+    std::vector<int64_t> obs_prefix(L + 1);
+    for (int l = 0; l <= L; ++l) obs_prefix[l] = lm_ptr[l];
+    const std::vector<int64_t> lcuts = balanced_cuts(obs_prefix, (M > 50000 && L > 4 * nt) ? nt : 1);
+    const int nth = (int)lcuts.size() - 1;
     std::vector<int32_t> obs_pose(M), obs_lm(M), dup_owner(M);
     std::vector<double2> uv(M);
     std::vector<double> info(p->obs_info ? 4 * M : 0);
     std::vector<uint8_t> blk_valid(M, 0);
+    std::vector<char> dups(nth, 0);
+    parallel_ranges(lcuts, [&](int t, int64_t l0, int64_t l1) {
+        for (int64_t l = l0; l < l1; ++l) {
+            std::stable_sort(perm.begin() + lm_ptr[l], perm.begin() + lm_ptr[l + 1],
+                             [&](int64_t a, int64_t b) { return p->obs_pose[a] < p->obs_pose[b]; });
+            for (int64_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i) {
+                const int64_t o = perm[i];
+                obs_pose[i] = p->obs_pose[o];
+                obs_lm[i] = p->obs_landmark[o];
+                uv[i] = make_double2(p->obs_uv[2 * o], p->obs_uv[2 * o + 1]);
+                if (p->obs_info)
+                    for (int k = 0; k < 4; ++k) info[4 * i + k] = p->obs_info[4 * o + k];
+                const bool same = i > lm_ptr[l] && obs_pose[i - 1] == obs_pose[i];
+                dup_owner[i] = same ? dup_owner[i - 1] : (int32_t)i;
+                if (same) dups[t] = 1;
+                blk_valid[i] = (!same && !p->pose_fixed[obs_pose[i]] && !p->landmark_fixed[obs_lm[i]]) ? 1 : 0;
+            }
+        }
+    });
     bool has_dups = false;
-    for (int64_t i = 0; i < M; ++i) {
-        const int64_t o = perm[i];
-        obs_pose[i] = p->obs_pose[o];
-        obs_lm[i] = p->obs_landmark[o];
-        uv[i] = make_double2(p->obs_uv[2 * o], p->obs_uv[2 * o + 1]);
-        if (p->obs_info)
-            for (int k = 0; k < 4; ++k) info[4 * i + k] = p->obs_info[4 * o + k];
-        const bool same = i > 0 && obs_lm[i - 1] == obs_lm[i] && obs_pose[i - 1] == obs_pose[i];
-        dup_owner[i] = same ? dup_owner[i - 1] : (int32_t)i;
-        has_dups = has_dups || same;
-        blk_valid[i] = (!same && !p->pose_fixed[obs_pose[i]] && !p->landmark_fixed[obs_lm[i]]) ? 1 : 0;
-    }
+    for (char d : dups) has_dups = has_dups || d;
     // pose-major lists of landmark-major indices, ascending
     std::vector<int32_t> pose_ptr(K + 1, 0), pose_obs(M);
     for (int64_t i = 0; i < M; ++i) pose_ptr[obs_pose[i] + 1]++;
@@ -375,34 +479,60 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         return (size_t)(key_base[w] + (int64_t)(i - wp[w]) * kw + (j - wp[w]));
     };
     const size_t nkeys = (size_t)key_base[nwin];
-    std::vector<int64_t> pair_count(nkeys, 0);
-    std::vector<int32_t> vb;
+    // Threads take landmark ranges of about equal triple counts; each counts
+    // its triples per key, then fills its share of every key's range after the
+    // shares of the threads before it, which is the landmark order a single
+    // pass would give.
+    std::vector<int64_t> tri_prefix(L + 1, 0);
     for (int l = 0; l < L; ++l) {
-        vb.clear();
-        for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
-            if (blk_valid[i]) vb.push_back(i);
-        for (size_t a = 0; a < vb.size(); ++a)
-            for (size_t b = 0; b <= a; ++b) pair_count[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++;
+        int64_t nv = 0;
+        for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i) nv += blk_valid[i];
+        tri_prefix[l + 1] = tri_prefix[l] + nv * (nv + 1) / 2;
     }
+    const int64_t ntriples = tri_prefix[L];
+    const int ntt = (ntriples > 200000 && L > 4 * nt && (size_t)nt * nkeys <= ((size_t)1 << 28)) ? nt : 1;
+    const std::vector<int64_t> tcuts = balanced_cuts(tri_prefix, ntt);
+    const int ntc = (int)tcuts.size() - 1;
+    std::vector<std::vector<int64_t>> counts(ntc, std::vector<int64_t>(nkeys, 0));
+    parallel_ranges(tcuts, [&](int t, int64_t l0, int64_t l1) {
+        std::vector<int32_t> vb;
+        std::vector<int64_t>& c = counts[t];
+        for (int64_t l = l0; l < l1; ++l) {
+            vb.clear();
+            for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
+                if (blk_valid[i]) vb.push_back(i);
+            for (size_t a = 0; a < vb.size(); ++a)
+                for (size_t b = 0; b <= a; ++b) c[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++;
+        }
+    });
     std::vector<int64_t> pair_off(nkeys + 1, 0);
+    std::vector<int64_t> pair_count(nkeys, 0);
     int npairs = 0;
     for (size_t k = 0; k < nkeys; ++k) {
-        pair_off[k + 1] = pair_off[k] + pair_count[k];
-        if (pair_count[k]) ++npairs;
+        int64_t tot = 0;
+        for (int t = 0; t < ntc; ++t) {
+            const int64_t c = counts[t][k];
+            counts[t][k] = pair_off[k] + tot;  // thread t's first position in key k
+            tot += c;
+        }
+        pair_count[k] = tot;
+        pair_off[k + 1] = pair_off[k] + tot;
+        if (tot) ++npairs;
     }
-    const int64_t ntriples = pair_off[nkeys];
     std::vector<int2> triples(ntriples);
-    {
-        std::vector<int64_t> fill(pair_off.begin(), pair_off.end() - 1);
-        for (int l = 0; l < L; ++l) {
+    parallel_ranges(tcuts, [&](int t, int64_t l0, int64_t l1) {
+        std::vector<int32_t> vb;
+        std::vector<int64_t>& pos = counts[t];
+        for (int64_t l = l0; l < l1; ++l) {
             vb.clear();
             for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
                 if (blk_valid[i]) vb.push_back(i);
             for (size_t a = 0; a < vb.size(); ++a)
                 for (size_t b = 0; b <= a; ++b)
-                    triples[fill[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++] = make_int2(vb[a], vb[b]);
+                    triples[pos[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++] = make_int2(vb[a], vb[b]);
         }
-    }
+    });
+    counts.clear();
     std::vector<int32_t> pair_i, pair_j;
     std::vector<int64_t> pair_chunk_ptr{0}, chunk_ptr{0};
     pair_i.reserve(npairs);
@@ -526,8 +656,9 @@ int zs_ba_set_problem(zs_ba_handle* h, const zs_ba_problem* p) {
     try {
         ZS_CUDA(cudaSetDevice(h->device));
         ZS_CUDA(cudaStreamSynchronize(h->stream));
-        h->release_problem();
+        h->release_problem(true);
         build_problem(h, p);
+        h->owned.trim();
         h->has_problem = true;
     } catch (const CudaError& e) {
         h->release_problem();
@@ -1381,7 +1512,7 @@ int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windo
 
         ZS_CUDA(cudaSetDevice(h->device));
         ZS_CUDA(cudaStreamSynchronize(h->stream));
-        h->release_problem();
+        h->release_problem(true);
         build_problem(h, &cat, &wp, &wl);
         // windows by reduced-system size bucket, largest first within a bucket
         BatchDev& B = h->B;
@@ -1411,6 +1542,7 @@ int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windo
         ZS_CUDA(cudaMemsetAsync(B.ctl, 0, sizeof(WinCtl) * num_windows, h->stream));
         ZS_CUDA(cudaMemsetAsync(B.rounds, 0, sizeof(int), h->stream));
         ZS_CUDA(cudaStreamSynchronize(h->stream));
+        h->owned.trim();
         h->wpose0 = wp;
         h->wlm0 = wl;
         h->batch = true;
