@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-windows measurement")
     ap.add_argument("--batch-windows", type=int, default=256)
     ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
+    ap.add_argument("--batch-profile", action="store_true",
+                    help="with --single batch-*: per-phase SM cycles of the window solves by keyframe range")
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
                     help="1: one graph launch per batched solve; 0: host loop over rounds (same kernels; "
                          "for profilers that cannot see kernels inside conditional graph nodes)")
@@ -169,12 +171,14 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
     T = schur_triples(sc)
     pipe = peaks["fp64_tflops"] if precision == 0 else peaks["fp32_tflops"]
     pipe_name = "fp64" if precision == 0 else "fp32"
+    rs = 20 if precision else 18  # H_pl / W record length (floats padded to 80 bytes)
     work = {
         # bytes: read observation + write H_pl, and H_ll / H_pp / b once
         "linearize": ("hbm", M * (24 + 18 * s) + L * 12 * s + K * 42 * s, None),
         "invert": ("hbm", L * (9 * 8 * 2) + M * 18 * s * 2, None),
-        # flops of the pair products W_i H_j^T (6x6x3 multiply-adds per triple)
-        "schur": (pipe_name, None, T * 216.0 + M * 36.0),
+        # bytes: the W and H_pl records once, the triple list, the chunk partials
+        # (memory-bound: L1/L2 latency of the record gathers, see profiles/)
+        "schur": ("hbm", M * 2 * rs * s + T * 8 + (T / 32.0) * 36 * s, T * 216.0 + M * 36.0),
         "factor": (pipe_name, None, n ** 3 / 3.0),
         "trisolve": ("hbm", n * n * s * 2, None),
         "update": ("hbm", M * 18 * s + L * 48 + K * 112, None),
@@ -185,16 +189,36 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
     top = max((p for p in work if calls.get(p, 0) > 0), key=lambda p: ms[p])
     bound, nbytes, flops = work[top]
     per_call_ms = ms[top] / calls[top]
+    extra = {}
     if nbytes is not None:
         achieved = nbytes / (per_call_ms * 1e-3) / 1e9
         peak, unit, fallback = hbm_gbs, "GB/s", "MEASURED_PEAKS.json hbm_gbs"
+        if flops is not None:
+            extra = {"flop_rate_tflops": flops / (per_call_ms * 1e-3) / 1e12, "flop_peak_tflops": pipe,
+                     "algorithmic_bytes": nbytes}
     else:
         achieved = flops / (per_call_ms * 1e-3) / 1e12
         peak, unit, fallback = pipe, "TFLOP/s", f"zs_pipe_peaks {pipe_name} FMA chain, measured in this run"
     return {"phase": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak if peak else None, "traffic": None, "peak_source": fallback,
-            "ms_per_call": per_call_ms, "calls": calls[top],
-            "phase_share": ms[top] / max(1e-9, sum(ms.values()))}
+            "frac": achieved / peak if peak else None, "traffic": phase_traffic(sc, precision, top),
+            "peak_source": fallback, "ms_per_call": per_call_ms, "calls": calls[top],
+            "phase_share": ms[top] / max(1e-9, sum(ms.values())), **extra}
+
+
+def phase_traffic(sc, precision: int, phase: str):
+    """DRAM bytes per launch of the phase's main kernel from the committed ncu
+    capture (profiles/traffic_walk_1M_mixed.json), for the scene it was taken on."""
+    path = os.path.join(ROOT, "profiles", "traffic_walk_1M_mixed.json")
+    if precision != 1 or sc.M != 1019227 or not os.path.exists(path):
+        return None
+    with open(path) as f:
+        t = json.load(f)
+    k = t["phase_kernel"].get(phase)
+    if not k:
+        return None
+    e = t["kernels"][k]
+    return {"bytes_per_launch": e["dram_read"] + e["dram_write"], "kernel": k,
+            "source": "profiles/traffic_walk_1M_mixed.json (one ncu capture)"}
 
 
 def run_solves(sc, precision: int, steps: int, warmup: int, iters: int, device: int, dist: Dist):
@@ -490,13 +514,28 @@ def single_solve(args):
         from zeroslam_gb300 import scenes
 
         wins = scenes.window_batch(args.batch_windows)
-        with ba.BundleAdjuster(precision=prec, batch_graph=args.batch_graph) as h:
+        with ba.BundleAdjuster(precision=prec, batch_graph=args.batch_graph,
+                               profile=1 if args.batch_profile else 0) as h:
             h.set_batch(wins)
             h.solve_batch(10)  # tunes and captures the graph
             h.reset_state()
             _, reps, brep = h.solve_batch(args.iterations or 10)
-        print(json.dumps({"single": args.single, "windows": len(wins), "rounds": brep.rounds,
-                          "ms_total": brep.ms_total, "kernel_launches": brep.kernel_launches}), flush=True)
+            prof = h.batch_solve_profile() if args.batch_profile else None
+        out = {"single": args.single, "windows": len(wins), "rounds": brep.rounds, "ms_total": brep.ms_total,
+               "kernel_launches": brep.kernel_launches, "bucket_threads": list(brep.bucket_threads)}
+        if prof is not None:
+            K = np.array([w.K for w in wins])
+            att = np.array([r.attempts for r in reps])
+            rows = {}
+            for lo, hi in ((5, 10), (11, 16), (17, 21), (22, 26), (27, 30)):
+                sel = (K >= lo) & (K <= hi)
+                per = prof[sel].sum(0) / max(1, att[sel].sum())
+                rows[f"K{lo}-{hi}"] = {"windows": int(sel.sum()), "kcycles_per_attempt": {
+                    "load": round(per[0] / 1e3, 1), "factor": round(per[1] / 1e3, 1),
+                    "first_solve": round(per[2] / 1e3, 1), "refinement": round(per[3] / 1e3, 1)},
+                    "refine_sweeps_per_attempt": round(float(per[4]), 2)}
+            out["phases"] = rows
+        print(json.dumps(out), flush=True)
         return
     sc = make_scene(args.workload)
     with ba.BundleAdjuster(precision=prec) as h:
