@@ -28,7 +28,8 @@ using namespace zs;
 
 namespace {
 
-constexpr int kChunk = 32;  // triples per Schur chunk
+constexpr int kSegment = 512;  // triples per Schur segment (a warp's share)
+
 
 struct CudaError {
     cudaError_t err;
@@ -462,6 +463,10 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         std::vector<int32_t> fill(pose_ptr.begin(), pose_ptr.end() - 1);
         for (int64_t i = 0; i < M; ++i) pose_obs[fill[obs_pose[i]]++] = (int32_t)i;
     }
+    // pose-major position of each observation: its H_pl / W / pose-partial
+    // records live there, so a pose's records are contiguous
+    std::vector<int32_t> pm(M);
+    for (int64_t q = 0; q < M; ++q) pm[pose_obs[q]] = (int32_t)q;
     // Schur triples: for each landmark, every (block a, block b) with pose_a >= pose_b,
     // grouped by pose pair (i, j) = (pose_a, pose_b), landmark order within a pair.
     // Pair keys are window-local: key = base_w + (i - p0_w) K_w + (j - p0_w).
@@ -529,12 +534,12 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
                 if (blk_valid[i]) vb.push_back(i);
             for (size_t a = 0; a < vb.size(); ++a)
                 for (size_t b = 0; b <= a; ++b)
-                    triples[pos[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++] = make_int2(vb[a], vb[b]);
+                    triples[pos[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++] = make_int2(pm[vb[a]], pm[vb[b]]);
         }
     });
     counts.clear();
-    std::vector<int32_t> pair_i, pair_j;
-    std::vector<int64_t> pair_chunk_ptr{0}, chunk_ptr{0};
+    std::vector<int32_t> pair_i, pair_j, seg_pair;
+    std::vector<int64_t> seg_ptr{0}, pair_seg_ptr{0};
     pair_i.reserve(npairs);
     pair_j.reserve(npairs);
     for (int w = 0; w < nwin; ++w) {
@@ -543,14 +548,16 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
             if (!pair_count[k]) continue;
             pair_i.push_back((int32_t)(wp[w] + (k - key_base[w]) / kw));
             pair_j.push_back((int32_t)(wp[w] + (k - key_base[w]) % kw));
-            for (int64_t t = pair_off[k]; t < pair_off[k + 1]; t += kChunk)
-                chunk_ptr.push_back(std::min<int64_t>(t + kChunk, pair_off[k + 1]));
-            pair_chunk_ptr.push_back((int64_t)chunk_ptr.size() - 1);
+            for (int64_t t = pair_off[k]; t < pair_off[k + 1]; t += kSegment) {
+                seg_ptr.push_back(std::min<int64_t>(t + kSegment, pair_off[k + 1]));
+                seg_pair.push_back((int32_t)pair_i.size() - 1);
+            }
+            pair_seg_ptr.push_back((int64_t)seg_pair.size());
         }
     }
     P.npairs = npairs;
     P.ntriples = ntriples;
-    P.nchunks = (int64_t)chunk_ptr.size() - 1;
+    P.nsegs = (int64_t)seg_pair.size();
 
     // state (padded device layout)
     std::vector<double> pose8((size_t)K * kPoseStride, 0.0), lm4((size_t)L * kLmStride, 0.0);
@@ -581,8 +588,10 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     P.dup_owner = has_dups ? upload(dup_owner, own, s) : nullptr;
     P.pair_i = upload(pair_i, own, s);
     P.pair_j = upload(pair_j, own, s);
-    P.pair_chunk_ptr = upload(pair_chunk_ptr, own, s);
-    P.chunk_ptr = upload(chunk_ptr, own, s);
+    P.seg_ptr = upload(seg_ptr, own, s);
+    P.seg_pair = upload(seg_pair, own, s);
+    P.pair_seg_ptr = upload(pair_seg_ptr, own, s);
+    P.pm = upload(pm, own, s);
     P.triples = upload(triples, own, s);
     P.nwin = nwin;
     std::vector<int64_t> win_s_off(nwin, 0);
@@ -622,13 +631,13 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     W.hpl = dalloc<char>(ts * rs * M, own);
     W.W = dalloc<char>(ts * rs * M, own);
     W.pose_aux = dalloc<double>((size_t)K * 24, own);
+    W.partial = dalloc<char>(ts * 36 * (size_t)P.nsegs, own);
     W.lm_part = dalloc<char>(ts * 12 * M, own);    // record-major, 9 values padded to 12
     W.pose_part = dalloc<char>(ts * 28 * M, own);  // record-major, 27 values padded to 28
     W.hpp = dalloc<double>((size_t)K * 36, own);
     W.hll = dalloc<double>((size_t)L * 9, own);
     W.hll_inv = dalloc<double>((size_t)L * 9, own);
     W.b = dalloc<double>((size_t)n + 3 * (size_t)L, own);
-    W.partial = dalloc<char>(ts * 36 * (size_t)P.nchunks, own);
     W.S = dalloc<double>((size_t)s_total, own);
     W.bs = dalloc<double>(n, own);
     if (!batched) {

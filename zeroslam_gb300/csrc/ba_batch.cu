@@ -6,8 +6,8 @@
 //   * the LM state machine (source/factor_graph.hpp:511-611) per window,
 //     advanced once per attempt round on the device (k_bdecide), with the
 //     same acceptance, damping, rollback and stop rules as zs_ba_solve;
-//   * the damped H_ll inverses, S block initialisation and Schur assembly
-//     at each window's own lambda, into the window's S block;
+//   * the damped H_ll inverses and S block initialisation at each window's
+//     own lambda (the pair products go into the window's S block);
 //   * the reduced solve: a persistent kernel per size bucket whose CTAs
 //     take windows from a device work queue (largest first), factor the
 //     window's S in shared memory (packed lower triangle, right-looking
@@ -127,31 +127,6 @@ __global__ void __launch_bounds__(kThreads) k_bs_init(DevProblem P, const double
     S[P.win_s_off[w] + idx] = v;
 }
 
-// S_w -= the pair's chunk partials (FP64, chunk order), as k_schur_assemble.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_bschur_assemble(DevProblem P, const T* __restrict__ partial, double* S,
-                                                              const WinCtl* __restrict__ ctl) {
-    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)P.npairs * 36) return;
-    const int p = (int)(idx / 36), e = (int)(idx % 36);
-    const int i = P.pair_i[p], j = P.pair_j[p];
-    const int w = P.pose_win[i];
-    if (!ctl[w].active) return;
-    double sum = 0.0;
-    const int64_t c1 = P.pair_chunk_ptr[p + 1];
-    for (int64_t c = P.pair_chunk_ptr[p]; c < c1; ++c) sum += (double)partial[c * 36 + e];
-    const int p0 = P.win_pose0[w];
-    const int64_t n = 6LL * (P.win_pose0[w + 1] - p0);
-    double* Sw = S + P.win_s_off[w];
-    const int64_t row = 6LL * (i - p0) + e / 6, col = 6LL * (j - p0) + e % 6;
-    if (i == j) {
-        Sw[row * n + col] = Sw[row * n + col] - sum;
-    } else {
-        Sw[row * n + col] = -sum;
-        Sw[col * n + row] = -sum;
-    }
-}
-
 // delta_l = H_ll^-1 (b_l - H_lp delta_p), as k_backsub.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bbacksub(DevProblem P, const T* __restrict__ hpl,
@@ -168,7 +143,7 @@ __global__ void __launch_bounds__(kThreads) k_bbacksub(DevProblem P, const T* __
     const int e = P.lm_ptr[l + 1];
     for (int o = P.lm_ptr[l]; o < e; ++o) {
         if (!P.blk_valid[o]) continue;
-        const T* h = hpl + (int64_t)o * RS;
+        const T* h = hpl + (int64_t)P.pm[o] * RS;
         const double* dp = delta + 6LL * P.obs_pose[o];
         T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
@@ -707,11 +682,7 @@ cudaError_t launch_batch_round(const DevProblem& P, DevWork& W, BatchDev& B, con
         const dim3 g(grid_for(36LL * kBatchMaxK * kBatchMaxK), P.nwin);
         k_bs_init<<<g, kThreads, 0, s>>>(P, W.hpp, W.S, B.st, B.ctl); note_launch();
     }
-    launch_schur_chunks<T>(P, W, s);
-    if (P.npairs > 0) {
-        k_bschur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, W.S, B.ctl);
-        note_launch();
-    }
+    launch_schur_pairs<T>(P, W, B.ctl, s);
     launch_bs<T>(P, W, s);
     BatchView V{W.S, W.bs, W.delta, B.st, B.ctl, P.win_pose0, P.win_s_off, B.prof};
     const int refine = sizeof(T) == 4 ? prm.refine_iters : 0;

@@ -36,15 +36,17 @@ struct DevProblem {
     int32_t* dup_owner = nullptr;  // [M] owner of the duplicate run (== self when unique), or null
     bool has_dups = false;
     // Schur structure: pairs (i >= j) of poses sharing landmarks; triples
-    // (block of pose i, block of pose j) grouped by pair, split into chunks.
+    // (block of pose i, block of pose j) grouped by pair, landmark order within a pair.
     int npairs = 0;
     int64_t ntriples = 0;
-    int64_t nchunks = 0;
     int32_t* pair_i = nullptr;         // [npairs]
     int32_t* pair_j = nullptr;         // [npairs]
-    int64_t* pair_chunk_ptr = nullptr; // [npairs+1]
-    int64_t* chunk_ptr = nullptr;      // [nchunks+1] ranges into triples
-    int2* triples = nullptr;           // [ntriples] (obs of pose i, obs of pose j)
+    int2* triples = nullptr;           // [ntriples] pose-major record positions (of pose i, of pose j)
+    int64_t nsegs = 0;                 // segments: <= 512 consecutive triples of one pair
+    int64_t* seg_ptr = nullptr;        // [nsegs+1] triple ranges per segment
+    int32_t* seg_pair = nullptr;       // [nsegs] pair of each segment
+    int64_t* pair_seg_ptr = nullptr;   // [npairs+1] segment ranges per pair
+    int32_t* pm = nullptr;             // [M] pose-major position of each (landmark-major) observation
     Intrinsics intr{};
     LossParams loss{};
     // Batched windows (null / 1 for a single problem): poses, landmarks and
@@ -65,16 +67,16 @@ struct DevProblem {
 // Working arrays of one precision (T = double for the plain form, float for
 // the mixed form).
 struct DevWork {
-    void* hpl = nullptr;       // [M*RS] T, RS = 18 (double) or 20 (float, padded)
-    void* W = nullptr;         // [M*RS] T
+    void* hpl = nullptr;       // [M*RS] T, RS = 18 (double) or 20 (float, padded); pose-major positions
+    void* W = nullptr;         // [M*RS] T, pose-major positions
     double* pose_aux = nullptr; // [K*24] mixed form: per-pose sandwich matrix, translation, rotation
+    void* partial = nullptr;   // [nsegs*36] T, Schur segment sums
     void* lm_part = nullptr;   // [M*12] T, per-observation landmark records (9 used)
-    void* pose_part = nullptr; // [M*28] T, per-observation pose records (27 used)
+    void* pose_part = nullptr; // [M*28] T, per-observation pose records (27 used), pose-major positions
     double* hpp = nullptr;     // [K*36]
     double* hll = nullptr;     // [L*9]
     double* hll_inv = nullptr; // [L*9]
     double* b = nullptr;       // [n + 3L] gradient vector (poses then landmarks)
-    void* partial = nullptr;   // [nchunks*36] T
     double* S = nullptr;       // [n*n] reduced camera matrix, FP64 in both forms
     void* F = nullptr;         // [n*n] Cholesky factor (lower): double (plain form) or float (mixed)
     void* D = nullptr;         // [ceil(n/32)*1024] T, inverses of F's diagonal blocks
@@ -139,9 +141,10 @@ void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s);
 // W = H_pl H_ll^-1 from the current inverses (no inversion).
 template <typename T>
 void launch_w(const DevProblem& P, DevWork& W, cudaStream_t s);
-// Per-chunk Schur pair partials (no assembly).
+// S_ij -= the pairs' W_i H_j^T sums (after the S blocks' initialisation);
+// with windows, stopped windows (ctl) are skipped.
 template <typename T>
-void launch_schur_chunks(const DevProblem& P, DevWork& W, cudaStream_t s);
+void launch_schur_pairs(const DevProblem& P, DevWork& W, const WinCtl* ctl, cudaStream_t s);
 void launch_update(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s);
 void launch_rollback(const DevProblem& P, const LmState* st, cudaStream_t s);
 void launch_scale(const DevProblem& P, DevWork& W, LmState* st, cudaStream_t s);

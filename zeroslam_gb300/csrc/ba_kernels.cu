@@ -19,6 +19,8 @@
 //   k_update, k_rollback                     source/factor_graph.hpp:809-846, 947-960
 //   k_cost_partial                           get_current_chi    source/factor_graph.hpp:618-629
 //   k_scale_partial, k_decide                LM acceptance      source/factor_graph.hpp:555-606
+#include <algorithm>
+
 #include "ba_internal.h"
 
 namespace zs {
@@ -99,8 +101,11 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
                                                         T* __restrict__ pose_part, const double* __restrict__ aux) {
     constexpr int RS = RecStride<T>::value;
-    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (o >= P.M) return;
+    // threads in pose-major order: the large records (H_pl, pose partials)
+    // are written coalesced and neighbouring threads share the pose's data
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= P.M) return;
+    const int64_t o = P.pose_obs[q];
     const int pi = P.obs_pose[o], li = P.obs_lm[o];
     const double* xp = P.lm + (int64_t)li * kLmStride;
     const double2 uv = P.obs_uv[o];
@@ -208,7 +213,7 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
     const T g0 = (T)(drho * orr0), g1 = (T)(drho * orr1);
     const bool pf = P.pose_fixed[pi] != 0, lf = P.lm_fixed[li] != 0;
 
-    T* hb = hpl + o * RS;
+    T* hb = hpl + q * RS;
     T prec[kPoseRec];
 #pragma unroll
     for (int k = 0; k < kPoseRec; ++k) prec[k] = T(0);
@@ -239,7 +244,7 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
 #pragma unroll
         for (int k = 0; k < 18; ++k) hb[k] = T(0);
     }
-    store_rec(pose_part + o * kPoseRec, prec);
+    store_rec(pose_part + q * kPoseRec, prec);
     T lrec[kLmRec];
 #pragma unroll
     for (int k = 0; k < kLmRec; ++k) lrec[k] = T(0);
@@ -271,16 +276,18 @@ __global__ void k_merge_dups(DevProblem P, T* hpl) {
     if (o >= P.M) return;
     if (P.dup_owner[o] != o) return;
     int64_t e = o + 1;
+    T* own = hpl + (int64_t)P.pm[o] * RS;
     T acc[18];
 #pragma unroll
-    for (int k = 0; k < 18; ++k) acc[k] = hpl[o * RS + k];
+    for (int k = 0; k < 18; ++k) acc[k] = own[k];
     while (e < P.M && P.dup_owner[e] == o) {
+        const T* r = hpl + (int64_t)P.pm[e] * RS;
 #pragma unroll
-        for (int k = 0; k < 18; ++k) acc[k] += hpl[e * RS + k];
+        for (int k = 0; k < 18; ++k) acc[k] += r[k];
         ++e;
     }
 #pragma unroll
-    for (int k = 0; k < 18; ++k) hpl[o * RS + k] = acc[k];
+    for (int k = 0; k < 18; ++k) own[k] = acc[k];
 }
 
 template <typename T>
@@ -302,8 +309,9 @@ __global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* _
 }
 
 // Per pose (a CTA): each thread sums its strided share of the pose's
-// observation records in T; the thread partials meet in FP64 through a
-// fixed tree (warp shuffles, then the warps' results in warp order).
+// observation records (pose-major, contiguous) in T; the thread partials meet
+// in FP64 through a fixed tree (warp shuffles, then the warps' results in
+// warp order).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T* __restrict__ pose_part, double* hpp,
                                                           double* b) {
@@ -316,7 +324,7 @@ __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T*
     for (int c = 0; c < kPoseRec; ++c) acc[c] = T(0);
     const int e = P.pose_ptr[k + 1];
     for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x)
-        add_rec(pose_part + (int64_t)P.pose_obs[i] * kPoseRec, acc);
+        add_rec(pose_part + (int64_t)i * kPoseRec, acc);  // the pose's records are contiguous
 #pragma unroll
     for (int c = 0; c < 27; ++c) {
         double v = (double)acc[c];
@@ -385,14 +393,16 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_w(DevProblem P, const T* __restrict__ hpl, const double* __restrict__ hinv,
                                                 T* __restrict__ W) {
     constexpr int RS = RecStride<T>::value;
-    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (o >= P.M || !P.blk_valid[o]) return;
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // pose-major position
+    if (q >= P.M) return;
+    const int64_t o = P.pose_obs[q];
+    if (!P.blk_valid[o]) return;
     const double* I = hinv + (int64_t)P.obs_lm[o] * 9;
     T iv[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) iv[i] = (T)I[i];
-    const T* h = hpl + o * RS;
-    T* w = W + o * RS;
+    const T* h = hpl + q * RS;
+    T* w = W + q * RS;
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
         const T h0 = h[a * 3], h1 = h[a * 3 + 1], h2 = h[a * 3 + 2];
@@ -419,18 +429,35 @@ __device__ __forceinline__ void load_rec(const double* p, double v[20]) {
     }
 }
 
-// Partial 6x6 sums W_i H_j^T over one chunk of a pose pair's triples.
+// Partial 6 x 6 sums W_i H_j^T over one segment (<= 512 consecutive triples
+// of one pose pair), a warp per segment: lane t takes the segment's triples
+// t, t + 32, ... (consecutive lanes read consecutive pose-major records,
+// coalesced) and accumulates in T; the 32 lane partials meet in a fixed tree
+// (FP32: an xor-shuffle butterfly, identical in every lane; FP64: a transpose
+// through shared memory and a column sum in lane order). With windows,
+// segments of stopped windows (ctl) are skipped.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_schur_chunks(DevProblem P, const T* __restrict__ W,
-                                                           const T* __restrict__ hpl, T* __restrict__ partial) {
+constexpr int schur_seg_threads() {
+    return sizeof(T) == 8 ? 128 : 256;  // FP64: 4 warps keep the transpose buffer under 48 KB
+}
+
+template <typename T>
+__global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevProblem P, const T* __restrict__ W,
+                                                                          const T* __restrict__ hpl,
+                                                                          T* __restrict__ part,
+                                                                          const WinCtl* __restrict__ ctl) {
     constexpr int RS = RecStride<T>::value;
-    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= P.nchunks) return;
+    constexpr int NW = schur_seg_threads<T>() / 32;
+    __shared__ double red[sizeof(T) == 8 ? NW : 1][32][37];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (g >= P.nsegs) return;
+    if (ctl && P.pose_win && !ctl[P.pose_win[P.pair_i[P.seg_pair[g]]]].active) return;
     T acc[36];
 #pragma unroll
     for (int e = 0; e < 36; ++e) acc[e] = T(0);
-    const int64_t e1 = P.chunk_ptr[c + 1];
-    for (int64_t t = P.chunk_ptr[c]; t < e1; ++t) {
+    const int64_t t1 = P.seg_ptr[g + 1];
+    for (int64_t t = P.seg_ptr[g] + lane; t < t1; t += 32) {
         const int2 tr = P.triples[t];
         T wv[20], hv[20];
         load_rec(W + (int64_t)tr.x * RS, wv);
@@ -441,9 +468,62 @@ __global__ void __launch_bounds__(kThreads) k_schur_chunks(DevProblem P, const T
             for (int d = 0; d < 6; ++d)
                 acc[a * 6 + d] += wv[a * 3] * hv[d * 3] + wv[a * 3 + 1] * hv[d * 3 + 1] + wv[a * 3 + 2] * hv[d * 3 + 2];
     }
-    T* out = partial + c * 36;
+    T* out = part + g * 36;
+    if (sizeof(T) == 4) {
 #pragma unroll
-    for (int e = 0; e < 36; ++e) out[e] = acc[e];
+        for (int e = 0; e < 36; ++e) {
+            T v = acc[e];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (e == lane || e == 32 + lane) out[e] = v;
+        }
+    } else {
+        double (*r)[37] = red[sizeof(T) == 8 ? wib : 0];
+#pragma unroll
+        for (int e = 0; e < 36; ++e) r[lane][e] = (double)acc[e];
+        __syncwarp();
+        double v0 = 0.0, v1 = 0.0;
+        for (int k = 0; k < 32; ++k) v0 += r[k][lane];
+        out[lane] = (T)v0;
+        if (lane < 4) {
+            for (int k = 0; k < 32; ++k) v1 += r[k][32 + lane];
+            out[32 + lane] = (T)v1;
+        }
+    }
+}
+
+// S_ij -= the pair's segment sums, added in FP64 in segment order: diagonal
+// pairs subtract from the H_pp + lambda I block written by k_s_init,
+// off-diagonal pairs write both blocks. With windows the pair's window S
+// block is used and stopped windows (ctl) are skipped.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const T* __restrict__ part, double* S,
+                                                             const WinCtl* __restrict__ ctl) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)P.npairs * 36) return;
+    const int p = (int)(idx / 36), e = (int)(idx % 36);
+    const int i = P.pair_i[p], j = P.pair_j[p];
+    int p0 = 0, nw = P.n;
+    int64_t soff = 0;
+    if (P.pose_win) {
+        const int w = P.pose_win[i];
+        if (ctl && !ctl[w].active) return;
+        p0 = P.win_pose0[w];
+        nw = 6 * (P.win_pose0[w + 1] - p0);
+        soff = P.win_s_off[w];
+    }
+    double sum = 0.0;
+    const int64_t g1 = P.pair_seg_ptr[p + 1];
+    for (int64_t g = P.pair_seg_ptr[p]; g < g1; ++g) sum += (double)part[g * 36 + e];
+    double* Sw = S + soff;
+    const int64_t n = nw;
+    const int64_t row = 6LL * (i - p0) + e / 6, col = 6LL * (j - p0) + e % 6;
+    if (i == j) {
+        Sw[row * n + col] = Sw[row * n + col] - sum;
+    } else {
+        Sw[row * n + col] = -sum;
+        Sw[col * n + row] = -sum;
+    }
 }
 
 // S = blockdiag(H_pp + lambda I); the pair sums are subtracted next.
@@ -461,27 +541,6 @@ __global__ void __launch_bounds__(kThreads) k_s_init(DevProblem P, const double*
     S[idx] = v;
 }
 
-// S (FP64) -= the pair's chunk partials, summed in FP64 in chunk order.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const T* __restrict__ partial, double* S) {
-    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)P.npairs * 36) return;
-    const int p = (int)(idx / 36), e = (int)(idx % 36);
-    double sum = 0.0;
-    const int64_t c1 = P.pair_chunk_ptr[p + 1];
-    for (int64_t c = P.pair_chunk_ptr[p]; c < c1; ++c) sum += (double)partial[c * 36 + e];
-    const int i = P.pair_i[p], j = P.pair_j[p];
-    const int64_t n = P.n;
-    const int64_t row = 6LL * i + e / 6, col = 6LL * j + e % 6;
-    if (i == j) {
-        S[row * n + col] = S[row * n + col] - sum;
-    } else {
-        S[row * n + col] = -sum;
-        S[col * n + row] = -sum;
-    }
-}
-
-// b_s = b_p - sum over the pose's blocks of W b_l.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bs(DevProblem P, const T* __restrict__ W, const double* __restrict__ b,
                                                  double* bs) {
@@ -493,7 +552,7 @@ __global__ void __launch_bounds__(kThreads) k_bs(DevProblem P, const T* __restri
     for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x) {
         const int64_t o = P.pose_obs[i];
         if (!P.blk_valid[o]) continue;
-        const T* w = W + o * RS;
+        const T* w = W + (int64_t)i * RS;  // pose-major records
         const double* bl = b + P.n + 3LL * P.obs_lm[o];
         const T b0 = (T)bl[0], b1 = (T)bl[1], b2 = (T)bl[2];
 #pragma unroll
@@ -520,7 +579,7 @@ __global__ void __launch_bounds__(kThreads) k_backsub(DevProblem P, const T* __r
     const int e = P.lm_ptr[l + 1];
     for (int o = P.lm_ptr[l]; o < e; ++o) {
         if (!P.blk_valid[o]) continue;
-        const T* h = hpl + (int64_t)o * RS;
+        const T* h = hpl + (int64_t)P.pm[o] * RS;
         const double* dp = delta + 6LL * P.obs_pose[o];
         T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
@@ -749,13 +808,22 @@ void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStr
 }
 
 template <typename T>
+void launch_schur_pairs(const DevProblem& P, DevWork& W, const WinCtl* ctl, cudaStream_t s) {
+    if (P.npairs > 0) {
+        constexpr int nt = schur_seg_threads<T>();
+        const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
+        k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial, ctl);
+        note_launch();
+        k_schur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, W.S, ctl);
+        note_launch();
+    }
+}
+
+template <typename T>
 void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
     const int64_t nn = (int64_t)P.n * P.n;
     if (nn > 0) { k_s_init<<<grid_for(nn), kThreads, 0, s>>>(P, W.hpp, (double*)W.S, st); note_launch(); }
-    if (P.nchunks > 0) {
-        k_schur_chunks<T><<<grid_for(P.nchunks), kThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial); note_launch();
-        k_schur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, (double*)W.S); note_launch();
-    }
+    launch_schur_pairs<T>(P, W, nullptr, s);
     if (P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
 }
 
@@ -769,12 +837,6 @@ void launch_w(const DevProblem& P, DevWork& W, cudaStream_t s) {
     if (P.M > 0) { k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch(); }
 }
 
-template <typename T>
-void launch_schur_chunks(const DevProblem& P, DevWork& W, cudaStream_t s) {
-    if (P.nchunks > 0) {
-        k_schur_chunks<T><<<grid_for(P.nchunks), kThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial); note_launch();
-    }
-}
 
 template <typename T>
 void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
@@ -830,7 +892,7 @@ template void launch_backsub<float>(const DevProblem&, DevWork&, const LmState*,
 template void launch_bs<float>(const DevProblem&, DevWork&, cudaStream_t);
 template void launch_w<double>(const DevProblem&, DevWork&, cudaStream_t);
 template void launch_w<float>(const DevProblem&, DevWork&, cudaStream_t);
-template void launch_schur_chunks<double>(const DevProblem&, DevWork&, cudaStream_t);
-template void launch_schur_chunks<float>(const DevProblem&, DevWork&, cudaStream_t);
+template void launch_schur_pairs<double>(const DevProblem&, DevWork&, const WinCtl*, cudaStream_t);
+template void launch_schur_pairs<float>(const DevProblem&, DevWork&, const WinCtl*, cudaStream_t);
 
 }  // namespace zs
