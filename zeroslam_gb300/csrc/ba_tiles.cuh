@@ -33,6 +33,20 @@ __device__ __forceinline__ TF* tile_at(TF* A, int ib, int jb) {
 // is the reference's test on the unscaled pivot
 // (source/matrix_decomposition_cholesky.hpp:40,53).
 // Returns 1 on success (uniform over the CTA).
+// Pivot d -> (L_cc, 1 / L_cc). The mixed form (float) uses the reciprocal
+// square root (its refinement corrects the factor's last bits); the plain
+// form keeps the reference's sqrt and division.
+__device__ __forceinline__ void pivot_root(float d, float& l, float& inv) {
+    inv = rsqrtf(d);
+    l = d * inv;
+}
+__device__ __forceinline__ void pivot_root(double d, double& l, double& inv) {
+    l = sqrt(d);
+    inv = 1.0 / l;
+}
+__device__ __forceinline__ float scale_by(float x, float l, float inv) { return x * inv; }
+__device__ __forceinline__ double scale_by(double x, double l, double inv) { return x / l; }
+
 template <typename TF>
 __device__ int cta_cholesky(TF* A, int nbw, int n, const TF* eps, TF* dinv, int* s_flag) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -44,13 +58,18 @@ __device__ int cta_cholesky(TF* A, int nbw, int n, const TF* eps, TF* dinv, int*
 #pragma unroll
             for (int j = 0; j < 32; ++j) row[j] = D[lane * kLd + j];
             int fail = 0;
+            TF own_inv = TF(1);
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 const TF d = __shfl_sync(0xffffffffu, row[c], c);
                 if (32 * kb + c < n && !(d > eps[32 * kb + c])) fail = 1;
-                const TF lcc = sqrt(d);
-                if (lane == c) row[c] = lcc;
-                if (lane > c) row[c] = row[c] / lcc;
+                TF lcc, inv;
+                pivot_root(d, lcc, inv);
+                if (lane == c) {
+                    row[c] = lcc;
+                    own_inv = inv;
+                }
+                if (lane > c) row[c] = scale_by(row[c], lcc, inv);
                 const TF lic = row[c];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
@@ -63,12 +82,7 @@ __device__ int cta_cholesky(TF* A, int nbw, int n, const TF* eps, TF* dinv, int*
 #pragma unroll
             for (int j = 0; j <= 31; ++j)
                 if (j <= lane) D[lane * kLd + j] = row[j];
-            // 1 / L_ii of this tile
-            TF lii = TF(0);
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if (j == lane) lii = row[j];
-            dinv[32 * kb + lane] = TF(1) / lii;
+            dinv[32 * kb + lane] = own_inv;  // 1 / L_ii of this tile
             __syncwarp();
             // column `lane` of L_kk^-1, right-looking
             TF acc[32];
@@ -76,7 +90,7 @@ __device__ int cta_cholesky(TF* A, int nbw, int n, const TF* eps, TF* dinv, int*
             for (int i = 0; i < 32; ++i) acc[i] = TF(0);
 #pragma unroll
             for (int m = 0; m < 32; ++m) {
-                const TF dm = TF(1) / D[m * kLd + m];
+                const TF dm = dinv[32 * kb + m];
                 const TF ym = (m < lane) ? TF(0) : ((m == lane) ? dm : -acc[m] * dm);
                 acc[m] = ym;  // acc[m] now holds y_m
 #pragma unroll
@@ -91,61 +105,66 @@ __device__ int cta_cholesky(TF* A, int nbw, int n, const TF* eps, TF* dinv, int*
         }
         __syncthreads();
         if (*s_flag) return 0;
-        // 2. panel: L(ib, kb) = A(ib, kb) L_kk^-T, a row per thread:
-        //    out_j = a_j / L_jj + sum_{m < j} a_m (L_kk^-1)[j][m]
+        // 2. panel: L(ib, kb) = A(ib, kb) L_kk^-T, four outputs of one row per
+        //    item: out_j = a_j / L_jj + sum_{m < j} a_m (L_kk^-1)[j][m]; the
+        //    outputs of a batch of items are kept in registers until every
+        //    thread has read its row (in place)
         const int rows = 32 * (nbw - kb - 1);
-        for (int t = tid; t < rows; t += blockDim.x) {
-            const int ib = kb + 1 + (t >> 5), r = t & 31;
-            TF* Ar = tile_at(A, ib, kb) + r * kLd;
-            TF a[32], o[32];
+        for (int base = 0; base < rows * 8; base += blockDim.x) {
+            const int it = base + tid;
+            TF o[4] = {TF(0), TF(0), TF(0), TF(0)};
+            int ib = 0, r = 0, j0 = 0;
+            const bool act = it < rows * 8;
+            if (act) {
+                const int row = it >> 3;
+                ib = kb + 1 + (row >> 5);
+                r = row & 31;
+                j0 = (it & 7) * 4;
+                const TF* Ar = tile_at(A, ib, kb) + r * kLd;
 #pragma unroll
-            for (int j = 0; j < 32; ++j) a[j] = Ar[j];
+                for (int q = 0; q < 4; ++q) o[q] = Ar[j0 + q] * dinv[32 * kb + j0 + q];
+                for (int m = 0; m < j0 + 3; ++m) {
+                    const TF am = Ar[m];
 #pragma unroll
-            for (int j = 0; j < 32; ++j) o[j] = a[j] * dinv[32 * kb + j];
+                    for (int q = 0; q < 4; ++q)
+                        if (m < j0 + q) o[q] += am * D[m * kLd + j0 + q];
+                }
+            }
+            __syncthreads();
+            if (act) {
+                TF* Ar = tile_at(A, ib, kb) + r * kLd;
 #pragma unroll
-            for (int m = 0; m < 32; ++m)
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (j > m) o[j] += a[m] * D[m * kLd + j];
-#pragma unroll
-            for (int j = 0; j < 32; ++j) Ar[j] = o[j];
+                for (int q = 0; q < 4; ++q) Ar[j0 + q] = o[q];
+            }
         }
         __syncthreads();
-        // 3. trailing update A(ib, jb) -= L(ib, kb) L(jb, kb)^T, 4 x 4 outputs per item
+        // 3. trailing update A(ib, jb) -= L(ib, kb) L(jb, kb)^T, 2 x 2 outputs per item
         const int m = nbw - kb - 1;
-        const int items = (m * (m + 1) / 2) * 64;
+        const int items = (m * (m + 1) / 2) * 256;
         for (int it = tid; it < items; it += blockDim.x) {
-            const int t = it >> 6, u = it & 63;
+            const int t = it >> 8, u = it & 255;
             int ta = 0;
             while ((ta + 1) * (ta + 2) / 2 <= t) ++ta;
             const int tb = t - ta * (ta + 1) / 2;
             const int ib = kb + 1 + ta, jb = kb + 1 + tb;
-            const int ur = (u >> 3) * 4, uc = (u & 7) * 4;
+            const int ur = (u >> 4) * 2, uc = (u & 15) * 2;
             if (ib == jb && uc > ur) continue;
             const TF* Li = tile_at(A, ib, kb) + ur * kLd;
             const TF* Lj = tile_at(A, jb, kb) + uc * kLd;
-            TF acc[4][4];
-#pragma unroll
-            for (int x = 0; x < 4; ++x)
-#pragma unroll
-                for (int y = 0; y < 4; ++y) acc[x][y] = TF(0);
+            TF a00 = TF(0), a01 = TF(0), a10 = TF(0), a11 = TF(0);
 #pragma unroll 8
             for (int k = 0; k < 32; ++k) {
-                TF av[4], bv[4];
-#pragma unroll
-                for (int x = 0; x < 4; ++x) av[x] = Li[x * kLd + k];
-#pragma unroll
-                for (int y = 0; y < 4; ++y) bv[y] = Lj[y * kLd + k];
-#pragma unroll
-                for (int x = 0; x < 4; ++x)
-#pragma unroll
-                    for (int y = 0; y < 4; ++y) acc[x][y] += av[x] * bv[y];
+                const TF x0 = Li[k], x1 = Li[kLd + k], y0 = Lj[k], y1 = Lj[kLd + k];
+                a00 += x0 * y0;
+                a01 += x0 * y1;
+                a10 += x1 * y0;
+                a11 += x1 * y1;
             }
             TF* O = tile_at(A, ib, jb) + ur * kLd + uc;
-#pragma unroll
-            for (int x = 0; x < 4; ++x)
-#pragma unroll
-                for (int y = 0; y < 4; ++y) O[x * kLd + y] -= acc[x][y];
+            O[0] -= a00;
+            O[1] -= a01;
+            O[kLd] -= a10;
+            O[kLd + 1] -= a11;
         }
         __syncthreads();
     }
