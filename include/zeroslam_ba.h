@@ -73,10 +73,11 @@ typedef struct zs_ba_options {
     double legacy_stop;         /* 1e-10: stop when the gain < legacy_stop * chi2_initial */
     double relative_tolerance;  /* 1e-6: stop when the gain < tol * max(last, floor) */
     double chi2_floor;          /* 1e-12 */
-    int32_t refine_iterations;  /* mixed form: FP64 refinement sweeps at most (8) */
-    double refine_tolerance;    /* mixed form: stop refining at ||b - S x|| <= tol ||b|| (1e-10) */
+    int32_t refine_iterations;  /* mixed form: conjugate-gradient iterations on the FP64 Schur operator
+                                   (batched windows: FP64 refinement sweeps) at most (8) */
+    double refine_tolerance;    /* mixed form: stop at ||b - S x|| <= tol ||b|| (1e-10) */
     int32_t device;             /* CUDA device ordinal (0) */
-    int32_t verbose;            /* 1: print [INIT]/[GOOD]/[ BAD] lines to stderr */
+    int32_t verbose;            /* 1: print [INIT]/[GOOD]/[ BAD] lines to stderr; 2: also each mixed-form refinement */
     int32_t profile;            /* 1: time each phase with CUDA events into zs_ba_report.ms_phase */
     int32_t batch_graph;        /* batched solve: 1 = one CUDA graph launch (conditional WHILE
                                    node over attempt rounds), 0 = host loop over rounds (1) */
@@ -112,7 +113,8 @@ typedef struct zs_ba_report {
     int32_t accepted;          /* accepted steps (the reference's solve() return value) */
     int32_t attempts;          /* damped linear solves attempted */
     int32_t cholesky_failures; /* attempts whose reduced Cholesky failed */
-    int32_t refine_sweeps;     /* mixed form: refinement sweeps over all attempts */
+    int32_t refine_sweeps;     /* mixed form: conjugate-gradient iterations (batched windows: refinement
+                                  sweeps) over all attempts */
     double chi2_initial;
     double chi2_final;
     double lambda_final;

@@ -467,6 +467,15 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     // records live there, so a pose's records are contiguous
     std::vector<int32_t> pm(M);
     for (int64_t q = 0; q < M; ++q) pm[pose_obs[q]] = (int32_t)q;
+    // chunks of the mixed form's Schur operator: <= kOpChunk pose-major
+    // positions of one pose each
+    std::vector<int32_t> opch_q, pose_opch(K + 1, 0);
+    for (int k = 0; k < K; ++k) {
+        pose_opch[k] = (int32_t)opch_q.size();
+        for (int32_t q = pose_ptr[k]; q < pose_ptr[k + 1]; q += kOpChunk) opch_q.push_back(q);
+    }
+    pose_opch[K] = (int32_t)opch_q.size();
+    opch_q.push_back((int32_t)M);
     // Schur triples: for each landmark, every (block a, block b) with pose_a >= pose_b,
     // grouped by pose pair (i, j) = (pose_a, pose_b), landmark order within a pair.
     // Pair keys are window-local: key = base_w + (i - p0_w) K_w + (j - p0_w).
@@ -592,6 +601,9 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     P.seg_pair = upload(seg_pair, own, s);
     P.pair_seg_ptr = upload(pair_seg_ptr, own, s);
     P.pm = upload(pm, own, s);
+    P.nopch = (int64_t)opch_q.size() - 1;
+    P.opch_q = upload(opch_q, own, s);
+    P.pose_opch = upload(pose_opch, own, s);
     P.triples = upload(triples, own, s);
     P.nwin = nwin;
     std::vector<int64_t> win_s_off(nwin, 0);
@@ -631,8 +643,9 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     W.hpl = dalloc<char>(ts * rs * M, own);
     W.W = dalloc<char>(ts * rs * M, own);
     W.pose_aux = dalloc<double>((size_t)K * 24, own);
-    W.partial = dalloc<char>(ts * 36 * (size_t)P.nsegs, own);
-    W.lm_part = dalloc<char>(ts * 12 * M, own);    // record-major, 9 values padded to 12
+    W.partial = dalloc<double>(36 * (size_t)P.nsegs, own);
+    if (h->tsize == 4) W.jac = dalloc<ObsJac>((size_t)M, own);
+    else W.lm_part = dalloc<char>(ts * 12 * M, own);  // record-major, 9 values padded to 12
     W.pose_part = dalloc<char>(ts * 28 * M, own);  // record-major, 27 values padded to 28
     W.hpp = dalloc<double>((size_t)K * 36, own);
     W.hll = dalloc<double>((size_t)L * 9, own);
@@ -647,6 +660,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         if (h->tsize == 4) {
             W.X = dalloc<char>(ts * (size_t)n * n, own);
             W.XT = dalloc<char>(ts * (size_t)n * n, own);
+            W.pcg = dalloc<double>(pcg_doubles(P), own);
         }
     }
     W.delta = dalloc<double>((size_t)n + 3 * (size_t)L, own);
@@ -756,6 +770,11 @@ void linearize(zs_ba_handle* h) {
     launch_linearize<T>(h->P, h->W, h->stream);
 }
 
+// Mixed form: relative diagonal shift of the preconditioner's retry
+// factorisation (S + mu diag(S)) after the FP32 factorisation of the
+// FP32-formed S failed.
+constexpr double kPreconditionerShift = 1e-5;
+
 // One damped solve at st->lambda: H_ll inverses, Schur complement, reduced
 // Cholesky solve into delta[0..n), landmark back-substitution.
 template <typename T>
@@ -774,24 +793,29 @@ void system_solve(zs_ba_handle* h) {
     }
     {
         PhaseScope ps(h->timer, ZS_PHASE_FACTOR, s);
-        ZS_CUDA((launch_factor<double, T>(P.n, W.S, (T*)W.F, (T*)W.D, h->st, s)));
+        if constexpr (sizeof(T) == 4)  // the conjugate-gradient preconditioner
+            ZS_CUDA(launch_factor_preconditioner(P.n, W.S, (float*)W.F, (float*)W.D, h->st, kPreconditionerShift, s));
+        else
+            ZS_CUDA((launch_factor<double, T>(P.n, W.S, (T*)W.F, (T*)W.D, h->st, s)));
     }
     {
         PhaseScope ps(h->timer, ZS_PHASE_TRISOLVE, s);
-        if (sizeof(T) == 4) {
-            // mixed form: explicit L^-1, then FP64 refinement by GEMVs
+        if constexpr (sizeof(T) == 4) {
+            // mixed form: explicit L^-1, then conjugate gradients on the FP64
+            // Schur operator preconditioned by X^T X; it also writes b_s and
+            // the landmark back-substitution
             ZS_CUDA((launch_tri_inverse<float>(P.n, (const float*)W.F, (const float*)W.D, (float*)W.X,
                                                (float*)W.XT, h->st, s)));
-            ZS_CUDA((launch_refine<double, float>(P.n, W.S, (const float*)W.X, (const float*)W.XT, W.bs, W.delta,
-                                                  W.work, h->st, std::max(0, h->opt.refine_iterations),
-                                                  h->opt.refine_tolerance, s)));
+            ZS_CUDA(launch_pcg(P, W, h->st, std::max(0, h->opt.refine_iterations), h->opt.refine_tolerance, s));
         } else {
             ZS_CUDA((launch_solve_refine<double, double>(P.n, W.S, (const double*)W.F, (const double*)W.D, W.bs,
                                                          W.delta, W.work, h->st, 0, 0.0, s)));
         }
     }
-    PhaseScope ps(h->timer, ZS_PHASE_UPDATE, s);
-    launch_backsub<T>(P, W, h->st, s);
+    if constexpr (sizeof(T) == 8) {
+        PhaseScope ps(h->timer, ZS_PHASE_UPDATE, s);
+        launch_backsub<T>(P, W, h->st, s);
+    }
 }
 
 template <typename T>
@@ -851,7 +875,13 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
                 if (!std::isfinite(lambda)) break;
                 continue;
             }
-            if (sizeof(T) == 4) r.refine_sweeps += hs.refine_sweeps;
+            if (sizeof(T) == 4) {
+                r.refine_sweeps += hs.refine_sweeps;
+                if (o.verbose > 1)
+                    std::fprintf(stderr, "  refinement: %d sweeps, |b - S x| / |b| = %.3e%s\n", hs.refine_sweeps,
+                                 hs.rhs_norm > 0.0 ? hs.resid_norm / hs.rhs_norm : 0.0,
+                                 hs.shifted ? ", preconditioner shifted" : "");
+            }
             if (hs.good) {
                 chi2 = hs.chi2;
                 ++success;

@@ -63,8 +63,6 @@ __device__ inline double cta_max(double v, double* sh) {
     return t;
 }
 
-__device__ inline int64_t tri(int i) { return (int64_t)i * (i + 1) / 2; }
-
 }  // namespace
 
 // ------------------------------------------------------------ per-window kernels

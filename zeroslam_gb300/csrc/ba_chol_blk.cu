@@ -212,9 +212,10 @@ __global__ void __launch_bounds__(kBlkThreads) k_chol_blk(int n, float* F, float
     __shared__ int s_flag;
     const float eps = (float)__ldcg(&st->eps_factor);
     const int G = gridDim.x;
-    const int nblk = (n + kP - 1) / kP;
+    const int skip = __ldcg(&st->skip_factor);  // written by an earlier launch: uniform
+    const int nblk = skip ? 0 : (n + kP - 1) / kP;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    if (blockIdx.x == 0) {
+    if (blockIdx.x == 0 && !skip) {
         if (!factor_diag64(F, n, 0, min(kP, n), eps, T, dinv, epsr, Inv, Li, &s_flag) && threadIdx.x == 0)
             st->solve_ok = 0;
     }

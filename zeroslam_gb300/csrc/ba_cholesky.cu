@@ -18,6 +18,8 @@
 // exceed 1e-14 * max|S_ii| and every |L_ii| must exceed 1e-7 * max|L_ii|.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "ba_internal.h"
 
 namespace cg = cooperative_groups;
@@ -117,6 +119,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_chol_coop(int n, T* F, LmState*
     __shared__ T sb[kNB][kNB + 1];
     __shared__ T dg[kNB];
     const int nblk = (n + kNB - 1) / kNB;
+    if (ldg2(&st->skip_factor)) return;  // written by an earlier launch: uniform
     const double eps = ldg2(&st->eps_factor);
     const int G = gridDim.x;
     if (blockIdx.x == 0) {
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) k_diag_inverses(int n, const T* __re
                                                             const LmState* st) {
     __shared__ T l[kNB][kNB + 1];
     __shared__ T x[kNB][kNB + 1];
-    if (!st->solve_ok) return;
+    if (!st->solve_ok || st->skip_factor) return;
     const int k0 = blockIdx.x * kNB, b = min(kNB, n - k0);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -269,7 +272,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_check_solve_eps(int n, const T* __restrict__ F, LmState* st) {
     __shared__ double sh[kThreads];
     __shared__ int bad;
-    if (!st->solve_ok) return;
+    if (!st->solve_ok || st->skip_factor) return;
     double m = 0.0;
     for (int i = threadIdx.x; i < n; i += kThreads) m = fmax(m, fabs((double)F[(int64_t)i * n + i]));
     sh[threadIdx.x] = m;
@@ -509,6 +512,60 @@ cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStr
     }
     k_check_solve_eps<TF><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
     k_diag_inverses<TF><<<nblk, kThreads, 0, s>>>(n, F, D, st); note_launch();
+    return cudaGetLastError();
+}
+
+// Preconditioner retry: armed only after a failed factorisation.
+__global__ void k_retry_arm(LmState* st) {
+    if (threadIdx.x == 0) {
+        const int failed = !st->solve_ok;
+        st->skip_factor = !failed;
+        st->shifted = failed;
+        if (failed) st->solve_ok = 1;
+    }
+}
+__global__ void k_retry_disarm(LmState* st) {
+    if (threadIdx.x == 0) st->skip_factor = 0;
+}
+// F = S + mu diag(S) (FP32) when a retry is armed.
+__global__ void __launch_bounds__(kThreads) k_convert_shift(int n, const double* __restrict__ S, float* __restrict__ F,
+                                                            double mu, const LmState* st) {
+    if (st->skip_factor) return;
+    const int64_t nn = (int64_t)n * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = S[i];
+        F[i] = (float)(i / n == i % n ? v + mu * fabs(v) : v);
+    }
+}
+
+cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float* D, LmState* st, double mu,
+                                         cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    cudaError_t e = launch_factor<double, float>(n, S, F, D, st, s);
+    if (e != cudaSuccess) return e;
+    k_retry_arm<<<1, 32, 0, s>>>(st); note_launch();
+    k_convert_shift<<<std::min<int64_t>(grid_for((int64_t)n * n), 4096), kThreads, 0, s>>>(n, S, F, mu, st);
+    note_launch();
+    const int nblk = (n + kNB - 1) / kNB;
+    if (n >= kBlkMinN) {
+        e = launch_chol_blk(n, F, D, st, s);
+        if (e != cudaSuccess) return e;
+    } else {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int blocks = sms;
+        if (blocks > nblk * (nblk + 1) / 2 + 1) blocks = nblk * (nblk + 1) / 2 + 1;
+        if (blocks < 1) blocks = 1;
+        int nn_i = n;
+        void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
+        e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<float>, dim3(blocks), dim3(kThreads), args, 0, s);
+        if (e != cudaSuccess) return e;
+        note_launch();
+    }
+    k_check_solve_eps<float><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
+    k_diag_inverses<float><<<nblk, kThreads, 0, s>>>(n, F, D, st); note_launch();
+    k_retry_disarm<<<1, 32, 0, s>>>(st); note_launch();
     return cudaGetLastError();
 }
 

@@ -62,7 +62,31 @@ struct DevProblem {
     int64_t* ochunk_ptr = nullptr; // [nochunks+1] observation ranges (never across windows)
     int32_t* ochunk_win = nullptr; // [nochunks] window of each chunk
     int32_t* win_ochunk = nullptr; // [nwin+1] chunk ranges per window
+    // Pose-major observation chunks of the mixed form's FP64 Schur operator:
+    // chunk c covers pose-major positions [opch_q[c], opch_q[c+1]) of one pose,
+    // pose k's chunks are [pose_opch[k], pose_opch[k+1]).
+    int64_t nopch = 0;
+    int32_t* opch_q = nullptr;     // [nopch+1]
+    int32_t* pose_opch = nullptr;  // [K+1]
 };
+
+// At most this many observations per operator chunk (a warp's share).
+constexpr int kOpChunk = 128;
+
+// Per-observation record of the mixed form (landmark-major, 112 bytes): the
+// FP32 Jacobian blocks J_p (2 x 6) and J_l (2 x 3) that the FP32 Schur
+// records are built from, the robust weight W (2 x 2, row-major, FP32) and
+// the gradient factor g = rho' Omega r as two double-float values (hi, lo,
+// hi, lo). The mixed form's FP64-accurate Schur operator, b_l and H_ll are
+// sums over exactly these values.
+struct alignas(16) ObsJac {
+    float g[4];
+    float jp[12];
+    float jl[6];
+    float w[4];
+    float pad[2];
+};
+static_assert(sizeof(ObsJac) == 112, "ObsJac is seven 16-byte vectors");
 
 // Working arrays of one precision (T = double for the plain form, float for
 // the mixed form).
@@ -70,8 +94,10 @@ struct DevWork {
     void* hpl = nullptr;       // [M*RS] T, RS = 18 (double) or 20 (float, padded); pose-major positions
     void* W = nullptr;         // [M*RS] T, pose-major positions
     double* pose_aux = nullptr; // [K*24] mixed form: per-pose sandwich matrix, translation, rotation
-    void* partial = nullptr;   // [nsegs*36] T, Schur segment sums
-    void* lm_part = nullptr;   // [M*12] T, per-observation landmark records (9 used)
+    double* partial = nullptr; // [nsegs*36] Schur segment sums (FP64)
+    void* lm_part = nullptr;   // plain form: [M*12] per-observation landmark records (9 used)
+    ObsJac* jac = nullptr;     // mixed form: [M] per-observation Jacobian records
+    double* pcg = nullptr;     // mixed form: PCG vectors and operator scratch (pcg_doubles)
     void* pose_part = nullptr; // [M*28] T, per-observation pose records (27 used), pose-major positions
     double* hpp = nullptr;     // [K*36]
     double* hll = nullptr;     // [L*9]
@@ -106,6 +132,8 @@ struct LmState {
     int32_t good;      // trial step accepted
     int32_t nonfinite;
     int32_t refine_sweeps;  // refinement sweeps of the last reduced solve
+    int32_t skip_factor;    // mixed form: the factor kernels return at once (no retry armed)
+    int32_t shifted;        // mixed form: the last preconditioner factor needed the diagonal shift
 };
 
 // Per-window LM control of a batched solve (source/factor_graph.hpp:538-611
@@ -254,6 +282,13 @@ template <typename TS, typename TF>
 cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double* bs, double* x, double* work,
                                  LmState* st, int refine_iters, double tol, cudaStream_t s);
 
+// Mixed form: launch_factor, then, when it failed, one more factorisation of
+// S + mu diag(S) (the factor is the conjugate-gradient preconditioner only,
+// and the FP32-formed S may be indefinite where the exact S is not). Sets
+// st->shifted.
+cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float* D, LmState* st, double mu,
+                                         cudaStream_t s);
+
 // ---- mixed form (ba_inverse.cu) ----
 // X = L^-1 and XT = X^T from the factor F and its diagonal-block inverses D.
 template <typename TX>
@@ -263,5 +298,12 @@ cudaError_t launch_tri_inverse(int n, const TX* F, const TX* D, TX* X, TX* XT, L
 template <typename TS, typename TX>
 cudaError_t launch_refine(int n, const TS* S, const TX* X, const TX* XT, const double* bs, double* x, double* work,
                           LmState* st, int refine_iters, double tol, cudaStream_t s);
+// Mixed-form reduced solve: preconditioned conjugate gradients on the FP64
+// Schur operator of the FP32 Jacobian records (W.jac), applied matrix-free,
+// preconditioned by X^T X. Writes b_s (W.bs), delta_p and the landmark
+// back-substitution delta_l (W.delta); stops at ||b_s - S x|| <= tol ||b_s||
+// or max_it iterations.
+cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s);
+size_t pcg_doubles(const DevProblem& P);
 
 }  // namespace zs

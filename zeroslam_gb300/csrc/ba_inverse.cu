@@ -13,6 +13,9 @@
 //    cooperative launch with a deterministic grid-wide norm.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
+#include "ba_df.cuh"
 #include "ba_internal.h"
 
 namespace cg = cooperative_groups;
@@ -261,6 +264,352 @@ cudaError_t launch_refine(int n, const TS* S, const TX* X, const TX* XT, const d
     if (blocks > sm_count()) blocks = sm_count();
     cudaError_t e =
         cudaLaunchCooperativeKernel((const void*)k_refine<TS, TX>, dim3(blocks), dim3(kThreads), args, 0, s);
+    if (e == cudaSuccess) note_launch();
+    return e;
+}
+
+// ------------------------------------------------------------ mixed-form PCG
+//
+// S formed from FP32 products is wrong by ~1e-7 ||H|| entrywise, which is of
+// the order of its smallest eigenvalues on long trajectories (condition
+// numbers ~1e8: H_pp and W H_pl^T cancel there), so refinement against it
+// converges to the wrong step. The mixed form therefore solves the exact Schur
+// system of its FP32 Jacobian J' (the values its FP32 records are built from;
+// rounding J perturbs singular values by ~1e-7 ||J||, not eigenvalues by
+// ~1e-7 ||J||^2) by conjugate gradients: the operator
+//     S v = (H_pp + lambda I) v - H_pl (H_ll + lambda I)^-1 H_lp v
+// is applied matrix-free from the per-observation Jacobian records in
+// double-float arithmetic (ba_df.cuh: ~48 bits on the FP32 pipe; per
+// observation the pose and landmark motions cancel to ~1e-4, which leaves
+// ~1e-10), and X^T X (X = L^-1 of the FP32 factor of the FP32-formed S) is
+// the preconditioner. The right-hand side b_s and the landmark
+// back-substitution come from the same passes. CG vectors are FP64; every sum
+// has a fixed order.
+
+// Warp w of block b is the grid's warp b + gridDim.x * w: consecutive work
+// items spread over all blocks (and SMs) first.
+__device__ __forceinline__ int64_t spread_warp() {
+    return blockIdx.x + (int64_t)gridDim.x * (threadIdx.x >> 5);
+}
+
+__device__ __forceinline__ df ld_df(const df* p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return df{v.x, v.y};
+}
+
+// Landmark pass (a warp per landmark, lanes over its observations):
+//   y_l = (H_ll + lambda I)^-1 u_l,  u_l = -sum_o J_l^T (c g_o + W_o J_p v_p)
+//   (= c b_l - H_lp v), then ws_o = W_o (J_p v_p + J_l y_l) + c g_o for each
+// observation (ws holds J_p v_p between the two loops). The lane partials of
+// u meet in a double-float butterfly (df_add is commutative bit for bit, so
+// every lane holds the same u and y). v (double-float) null: v = 0. y
+// (optional) receives y_l in FP64; with ws null only y is computed.
+__device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac, const df* hinv, const df* v, bool c,
+                             float4* ws, double* y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t l = spread_warp(); l < P.L; l += nw) {
+        const int o0 = P.lm_ptr[l], o1 = P.lm_ptr[l + 1];
+        df_dot ua[3];
+        for (int o = o0 + lane; o < o1; o += 32) {
+            const float4* r = reinterpret_cast<const float4*>(jac + o);
+            const float4 G = __ldg(r);
+            df t0 = df_zero(), t1 = df_zero();
+            if (v) {
+                const df* vp = v + 6LL * P.obs_pose[o];
+                const float4 a = __ldg(r + 1), b = __ldg(r + 2), d = __ldg(r + 3);
+                df x[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) x[k] = ld_df(vp + k);
+                df_dot s0, s1;
+                s0.add(a.x, x[0]); s0.add(a.y, x[1]); s0.add(a.z, x[2]);
+                s0.add(a.w, x[3]); s0.add(b.x, x[4]); s0.add(b.y, x[5]);
+                s1.add(b.z, x[0]); s1.add(b.w, x[1]); s1.add(d.x, x[2]);
+                s1.add(d.y, x[3]); s1.add(d.z, x[4]); s1.add(d.w, x[5]);
+                t0 = s0.result();
+                t1 = s1.result();
+            }
+            const float4 e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
+            // w = W t + c g, W = [f.z f.w; h.x h.y]
+            df_dot q0, q1;
+            q0.add(f.z, t0); q0.add(f.w, t1);
+            q1.add(h.x, t0); q1.add(h.y, t1);
+            if (c) {
+                q0.add_df(df{G.x, G.y});
+                q1.add_df(df{G.z, G.w});
+            }
+            const df w0 = q0.result(), w1 = q1.result();
+            // u -= J_l^T w, J_l = [e.x e.y e.z; e.w f.x f.y]
+            ua[0].add(-e.x, w0); ua[0].add(-e.w, w1);
+            ua[1].add(-e.y, w0); ua[1].add(-f.x, w1);
+            ua[2].add(-e.z, w0); ua[2].add(-f.y, w1);
+            if (ws) ws[o] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        }
+        df u[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            df t = ua[k].result();
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const df oth{__shfl_xor_sync(0xffffffffu, t.hi, off), __shfl_xor_sync(0xffffffffu, t.lo, off)};
+                t = df_add(t, oth);
+            }
+            u[k] = t;
+        }
+        const df* hi = hinv + 9LL * l;
+        df yv[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            df acc = df_zero();
+#pragma unroll
+            for (int b = 0; b < 3; ++b) acc = df_add(acc, df_mul(ld_df(hi + 3 * a + b), u[b]));
+            yv[a] = acc;
+        }
+        if (y && lane < 3) y[3 * l + lane] = df_to_double(lane == 0 ? yv[0] : (lane == 1 ? yv[1] : yv[2]));
+        if (!ws) continue;
+        for (int o = o0 + lane; o < o1; o += 32) {
+            const float4* r = reinterpret_cast<const float4*>(jac + o);
+            const float4 G = __ldg(r), e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
+            const float4 tt = ws[o];  // this lane's own write above
+            // s = J_p v + J_l y
+            df_dot m0, m1;
+            m0.add_df(df{tt.x, tt.y});
+            m0.add(e.x, yv[0]); m0.add(e.y, yv[1]); m0.add(e.z, yv[2]);
+            m1.add_df(df{tt.z, tt.w});
+            m1.add(e.w, yv[0]); m1.add(f.x, yv[1]); m1.add(f.y, yv[2]);
+            const df s0 = m0.result(), s1 = m1.result();
+            // ws = W s + c g
+            df_dot n0, n1;
+            n0.add(f.z, s0); n0.add(f.w, s1);
+            n1.add(h.x, s0); n1.add(h.y, s1);
+            if (c) {
+                n0.add_df(df{G.x, G.y});
+                n1.add_df(df{G.z, G.w});
+            }
+            const df a0 = n0.result(), a1 = n1.result();
+            ws[o] = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
+        }
+    }
+}
+
+// Pose pass: a warp per observation chunk, part[6 ch + a] = sum over the
+// chunk of (J_p^T ws_o)_a: lanes strided, then a double-float butterfly
+// (df_add is commutative bit for bit, so every lane ends with the same value).
+__device__ void op_pose_chunks(const DevProblem& P, const ObsJac* __restrict__ jac, const float4* ws, df* part) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t ch = spread_warp(); ch < P.nopch; ch += nw) {
+        const int q1 = P.opch_q[ch + 1];
+        df_dot acc[6];
+        for (int q = P.opch_q[ch] + lane; q < q1; q += 32) {
+            const int o = P.pose_obs[q];
+            const float4* r = reinterpret_cast<const float4*>(jac + o);
+            const float4 a = __ldg(r + 1), b = __ldg(r + 2), d = __ldg(r + 3);
+            const float4 sv = __ldcg(ws + o);
+            const df s0{sv.x, sv.y}, s1{sv.z, sv.w};
+            const float j0[6] = {a.x, a.y, a.z, a.w, b.x, b.y}, j1[6] = {b.z, b.w, d.x, d.y, d.z, d.w};
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                acc[k].add(j0[k], s0);
+                acc[k].add(j1[k], s1);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            df t = acc[k].result();
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const df o{__shfl_xor_sync(0xffffffffu, t.hi, off), __shfl_xor_sync(0xffffffffu, t.lo, off)};
+                t = df_add(t, o);
+            }
+            if (lane == k) part[6 * ch + k] = t;
+        }
+    }
+}
+
+// sum of pose k's chunk partials of component a (i = 6 k + a), chunks in order.
+__device__ __forceinline__ double chunk_sum(const DevProblem& P, const df* part, int i) {
+    const int k = i / 6, a = i - 6 * (i / 6);
+    df s = df_zero();
+    const int c1 = P.pose_opch[k + 1];
+    for (int ch = P.pose_opch[k]; ch < c1; ++ch) s = df_add(s, ld_df(part + 6LL * ch + a));
+    return df_to_double(s);
+}
+
+// Deterministic grid-wide sum of one value per thread, the same in every
+// block: warp butterflies, the warps in order, then the block partials
+// (written to slot) in a fixed lane-strided order. One grid barrier.
+__device__ double grid_sum(cg::grid_group& grid, double v, double* slot, double* sh) {
+    constexpr int NW = kThreads / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = wsum(v);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NW; ++w) s += sh[w];
+        slot[blockIdx.x] = s;
+    }
+    grid.sync();
+    if (warp == 0) {
+        double t = 0.0;
+        for (unsigned b = lane; b < gridDim.x; b += 32) t += __ldcg(slot + b);
+        t = wsum(t);
+        if (lane == 0) sh[NW] = t;
+    }
+    __syncthreads();
+    const double t = sh[NW];
+    __syncthreads();
+    return t;
+}
+
+constexpr int kPcgMaxBlocks = 2048;
+
+__global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac* __restrict__ jac,
+                                                  const double* __restrict__ hinv, const float* __restrict__ X,
+                                                  const float* __restrict__ XT, double* delta, double* bs, double* buf,
+                                                  int max_it, double tol, LmState* st) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[kThreads / 32 + 1];
+    if (!__ldcg(&st->solve_ok)) return;  // written by an earlier launch: uniform
+    const int n = P.n;
+    const double lam = __ldcg(&st->lambda);
+    double* r = buf;
+    double* z = r + n;
+    double* p = z + n;
+    double* q = p + n;
+    double* u = q + n;
+    df* pdf = reinterpret_cast<df*>(u + n);  // double-float copies of p and of x
+    df* xdf = pdf + n;
+    df* part = xdf + n;                       // [6 nopch] chunk partials
+    df* hdf = part + 6 * P.nopch;             // [9 L] double-float (H_ll + lambda I)^-1
+    double* slots = reinterpret_cast<double*>(hdf + 9LL * P.L + ((9LL * P.L) & 1));  // [2 kPcgMaxBlocks]
+    float4* ws = reinterpret_cast<float4*>(slots + 2 * kPcgMaxBlocks);  // [M]
+    // grid sums alternate between two slot buffers: consecutive sums never
+    // share one, and a barrier separates every reuse
+    int red = 0;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+
+    for (int64_t i = tid; i < 9LL * P.L; i += nth) hdf[i] = df_from_double(hinv[i]);
+    grid.sync();
+    // r = b_s = b_p - H_pl (H_ll + lambda I)^-1 b_l, x = 0
+    op_landmarks(P, jac, hdf, nullptr, true, ws, nullptr);
+    grid.sync();
+    op_pose_chunks(P, jac, ws, part);
+    grid.sync();
+    double acc = 0.0;
+    for (int i = tid; i < n; i += nth) {
+        const double v = -chunk_sum(P, part, i);
+        r[i] = v;
+        bs[i] = v;
+        delta[i] = 0.0;
+        xdf[i] = df_zero();
+        acc += v * v;
+    }
+    const double bn2 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
+    double rn2 = bn2;
+    int it = 0;
+    bool indefinite = false;
+    if (bn2 > 0.0 && max_it > 0) {
+        // z = X^T X r, p = z
+        gemv_rows<float>(n, X, r, u, 0, nullptr, nullptr);
+        grid.sync();
+        gemv_rows<float>(n, XT, u, z, 1, nullptr, nullptr);
+        grid.sync();
+        acc = 0.0;
+        for (int i = tid; i < n; i += nth) {
+            const double zi = __ldcg(z + i);
+            p[i] = zi;
+            pdf[i] = df_from_double(zi);
+            acc += __ldcg(r + i) * zi;
+        }
+        double rz = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
+        for (;;) {
+            // q = S p
+            op_landmarks(P, jac, hdf, pdf, false, ws, nullptr);
+            grid.sync();
+            op_pose_chunks(P, jac, ws, part);
+            grid.sync();
+            acc = 0.0;
+            for (int i = tid; i < n; i += nth) {
+                const double pi = __ldcg(p + i);
+                const double qi = lam * pi + chunk_sum(P, part, i);
+                q[i] = qi;
+                acc += pi * qi;
+            }
+            const double pq = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
+            if (!(pq > 0.0)) {  // uniform: S is not positive definite, as a failed FP64 factorisation
+                indefinite = true;
+                break;
+            }
+            const double alpha = rz / pq;
+            acc = 0.0;
+            for (int i = tid; i < n; i += nth) {
+                const double xi = __ldcg(delta + i) + alpha * __ldcg(p + i);
+                delta[i] = xi;
+                xdf[i] = df_from_double(xi);
+                const double ri = __ldcg(r + i) - alpha * __ldcg(q + i);
+                r[i] = ri;
+                acc += ri * ri;
+            }
+            rn2 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
+            ++it;
+            if (!(rn2 > tol * tol * bn2) || it >= max_it) break;
+            gemv_rows<float>(n, X, r, u, 0, nullptr, nullptr);
+            grid.sync();
+            gemv_rows<float>(n, XT, u, z, 1, nullptr, nullptr);
+            grid.sync();
+            acc = 0.0;
+            for (int i = tid; i < n; i += nth) acc += __ldcg(r + i) * __ldcg(z + i);
+            const double rz1 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
+            const double beta = rz1 / rz;
+            rz = rz1;
+            for (int i = tid; i < n; i += nth) {
+                const double pi = __ldcg(z + i) + beta * __ldcg(p + i);
+                p[i] = pi;
+                pdf[i] = df_from_double(pi);
+            }
+            grid.sync();
+        }
+    }
+    if (indefinite) {
+        if (tid == 0) st->solve_ok = 0;
+        return;
+    }
+    // landmark back-substitution delta_l = (H_ll + lambda I)^-1 (b_l - H_lp delta_p)
+    // (xdf was written before the last grid barrier)
+    op_landmarks(P, jac, hdf, xdf, true, nullptr, delta + n);
+    if (tid == 0) {
+        st->resid_norm = sqrt(rn2);
+        st->rhs_norm = sqrt(bn2);
+        st->refine_sweeps = it;
+    }
+}
+
+size_t pcg_doubles(const DevProblem& P) {
+    // r z p q u, the two double-float copies, chunk partials, the double-float
+    // landmark inverses, slots, ws (16 B each); 8-byte units, ws 16-byte aligned
+    return 7 * (size_t)P.n + 6 * (size_t)P.nopch + 9 * (size_t)P.L + ((9 * (size_t)P.L) & 1) +
+           2 * (size_t)kPcgMaxBlocks + 2 * (size_t)P.M;
+}
+
+cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s) {
+    if (P.n <= 0) return cudaSuccess;
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg, kThreads, 0);
+    if (e != cudaSuccess) return e;
+    const int blocks = std::max(1, std::min(kPcgMaxBlocks, occ * sm_count()));
+    DevProblem Pv = P;
+    const ObsJac* jac = W.jac;
+    const double* hinv = W.hll_inv;
+    const float* X = (const float*)W.X;
+    const float* XT = (const float*)W.XT;
+    double* delta = W.delta;
+    double* bs = W.bs;
+    double* buf = W.pcg;
+    void* args[] = {(void*)&Pv,    (void*)&jac, (void*)&hinv,   (void*)&X,   (void*)&XT, (void*)&delta,
+                    (void*)&bs,    (void*)&buf, (void*)&max_it, (void*)&tol, (void*)&st};
+    e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(blocks), dim3(kThreads), args, 0, s);
     if (e == cudaSuccess) note_launch();
     return e;
 }

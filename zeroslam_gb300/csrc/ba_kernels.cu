@@ -11,7 +11,8 @@
 //                                            robust_info        source/factor_graph.hpp:254-269
 //   k_invert, k_w                            damping + invert<3> source/factor_graph.hpp:738-765,
 //                                                               source/matrix.hpp:749-774
-//   k_schur_chunks, k_schur_assemble, k_bs   W = H_pl H_ll^-1, S = H_pp - W H_lp, b_s = b_p - W b_l
+//   k_reduce_lm_jac (mixed form)             H_ll, b_l in double-float from the FP32 Jacobian records
+//   k_schur_segments, k_schur_assemble, k_bs W = H_pl H_ll^-1, S = H_pp - W H_lp, b_s = b_p - W b_l
 //                                            source/factor_graph.hpp:768-781,
 //                                            source/matrix_sparse_block.hpp:158-196,
 //                                            source/matrix_sparse_block_diagonal.hpp:107-142
@@ -21,6 +22,7 @@
 //   k_scale_partial, k_decide                LM acceptance      source/factor_graph.hpp:555-606
 #include <algorithm>
 
+#include "ba_df.cuh"
 #include "ba_internal.h"
 
 namespace zs {
@@ -99,7 +101,8 @@ __global__ void __launch_bounds__(kThreads) k_pose_aux(DevProblem P, double* aux
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
-                                                        T* __restrict__ pose_part, const double* __restrict__ aux) {
+                                                        T* __restrict__ pose_part, const double* __restrict__ aux,
+                                                        ObsJac* __restrict__ jac) {
     constexpr int RS = RecStride<T>::value;
     // threads in pose-major order: the large records (H_pl, pose partials)
     // are written coalesced and neighbouring threads share the pose's data
@@ -154,9 +157,15 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         } else {
             const T iz = T(1) / Zv;
             const T fx = (T)P.intr.fx, fy = (T)P.intr.fy;
-            const T u0 = (T)(uv.x - P.intr.cx), v0 = (T)(uv.y - P.intr.cy);
-            r[0] = (double)(u0 - fx * (Xv * iz));
-            r[1] = (double)(v0 - fy * (Yv * iz));
+            // The residual subtracts two pixel coordinates of a few hundred
+            // pixels to get about one, so it is formed in FP64 (in FP32 its
+            // rounding, ~1e-5 px, dominates the gradient near convergence).
+            // 1/z: the FP32 reciprocal refined by one Newton-Raphson step,
+            // y' = y + y (1 - z y), which squares its relative error.
+            double izd = (double)iz;
+            izd = fma(izd, fma(-zc, izd, 1.0), izd);
+            r[0] = (uv.x - P.intr.cx) - P.intr.fx * (xc * izd);
+            r[1] = (uv.y - P.intr.cy) - P.intr.fy * (yc * izd);
             const T iz2 = iz * iz;
             Jc[0] = fx * iz; Jc[1] = T(0); Jc[2] = -fx * Xv * iz2;
             Jc[3] = T(0); Jc[4] = fy * iz; Jc[5] = -fy * Yv * iz2;
@@ -245,6 +254,24 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         for (int k = 0; k < 18; ++k) hb[k] = T(0);
     }
     store_rec(pose_part + q * kPoseRec, prec);
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: the Jacobian record (H_ll and b are its FP64 Gram sums)
+        float4* d = reinterpret_cast<float4*>(jac + o);
+        const df g0 = df_from_double(drho * orr0), g1 = df_from_double(drho * orr1);
+        d[0] = make_float4(g0.hi, g0.lo, g1.hi, g1.lo);
+        float jp[12], jl[6];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) jp[k] = pf ? 0.f : (float)Jp[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) jl[k] = lf ? 0.f : (float)Jl[k];
+        d[1] = make_float4(jp[0], jp[1], jp[2], jp[3]);
+        d[2] = make_float4(jp[4], jp[5], jp[6], jp[7]);
+        d[3] = make_float4(jp[8], jp[9], jp[10], jp[11]);
+        d[4] = make_float4(jl[0], jl[1], jl[2], jl[3]);
+        d[5] = make_float4(jl[4], jl[5], (float)W00, (float)W01);
+        d[6] = make_float4((float)W10, (float)W11, 0.f, 0.f);
+        return;
+    } else {
     T lrec[kLmRec];
 #pragma unroll
     for (int k = 0; k < kLmRec; ++k) lrec[k] = T(0);
@@ -265,6 +292,7 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         for (int a = 0; a < 3; ++a) lrec[6 + a] = -(Jl[a] * g0 + Jl[3 + a] * g1);
     }
     store_rec(lm_part + o * kLmRec, lrec);
+    }
 }
 
 // Duplicate (pose, landmark) observations: the run's owner gets the sum of
@@ -306,6 +334,71 @@ __global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* _
     h[6] = acc[2]; h[7] = acc[4]; h[8] = acc[5];
     double* bl = b + P.n + 3LL * l;
     bl[0] = acc[6]; bl[1] = acc[7]; bl[2] = acc[8];
+}
+
+// Mixed form: H_ll = sum J_l^T W J_l and b_l = -sum J_l^T g per landmark from
+// the FP32 Jacobian records, observations in order, in double-float (the
+// products of FP32 values are exact, the sums carry ~48 bits): H_ll must be
+// accurate far beyond FP32 for the Schur operator of launch_pcg.
+__global__ void __launch_bounds__(kThreads) k_reduce_lm_jac(DevProblem P, const ObsJac* __restrict__ jac, double* hll,
+                                                            double* b) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= P.L) return;
+    df h[6], bl[3];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) h[k] = df_zero();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) bl[k] = df_zero();
+    const int e = P.lm_ptr[l + 1];
+    for (int o = P.lm_ptr[l]; o < e; ++o) {
+        const float4* r = reinterpret_cast<const float4*>(jac + o);
+        const float4 G = __ldg(r), a = __ldg(r + 4), c = __ldg(r + 5), d = __ldg(r + 6);
+        const float J0[3] = {a.x, a.y, a.z}, J1[3] = {a.w, c.x, c.y};
+        const df g0{G.x, G.y}, g1{G.z, G.w};
+        // B = J^T W (3 x 2): B0 = column 0, B1 = column 1
+        df B0[3], B1[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            df_dot s0, s1;
+            s0.add(J0[k], df{c.z, 0.f});
+            s0.add(J1[k], df{d.x, 0.f});
+            s1.add(J0[k], df{c.w, 0.f});
+            s1.add(J1[k], df{d.y, 0.f});
+            B0[k] = s0.result();
+            B1[k] = s1.result();
+        }
+        // H(a, c) = B0[a] J0[c] + B1[a] J1[c], upper triangle row by row
+        auto entry = [&](df hk, int a, int cc) {
+            df_dot s;
+            s.add(J0[cc], B0[a]);
+            s.add(J1[cc], B1[a]);
+            s.add_df(hk);
+            return s.result();
+        };
+        h[0] = entry(h[0], 0, 0);
+        h[1] = entry(h[1], 0, 1);
+        h[2] = entry(h[2], 0, 2);
+        h[3] = entry(h[3], 1, 1);
+        h[4] = entry(h[4], 1, 2);
+        h[5] = entry(h[5], 2, 2);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            df_dot s;
+            s.add(-J0[k], g0);
+            s.add(-J1[k], g1);
+            s.add_df(bl[k]);
+            bl[k] = s.result();
+        }
+    }
+    double hd[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) hd[k] = df_to_double(h[k]);
+    double* o9 = hll + (int64_t)l * 9;
+    o9[0] = hd[0]; o9[1] = hd[1]; o9[2] = hd[2];
+    o9[3] = hd[1]; o9[4] = hd[3]; o9[5] = hd[4];
+    o9[6] = hd[2]; o9[7] = hd[4]; o9[8] = hd[5];
+    double* bo = b + P.n + 3LL * l;
+    bo[0] = df_to_double(bl[0]); bo[1] = df_to_double(bl[1]); bo[2] = df_to_double(bl[2]);
 }
 
 // Per pose (a CTA): each thread sums its strided share of the pose's
@@ -432,23 +525,20 @@ __device__ __forceinline__ void load_rec(const double* p, double v[20]) {
 // Partial 6 x 6 sums W_i H_j^T over one segment (<= 512 consecutive triples
 // of one pose pair), a warp per segment: lane t takes the segment's triples
 // t, t + 32, ... (consecutive lanes read consecutive pose-major records,
-// coalesced) and accumulates in T; the 32 lane partials meet in a fixed tree
-// (FP32: an xor-shuffle butterfly, identical in every lane; FP64: a transpose
-// through shared memory and a column sum in lane order). With windows,
-// segments of stopped windows (ctl) are skipped.
-template <typename T>
-constexpr int schur_seg_threads() {
-    return sizeof(T) == 8 ? 128 : 256;  // FP64: 4 warps keep the transpose buffer under 48 KB
-}
+// coalesced) and accumulates in T (at most 16 triples per lane); the 32
+// lane partials meet in FP64 (a transpose through shared memory, then a
+// column sum in lane order) and the segment sum is kept in FP64: the
+// diagonal blocks S_ii = H_pp - sum W H^T cancel strongly, so no sum of many
+// terms is rounded to FP32. With windows, segments of stopped windows (ctl)
+// are skipped.
+constexpr int kSegThreads = 128;  // 4 warps: the transpose buffers stay under 48 KB
 
 template <typename T>
-__global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevProblem P, const T* __restrict__ W,
-                                                                          const T* __restrict__ hpl,
-                                                                          T* __restrict__ part,
-                                                                          const WinCtl* __restrict__ ctl) {
+__global__ void __launch_bounds__(kSegThreads) k_schur_segments(DevProblem P, const T* __restrict__ W,
+                                                                const T* __restrict__ hpl, double* __restrict__ part,
+                                                                const WinCtl* __restrict__ ctl) {
     constexpr int RS = RecStride<T>::value;
-    constexpr int NW = schur_seg_threads<T>() / 32;
-    __shared__ double red[sizeof(T) == 8 ? NW : 1][32][37];
+    __shared__ double red[kSegThreads / 32][32][37];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (g >= P.nsegs) return;
@@ -468,27 +558,18 @@ __global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevPr
             for (int d = 0; d < 6; ++d)
                 acc[a * 6 + d] += wv[a * 3] * hv[d * 3] + wv[a * 3 + 1] * hv[d * 3 + 1] + wv[a * 3 + 2] * hv[d * 3 + 2];
     }
-    T* out = part + g * 36;
-    if (sizeof(T) == 4) {
+    double (*r)[37] = red[wib];
 #pragma unroll
-        for (int e = 0; e < 36; ++e) {
-            T v = acc[e];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-            if (e == lane || e == 32 + lane) out[e] = v;
-        }
-    } else {
-        double (*r)[37] = red[sizeof(T) == 8 ? wib : 0];
-#pragma unroll
-        for (int e = 0; e < 36; ++e) r[lane][e] = (double)acc[e];
-        __syncwarp();
-        double v0 = 0.0, v1 = 0.0;
-        for (int k = 0; k < 32; ++k) v0 += r[k][lane];
-        out[lane] = (T)v0;
-        if (lane < 4) {
-            for (int k = 0; k < 32; ++k) v1 += r[k][32 + lane];
-            out[32 + lane] = (T)v1;
-        }
+    for (int e = 0; e < 36; ++e) r[lane][e] = (double)acc[e];
+    __syncwarp();
+    double* out = part + g * 36;
+    double v0 = 0.0;
+    for (int k = 0; k < 32; ++k) v0 += r[k][lane];
+    out[lane] = v0;
+    if (lane < 4) {
+        double v1 = 0.0;
+        for (int k = 0; k < 32; ++k) v1 += r[k][32 + lane];
+        out[32 + lane] = v1;
     }
 }
 
@@ -496,8 +577,7 @@ __global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevPr
 // pairs subtract from the H_pp + lambda I block written by k_s_init,
 // off-diagonal pairs write both blocks. With windows the pair's window S
 // block is used and stopped windows (ctl) are skipped.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const T* __restrict__ part, double* S,
+__global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const double* __restrict__ part, double* S,
                                                              const WinCtl* __restrict__ ctl) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= (int64_t)P.npairs * 36) return;
@@ -514,7 +594,7 @@ __global__ void __launch_bounds__(kThreads) k_schur_assemble(DevProblem P, const
     }
     double sum = 0.0;
     const int64_t g1 = P.pair_seg_ptr[p + 1];
-    for (int64_t g = P.pair_seg_ptr[p]; g < g1; ++g) sum += (double)part[g * 36 + e];
+    for (int64_t g = P.pair_seg_ptr[p]; g < g1; ++g) sum += part[g * 36 + e];
     double* Sw = S + soff;
     const int64_t n = nw;
     const int64_t row = 6LL * (i - p0) + e / 6, col = 6LL * (j - p0) + e % 6;
@@ -794,11 +874,19 @@ void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
         k_pose_aux<<<grid_for(P.K), kThreads, 0, s>>>(P, W.pose_aux); note_launch();
     }
     if (P.M > 0) {
-        k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part, W.pose_aux); note_launch();
+        k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part, W.pose_aux,
+                                                          W.jac); note_launch();
         if (P.has_dups) { k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch(); }
     }
-    if (P.L > 0) { k_reduce_lm<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.lm_part, W.hll, W.b); note_launch(); }
-    if (P.K > 0) { k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b); note_launch(); }
+    if (P.L > 0) {
+        if (sizeof(T) == 4) k_reduce_lm_jac<<<grid_for(P.L), kThreads, 0, s>>>(P, W.jac, W.hll, W.b);
+        else k_reduce_lm<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.lm_part, W.hll, W.b);
+        note_launch();
+    }
+    if (P.K > 0) {
+        k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b);
+        note_launch();
+    }
 }
 
 template <typename T>
@@ -810,11 +898,10 @@ void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStr
 template <typename T>
 void launch_schur_pairs(const DevProblem& P, DevWork& W, const WinCtl* ctl, cudaStream_t s) {
     if (P.npairs > 0) {
-        constexpr int nt = schur_seg_threads<T>();
-        const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
-        k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, (T*)W.partial, ctl);
+        const int64_t blocks = (P.nsegs * 32 + kSegThreads - 1) / kSegThreads;
+        k_schur_segments<T><<<(int)blocks, kSegThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
         note_launch();
-        k_schur_assemble<T><<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, (const T*)W.partial, W.S, ctl);
+        k_schur_assemble<<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, W.partial, W.S, ctl);
         note_launch();
     }
 }
@@ -824,7 +911,8 @@ void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream
     const int64_t nn = (int64_t)P.n * P.n;
     if (nn > 0) { k_s_init<<<grid_for(nn), kThreads, 0, s>>>(P, W.hpp, (double*)W.S, st); note_launch(); }
     launch_schur_pairs<T>(P, W, nullptr, s);
-    if (P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
+    // (the mixed form's b_s comes from its FP64 operator, launch_pcg)
+    if (sizeof(T) == 8 && P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
 }
 
 template <typename T>

@@ -303,6 +303,17 @@ def _finish(name, q_gt, t_gt, X_gt, obs_pose, obs_lm, obs_uv, q0, t0, X0, iterat
     )
 
 
+def _map_gauge(sc: Scene) -> Scene:
+    """zeroslam's gauge for a map with more than two frames: frames 0 and 1
+    fixed (source/map.hpp:134). With pose 0 alone the monocular scale is free,
+    S is singular along it and only the damping regularises it; at small
+    lambda the steps then blow up along that direction and the accept /
+    reject sequence of LM depends on rounding."""
+    if sc.K > 2:
+        sc.pose_fixed[1] = 1
+    return sc
+
+
 def _depth_relative_noise(X, centre, obs_pose, obs_lm, rng, rel):
     """Isotropic Gaussian landmark noise with sigma = rel x the distance from
     the landmark to the first camera that observes it."""
@@ -373,8 +384,9 @@ def walk_scene(K: int = 200, L: int = 50000, seed: int = 1, iterations: int = 20
     X0 = X + _depth_relative_noise(X, centre, obs_pose, obs_lm, rng, landmark_rel_noise)
     meta = dict(generator="walk", K=K, L_requested=L, seed=seed, dmax=dmax, sigma_px=sigma_px,
                 landmark_rel_noise=landmark_rel_noise)
-    return _finish(f"walk_K{K}_L{L}_s{seed}", q_gt, t_gt, X, obs_pose, obs_lm, obs_uv,
-                   q0, t0, X0, iterations, meta)
+    sc = _finish(f"walk_K{K}_L{L}_s{seed}", q_gt, t_gt, X, obs_pose, obs_lm, obs_uv,
+                 q0, t0, X0, iterations, meta)
+    return _map_gauge(sc)
 
 
 LOOP_DMAX = 5.6
@@ -417,8 +429,9 @@ def loop_scene(K: int = 1000, L: int = 200000, seed: int = 4, iterations: int = 
     X0 = X + _depth_relative_noise(X, centre, obs_pose, obs_lm, rng, landmark_rel_noise)
     meta = dict(generator="loop", K=K, L_requested=L, seed=seed, dmax=dmax, sigma_px=sigma_px,
                 landmark_rel_noise=landmark_rel_noise)
-    return _finish(f"loop_K{K}_L{L}_s{seed}", q_gt, t_gt, X, obs_pose, obs_lm, obs_uv,
-                   q0, t0, X0, iterations, meta)
+    sc = _finish(f"loop_K{K}_L{L}_s{seed}", q_gt, t_gt, X, obs_pose, obs_lm, obs_uv,
+                 q0, t0, X0, iterations, meta)
+    return _map_gauge(sc)
 
 
 def window_batch(n_windows: int = 256, seed: int = 2, iterations: int = 10,
