@@ -476,6 +476,12 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     }
     pose_opch[K] = (int32_t)opch_q.size();
     opch_q.push_back((int32_t)M);
+    std::vector<int32_t> lmch_l{0};
+    for (int l = 0; l < L; ++l) {
+        const int32_t start = lm_ptr[lmch_l.back()];
+        if (l > lmch_l.back() && lm_ptr[l + 1] - start > kOpChunk) lmch_l.push_back(l);
+    }
+    if (lmch_l.back() != L) lmch_l.push_back(L);
     // Schur triples: for each landmark, every (block a, block b) with pose_a >= pose_b,
     // grouped by pose pair (i, j) = (pose_a, pose_b), landmark order within a pair.
     // Pair keys are window-local: key = base_w + (i - p0_w) K_w + (j - p0_w).
@@ -604,6 +610,8 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     P.nopch = (int64_t)opch_q.size() - 1;
     P.opch_q = upload(opch_q, own, s);
     P.pose_opch = upload(pose_opch, own, s);
+    P.nlmch = (int64_t)lmch_l.size() - 1;
+    P.lmch_l = upload(lmch_l, own, s);
     P.triples = upload(triples, own, s);
     P.nwin = nwin;
     std::vector<int64_t> win_s_off(nwin, 0);
@@ -644,7 +652,10 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     W.W = dalloc<char>(ts * rs * M, own);
     W.pose_aux = dalloc<double>((size_t)K * 24, own);
     W.partial = dalloc<double>(36 * (size_t)P.nsegs, own);
-    if (h->tsize == 4) W.jac = dalloc<ObsJac>((size_t)M, own);
+    if (h->tsize == 4) {
+        W.jac = dalloc<ObsJac>((size_t)M, own);
+        W.jp_pm = dalloc<float4>(3 * (size_t)M, own);
+    }
     else W.lm_part = dalloc<char>(ts * 12 * M, own);  // record-major, 9 values padded to 12
     W.pose_part = dalloc<char>(ts * 28 * M, own);  // record-major, 27 values padded to 28
     W.hpp = dalloc<double>((size_t)K * 36, own);

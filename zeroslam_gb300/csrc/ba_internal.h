@@ -68,10 +68,15 @@ struct DevProblem {
     int64_t nopch = 0;
     int32_t* opch_q = nullptr;     // [nopch+1]
     int32_t* pose_opch = nullptr;  // [K+1]
+    // Landmark chunks of the same operator: chunk c holds landmarks
+    // [lmch_l[c], lmch_l[c+1]), consecutive, <= kOpChunk observations in all
+    // (or one landmark with more).
+    int64_t nlmch = 0;
+    int32_t* lmch_l = nullptr;     // [nlmch+1]
 };
 
 // At most this many observations per operator chunk (a warp's share).
-constexpr int kOpChunk = 128;
+constexpr int kOpChunk = 64;
 
 // Per-observation record of the mixed form (landmark-major, 112 bytes): the
 // FP32 Jacobian blocks J_p (2 x 6) and J_l (2 x 3) that the FP32 Schur
@@ -97,6 +102,7 @@ struct DevWork {
     double* partial = nullptr; // [nsegs*36] Schur segment sums (FP64)
     void* lm_part = nullptr;   // plain form: [M*12] per-observation landmark records (9 used)
     ObsJac* jac = nullptr;     // mixed form: [M] per-observation Jacobian records
+    float4* jp_pm = nullptr;   // mixed form: [3M] J_p of each record again, pose-major positions
     double* pcg = nullptr;     // mixed form: PCG vectors and operator scratch (pcg_doubles)
     void* pose_part = nullptr; // [M*28] T, per-observation pose records (27 used), pose-major positions
     double* hpp = nullptr;     // [K*36]

@@ -297,86 +297,130 @@ __device__ __forceinline__ df ld_df(const df* p) {
     return df{v.x, v.y};
 }
 
-// Landmark pass (a warp per landmark, lanes over its observations):
-//   y_l = (H_ll + lambda I)^-1 u_l,  u_l = -sum_o J_l^T (c g_o + W_o J_p v_p)
-//   (= c b_l - H_lp v), then ws_o = W_o (J_p v_p + J_l y_l) + c g_o for each
-// observation (ws holds J_p v_p between the two loops). The lane partials of
-// u meet in a double-float butterfly (df_add is commutative bit for bit, so
-// every lane holds the same u and y). v (double-float) null: v = 0. y
-// (optional) receives y_l in FP64; with ws null only y is computed.
+// Landmark pass: a warp per landmark chunk (P.lmch_l), 32 consecutive
+// observations (landmark-major) at a time, lane i taking observation
+// base + i:
+//   u_l = -sum_o J_l^T (c g_o + W_o J_p v_p)   (= c b_l - H_lp v),
+//   y_l = (H_ll + lambda I)^-1 u_l,
+// then ws_o = W_o (J_p v_p + J_l y_l) + c g_o for each observation (ws holds
+// J_p v_p in between). The per-observation terms of u meet in a segmented
+// inclusive scan over the lanes (segments: runs of one landmark; a
+// Hillis-Steele scan in double-float) plus the running sum carried over from
+// the previous 32; the lane holding a landmark's last observation forms y_l
+// and stores it (yst). ws_o goes to wsp at the observation's pose-major
+// position. v (double-float) null: v = 0. y (optional) receives y_l in FP64;
+// with ws null only y is computed.
 __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac, const df* hinv, const df* v, bool c,
-                             float4* ws, double* y) {
+                             float4* ws, float4* wsp, df* yst, double* y) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t l = spread_warp(); l < P.L; l += nw) {
-        const int o0 = P.lm_ptr[l], o1 = P.lm_ptr[l + 1];
-        df_dot ua[3];
-        for (int o = o0 + lane; o < o1; o += 32) {
-            const float4* r = reinterpret_cast<const float4*>(jac + o);
-            const float4 G = __ldg(r);
-            df t0 = df_zero(), t1 = df_zero();
-            if (v) {
-                const df* vp = v + 6LL * P.obs_pose[o];
-                const float4 a = __ldg(r + 1), b = __ldg(r + 2), d = __ldg(r + 3);
-                df x[6];
+    for (int64_t ch = spread_warp(); ch < P.nlmch; ch += nw) {
+        const int l0 = P.lmch_l[ch], l1 = P.lmch_l[ch + 1];
+        const int O0 = P.lm_ptr[l0], O1 = P.lm_ptr[l1];
+        df carry[3] = {df_zero(), df_zero(), df_zero()};
+        int carry_l = -1;
+        for (int base = O0; base < O1; base += 32) {
+            const int o = base + lane;
+            const bool valid = o < O1;
+            const int l = valid ? P.obs_lm[o] : -1 - lane;  // invalid lanes: segments of their own
+            df k[3] = {df_zero(), df_zero(), df_zero()};
+            if (valid) {
+                const float4* r = reinterpret_cast<const float4*>(jac + o);
+                const float4 G = __ldg(r);
+                df t0 = df_zero(), t1 = df_zero();
+                if (v) {
+                    const df* vp = v + 6LL * P.obs_pose[o];
+                    const float4 a = __ldg(r + 1), b = __ldg(r + 2), d = __ldg(r + 3);
+                    df x[6];
 #pragma unroll
-                for (int k = 0; k < 6; ++k) x[k] = ld_df(vp + k);
-                df_dot s0, s1;
-                s0.add(a.x, x[0]); s0.add(a.y, x[1]); s0.add(a.z, x[2]);
-                s0.add(a.w, x[3]); s0.add(b.x, x[4]); s0.add(b.y, x[5]);
-                s1.add(b.z, x[0]); s1.add(b.w, x[1]); s1.add(d.x, x[2]);
-                s1.add(d.y, x[3]); s1.add(d.z, x[4]); s1.add(d.w, x[5]);
-                t0 = s0.result();
-                t1 = s1.result();
+                    for (int q = 0; q < 6; ++q) x[q] = ld_df(vp + q);
+                    df_dot s0, s1;
+                    s0.add(a.x, x[0]); s0.add(a.y, x[1]); s0.add(a.z, x[2]);
+                    s0.add(a.w, x[3]); s0.add(b.x, x[4]); s0.add(b.y, x[5]);
+                    s1.add(b.z, x[0]); s1.add(b.w, x[1]); s1.add(d.x, x[2]);
+                    s1.add(d.y, x[3]); s1.add(d.z, x[4]); s1.add(d.w, x[5]);
+                    t0 = s0.result();
+                    t1 = s1.result();
+                }
+                const float4 e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
+                // w = W t + c g, W = [f.z f.w; h.x h.y]
+                df_dot q0, q1;
+                q0.add(f.z, t0); q0.add(f.w, t1);
+                q1.add(h.x, t0); q1.add(h.y, t1);
+                if (c) {
+                    q0.add_df(df{G.x, G.y});
+                    q1.add_df(df{G.z, G.w});
+                }
+                const df w0 = q0.result(), w1 = q1.result();
+                // k = -J_l^T w, J_l = [e.x e.y e.z; e.w f.x f.y]
+                df_dot k0, k1, k2;
+                k0.add(-e.x, w0); k0.add(-e.w, w1);
+                k1.add(-e.y, w0); k1.add(-f.x, w1);
+                k2.add(-e.z, w0); k2.add(-f.y, w1);
+                k[0] = k0.result();
+                k[1] = k1.result();
+                k[2] = k2.result();
+                if (ws) ws[o] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
             }
-            const float4 e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
-            // w = W t + c g, W = [f.z f.w; h.x h.y]
-            df_dot q0, q1;
-            q0.add(f.z, t0); q0.add(f.w, t1);
-            q1.add(h.x, t0); q1.add(h.y, t1);
-            if (c) {
-                q0.add_df(df{G.x, G.y});
-                q1.add_df(df{G.z, G.w});
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int lo = __shfl_up_sync(0xffffffffu, l, off);
+                df kk[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    kk[a].hi = __shfl_up_sync(0xffffffffu, k[a].hi, off);
+                    kk[a].lo = __shfl_up_sync(0xffffffffu, k[a].lo, off);
+                }
+                if (lane >= off && lo == l) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) k[a] = df_add(kk[a], k[a]);
+                }
             }
-            const df w0 = q0.result(), w1 = q1.result();
-            // u -= J_l^T w, J_l = [e.x e.y e.z; e.w f.x f.y]
-            ua[0].add(-e.x, w0); ua[0].add(-e.w, w1);
-            ua[1].add(-e.y, w0); ua[1].add(-f.x, w1);
-            ua[2].add(-e.z, w0); ua[2].add(-f.y, w1);
-            if (ws) ws[o] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
-        }
-        df u[3];
+            if (l == carry_l) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            df t = ua[k].result();
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const df oth{__shfl_xor_sync(0xffffffffu, t.hi, off), __shfl_xor_sync(0xffffffffu, t.lo, off)};
-                t = df_add(t, oth);
+                for (int a = 0; a < 3; ++a) k[a] = df_add(carry[a], k[a]);
             }
-            u[k] = t;
-        }
-        const df* hi = hinv + 9LL * l;
-        df yv[3];
+            if (valid && o + 1 == P.lm_ptr[l + 1]) {  // the landmark's last observation
+                const df* hi = hinv + 9LL * l;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            df acc = df_zero();
+                for (int a = 0; a < 3; ++a) {
+                    df acc = df_zero();
 #pragma unroll
-            for (int b = 0; b < 3; ++b) acc = df_add(acc, df_mul(ld_df(hi + 3 * a + b), u[b]));
-            yv[a] = acc;
+                    for (int b = 0; b < 3; ++b) acc = df_add(acc, df_mul(ld_df(hi + 3 * a + b), k[b]));
+                    yst[3LL * l + a] = acc;
+                    if (y) y[3LL * l + a] = df_to_double(acc);
+                }
+            }
+            carry_l = __shfl_sync(0xffffffffu, l, 31);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                carry[a].hi = __shfl_sync(0xffffffffu, k[a].hi, 31);
+                carry[a].lo = __shfl_sync(0xffffffffu, k[a].lo, 31);
+            }
         }
-        if (y && lane < 3) y[3 * l + lane] = df_to_double(lane == 0 ? yv[0] : (lane == 1 ? yv[1] : yv[2]));
+        for (int l = l0 + lane; l < l1; l += 32) {  // landmarks without observations: y = 0
+            if (P.lm_ptr[l] == P.lm_ptr[l + 1]) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    yst[3LL * l + a] = df_zero();
+                    if (y) y[3LL * l + a] = 0.0;
+                }
+            }
+        }
         if (!ws) continue;
-        for (int o = o0 + lane; o < o1; o += 32) {
+        __syncwarp();  // yst of this chunk written by the warp's lanes
+        for (int o = O0 + lane; o < O1; o += 32) {
+            const int l = P.obs_lm[o];
             const float4* r = reinterpret_cast<const float4*>(jac + o);
             const float4 G = __ldg(r), e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
             const float4 tt = ws[o];  // this lane's own write above
+            const df y0 = yst[3LL * l], y1 = yst[3LL * l + 1], y2 = yst[3LL * l + 2];
             // s = J_p v + J_l y
             df_dot m0, m1;
             m0.add_df(df{tt.x, tt.y});
-            m0.add(e.x, yv[0]); m0.add(e.y, yv[1]); m0.add(e.z, yv[2]);
+            m0.add(e.x, y0); m0.add(e.y, y1); m0.add(e.z, y2);
             m1.add_df(df{tt.z, tt.w});
-            m1.add(e.w, yv[0]); m1.add(f.x, yv[1]); m1.add(f.y, yv[2]);
+            m1.add(e.w, y0); m1.add(f.x, y1); m1.add(f.y, y2);
             const df s0 = m0.result(), s1 = m1.result();
             // ws = W s + c g
             df_dot n0, n1;
@@ -387,25 +431,24 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
                 n1.add_df(df{G.z, G.w});
             }
             const df a0 = n0.result(), a1 = n1.result();
-            ws[o] = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
+            wsp[P.pm[o]] = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
         }
     }
 }
 
 // Pose pass: a warp per observation chunk, part[6 ch + a] = sum over the
-// chunk of (J_p^T ws_o)_a: lanes strided, then a double-float butterfly
-// (df_add is commutative bit for bit, so every lane ends with the same value).
-__device__ void op_pose_chunks(const DevProblem& P, const ObsJac* __restrict__ jac, const float4* ws, df* part) {
+// chunk of (J_p^T ws_o)_a, read pose-major (contiguous): lanes strided, then
+// a double-float butterfly (df_add is commutative bit for bit, so every lane
+// ends with the same value).
+__device__ void op_pose_chunks(const DevProblem& P, const float4* __restrict__ jp_pm, const float4* wsp, df* part) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t ch = spread_warp(); ch < P.nopch; ch += nw) {
         const int q1 = P.opch_q[ch + 1];
         df_dot acc[6];
         for (int q = P.opch_q[ch] + lane; q < q1; q += 32) {
-            const int o = P.pose_obs[q];
-            const float4* r = reinterpret_cast<const float4*>(jac + o);
-            const float4 a = __ldg(r + 1), b = __ldg(r + 2), d = __ldg(r + 3);
-            const float4 sv = __ldcg(ws + o);
+            const float4 a = __ldg(jp_pm + 3LL * q), b = __ldg(jp_pm + 3LL * q + 1), d = __ldg(jp_pm + 3LL * q + 2);
+            const float4 sv = __ldcg(wsp + q);
             const df s0{sv.x, sv.y}, s1{sv.z, sv.w};
             const float j0[6] = {a.x, a.y, a.z, a.w, b.x, b.y}, j1[6] = {b.z, b.w, d.x, d.y, d.z, d.w};
 #pragma unroll
@@ -466,6 +509,7 @@ __device__ double grid_sum(cg::grid_group& grid, double v, double* slot, double*
 constexpr int kPcgMaxBlocks = 2048;
 
 __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac* __restrict__ jac,
+                                                  const float4* __restrict__ jp_pm,
                                                   const double* __restrict__ hinv, const float* __restrict__ X,
                                                   const float* __restrict__ XT, double* delta, double* bs, double* buf,
                                                   int max_it, double tol, LmState* st) {
@@ -483,8 +527,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     df* xdf = pdf + n;
     df* part = xdf + n;                       // [6 nopch] chunk partials
     df* hdf = part + 6 * P.nopch;             // [9 L] double-float (H_ll + lambda I)^-1
-    double* slots = reinterpret_cast<double*>(hdf + 9LL * P.L + ((9LL * P.L) & 1));  // [2 kPcgMaxBlocks]
-    float4* ws = reinterpret_cast<float4*>(slots + 2 * kPcgMaxBlocks);  // [M]
+    df* yst = hdf + 9LL * P.L;                // [3 L] double-float y of the landmark pass
+    double* slots = reinterpret_cast<double*>(yst + 3LL * P.L);       // [2 kPcgMaxBlocks]
+    float4* ws = reinterpret_cast<float4*>(slots + 2 * kPcgMaxBlocks);  // [M] landmark-major
+    float4* wsp = ws + P.M;                                             // [M] pose-major
     // grid sums alternate between two slot buffers: consecutive sums never
     // share one, and a barrier separates every reuse
     int red = 0;
@@ -493,9 +539,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     for (int64_t i = tid; i < 9LL * P.L; i += nth) hdf[i] = df_from_double(hinv[i]);
     grid.sync();
     // r = b_s = b_p - H_pl (H_ll + lambda I)^-1 b_l, x = 0
-    op_landmarks(P, jac, hdf, nullptr, true, ws, nullptr);
+    op_landmarks(P, jac, hdf, nullptr, true, ws, wsp, yst, nullptr);
     grid.sync();
-    op_pose_chunks(P, jac, ws, part);
+    op_pose_chunks(P, jp_pm, wsp, part);
     grid.sync();
     double acc = 0.0;
     for (int i = tid; i < n; i += nth) {
@@ -526,9 +572,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
         double rz = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
         for (;;) {
             // q = S p
-            op_landmarks(P, jac, hdf, pdf, false, ws, nullptr);
+            op_landmarks(P, jac, hdf, pdf, false, ws, wsp, yst, nullptr);
             grid.sync();
-            op_pose_chunks(P, jac, ws, part);
+            op_pose_chunks(P, jp_pm, wsp, part);
             grid.sync();
             acc = 0.0;
             for (int i = tid; i < n; i += nth) {
@@ -578,7 +624,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     }
     // landmark back-substitution delta_l = (H_ll + lambda I)^-1 (b_l - H_lp delta_p)
     // (xdf was written before the last grid barrier)
-    op_landmarks(P, jac, hdf, xdf, true, nullptr, delta + n);
+    op_landmarks(P, jac, hdf, xdf, true, nullptr, nullptr, yst, delta + n);
     if (tid == 0) {
         st->resid_norm = sqrt(rn2);
         st->rhs_norm = sqrt(bn2);
@@ -588,9 +634,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
 
 size_t pcg_doubles(const DevProblem& P) {
     // r z p q u, the two double-float copies, chunk partials, the double-float
-    // landmark inverses, slots, ws (16 B each); 8-byte units, ws 16-byte aligned
-    return 7 * (size_t)P.n + 6 * (size_t)P.nopch + 9 * (size_t)P.L + ((9 * (size_t)P.L) & 1) +
-           2 * (size_t)kPcgMaxBlocks + 2 * (size_t)P.M;
+    // landmark inverses and y, slots, ws (16 B each); in 8-byte units (the
+    // sum before ws is even, so ws is 16-byte aligned)
+    return 7 * (size_t)P.n + 6 * (size_t)P.nopch + 12 * (size_t)P.L + 2 * (size_t)kPcgMaxBlocks + 4 * (size_t)P.M;
 }
 
 cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s) {
@@ -601,14 +647,15 @@ cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it,
     const int blocks = std::max(1, std::min(kPcgMaxBlocks, occ * sm_count()));
     DevProblem Pv = P;
     const ObsJac* jac = W.jac;
+    const float4* jp_pm = W.jp_pm;
     const double* hinv = W.hll_inv;
     const float* X = (const float*)W.X;
     const float* XT = (const float*)W.XT;
     double* delta = W.delta;
     double* bs = W.bs;
     double* buf = W.pcg;
-    void* args[] = {(void*)&Pv,    (void*)&jac, (void*)&hinv,   (void*)&X,   (void*)&XT, (void*)&delta,
-                    (void*)&bs,    (void*)&buf, (void*)&max_it, (void*)&tol, (void*)&st};
+    void* args[] = {(void*)&Pv,  (void*)&jac, (void*)&jp_pm,  (void*)&hinv, (void*)&X,  (void*)&XT,
+                    (void*)&delta, (void*)&bs, (void*)&buf, (void*)&max_it, (void*)&tol, (void*)&st};
     e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(blocks), dim3(kThreads), args, 0, s);
     if (e == cudaSuccess) note_launch();
     return e;

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kThreads) k_pose_aux(DevProblem P, double* aux
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
                                                         T* __restrict__ pose_part, const double* __restrict__ aux,
-                                                        ObsJac* __restrict__ jac) {
+                                                        ObsJac* __restrict__ jac, float4* __restrict__ jp_pm) {
     constexpr int RS = RecStride<T>::value;
     // threads in pose-major order: the large records (H_pl, pose partials)
     // are written coalesced and neighbouring threads share the pose's data
@@ -267,6 +267,9 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         d[1] = make_float4(jp[0], jp[1], jp[2], jp[3]);
         d[2] = make_float4(jp[4], jp[5], jp[6], jp[7]);
         d[3] = make_float4(jp[8], jp[9], jp[10], jp[11]);
+        jp_pm[3 * q] = d[1];  // pose-major copy for the operator's pose pass
+        jp_pm[3 * q + 1] = d[2];
+        jp_pm[3 * q + 2] = d[3];
         d[4] = make_float4(jl[0], jl[1], jl[2], jl[3]);
         d[5] = make_float4(jl[4], jl[5], (float)W00, (float)W01);
         d[6] = make_float4((float)W10, (float)W11, 0.f, 0.f);
@@ -875,7 +878,7 @@ void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
     }
     if (P.M > 0) {
         k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part, W.pose_aux,
-                                                          W.jac); note_launch();
+                                                          W.jac, W.jp_pm); note_launch();
         if (P.has_dups) { k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch(); }
     }
     if (P.L > 0) {
