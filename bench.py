@@ -172,15 +172,27 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
     pipe = peaks["fp64_tflops"] if precision == 0 else peaks["fp32_tflops"]
     pipe_name = "fp64" if precision == 0 else "fp32"
     rs = 20 if precision else 18  # H_pl / W record length (floats padded to 80 bytes)
+    # mixed form: the reduced solve is X = L^-1 (reads F, writes X and X^T) and
+    # conjugate gradients on the matrix-free Schur operator: 1 application for
+    # b_s, one per iteration, half of one for the landmark back-substitution;
+    # 224 bytes per observation each (the 112-byte Jacobian record, J_p v
+    # stashed and read back, the weighted residual scattered pose-major, the
+    # pose-major J_p and that residual read back), plus X and X^T per iteration
+    cg_it = prof.get("refine_sweeps", 0) / max(1, prof.get("attempts", 1))
+    trisolve_bytes = (n * n * s * 2 if precision == 0 else
+                      10.0 * n * n + (1.5 + cg_it) * 224.0 * M + cg_it * 4.0 * n * n + 144.0 * L)
     work = {
         # bytes: read observation + write H_pl, and H_ll / H_pp / b once
-        "linearize": ("hbm", M * (24 + 18 * s) + L * 12 * s + K * 42 * s, None),
+        # (mixed form: also the 112-byte Jacobian record and the 48-byte
+        # pose-major J_p per observation)
+        "linearize": ("hbm", M * (24 + 18 * s + (160 if precision else 0)) + L * 12 * s + K * 42 * s, None),
         "invert": ("hbm", L * (9 * 8 * 2) + M * 18 * s * 2, None),
-        # bytes: the W and H_pl records once, the triple list, the chunk partials
-        # (memory-bound: L1/L2 latency of the record gathers, see profiles/)
-        "schur": ("hbm", M * 2 * rs * s + T * 8 + (T / 32.0) * 36 * s, T * 216.0 + M * 36.0),
+        # bytes: the W and H_pl records once and the triple list (the FP64
+        # segment sums, one 288-byte record per pose pair and 512 triples, are
+        # left out); memory-bound on the L1/L2 latency of the record gathers
+        "schur": ("hbm", M * 2 * rs * s + T * 8, T * 216.0 + M * 36.0),
         "factor": (pipe_name, None, n ** 3 / 3.0),
-        "trisolve": ("hbm", n * n * s * 2, None),
+        "trisolve": ("hbm", trisolve_bytes, None),
         "update": ("hbm", M * 18 * s + L * 48 + K * 112, None),
         "cost": ("hbm", M * 24 + L * 32 + K * 64, None),
     }

@@ -528,20 +528,26 @@ __device__ __forceinline__ void load_rec(const double* p, double v[20]) {
 // Partial 6 x 6 sums W_i H_j^T over one segment (<= 512 consecutive triples
 // of one pose pair), a warp per segment: lane t takes the segment's triples
 // t, t + 32, ... (consecutive lanes read consecutive pose-major records,
-// coalesced) and accumulates in T (at most 16 triples per lane); the 32
-// lane partials meet in FP64 (a transpose through shared memory, then a
-// column sum in lane order) and the segment sum is kept in FP64: the
-// diagonal blocks S_ii = H_pp - sum W H^T cancel strongly, so no sum of many
-// terms is rounded to FP32. With windows, segments of stopped windows (ctl)
-// are skipped.
-constexpr int kSegThreads = 128;  // 4 warps: the transpose buffers stay under 48 KB
+// coalesced) and accumulates in T (at most 16 triples per lane); the 32 lane
+// partials meet in a fixed tree (FP32: an xor-shuffle butterfly, identical in
+// every lane; FP64: a transpose through shared memory and a column sum in
+// lane order) and the segment sum is stored in FP64. (The mixed form's S is
+// the preconditioner of its conjugate-gradient solve, launch_pcg, so FP32
+// sums suffice there.) With windows, segments of stopped windows (ctl) are
+// skipped.
+template <typename T>
+constexpr int schur_seg_threads() {
+    return sizeof(T) == 8 ? 128 : 256;  // FP64: 4 warps keep the transpose buffer under 48 KB
+}
 
 template <typename T>
-__global__ void __launch_bounds__(kSegThreads) k_schur_segments(DevProblem P, const T* __restrict__ W,
-                                                                const T* __restrict__ hpl, double* __restrict__ part,
-                                                                const WinCtl* __restrict__ ctl) {
+__global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevProblem P, const T* __restrict__ W,
+                                                                          const T* __restrict__ hpl,
+                                                                          double* __restrict__ part,
+                                                                          const WinCtl* __restrict__ ctl) {
     constexpr int RS = RecStride<T>::value;
-    __shared__ double red[kSegThreads / 32][32][37];
+    constexpr int NW = schur_seg_threads<T>() / 32;
+    __shared__ double red[sizeof(T) == 8 ? NW : 1][32][37];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (g >= P.nsegs) return;
@@ -561,18 +567,28 @@ __global__ void __launch_bounds__(kSegThreads) k_schur_segments(DevProblem P, co
             for (int d = 0; d < 6; ++d)
                 acc[a * 6 + d] += wv[a * 3] * hv[d * 3] + wv[a * 3 + 1] * hv[d * 3 + 1] + wv[a * 3 + 2] * hv[d * 3 + 2];
     }
-    double (*r)[37] = red[wib];
-#pragma unroll
-    for (int e = 0; e < 36; ++e) r[lane][e] = (double)acc[e];
-    __syncwarp();
     double* out = part + g * 36;
-    double v0 = 0.0;
-    for (int k = 0; k < 32; ++k) v0 += r[k][lane];
-    out[lane] = v0;
-    if (lane < 4) {
-        double v1 = 0.0;
-        for (int k = 0; k < 32; ++k) v1 += r[k][32 + lane];
-        out[32 + lane] = v1;
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int e = 0; e < 36; ++e) {
+            T v = acc[e];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (e == lane || e == 32 + lane) out[e] = (double)v;
+        }
+    } else {
+        double (*r)[37] = red[wib];
+#pragma unroll
+        for (int e = 0; e < 36; ++e) r[lane][e] = (double)acc[e];
+        __syncwarp();
+        double v0 = 0.0;
+        for (int k = 0; k < 32; ++k) v0 += r[k][lane];
+        out[lane] = v0;
+        if (lane < 4) {
+            double v1 = 0.0;
+            for (int k = 0; k < 32; ++k) v1 += r[k][32 + lane];
+            out[32 + lane] = v1;
+        }
     }
 }
 
@@ -901,8 +917,9 @@ void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStr
 template <typename T>
 void launch_schur_pairs(const DevProblem& P, DevWork& W, const WinCtl* ctl, cudaStream_t s) {
     if (P.npairs > 0) {
-        const int64_t blocks = (P.nsegs * 32 + kSegThreads - 1) / kSegThreads;
-        k_schur_segments<T><<<(int)blocks, kSegThreads, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
+        constexpr int nt = schur_seg_threads<T>();
+        const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
+        k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
         note_launch();
         k_schur_assemble<<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, W.partial, W.S, ctl);
         note_launch();
