@@ -307,11 +307,10 @@ __device__ __forceinline__ df ld_df(const df* p) {
 // inclusive scan over the lanes (segments: runs of one landmark; a
 // Hillis-Steele scan in double-float) plus the running sum carried over from
 // the previous 32; the lane holding a landmark's last observation forms y_l
-// and stores it (yst). ws_o goes to wsp at the observation's pose-major
-// position. v (double-float) null: v = 0. y (optional) receives y_l in FP64;
-// with ws null only y is computed.
+// and stores it (yst, read again by the caller). ws_o goes to wsp at the
+// observation's pose-major position. v (double-float) null: v = 0.
 __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac, const df* hinv, const df* v, bool c,
-                             float4* ws, float4* wsp, df* yst, double* y) {
+                             float4* ws, float4* wsp, df* yst) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t ch = spread_warp(); ch < P.nlmch; ch += nw) {
@@ -360,7 +359,7 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
                 k[0] = k0.result();
                 k[1] = k1.result();
                 k[2] = k2.result();
-                if (ws) ws[o] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+                ws[o] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
             }
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
@@ -388,7 +387,6 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
 #pragma unroll
                     for (int b = 0; b < 3; ++b) acc = df_add(acc, df_mul(ld_df(hi + 3 * a + b), k[b]));
                     yst[3LL * l + a] = acc;
-                    if (y) y[3LL * l + a] = df_to_double(acc);
                 }
             }
             carry_l = __shfl_sync(0xffffffffu, l, 31);
@@ -401,13 +399,9 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
         for (int l = l0 + lane; l < l1; l += 32) {  // landmarks without observations: y = 0
             if (P.lm_ptr[l] == P.lm_ptr[l + 1]) {
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    yst[3LL * l + a] = df_zero();
-                    if (y) y[3LL * l + a] = 0.0;
-                }
+                for (int a = 0; a < 3; ++a) yst[3LL * l + a] = df_zero();
             }
         }
-        if (!ws) continue;
         __syncwarp();  // yst of this chunk written by the warp's lanes
         for (int o = O0 + lane; o < O1; o += 32) {
             const int l = P.obs_lm[o];
@@ -523,9 +517,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     double* p = z + n;
     double* q = p + n;
     double* u = q + n;
-    df* pdf = reinterpret_cast<df*>(u + n);  // double-float copies of p and of x
-    df* xdf = pdf + n;
-    df* part = xdf + n;                       // [6 nopch] chunk partials
+    df* pdf = reinterpret_cast<df*>(u + n);  // double-float copy of p
+    df* part = pdf + 2 * n;                   // [6 nopch] chunk partials (n df unused before them)
     df* hdf = part + 6 * P.nopch;             // [9 L] double-float (H_ll + lambda I)^-1
     df* yst = hdf + 9LL * P.L;                // [3 L] double-float y of the landmark pass
     double* slots = reinterpret_cast<double*>(yst + 3LL * P.L);       // [2 kPcgMaxBlocks]
@@ -539,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     for (int64_t i = tid; i < 9LL * P.L; i += nth) hdf[i] = df_from_double(hinv[i]);
     grid.sync();
     // r = b_s = b_p - H_pl (H_ll + lambda I)^-1 b_l, x = 0
-    op_landmarks(P, jac, hdf, nullptr, true, ws, wsp, yst, nullptr);
+    op_landmarks(P, jac, hdf, nullptr, true, ws, wsp, yst);
     grid.sync();
     op_pose_chunks(P, jp_pm, wsp, part);
     grid.sync();
@@ -549,9 +542,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
         r[i] = v;
         bs[i] = v;
         delta[i] = 0.0;
-        xdf[i] = df_zero();
         acc += v * v;
     }
+    // landmark back-substitution delta_l = y(x) = (H_ll + lambda I)^-1 (b_l - H_lp x)
+    // is linear in x: y(0) now, plus alpha y_0(p) with each step (y_0(p), the
+    // landmark pass of S p, is left in yst by op_landmarks)
+    for (int64_t i = tid; i < 3LL * P.L; i += nth) delta[n + i] = df_to_double(ld_df(yst + i));
     const double bn2 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
     double rn2 = bn2;
     int it = 0;
@@ -572,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
         double rz = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
         for (;;) {
             // q = S p
-            op_landmarks(P, jac, hdf, pdf, false, ws, wsp, yst, nullptr);
+            op_landmarks(P, jac, hdf, pdf, false, ws, wsp, yst);
             grid.sync();
             op_pose_chunks(P, jp_pm, wsp, part);
             grid.sync();
@@ -591,13 +587,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
             const double alpha = rz / pq;
             acc = 0.0;
             for (int i = tid; i < n; i += nth) {
-                const double xi = __ldcg(delta + i) + alpha * __ldcg(p + i);
-                delta[i] = xi;
-                xdf[i] = df_from_double(xi);
+                delta[i] = __ldcg(delta + i) + alpha * __ldcg(p + i);
                 const double ri = __ldcg(r + i) - alpha * __ldcg(q + i);
                 r[i] = ri;
                 acc += ri * ri;
             }
+            for (int64_t i = tid; i < 3LL * P.L; i += nth)
+                delta[n + i] = __ldcg(delta + n + i) + alpha * df_to_double(ld_df(yst + i));
             rn2 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
             ++it;
             if (!(rn2 > tol * tol * bn2) || it >= max_it) break;
@@ -622,9 +618,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
         if (tid == 0) st->solve_ok = 0;
         return;
     }
-    // landmark back-substitution delta_l = (H_ll + lambda I)^-1 (b_l - H_lp delta_p)
-    // (xdf was written before the last grid barrier)
-    op_landmarks(P, jac, hdf, xdf, true, nullptr, nullptr, yst, delta + n);
     if (tid == 0) {
         st->resid_norm = sqrt(rn2);
         st->rhs_norm = sqrt(bn2);
