@@ -212,14 +212,17 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
         achieved = flops / (per_call_ms * 1e-3) / 1e12
         peak, unit, fallback = pipe, "TFLOP/s", f"zs_pipe_peaks {pipe_name} FMA chain, measured in this run"
     return {"phase": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak if peak else None, "traffic": phase_traffic(sc, precision, top),
+            "frac": achieved / peak if peak else None, "traffic": phase_traffic(sc, precision, top, cg_it),
             "peak_source": fallback, "ms_per_call": per_call_ms, "calls": calls[top],
             "phase_share": ms[top] / max(1e-9, sum(ms.values())), **extra}
 
 
-def phase_traffic(sc, precision: int, phase: str):
+def phase_traffic(sc, precision: int, phase: str, cg_it: float = 0.0):
     """DRAM bytes per launch of the phase's main kernel from the committed ncu
-    capture (profiles/traffic_walk_1M_mixed.json), for the scene it was taken on."""
+    capture (profiles/traffic_walk_1M_mixed.json), for the scene it was taken on.
+    The reduced solve (trisolve) is X = L^-1 plus the conjugate-gradient launch,
+    whose captured launch made 3 operator applications; its bytes are scaled to
+    the average attempt's 1 + cg_it applications."""
     path = os.path.join(ROOT, "profiles", "traffic_walk_1M_mixed.json")
     if precision != 1 or sc.M != 1019227 or not os.path.exists(path):
         return None
@@ -229,8 +232,15 @@ def phase_traffic(sc, precision: int, phase: str):
     if not k:
         return None
     e = t["kernels"][k]
-    return {"bytes_per_launch": e["dram_read"] + e["dram_write"], "kernel": k,
-            "source": "profiles/traffic_walk_1M_mixed.json (one ncu capture)"}
+    nbytes = e["dram_read"] + e["dram_write"]
+    out = {"kernel": k, "source": "profiles/traffic_walk_1M_mixed.json (one ncu capture)"}
+    if phase == "trisolve":
+        x = t["kernels"]["k_tri_inverse64"]
+        nbytes = nbytes * (1.0 + cg_it) / 3.0 + x["dram_read"] + x["dram_write"]
+        out["kernel"] = "k_tri_inverse64 + k_pcg"
+        out["scaled"] = f"k_pcg bytes x (1 + {cg_it:.2f}) / 3 operator applications"
+    out["bytes_per_launch"] = nbytes
+    return out
 
 
 def run_solves(sc, precision: int, steps: int, warmup: int, iters: int, device: int, dist: Dist):
