@@ -124,6 +124,9 @@ typedef struct zs_ba_report {
     double ms_phase[8];
     int32_t phase_calls[8];
     int64_t kernel_launches;   /* kernels this library launched during the solve */
+    int32_t preconditioner_retries; /* mixed form: attempts whose FP32 factorisation of the FP32-formed S
+                                       failed and was retried on S + 1e-5 diag(S) (the factor only
+                                       preconditions the conjugate-gradient solve) */
 } zs_ba_report;
 
 /* Phases of zs_ba_report.ms_phase. */

@@ -53,7 +53,8 @@ class Report(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("accepted", C.c_int32), ("attempts", C.c_int32),
                 ("cholesky_failures", C.c_int32), ("refine_sweeps", C.c_int32), ("chi2_initial", C.c_double),
                 ("chi2_final", C.c_double), ("lambda_final", C.c_double), ("ms_total", C.c_double),
-                ("ms_phase", C.c_double * 8), ("phase_calls", C.c_int32 * 8), ("kernel_launches", C.c_int64)]
+                ("ms_phase", C.c_double * 8), ("phase_calls", C.c_int32 * 8), ("kernel_launches", C.c_int64),
+                ("preconditioner_retries", C.c_int32)]
 
     PHASES = ("linearize", "invert", "schur", "factor", "trisolve", "update", "cost", "other")
 

@@ -881,6 +881,7 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
             lambda = hs.lambda;
             if (!hs.solve_ok) {
                 r.cholesky_failures++;
+                if (sizeof(T) == 4) r.preconditioner_retries += hs.shifted;
                 if (o.verbose) std::fprintf(stderr, "Cholesky solver failed!\n");
                 ++failures;
                 if (!std::isfinite(lambda)) break;
@@ -888,6 +889,7 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
             }
             if (sizeof(T) == 4) {
                 r.refine_sweeps += hs.refine_sweeps;
+                r.preconditioner_retries += hs.shifted;
                 if (o.verbose > 1)
                     std::fprintf(stderr, "  refinement: %d sweeps, |b - S x| / |b| = %.3e%s\n", hs.refine_sweeps,
                                  hs.rhs_norm > 0.0 ? hs.resid_norm / hs.rhs_norm : 0.0,
