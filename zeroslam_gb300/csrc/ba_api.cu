@@ -655,6 +655,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     if (h->tsize == 4) {
         W.jac = dalloc<ObsJac>((size_t)M, own);
         W.jp_pm = dalloc<float4>(3 * (size_t)M, own);
+        W.hll_inv_f = dalloc<float>(12 * (size_t)std::max(L, 1), own);
     }
     else W.lm_part = dalloc<char>(ts * 12 * M, own);  // record-major, 9 values padded to 12
     W.pose_part = dalloc<char>(ts * 28 * M, own);  // record-major, 27 values padded to 28

@@ -69,42 +69,14 @@ __device__ inline double cta_max(double v, double* sh) {
 
 // matrix::invert<3> on H_ll + lambda_w I, as k_invert (source/matrix.hpp:749-774).
 __global__ void __launch_bounds__(kThreads) k_binvert(DevProblem P, const double* __restrict__ hll, double* hinv,
-                                                      const LmState* __restrict__ st, const WinCtl* __restrict__ ctl) {
+                                                      float* hinv_f, const LmState* __restrict__ st,
+                                                      const WinCtl* __restrict__ ctl) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= P.L) return;
     const int w = P.lm_win[l];
     if (!ctl[w].active) return;
-    double* o = hinv + (int64_t)l * 9;
-    if (P.lm_fixed[l]) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) o[i] = 0.0;
-        return;
-    }
-    const double lam = st[w].lambda;
-    double a[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) a[i] = hll[(int64_t)l * 9 + i];
-    a[0] += lam; a[4] += lam; a[8] += lam;
-    const double det = +a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
-                       a[2] * (a[3] * a[7] - a[4] * a[6]);
-    double scale = 0.0;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
-    if (!(fabs(det) > scale * scale * scale * 1e-12)) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) o[i] = 0.0;
-        return;
-    }
-    const double id = 1.0 / det;
-    o[0] = (a[4] * a[8] - a[7] * a[5]) * id;
-    o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
-    o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
-    o[3] = (a[5] * a[6] - a[3] * a[8]) * id;
-    o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
-    o[5] = (a[3] * a[2] - a[0] * a[5]) * id;
-    o[6] = (a[3] * a[7] - a[6] * a[4]) * id;
-    o[7] = (a[6] * a[1] - a[0] * a[7]) * id;
-    o[8] = (a[0] * a[4] - a[3] * a[1]) * id;
+    landmark_inverse(hll + (int64_t)l * 9, st[w].lambda, P.lm_fixed[l] != 0, hinv + (int64_t)l * 9,
+                     hinv_f ? hinv_f + (int64_t)l * 12 : nullptr);
 }
 
 // S_w = blockdiag(H_pp) + lambda_w I; blockIdx.y = window.
@@ -674,7 +646,11 @@ template <typename T>
 cudaError_t launch_batch_round(const DevProblem& P, DevWork& W, BatchDev& B, const BatchParams& prm,
                                cudaStream_t s) {
     launch_linearize<T>(P, W, s);
-    if (P.L > 0) { k_binvert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, B.st, B.ctl); note_launch(); }
+    if (P.L > 0) {
+        k_binvert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, sizeof(T) == 4 ? W.hll_inv_f : nullptr,
+                                                     B.st, B.ctl);
+        note_launch();
+    }
     launch_w<T>(P, W, s);
     {
         const dim3 g(grid_for(36LL * kBatchMaxK * kBatchMaxK), P.nwin);

@@ -225,6 +225,47 @@ constexpr int kPoseAux = 24;
 __device__ inline double cost_fast(const double* __restrict__ a, const double* __restrict__ X, double u_obs,
                                    double v_obs, const Intrinsics& in, const double* om, const LossParams& loss);
 
+// matrix::invert<3> of H_ll + lambda I for one landmark
+// (source/matrix.hpp:749-774): fixed landmarks and singular blocks
+// (|det| <= 1e-12 max|a|^3) get a zero inverse, as solve_linear_system
+// ignores the failed inversion (source/factor_graph.hpp:763). of (optional,
+// mixed form) also receives the inverse in FP32, padded to 12 floats.
+__device__ inline void landmark_inverse(const double* __restrict__ hll_l, double lam, bool fixed, double* o,
+                                        float* of) {
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (!fixed) {
+        double a[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) a[i] = hll_l[i];
+        a[0] += lam; a[4] += lam; a[8] += lam;
+        const double det = +a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                           a[2] * (a[3] * a[7] - a[4] * a[6]);
+        double scale = 0.0;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
+        if (fabs(det) > scale * scale * scale * 1e-12) {
+            const double id = 1.0 / det;
+            v[0] = (a[4] * a[8] - a[7] * a[5]) * id;
+            v[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+            v[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+            v[3] = (a[5] * a[6] - a[3] * a[8]) * id;
+            v[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+            v[5] = (a[3] * a[2] - a[0] * a[5]) * id;
+            v[6] = (a[3] * a[7] - a[6] * a[4]) * id;
+            v[7] = (a[6] * a[1] - a[0] * a[7]) * id;
+            v[8] = (a[0] * a[4] - a[3] * a[1]) * id;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) o[i] = v[i];
+    if (of) {
+        float4* f = reinterpret_cast<float4*>(of);
+        f[0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+        f[1] = make_float4((float)v[4], (float)v[5], (float)v[6], (float)v[7]);
+        f[2] = make_float4((float)v[8], 0.f, 0.f, 0.f);
+    }
+}
+
 // Deterministic block sum of one value per thread (fixed tree over
 // blockDim.x = kThreads threads). Result valid in thread 0.
 template <typename V>

@@ -108,6 +108,7 @@ struct DevWork {
     double* hpp = nullptr;     // [K*36]
     double* hll = nullptr;     // [L*9]
     double* hll_inv = nullptr; // [L*9]
+    float* hll_inv_f = nullptr; // mixed form: [L*12] the same in FP32, padded for 16-byte loads
     double* b = nullptr;       // [n + 3L] gradient vector (poses then landmarks)
     double* S = nullptr;       // [n*n] reduced camera matrix, FP64 in both forms
     void* F = nullptr;         // [n*n] Cholesky factor (lower): double (plain form) or float (mixed)

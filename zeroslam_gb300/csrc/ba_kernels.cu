@@ -340,68 +340,107 @@ __global__ void __launch_bounds__(kThreads) k_reduce_lm(DevProblem P, const T* _
 }
 
 // Mixed form: H_ll = sum J_l^T W J_l and b_l = -sum J_l^T g per landmark from
-// the FP32 Jacobian records, observations in order, in double-float (the
-// products of FP32 values are exact, the sums carry ~48 bits): H_ll must be
-// accurate far beyond FP32 for the Schur operator of launch_pcg.
+// the FP32 Jacobian records in double-float (the products of FP32 values are
+// exact, the sums carry ~48 bits): H_ll must be accurate far beyond FP32 for
+// the Schur operator of launch_pcg. A warp per landmark chunk (P.lmch_l), 32
+// consecutive observations at a time: each lane forms its observation's 9
+// terms, a segmented inclusive scan over the lanes (runs of one landmark) plus
+// the sum carried from the previous 32 gives each landmark's total in the
+// lane holding its last observation, which writes H_ll and b_l.
 __global__ void __launch_bounds__(kThreads) k_reduce_lm_jac(DevProblem P, const ObsJac* __restrict__ jac, double* hll,
                                                             double* b) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= P.L) return;
-    df h[6], bl[3];
+    const int lane = threadIdx.x & 31;
+    const int64_t ch = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (ch >= P.nlmch) return;
+    const int l0 = P.lmch_l[ch], l1 = P.lmch_l[ch + 1];
+    const int O0 = P.lm_ptr[l0], O1 = P.lm_ptr[l1];
+    df carry[9];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) h[k] = df_zero();
+    for (int k = 0; k < 9; ++k) carry[k] = df_zero();
+    int carry_l = -1;
+    for (int base = O0; base < O1; base += 32) {
+        const int o = base + lane;
+        const bool valid = o < O1;
+        const int l = valid ? P.obs_lm[o] : -1 - lane;
+        df v[9];  // H_ll upper triangle (00 01 02 11 12 22), then b_l
 #pragma unroll
-    for (int k = 0; k < 3; ++k) bl[k] = df_zero();
-    const int e = P.lm_ptr[l + 1];
-    for (int o = P.lm_ptr[l]; o < e; ++o) {
-        const float4* r = reinterpret_cast<const float4*>(jac + o);
-        const float4 G = __ldg(r), a = __ldg(r + 4), c = __ldg(r + 5), d = __ldg(r + 6);
-        const float J0[3] = {a.x, a.y, a.z}, J1[3] = {a.w, c.x, c.y};
-        const df g0{G.x, G.y}, g1{G.z, G.w};
-        // B = J^T W (3 x 2): B0 = column 0, B1 = column 1
-        df B0[3], B1[3];
+        for (int k = 0; k < 9; ++k) v[k] = df_zero();
+        if (valid) {
+            const float4* r = reinterpret_cast<const float4*>(jac + o);
+            const float4 G = __ldg(r), a = __ldg(r + 4), c = __ldg(r + 5), d = __ldg(r + 6);
+            const float J0[3] = {a.x, a.y, a.z}, J1[3] = {a.w, c.x, c.y};
+            const df g0{G.x, G.y}, g1{G.z, G.w};
+            // B = J^T W (3 x 2): B0 = column 0, B1 = column 1
+            df B0[3], B1[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            df_dot s0, s1;
-            s0.add(J0[k], df{c.z, 0.f});
-            s0.add(J1[k], df{d.x, 0.f});
-            s1.add(J0[k], df{c.w, 0.f});
-            s1.add(J1[k], df{d.y, 0.f});
-            B0[k] = s0.result();
-            B1[k] = s1.result();
+            for (int k = 0; k < 3; ++k) {
+                df_dot s0, s1;
+                s0.add(J0[k], df{c.z, 0.f});
+                s0.add(J1[k], df{d.x, 0.f});
+                s1.add(J0[k], df{c.w, 0.f});
+                s1.add(J1[k], df{d.y, 0.f});
+                B0[k] = s0.result();
+                B1[k] = s1.result();
+            }
+            // H(a, c) = B0[a] J0[c] + B1[a] J1[c], upper triangle row by row
+            auto entry = [&](int ia, int ic) {
+                df_dot s;
+                s.add(J0[ic], B0[ia]);
+                s.add(J1[ic], B1[ia]);
+                return s.result();
+            };
+            v[0] = entry(0, 0);
+            v[1] = entry(0, 1);
+            v[2] = entry(0, 2);
+            v[3] = entry(1, 1);
+            v[4] = entry(1, 2);
+            v[5] = entry(2, 2);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                df_dot s;
+                s.add(-J0[k], g0);
+                s.add(-J1[k], g1);
+                v[6 + k] = s.result();
+            }
         }
-        // H(a, c) = B0[a] J0[c] + B1[a] J1[c], upper triangle row by row
-        auto entry = [&](df hk, int a, int cc) {
-            df_dot s;
-            s.add(J0[cc], B0[a]);
-            s.add(J1[cc], B1[a]);
-            s.add_df(hk);
-            return s.result();
-        };
-        h[0] = entry(h[0], 0, 0);
-        h[1] = entry(h[1], 0, 1);
-        h[2] = entry(h[2], 0, 2);
-        h[3] = entry(h[3], 1, 1);
-        h[4] = entry(h[4], 1, 2);
-        h[5] = entry(h[5], 2, 2);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            df_dot s;
-            s.add(-J0[k], g0);
-            s.add(-J1[k], g1);
-            s.add_df(bl[k]);
-            bl[k] = s.result();
+        for (int off = 1; off < 32; off <<= 1) {
+            const int lo = __shfl_up_sync(0xffffffffu, l, off);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const df u{__shfl_up_sync(0xffffffffu, v[k].hi, off), __shfl_up_sync(0xffffffffu, v[k].lo, off)};
+                if (lane >= off && lo == l) v[k] = df_add(u, v[k]);
+            }
+        }
+        if (l == carry_l) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) v[k] = df_add(carry[k], v[k]);
+        }
+        if (valid && o + 1 == P.lm_ptr[l + 1]) {  // the landmark's last observation
+            double hd[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) hd[k] = df_to_double(v[k]);
+            double* o9 = hll + (int64_t)l * 9;
+            o9[0] = hd[0]; o9[1] = hd[1]; o9[2] = hd[2];
+            o9[3] = hd[1]; o9[4] = hd[3]; o9[5] = hd[4];
+            o9[6] = hd[2]; o9[7] = hd[4]; o9[8] = hd[5];
+            double* bo = b + P.n + 3LL * l;
+            bo[0] = df_to_double(v[6]); bo[1] = df_to_double(v[7]); bo[2] = df_to_double(v[8]);
+        }
+        carry_l = __shfl_sync(0xffffffffu, l, 31);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            carry[k].hi = __shfl_sync(0xffffffffu, v[k].hi, 31);
+            carry[k].lo = __shfl_sync(0xffffffffu, v[k].lo, 31);
         }
     }
-    double hd[6];
+    for (int l = l0 + lane; l < l1; l += 32) {  // landmarks without observations
+        if (P.lm_ptr[l] == P.lm_ptr[l + 1]) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) hd[k] = df_to_double(h[k]);
-    double* o9 = hll + (int64_t)l * 9;
-    o9[0] = hd[0]; o9[1] = hd[1]; o9[2] = hd[2];
-    o9[3] = hd[1]; o9[4] = hd[3]; o9[5] = hd[4];
-    o9[6] = hd[2]; o9[7] = hd[4]; o9[8] = hd[5];
-    double* bo = b + P.n + 3LL * l;
-    bo[0] = df_to_double(bl[0]); bo[1] = df_to_double(bl[1]); bo[2] = df_to_double(bl[2]);
+            for (int k = 0; k < 9; ++k) hll[(int64_t)l * 9 + k] = 0.0;
+            b[P.n + 3LL * l] = 0.0; b[P.n + 3LL * l + 1] = 0.0; b[P.n + 3LL * l + 2] = 0.0;
+        }
+    }
 }
 
 // Per pose (a CTA): each thread sums its strided share of the pose's
@@ -444,66 +483,59 @@ __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T*
     }
 }
 
-// matrix::invert<3> on H_ll + lambda I (source/matrix.hpp:749-774); fixed or
-// singular blocks leave a zero inverse, as solve_linear_system ignores the
-// failed inversion (source/factor_graph.hpp:763).
+// Damped 3x3 landmark inverses (landmark_inverse).
 __global__ void __launch_bounds__(kThreads) k_invert(DevProblem P, const double* __restrict__ hll, double* hinv,
-                                                     const LmState* st) {
+                                                     float* hinv_f, const LmState* st) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= P.L) return;
-    double* o = hinv + (int64_t)l * 9;
-    if (P.lm_fixed[l]) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) o[i] = 0.0;
-        return;
-    }
-    const double lam = st->lambda;
-    double a[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) a[i] = hll[(int64_t)l * 9 + i];
-    a[0] += lam; a[4] += lam; a[8] += lam;
-    const double det = +a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
-                       a[2] * (a[3] * a[7] - a[4] * a[6]);
-    double scale = 0.0;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
-    if (!(fabs(det) > scale * scale * scale * 1e-12)) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) o[i] = 0.0;
-        return;
-    }
-    const double id = 1.0 / det;
-    o[0] = (a[4] * a[8] - a[7] * a[5]) * id;
-    o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
-    o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
-    o[3] = (a[5] * a[6] - a[3] * a[8]) * id;
-    o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
-    o[5] = (a[3] * a[2] - a[0] * a[5]) * id;
-    o[6] = (a[3] * a[7] - a[6] * a[4]) * id;
-    o[7] = (a[6] * a[1] - a[0] * a[7]) * id;
-    o[8] = (a[0] * a[4] - a[3] * a[1]) * id;
+    landmark_inverse(hll + (int64_t)l * 9, st->lambda, P.lm_fixed[l] != 0, hinv + (int64_t)l * 9,
+                     hinv_f ? hinv_f + (int64_t)l * 12 : nullptr);
 }
 
-// W = H_pl H_ll^-1 per block.
+// W = H_pl H_ll^-1 per block. Mixed form: the FP32 inverses (hinv_f, 12
+// floats per landmark) and 16-byte record loads and stores.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_w(DevProblem P, const T* __restrict__ hpl, const double* __restrict__ hinv,
-                                                T* __restrict__ W) {
+                                                const float* __restrict__ hinv_f, T* __restrict__ W) {
     constexpr int RS = RecStride<T>::value;
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // pose-major position
     if (q >= P.M) return;
     const int64_t o = P.pose_obs[q];
     if (!P.blk_valid[o]) return;
-    const double* I = hinv + (int64_t)P.obs_lm[o] * 9;
-    T iv[9];
+    if constexpr (sizeof(T) == 4) {
+        const float4* I4 = reinterpret_cast<const float4*>(hinv_f + (int64_t)P.obs_lm[o] * 12);
+        const float4 i0 = __ldg(I4), i1 = __ldg(I4 + 1), i2 = __ldg(I4 + 2);
+        const float iv[9] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w, i2.x};
+        const float4* h4 = reinterpret_cast<const float4*>(hpl + q * RS);
+        float h[20];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) iv[i] = (T)I[i];
-    const T* h = hpl + q * RS;
-    T* w = W + q * RS;
+        for (int i = 0; i < 5; ++i) {
+            const float4 t = __ldg(h4 + i);
+            h[4 * i] = t.x; h[4 * i + 1] = t.y; h[4 * i + 2] = t.z; h[4 * i + 3] = t.w;
+        }
+        float w[20];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) {
-        const T h0 = h[a * 3], h1 = h[a * 3 + 1], h2 = h[a * 3 + 2];
+        for (int a = 0; a < 6; ++a)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) w[a * 3 + c] = h0 * iv[c] + h1 * iv[3 + c] + h2 * iv[6 + c];
+            for (int c = 0; c < 3; ++c) w[a * 3 + c] = h[a * 3] * iv[c] + h[a * 3 + 1] * iv[3 + c] + h[a * 3 + 2] * iv[6 + c];
+        w[18] = 0.f;
+        w[19] = 0.f;
+        float4* w4 = reinterpret_cast<float4*>(W + q * RS);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) w4[i] = make_float4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+    } else {
+        const double* I = hinv + (int64_t)P.obs_lm[o] * 9;
+        T iv[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) iv[i] = (T)I[i];
+        const T* h = hpl + q * RS;
+        T* w = W + q * RS;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            const T h0 = h[a * 3], h1 = h[a * 3 + 1], h2 = h[a * 3 + 2];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) w[a * 3 + c] = h0 * iv[c] + h1 * iv[3 + c] + h2 * iv[6 + c];
+        }
     }
 }
 
@@ -898,7 +930,7 @@ void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
         if (P.has_dups) { k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch(); }
     }
     if (P.L > 0) {
-        if (sizeof(T) == 4) k_reduce_lm_jac<<<grid_for(P.L), kThreads, 0, s>>>(P, W.jac, W.hll, W.b);
+        if (sizeof(T) == 4) k_reduce_lm_jac<<<grid_for(32 * P.nlmch), kThreads, 0, s>>>(P, W.jac, W.hll, W.b);
         else k_reduce_lm<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.lm_part, W.hll, W.b);
         note_launch();
     }
@@ -910,8 +942,14 @@ void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
 
 template <typename T>
 void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
-    if (P.L > 0) { k_invert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, st); note_launch(); }
-    if (P.M > 0) { k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch(); }
+    if (P.L > 0) {
+        k_invert<<<grid_for(P.L), kThreads, 0, s>>>(P, W.hll, W.hll_inv, sizeof(T) == 4 ? W.hll_inv_f : nullptr, st);
+        note_launch();
+    }
+    if (P.M > 0) {
+        k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.hll_inv_f, (T*)W.W);
+        note_launch();
+    }
 }
 
 template <typename T>
@@ -942,7 +980,10 @@ void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s) {
 
 template <typename T>
 void launch_w(const DevProblem& P, DevWork& W, cudaStream_t s) {
-    if (P.M > 0) { k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, (T*)W.W); note_launch(); }
+    if (P.M > 0) {
+        k_w<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.hll_inv_f, (T*)W.W);
+        note_launch();
+    }
 }
 
 
