@@ -464,13 +464,52 @@ __device__ void op_pose_chunks(const DevProblem& P, const float4* __restrict__ j
     }
 }
 
-// sum of pose k's chunk partials of component a (i = 6 k + a), chunks in order.
-__device__ __forceinline__ double chunk_sum(const DevProblem& P, const df* part, int i) {
-    const int k = i / 6, a = i - 6 * (i / 6);
-    df s = df_zero();
-    const int c1 = P.pose_opch[k + 1];
-    for (int ch = P.pose_opch[k]; ch < c1; ++ch) s = df_add(s, ld_df(part + 6LL * ch + a));
-    return df_to_double(s);
+// Pose k's totals of the pose pass: a warp per pose (spread over the grid),
+// lanes strided over the pose's chunks, then a double-float butterfly; every
+// lane of the warp returns with tot[0..5]. Calls f(k, tot) for each pose the
+// warp owns.
+template <typename F>
+__device__ __forceinline__ void for_pose_sums(const DevProblem& P, const df* part, F f) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t k = spread_warp(); k < P.K; k += nw) {
+        const int c0 = P.pose_opch[k], c1 = P.pose_opch[k + 1];
+        df t[6] = {df_zero(), df_zero(), df_zero(), df_zero(), df_zero(), df_zero()};
+        for (int ch = c0 + lane; ch < c1; ch += 32) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a) t[a] = df_add(t[a], ld_df(part + 6LL * ch + a));
+        }
+        double tot[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            df v = t[a];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const df o{__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off)};
+                v = df_add(v, o);
+            }
+            tot[a] = df_to_double(v);
+        }
+        f((int)k, tot);
+    }
+}
+
+// out = M v for a triangular FP32 matrix (mode 0: lower, c <= i; 1: upper,
+// c >= i), a warp per row, FP32 accumulation: the conjugate-gradient
+// preconditioner needs no more (the operator it preconditions is exact).
+__device__ void gemv_f32(int n, const float* __restrict__ M, const float* v, float* out, int mode) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < n; i += nw) {
+        const int lo = (mode == 1) ? i : 0;
+        const int hi = (mode == 0) ? i + 1 : n;
+        float acc = 0.f;
+        for (int c = lo + lane; c < hi; c += 32) acc += M[(int64_t)i * n + c] * __ldcg(v + c);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if (lane == 0) out[i] = acc;
+    }
 }
 
 // Deterministic grid-wide sum of one value per thread, the same in every
@@ -513,12 +552,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     const int n = P.n;
     const double lam = __ldcg(&st->lambda);
     double* r = buf;
-    double* z = r + n;
-    double* p = z + n;
+    double* p = r + n;
     double* q = p + n;
-    double* u = q + n;
-    df* pdf = reinterpret_cast<df*>(u + n);  // double-float copy of p
-    df* part = pdf + 2 * n;                   // [6 nopch] chunk partials (n df unused before them)
+    float* rf = reinterpret_cast<float*>(q + n);  // FP32 r, X r and X^T X r of the preconditioner
+    float* uf = rf + n;
+    float* zf = uf + n;                      // (3n floats within the 2n doubles below pdf)
+    df* pdf = reinterpret_cast<df*>(q + 3 * n);  // double-float copy of p
+    df* part = pdf + n;                       // [6 nopch] chunk partials
     df* hdf = part + 6 * P.nopch;             // [9 L] double-float (H_ll + lambda I)^-1
     df* yst = hdf + 9LL * P.L;                // [3 L] double-float y of the landmark pass
     double* slots = reinterpret_cast<double*>(yst + 3LL * P.L);       // [2 kPcgMaxBlocks]
@@ -537,13 +577,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     op_pose_chunks(P, jp_pm, wsp, part);
     grid.sync();
     double acc = 0.0;
-    for (int i = tid; i < n; i += nth) {
-        const double v = -chunk_sum(P, part, i);
-        r[i] = v;
-        bs[i] = v;
-        delta[i] = 0.0;
-        acc += v * v;
-    }
+    for_pose_sums(P, part, [&](int k, const double* tot) {
+        const int lane = threadIdx.x & 31;
+        if (lane < 6) {
+            const int i = 6 * k + lane;
+            const double v = -(lane == 0 ? tot[0] : lane == 1 ? tot[1] : lane == 2 ? tot[2]
+                               : lane == 3 ? tot[3] : lane == 4 ? tot[4] : tot[5]);
+            r[i] = v;
+            bs[i] = v;
+            delta[i] = 0.0;
+            rf[i] = (float)v;
+            acc += v * v;
+        }
+    });
     // landmark back-substitution delta_l = y(x) = (H_ll + lambda I)^-1 (b_l - H_lp x)
     // is linear in x: y(0) now, plus alpha y_0(p) with each step (y_0(p), the
     // landmark pass of S p, is left in yst by op_landmarks)
@@ -554,13 +600,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     bool indefinite = false;
     if (bn2 > 0.0 && max_it > 0) {
         // z = X^T X r, p = z
-        gemv_rows<float>(n, X, r, u, 0, nullptr, nullptr);
+        gemv_f32(n, X, rf, uf, 0);
         grid.sync();
-        gemv_rows<float>(n, XT, u, z, 1, nullptr, nullptr);
+        gemv_f32(n, XT, uf, zf, 1);
         grid.sync();
         acc = 0.0;
         for (int i = tid; i < n; i += nth) {
-            const double zi = __ldcg(z + i);
+            const double zi = (double)__ldcg(zf + i);
             p[i] = zi;
             pdf[i] = df_from_double(zi);
             acc += __ldcg(r + i) * zi;
@@ -573,12 +619,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
             op_pose_chunks(P, jp_pm, wsp, part);
             grid.sync();
             acc = 0.0;
-            for (int i = tid; i < n; i += nth) {
-                const double pi = __ldcg(p + i);
-                const double qi = lam * pi + chunk_sum(P, part, i);
-                q[i] = qi;
-                acc += pi * qi;
-            }
+            for_pose_sums(P, part, [&](int k, const double* tot) {
+                const int lane = threadIdx.x & 31;
+                if (lane < 6) {
+                    const int i = 6 * k + lane;
+                    const double pi = __ldcg(p + i);
+                    const double qi = lam * pi + (lane == 0 ? tot[0] : lane == 1 ? tot[1] : lane == 2 ? tot[2]
+                                                  : lane == 3 ? tot[3] : lane == 4 ? tot[4] : tot[5]);
+                    q[i] = qi;
+                    acc += pi * qi;
+                }
+            });
             const double pq = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
             if (!(pq > 0.0)) {  // uniform: S is not positive definite, as a failed FP64 factorisation
                 indefinite = true;
@@ -590,6 +641,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
                 delta[i] = __ldcg(delta + i) + alpha * __ldcg(p + i);
                 const double ri = __ldcg(r + i) - alpha * __ldcg(q + i);
                 r[i] = ri;
+                rf[i] = (float)ri;
                 acc += ri * ri;
             }
             for (int64_t i = tid; i < 3LL * P.L; i += nth)
@@ -597,17 +649,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
             rn2 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
             ++it;
             if (!(rn2 > tol * tol * bn2) || it >= max_it) break;
-            gemv_rows<float>(n, X, r, u, 0, nullptr, nullptr);
+            gemv_f32(n, X, rf, uf, 0);
             grid.sync();
-            gemv_rows<float>(n, XT, u, z, 1, nullptr, nullptr);
+            gemv_f32(n, XT, uf, zf, 1);
             grid.sync();
             acc = 0.0;
-            for (int i = tid; i < n; i += nth) acc += __ldcg(r + i) * __ldcg(z + i);
+            for (int i = tid; i < n; i += nth) acc += __ldcg(r + i) * (double)__ldcg(zf + i);
             const double rz1 = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
             const double beta = rz1 / rz;
             rz = rz1;
             for (int i = tid; i < n; i += nth) {
-                const double pi = __ldcg(z + i) + beta * __ldcg(p + i);
+                const double pi = (double)__ldcg(zf + i) + beta * __ldcg(p + i);
                 p[i] = pi;
                 pdf[i] = df_from_double(pi);
             }
@@ -626,10 +678,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
 }
 
 size_t pcg_doubles(const DevProblem& P) {
-    // r z p q u, the two double-float copies, chunk partials, the double-float
-    // landmark inverses and y, slots, ws (16 B each); in 8-byte units (the
-    // sum before ws is even, so ws is 16-byte aligned)
-    return 7 * (size_t)P.n + 6 * (size_t)P.nopch + 12 * (size_t)P.L + 2 * (size_t)kPcgMaxBlocks + 4 * (size_t)P.M;
+    // r p q (FP64), rf uf zf (FP32, 2n doubles' room), the double-float p,
+    // chunk partials, the double-float landmark inverses and y, slots, ws
+    // (16 B each); in 8-byte units (the sum before ws is even: ws is 16-byte
+    // aligned)
+    return 6 * (size_t)P.n + 6 * (size_t)P.nopch + 12 * (size_t)P.L + 2 * (size_t)kPcgMaxBlocks + 4 * (size_t)P.M;
 }
 
 cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s) {
