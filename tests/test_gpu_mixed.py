@@ -114,3 +114,26 @@ def test_mixed_degenerate_landmarks(zs_lib, oracle):
     assert abs(r.chi2_final - ro.chi2_final) <= MIXED_COST_TOL * ro.chi2_final
     for l in (3, 50, 400):
         assert np.array_equal(L[l], sc.landmarks[l])  # unobserved landmarks stay where they are
+
+
+def test_mixed_robust_with_information(zs_lib, oracle):
+    """The general operator (a robust weight W per observation): Huber loss and
+    a 2 x 2 information matrix per observation, against the oracle: a single
+    damped step, and the cost after 8 iterations (multi-step robust solves
+    are compared at 1e-5, as for the plain form)."""
+    sc = scenes.arc_scene(25, 2500, seed=3, huber=True)
+    rng = np.random.default_rng(4)
+    s = rng.uniform(0.5, 2.0, size=(sc.M, 1))
+    sc.obs_info = np.concatenate([1.0 * s, 0.2 * s, 0.2 * s, 0.6 * s], axis=1)
+    lam = oracle.initial_lambda(sc)
+    o = oracle.linear_step(sc, lam, want_S=False)
+    with _ba(1) as h:
+        h.set_problem(sc)
+        g = h.linear_step(lam, want_S=False)
+    assert o["ok"] and g["ok"]
+    assert rel_err(g["delta"], o["delta"]) < STEP_TOL
+    _, _, ro = oracle.solve(sc, 8)
+    with _ba(1) as h:
+        h.set_problem(sc)
+        r = h.solve(8)
+    assert abs(r.chi2_final - ro.chi2_final) <= 1e-5 * ro.chi2_final

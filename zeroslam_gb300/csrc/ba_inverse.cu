@@ -309,6 +309,7 @@ __device__ __forceinline__ df ld_df(const df* p) {
 // the previous 32; the lane holding a landmark's last observation forms y_l
 // and stores it (yst, read again by the caller). ws_o goes to wsp at the
 // observation's pose-major position. v (double-float) null: v = 0.
+template <bool kIdW>
 __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac, const df* hinv, const df* v, bool c,
                              float4* ws, float4* wsp, df* yst) {
     const int lane = threadIdx.x & 31;
@@ -341,16 +342,24 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
                     t0 = s0.result();
                     t1 = s1.result();
                 }
-                const float4 e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
-                // w = W t + c g, W = [f.z f.w; h.x h.y]
-                df_dot q0, q1;
-                q0.add(f.z, t0); q0.add(f.w, t1);
-                q1.add(h.x, t0); q1.add(h.y, t1);
-                if (c) {
-                    q0.add_df(df{G.x, G.y});
-                    q1.add_df(df{G.z, G.w});
+                const float4 e = __ldg(r + 4), f = __ldg(r + 5);
+                // w = W t + c g, W = [f.z f.w; h.x h.y] (the identity when kIdW)
+                df w0, w1;
+                if constexpr (kIdW) {
+                    w0 = c ? df_add(t0, df{G.x, G.y}) : t0;
+                    w1 = c ? df_add(t1, df{G.z, G.w}) : t1;
+                } else {
+                    const float4 h = __ldg(r + 6);
+                    df_dot q0, q1;
+                    q0.add(f.z, t0); q0.add(f.w, t1);
+                    q1.add(h.x, t0); q1.add(h.y, t1);
+                    if (c) {
+                        q0.add_df(df{G.x, G.y});
+                        q1.add_df(df{G.z, G.w});
+                    }
+                    w0 = q0.result();
+                    w1 = q1.result();
                 }
-                const df w0 = q0.result(), w1 = q1.result();
                 // k = -J_l^T w, J_l = [e.x e.y e.z; e.w f.x f.y]
                 df_dot k0, k1, k2;
                 k0.add(-e.x, w0); k0.add(-e.w, w1);
@@ -406,7 +415,7 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
         for (int o = O0 + lane; o < O1; o += 32) {
             const int l = P.obs_lm[o];
             const float4* r = reinterpret_cast<const float4*>(jac + o);
-            const float4 G = __ldg(r), e = __ldg(r + 4), f = __ldg(r + 5), h = __ldg(r + 6);
+            const float4 G = __ldg(r), e = __ldg(r + 4), f = __ldg(r + 5);
             const float4 tt = ws[o];  // this lane's own write above
             const df y0 = yst[3LL * l], y1 = yst[3LL * l + 1], y2 = yst[3LL * l + 2];
             // s = J_p v + J_l y
@@ -417,14 +426,22 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
             m1.add(e.w, y0); m1.add(f.x, y1); m1.add(f.y, y2);
             const df s0 = m0.result(), s1 = m1.result();
             // ws = W s + c g
-            df_dot n0, n1;
-            n0.add(f.z, s0); n0.add(f.w, s1);
-            n1.add(h.x, s0); n1.add(h.y, s1);
-            if (c) {
-                n0.add_df(df{G.x, G.y});
-                n1.add_df(df{G.z, G.w});
+            df a0, a1;
+            if constexpr (kIdW) {
+                a0 = c ? df_add(s0, df{G.x, G.y}) : s0;
+                a1 = c ? df_add(s1, df{G.z, G.w}) : s1;
+            } else {
+                const float4 h = __ldg(r + 6);
+                df_dot n0, n1;
+                n0.add(f.z, s0); n0.add(f.w, s1);
+                n1.add(h.x, s0); n1.add(h.y, s1);
+                if (c) {
+                    n0.add_df(df{G.x, G.y});
+                    n1.add_df(df{G.z, G.w});
+                }
+                a0 = n0.result();
+                a1 = n1.result();
             }
-            const df a0 = n0.result(), a1 = n1.result();
             wsp[P.pm[o]] = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
         }
     }
@@ -541,6 +558,7 @@ __device__ double grid_sum(cg::grid_group& grid, double v, double* slot, double*
 
 constexpr int kPcgMaxBlocks = 2048;
 
+template <bool kIdW>
 __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac* __restrict__ jac,
                                                   const float4* __restrict__ jp_pm,
                                                   const double* __restrict__ hinv, const float* __restrict__ X,
@@ -572,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     for (int64_t i = tid; i < 9LL * P.L; i += nth) hdf[i] = df_from_double(hinv[i]);
     grid.sync();
     // r = b_s = b_p - H_pl (H_ll + lambda I)^-1 b_l, x = 0
-    op_landmarks(P, jac, hdf, nullptr, true, ws, wsp, yst);
+    op_landmarks<kIdW>(P, jac, hdf, nullptr, true, ws, wsp, yst);
     grid.sync();
     op_pose_chunks(P, jp_pm, wsp, part);
     grid.sync();
@@ -614,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
         double rz = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
         for (;;) {
             // q = S p
-            op_landmarks(P, jac, hdf, pdf, false, ws, wsp, yst);
+            op_landmarks<kIdW>(P, jac, hdf, pdf, false, ws, wsp, yst);
             grid.sync();
             op_pose_chunks(P, jp_pm, wsp, part);
             grid.sync();
@@ -687,8 +705,12 @@ size_t pcg_doubles(const DevProblem& P) {
 
 cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s) {
     if (P.n <= 0) return cudaSuccess;
+    // W = I for every observation (no robust loss, no information matrices):
+    // the operator skips the weight products
+    const bool id_w = P.loss.kind == 0 && P.obs_info == nullptr;  // 0: no robust loss
+    const void* kern = id_w ? (const void*)k_pcg<true> : (const void*)k_pcg<false>;
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg, kThreads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, 0);
     if (e != cudaSuccess) return e;
     const int blocks = std::max(1, std::min(kPcgMaxBlocks, occ * sm_count()));
     DevProblem Pv = P;
@@ -702,7 +724,7 @@ cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it,
     double* buf = W.pcg;
     void* args[] = {(void*)&Pv,  (void*)&jac, (void*)&jp_pm,  (void*)&hinv, (void*)&X,  (void*)&XT,
                     (void*)&delta, (void*)&bs, (void*)&buf, (void*)&max_it, (void*)&tol, (void*)&st};
-    e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(blocks), dim3(kThreads), args, 0, s);
+    e = cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kThreads), args, 0, s);
     if (e == cudaSuccess) note_launch();
     return e;
 }

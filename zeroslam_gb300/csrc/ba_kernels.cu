@@ -115,8 +115,13 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
     const double* om = P.obs_info ? P.obs_info + 4 * o : nullptr;
     T Jc[6], Xv, Yv, Zv, Rm[9];
     double r[2];
-    if (sizeof(T) == 8) {
-        // plain form: residual rounded exactly as the reference's
+    if (sizeof(T) == 8 || P.loss.kind != 0) {
+        // plain form, and the mixed form under a robust loss: residual rounded
+        // exactly as the reference's. For Huber outliers rho' + 2 rho'' e2 is
+        // zero in exact arithmetic and the rank-one weight term below is added
+        // or not by its rounding; any other rounding of e2 takes the other
+        // branch for some observations and changes their whole curvature along
+        // the residual.
         const double* pp = P.pose + (int64_t)pi * kPoseStride;
         double p[7], X[3], Xc[3];
 #pragma unroll
