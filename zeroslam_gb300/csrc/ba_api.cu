@@ -217,6 +217,60 @@ struct PhaseScope {
     }
 };
 
+namespace {
+
+// Host scratch of build_problem, kept by the handle across set_problem calls:
+// slot i (in call order) grows to the largest size asked for and is not
+// cleared between problems, so a repeated problem of similar size touches no
+// fresh pages (allocating and zeroing ~150 MB per call cost more than the
+// structure analysis itself); it is pinned, so uploads from it are DMA copies.
+struct HostScratch {
+    std::vector<std::pair<void*, size_t>> slots;
+    size_t next = 0;
+    void* get(size_t bytes) {
+        if (next == slots.size()) slots.push_back({nullptr, 0});
+        auto& sl = slots[next++];
+        if (sl.second < bytes) {
+            if (sl.first) cudaFreeHost(sl.first);
+            sl = {nullptr, 0};
+            ZS_CUDA(cudaMallocHost(&sl.first, std::max<size_t>(bytes, 1)));
+            sl.second = bytes;
+        }
+        return sl.first;
+    }
+    void release() {
+        for (auto& sl : slots)
+            if (sl.first) cudaFreeHost(sl.first);
+        slots.clear();
+        next = 0;
+    }
+};
+
+// A view of n elements of scratch (contents undefined until written).
+template <typename T>
+struct HostArray {
+    T* p = nullptr;
+    size_t n = 0;
+    T& operator[](size_t i) { return p[i]; }
+    const T& operator[](size_t i) const { return p[i]; }
+    size_t size() const { return n; }
+    const T* data() const { return p; }
+};
+
+template <typename T>
+HostArray<T> scratch_array(HostScratch& hs, size_t n) {
+    return HostArray<T>{static_cast<T*>(hs.get(n * sizeof(T))), n};
+}
+
+template <typename T>
+T* upload(const HostArray<T>& v, DevPool& pool, cudaStream_t s) {
+    T* d = dalloc<T>(v.size(), pool);
+    if (v.size()) ZS_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+}  // namespace
+
 struct zs_ba_handle {
     zs_ba_options opt{};
     PhaseTimer timer;
@@ -234,6 +288,7 @@ struct zs_ba_handle {
     double* adj_vec = nullptr;   // a, v, r, z, p, q, zero: 7 x (n + 3L)
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
+    HostScratch hscratch;        // build_problem's host arrays (pinned, reused)
     // batched windows
     bool batch = false;
     BatchDev B;
@@ -363,6 +418,7 @@ void zs_ba_destroy(zs_ba_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     h->timer.destroy();
     h->release_problem();
+    h->hscratch.release();
     if (h->st) cudaFree(h->st);
     if (h->st_host) cudaFreeHost(h->st_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -399,6 +455,15 @@ static int validate(const zs_ba_problem* p) {
 static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::vector<int32_t>* wpose0 = nullptr,
                           const std::vector<int32_t>* wlm0 = nullptr) {
     cudaStream_t s = h->stream;
+    // with options.verbose >= 3: host milliseconds of the steps below
+    auto t_prev = std::chrono::steady_clock::now();
+    auto stamp = [&](const char* what) {
+        if (h->opt.verbose < 3) return;
+        const auto t = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "  set_problem %-22s %7.2f ms\n", what,
+                     std::chrono::duration<double, std::milli>(t - t_prev).count());
+        t_prev = t;
+    };
     const int K = p->num_poses, L = p->num_landmarks;
     const int64_t M = p->num_obs;
     const bool batched = wpose0 != nullptr;
@@ -430,10 +495,13 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     for (int l = 0; l <= L; ++l) obs_prefix[l] = lm_ptr[l];
     const std::vector<int64_t> lcuts = balanced_cuts(obs_prefix, (M > 50000 && L > 4 * nt) ? nt : 1);
     const int nth = (int)lcuts.size() - 1;
-    std::vector<int32_t> obs_pose(M), obs_lm(M), dup_owner(M);
-    std::vector<double2> uv(M);
-    std::vector<double> info(p->obs_info ? 4 * M : 0);
-    std::vector<uint8_t> blk_valid(M, 0);
+    HostScratch& hs = h->hscratch;
+    hs.next = 0;
+    HostArray<int32_t> obs_pose = scratch_array<int32_t>(hs, M), obs_lm = scratch_array<int32_t>(hs, M),
+                       dup_owner = scratch_array<int32_t>(hs, M);
+    HostArray<double2> uv = scratch_array<double2>(hs, M);
+    HostArray<double> info = scratch_array<double>(hs, p->obs_info ? 4 * M : 0);
+    HostArray<uint8_t> blk_valid = scratch_array<uint8_t>(hs, M);
     std::vector<char> dups(nth, 0);
     parallel_ranges(lcuts, [&](int t, int64_t l0, int64_t l1) {
         for (int64_t l = l0; l < l1; ++l) {
@@ -455,18 +523,39 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     });
     bool has_dups = false;
     for (char d : dups) has_dups = has_dups || d;
+    stamp("landmark-major order");
     // pose-major lists of landmark-major indices, ascending
-    std::vector<int32_t> pose_ptr(K + 1, 0), pose_obs(M);
-    for (int64_t i = 0; i < M; ++i) pose_ptr[obs_pose[i] + 1]++;
-    for (int k = 0; k < K; ++k) pose_ptr[k + 1] += pose_ptr[k];
+    // (a stable counting sort by pose over index ranges of equal length: each
+    // thread counts its range per pose and fills after the threads before it)
+    // pm: pose-major position of each observation, where its H_pl / W /
+    // pose-partial records live, so a pose's records are contiguous
+    std::vector<int32_t> pose_ptr(K + 1, 0);
+    HostArray<int32_t> pose_obs = scratch_array<int32_t>(hs, M), pm = scratch_array<int32_t>(hs, M);
     {
-        std::vector<int32_t> fill(pose_ptr.begin(), pose_ptr.end() - 1);
-        for (int64_t i = 0; i < M; ++i) pose_obs[fill[obs_pose[i]]++] = (int32_t)i;
+        std::vector<int64_t> uni(nth + 1);
+        for (int t = 0; t <= nth; ++t) uni[t] = M * t / nth;
+        std::vector<std::vector<int32_t>> cnt(nth, std::vector<int32_t>(K, 0));
+        parallel_ranges(uni, [&](int t, int64_t i0, int64_t i1) {
+            for (int64_t i = i0; i < i1; ++i) cnt[t][obs_pose[i]]++;
+        });
+        for (int k = 0; k < K; ++k) {
+            int32_t run = pose_ptr[k];
+            for (int t = 0; t < nth; ++t) {
+                const int32_t c = cnt[t][k];
+                cnt[t][k] = run;  // thread t's first position for pose k
+                run += c;
+            }
+            pose_ptr[k + 1] = run;
+        }
+        parallel_ranges(uni, [&](int t, int64_t i0, int64_t i1) {
+            std::vector<int32_t>& pos = cnt[t];
+            for (int64_t i = i0; i < i1; ++i) {
+                const int32_t q = pos[obs_pose[i]]++;
+                pose_obs[q] = (int32_t)i;
+                pm[i] = q;
+            }
+        });
     }
-    // pose-major position of each observation: its H_pl / W / pose-partial
-    // records live there, so a pose's records are contiguous
-    std::vector<int32_t> pm(M);
-    for (int64_t q = 0; q < M; ++q) pm[pose_obs[q]] = (int32_t)q;
     // chunks of the mixed form's Schur operator: <= kOpChunk pose-major
     // positions of one pose each
     std::vector<int32_t> opch_q, pose_opch(K + 1, 0);
@@ -482,6 +571,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         if (l > lmch_l.back() && lm_ptr[l + 1] - start > kOpChunk) lmch_l.push_back(l);
     }
     if (lmch_l.back() != L) lmch_l.push_back(L);
+    stamp("pose lists, chunks");
     // Schur triples: for each landmark, every (block a, block b) with pose_a >= pose_b,
     // grouped by pose pair (i, j) = (pose_a, pose_b), landmark order within a pair.
     // Pair keys are window-local: key = base_w + (i - p0_w) K_w + (j - p0_w).
@@ -510,6 +600,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         tri_prefix[l + 1] = tri_prefix[l] + nv * (nv + 1) / 2;
     }
     const int64_t ntriples = tri_prefix[L];
+    stamp("triple counts");
     const int ntt = (ntriples > 200000 && L > 4 * nt && (size_t)nt * nkeys <= ((size_t)1 << 28)) ? nt : 1;
     const std::vector<int64_t> tcuts = balanced_cuts(tri_prefix, ntt);
     const int ntc = (int)tcuts.size() - 1;
@@ -539,7 +630,8 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         pair_off[k + 1] = pair_off[k] + tot;
         if (tot) ++npairs;
     }
-    std::vector<int2> triples(ntriples);
+    stamp("pair counts");
+    HostArray<int2> triples = scratch_array<int2>(hs, ntriples);
     parallel_ranges(tcuts, [&](int t, int64_t l0, int64_t l1) {
         std::vector<int32_t> vb;
         std::vector<int64_t>& pos = counts[t];
@@ -553,6 +645,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         }
     });
     counts.clear();
+    stamp("triples");
     std::vector<int32_t> pair_i, pair_j, seg_pair;
     std::vector<int64_t> seg_ptr{0}, pair_seg_ptr{0};
     pair_i.reserve(npairs);
@@ -573,6 +666,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     P.npairs = npairs;
     P.ntriples = ntriples;
     P.nsegs = (int64_t)seg_pair.size();
+    stamp("segments");
 
     // state (padded device layout)
     std::vector<double> pose8((size_t)K * kPoseStride, 0.0), lm4((size_t)L * kLmStride, 0.0);
@@ -613,6 +707,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     P.nlmch = (int64_t)lmch_l.size() - 1;
     P.lmch_l = upload(lmch_l, own, s);
     P.triples = upload(triples, own, s);
+    stamp("uploads");
     P.nwin = nwin;
     std::vector<int64_t> win_s_off(nwin, 0);
     int64_t s_total = 0;
@@ -682,6 +777,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     ZS_CUDA(cudaMemsetAsync(W.delta, 0, sizeof(double) * std::max<size_t>(1, (size_t)n + 3 * (size_t)L), s));
     ZS_CUDA(cudaStreamSynchronize(s));
     ZS_CUDA(cudaGetLastError());
+    stamp("allocations, sync");
 }
 
 int zs_ba_set_problem(zs_ba_handle* h, const zs_ba_problem* p) {
