@@ -18,6 +18,8 @@
 #include <set>
 #include <string>
 #include <thread>
+#include <condition_variable>
+#include <functional>
 #include <tuple>
 #include <vector>
 
@@ -103,6 +105,73 @@ int host_threads() {
     return n;
 }
 
+// Persistent workers for the structure analysis (host_threads() - 1 of them,
+// shared by all handles; one dispatch at a time, the caller takes part):
+// starting threads for each of the analysis's parallel steps cost ~0.3 ms
+// per step.
+class HostPool {
+  public:
+    static HostPool& get() {
+        static HostPool pool;
+        return pool;
+    }
+    int workers() const { return (int)threads_.size(); }
+    // f(t) for t in [0, n), n <= workers() + 1; t = 0 on the calling thread
+    void run(int n, const std::function<void(int)>& f) {
+        std::lock_guard<std::mutex> one(run_mu_);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            task_ = &f;
+            ntask_ = n;
+            pending_ = (int)threads_.size();
+            ++generation_;
+        }
+        cv_.notify_all();
+        f(0);
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return pending_ == 0; });
+        task_ = nullptr;
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : threads_) t.join();
+    }
+
+  private:
+    HostPool() {
+        for (int i = 1; i < host_threads(); ++i) threads_.emplace_back([this, i] { loop(i); });
+    }
+    void loop(int id) {
+        long long seen = 0;
+        for (;;) {
+            const std::function<void(int)>* f = nullptr;
+            int n = 0;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || generation_ != seen; });
+                if (stop_) return;
+                seen = generation_;
+                f = task_;
+                n = ntask_;
+            }
+            if (id < n) (*f)(id);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+    std::vector<std::thread> threads_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)>* task_ = nullptr;
+    int ntask_ = 0, pending_ = 0;
+    long long generation_ = 0;
+    bool stop_ = false;
+};
+
 // f(t, begin, end) on nt threads over [cuts[t], cuts[t + 1]).
 template <typename F>
 void parallel_ranges(const std::vector<int64_t>& cuts, F f) {
@@ -111,11 +180,15 @@ void parallel_ranges(const std::vector<int64_t>& cuts, F f) {
         if (nt == 1) f(0, cuts[0], cuts[1]);
         return;
     }
-    std::vector<std::thread> th;
-    th.reserve(nt - 1);
-    for (int t = 1; t < nt; ++t) th.emplace_back(f, t, cuts[t], cuts[t + 1]);
-    f(0, cuts[0], cuts[1]);
-    for (auto& x : th) x.join();
+    HostPool& pool = HostPool::get();
+    if (nt > pool.workers() + 1) {  // more ranges than threads: each thread takes every k-th
+        const int w = pool.workers() + 1;
+        pool.run(w, [&](int t) {
+            for (int r = t; r < nt; r += w) f(r, cuts[r], cuts[r + 1]);
+        });
+        return;
+    }
+    pool.run(nt, [&](int t) { f(t, cuts[t], cuts[t + 1]); });
 }
 
 // Cuts [0, n) into nt ranges of about equal weight (prefix[i] = weight of [0, i)).
@@ -479,17 +552,50 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     P.intr = Intrinsics{p->intrinsics[0], p->intrinsics[1], p->intrinsics[2], p->intrinsics[3]};
     P.loss = LossParams{p->loss_kind, p->loss_delta};
 
-    // landmark-major order, poses ascending within a landmark (stable)
-    std::vector<int32_t> lm_ptr(L + 1, 0);
-    for (int64_t o = 0; o < M; ++o) lm_ptr[p->obs_landmark[o] + 1]++;
-    for (int l = 0; l < L; ++l) lm_ptr[l + 1] += lm_ptr[l];
-    std::vector<int64_t>& perm = h->perm;
-    perm.assign(M, 0);
-    {
-        std::vector<int32_t> fill(lm_ptr.begin(), lm_ptr.end() - 1);
-        for (int64_t o = 0; o < M; ++o) perm[fill[p->obs_landmark[o]]++] = o;
-    }
+    // landmark-major order, poses ascending within a landmark (stable): a
+    // parallel counting sort (threads count index ranges per landmark; the
+    // landmark totals, then each thread's offsets, by landmark ranges) and a
+    // per-landmark sort by pose below
     const int nt = host_threads();
+    std::vector<int32_t> lm_ptr(L + 1, 0);
+    std::vector<int64_t>& perm = h->perm;
+    perm.resize(M);
+    {
+        const int ntu = (M > 50000 && L > 4 * nt) ? nt : 1;
+        std::vector<int64_t> uo(ntu + 1), ul(ntu + 1);
+        for (int t = 0; t <= ntu; ++t) {
+            uo[t] = M * t / ntu;
+            ul[t] = (int64_t)L * t / ntu;
+        }
+        std::vector<std::vector<int32_t>> cnt(ntu);
+        parallel_ranges(uo, [&](int t, int64_t o0, int64_t o1) {
+            std::vector<int32_t>& c = cnt[t];
+            c.assign(L, 0);
+            for (int64_t o = o0; o < o1; ++o) c[p->obs_landmark[o]]++;
+        });
+        parallel_ranges(ul, [&](int, int64_t l0, int64_t l1) {
+            for (int64_t l = l0; l < l1; ++l) {
+                int32_t tot = 0;
+                for (int t = 0; t < ntu; ++t) tot += cnt[t][l];
+                lm_ptr[l + 1] = tot;
+            }
+        });
+        for (int l = 0; l < L; ++l) lm_ptr[l + 1] += lm_ptr[l];
+        parallel_ranges(ul, [&](int, int64_t l0, int64_t l1) {
+            for (int64_t l = l0; l < l1; ++l) {
+                int32_t run = lm_ptr[l];
+                for (int t = 0; t < ntu; ++t) {
+                    const int32_t c = cnt[t][l];
+                    cnt[t][l] = run;  // thread t's first position for landmark l
+                    run += c;
+                }
+            }
+        });
+        parallel_ranges(uo, [&](int t, int64_t o0, int64_t o1) {
+            std::vector<int32_t>& pos = cnt[t];
+            for (int64_t o = o0; o < o1; ++o) perm[pos[p->obs_landmark[o]]++] = o;
+        });
+    }
     // landmark ranges of about equal observation counts
     std::vector<int64_t> obs_prefix(L + 1);
     for (int l = 0; l <= L; ++l) obs_prefix[l] = lm_ptr[l];
