@@ -700,20 +700,24 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     // shares of the threads before it, which is the landmark order a single
     // pass would give.
     std::vector<int64_t> tri_prefix(L + 1, 0);
-    for (int l = 0; l < L; ++l) {
-        int64_t nv = 0;
-        for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i) nv += blk_valid[i];
-        tri_prefix[l + 1] = tri_prefix[l] + nv * (nv + 1) / 2;
-    }
+    parallel_ranges(lcuts, [&](int, int64_t l0, int64_t l1) {
+        for (int64_t l = l0; l < l1; ++l) {
+            int64_t nv = 0;
+            for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i) nv += blk_valid[i];
+            tri_prefix[l + 1] = nv * (nv + 1) / 2;
+        }
+    });
+    for (int l = 0; l < L; ++l) tri_prefix[l + 1] += tri_prefix[l];
     const int64_t ntriples = tri_prefix[L];
     stamp("triple counts");
     const int ntt = (ntriples > 200000 && L > 4 * nt && (size_t)nt * nkeys <= ((size_t)1 << 28)) ? nt : 1;
     const std::vector<int64_t> tcuts = balanced_cuts(tri_prefix, ntt);
     const int ntc = (int)tcuts.size() - 1;
-    std::vector<std::vector<int64_t>> counts(ntc, std::vector<int64_t>(nkeys, 0));
+    std::vector<std::vector<int64_t>> counts(ntc);
     parallel_ranges(tcuts, [&](int t, int64_t l0, int64_t l1) {
         std::vector<int32_t> vb;
         std::vector<int64_t>& c = counts[t];
+        c.assign(nkeys, 0);
         for (int64_t l = l0; l < l1; ++l) {
             vb.clear();
             for (int32_t i = lm_ptr[l]; i < lm_ptr[l + 1]; ++i)
@@ -722,20 +726,34 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
                 for (size_t b = 0; b <= a; ++b) c[pair_key(obs_pose[vb[a]], obs_pose[vb[b]])]++;
         }
     });
+    // key totals, their prefix, then each thread's first position per key
+    // (by key ranges)
     std::vector<int64_t> pair_off(nkeys + 1, 0);
     std::vector<int64_t> pair_count(nkeys, 0);
+    std::vector<int64_t> kr(ntc + 1);
+    for (int t = 0; t <= ntc; ++t) kr[t] = (int64_t)nkeys * t / ntc;
+    parallel_ranges(kr, [&](int, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            int64_t tot = 0;
+            for (int t = 0; t < ntc; ++t) tot += counts[t][k];
+            pair_count[k] = tot;
+        }
+    });
     int npairs = 0;
     for (size_t k = 0; k < nkeys; ++k) {
-        int64_t tot = 0;
-        for (int t = 0; t < ntc; ++t) {
-            const int64_t c = counts[t][k];
-            counts[t][k] = pair_off[k] + tot;  // thread t's first position in key k
-            tot += c;
-        }
-        pair_count[k] = tot;
-        pair_off[k + 1] = pair_off[k] + tot;
-        if (tot) ++npairs;
+        pair_off[k + 1] = pair_off[k] + pair_count[k];
+        if (pair_count[k]) ++npairs;
     }
+    parallel_ranges(kr, [&](int, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            int64_t run = pair_off[k];
+            for (int t = 0; t < ntc; ++t) {
+                const int64_t c = counts[t][k];
+                counts[t][k] = run;  // thread t's first position in key k
+                run += c;
+            }
+        }
+    });
     stamp("pair counts");
     HostArray<int2> triples = scratch_array<int2>(hs, ntriples);
     parallel_ranges(tcuts, [&](int t, int64_t l0, int64_t l1) {
