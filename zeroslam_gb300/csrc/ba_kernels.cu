@@ -269,12 +269,16 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
         for (int k = 0; k < 12; ++k) jp[k] = pf ? 0.f : (float)Jp[k];
 #pragma unroll
         for (int k = 0; k < 6; ++k) jl[k] = lf ? 0.f : (float)Jl[k];
-        d[1] = make_float4(jp[0], jp[1], jp[2], jp[3]);
-        d[2] = make_float4(jp[4], jp[5], jp[6], jp[7]);
-        d[3] = make_float4(jp[8], jp[9], jp[10], jp[11]);
-        jp_pm[3 * q] = d[1];  // pose-major copy for the operator's pose pass
-        jp_pm[3 * q + 1] = d[2];
-        jp_pm[3 * q + 2] = d[3];
+        if (jp_pm) {  // J_p is read only by the single problem's conjugate-gradient operator
+            const float4 j0 = make_float4(jp[0], jp[1], jp[2], jp[3]), j1 = make_float4(jp[4], jp[5], jp[6], jp[7]),
+                         j2 = make_float4(jp[8], jp[9], jp[10], jp[11]);
+            d[1] = j0;
+            d[2] = j1;
+            d[3] = j2;
+            jp_pm[3 * q] = j0;  // pose-major copy for the operator's pose pass
+            jp_pm[3 * q + 1] = j1;
+            jp_pm[3 * q + 2] = j2;
+        }
         d[4] = make_float4(jl[0], jl[1], jl[2], jl[3]);
         d[5] = make_float4(jl[4], jl[5], (float)W00, (float)W01);
         d[6] = make_float4((float)W10, (float)W11, 0.f, 0.f);
@@ -931,7 +935,7 @@ void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
     }
     if (P.M > 0) {
         k_linearize<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl, (T*)W.lm_part, (T*)W.pose_part, W.pose_aux,
-                                                          W.jac, W.jp_pm); note_launch();
+                                                          W.jac, P.pose_win ? nullptr : W.jp_pm); note_launch();
         if (P.has_dups) { k_merge_dups<T><<<grid_for(P.M), kThreads, 0, s>>>(P, (T*)W.hpl); note_launch(); }
     }
     if (P.L > 0) {
