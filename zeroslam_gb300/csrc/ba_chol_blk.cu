@@ -154,14 +154,16 @@ __device__ int factor_diag64(float* F, int n, int k0, int kb, float eps, float* 
     __syncthreads();
     if (nbw == 2) {
         // W = Lb Xa (32 x 32) into the lower-left quadrant of Inv, then Xc W
-        float w[4];
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * blockDim.x;
-            const int r = e >> 5, c = e & 31;
-            const float* Lb = tile_at(T, 1, 0) + r * kLd;
-            float s = 0.f;
-            for (int m = c; m < 32; ++m) s = fmaf(Lb[m], Inv[m * kPL + c], s);
-            w[q] = s;
+        // (Xa is lower triangular and Inv holds zeros above it, so every lane
+        // runs the full 32 terms: no divergence, four independent chains)
+        float w[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * blockDim.x;
+                w[q] = fmaf(tile_at(T, 1, 0)[(e >> 5) * kLd + m], Inv[m * kPL + (e & 31)], w[q]);
+            }
         }
         __syncthreads();
         for (int q = 0; q < 4; ++q) {
@@ -169,13 +171,19 @@ __device__ int factor_diag64(float* F, int n, int k0, int kb, float eps, float* 
             Inv[(32 + (e >> 5)) * kPL + (e & 31)] = w[q];
         }
         __syncthreads();
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * blockDim.x;
-            const int r = e >> 5, c = e & 31;
-            float s = 0.f;
-            for (int m = 0; m <= r; ++m) s = fmaf(Inv[(32 + r) * kPL + 32 + m], Inv[(32 + m) * kPL + c], s);
-            w[q] = -s;
+        // (Xc is lower triangular with zeros above it in Inv: the full 32 terms)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = 0.f;
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * blockDim.x;
+                w[q] = fmaf(Inv[(32 + (e >> 5)) * kPL + 32 + m], Inv[(32 + m) * kPL + (e & 31)], w[q]);
+            }
         }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = -w[q];
         __syncthreads();
         for (int q = 0; q < 4; ++q) {
             const int e = threadIdx.x + q * blockDim.x;
@@ -183,16 +191,19 @@ __device__ int factor_diag64(float* F, int n, int k0, int kb, float eps, float* 
         }
         __syncthreads();
     }
-    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
-        const int i = e >> 6, j = e & 63;
-        Li[e] = Inv[i * kPL + j];
-        if (i < kb && j < kb) {
-            float v = 0.f;
-            if (j < i) v = tile_at(T, i >> 5, j >> 5)[(i & 31) * kLd + (j & 31)];
-            else if (j == i) v = tile_at(T, i >> 5, i >> 5)[(i & 31) * (kLd + 1)];
-            else if ((j >> 5) != (i >> 5)) continue;  // upper blocks outside the diagonal 32-blocks keep S
-            F[(int64_t)(k0 + i) * n + k0 + j] = v;
-        }
+    // Li = Inv, as 16-byte copies (Inv rows are 16-byte aligned)
+    for (int e4 = threadIdx.x; e4 < 64 * 16; e4 += blockDim.x)
+        reinterpret_cast<float4*>(Li)[e4] = *reinterpret_cast<const float4*>(Inv + (e4 >> 4) * kPL + (e4 & 15) * 4);
+    // L into F: the diagonal 32-blocks (zeros above their diagonals) and the
+    // lower-left block; the upper-right block keeps S
+    for (int e = threadIdx.x; e < 3 * 1024; e += blockDim.x) {
+        const int blk = e >> 10, rr = (e >> 5) & 31, cc = e & 31;
+        const int bi = blk == 0 ? 0 : 1, bj = blk == 2 ? 1 : 0;  // (0, 0), (1, 0), (1, 1)
+        const int i = 32 * bi + rr, j = 32 * bj + cc;
+        if (i >= kb || j >= kb) continue;
+        const float* Tb = tile_at(T, bi, bj);
+        const float v = (bi != bj || cc < rr) ? Tb[rr * kLd + cc] : (cc == rr ? Tb[rr * (kLd + 1)] : 0.f);
+        F[(int64_t)(k0 + i) * n + k0 + j] = v;
     }
     __syncthreads();
     return 1;
