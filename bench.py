@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-windows measurement")
     ap.add_argument("--batch-windows", type=int, default=256)
     ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiable solve) timing")
     ap.add_argument("--batch-profile", action="store_true",
                     help="with --single batch-*: per-phase SM cycles of the window solves by keyframe range")
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
@@ -350,6 +351,37 @@ def loop_section(args, dist: Dist) -> dict:
     return out
 
 
+def adjoint_section(args, dist: Dist) -> dict:
+    """Configuration 3, the differentiable solve: the 50-keyframe / 10,000-landmark
+    scene solved to convergence in FP64, then dL/d(pixels) and dL/d(intrinsics)
+    of a scalar loss of the converged state by the implicit-function adjoint
+    (zs_ba_adjoint): a seeded dL/dx (the adjoint's cost does not depend on its
+    values), one warm-up and `steps` timed adjoint solves (device time)."""
+    from zeroslam_gb300 import ba, scenes
+
+    sc = scenes.adjoint_scene()
+    rng = np.random.default_rng(11)
+    a_pose = rng.normal(size=(sc.K, 6)) * (sc.pose_fixed[:, None] == 0)
+    a_lm = rng.normal(size=(sc.L, 3)) * (sc.landmark_fixed[:, None] == 0)
+    with ba.BundleAdjuster(precision=ba.FP64, device=dist.local) as h:
+        h.set_problem(sc)
+        fwd = h.solve(sc.iterations)
+        h.adjoint(a_pose, a_lm)
+        dist.barrier()
+        ms, its, res = [], [], []
+        for _ in range(max(1, args.steps)):
+            _, _, rep = h.adjoint(a_pose, a_lm)
+            ms.append(rep.ms_total)
+            its.append(rep.iterations)
+            res.append(rep.rel_residual)
+    t = dist.max(float(np.mean(ms)))
+    return {"workload": f"adjoint: K={sc.K} poses, L={sc.L} landmarks, M={sc.M} observations, FP64, "
+                        f"forward {sc.iterations} LM iterations then dL/duv and dL/dintrinsics",
+            "ms_per_adjoint": t, "adjoints_per_s": dist.world / (t * 1e-3), "cg_iterations": int(np.max(its)),
+            "rel_residual": float(np.max(res)), "forward_ms": fwd.ms_total, "forward_iterations": fwd.iterations,
+            "observations": sc.M}
+
+
 def profile_solve(sc, precision: int, iters: int, device: int) -> dict:
     from zeroslam_gb300 import ba
 
@@ -468,6 +500,7 @@ def ours_arm(args, dist: Dist):
 
     batch = None if args.no_batch else batch_section(args, dist)
     loop = None if args.no_loop else loop_section(args, dist)
+    adjoint = None if args.no_adjoint else adjoint_section(args, dist)
 
     prof_m = profile_solve(sc, ba.MIXED, iters, device)
     prof_d = profile_solve(sc, ba.FP64, iters, device)
@@ -523,6 +556,7 @@ def ours_arm(args, dist: Dist):
         "gpu_launches": int(dist.sum(mixed["launches"])),
         "batched_windows": batch,
         "loop_4m": loop,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
 
