@@ -292,6 +292,16 @@ __device__ __forceinline__ int64_t spread_warp() {
     return blockIdx.x + (int64_t)gridDim.x * (threadIdx.x >> 5);
 }
 
+// Chunks of a pass are taken from a queue (an integer counter): warps that
+// finish early take more, so the pass ends with the last chunk, not with the
+// most loaded warp. Each chunk writes fixed locations, so the results do not
+// depend on which warp takes it.
+__device__ __forceinline__ int64_t next_chunk(int* queue) {
+    int c = 0;
+    if ((threadIdx.x & 31) == 0) c = atomicAdd(queue, 1);
+    return __shfl_sync(0xffffffffu, c, 0);
+}
+
 __device__ __forceinline__ df ld_df(const df* p) {
     const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
     return df{v.x, v.y};
@@ -311,10 +321,9 @@ __device__ __forceinline__ df ld_df(const df* p) {
 // observation's pose-major position. v (double-float) null: v = 0.
 template <bool kIdW>
 __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac, const df* hinv, const df* v, bool c,
-                             float4* ws, float4* wsp, df* yst) {
+                             float4* ws, float4* wsp, df* yst, int* queue) {
     const int lane = threadIdx.x & 31;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t ch = spread_warp(); ch < P.nlmch; ch += nw) {
+    for (int64_t ch = next_chunk(queue); ch < P.nlmch; ch = next_chunk(queue)) {
         const int l0 = P.lmch_l[ch], l1 = P.lmch_l[ch + 1];
         const int O0 = P.lm_ptr[l0], O1 = P.lm_ptr[l1];
         df carry[3] = {df_zero(), df_zero(), df_zero()};
@@ -451,10 +460,10 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
 // chunk of (J_p^T ws_o)_a, read pose-major (contiguous): lanes strided, then
 // a double-float butterfly (df_add is commutative bit for bit, so every lane
 // ends with the same value).
-__device__ void op_pose_chunks(const DevProblem& P, const float4* __restrict__ jp_pm, const float4* wsp, df* part) {
+__device__ void op_pose_chunks(const DevProblem& P, const float4* __restrict__ jp_pm, const float4* wsp, df* part,
+                               int* queue) {
     const int lane = threadIdx.x & 31;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t ch = spread_warp(); ch < P.nopch; ch += nw) {
+    for (int64_t ch = next_chunk(queue); ch < P.nopch; ch = next_chunk(queue)) {
         const int q1 = P.opch_q[ch + 1];
         df_dot acc[6];
         for (int q = P.opch_q[ch] + lane; q < q1; q += 32) {
@@ -580,7 +589,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     df* hdf = part + 6 * P.nopch;             // [9 L] double-float (H_ll + lambda I)^-1
     df* yst = hdf + 9LL * P.L;                // [3 L] double-float y of the landmark pass
     double* slots = reinterpret_cast<double*>(yst + 3LL * P.L);       // [2 kPcgMaxBlocks]
-    float4* ws = reinterpret_cast<float4*>(slots + 2 * kPcgMaxBlocks);  // [M] landmark-major
+    int* queues = reinterpret_cast<int*>(slots + 2 * kPcgMaxBlocks);    // [4]: landmark, pose passes x 2
+    float4* ws = reinterpret_cast<float4*>(slots + 2 * kPcgMaxBlocks + 2);  // [M] landmark-major
     float4* wsp = ws + P.M;                                             // [M] pose-major
     // grid sums alternate between two slot buffers: consecutive sums never
     // share one, and a barrier separates every reuse
@@ -588,11 +598,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
 
     for (int64_t i = tid; i < 9LL * P.L; i += nth) hdf[i] = df_from_double(hinv[i]);
+    if (tid < 4) queues[tid] = 0;
+    // pass k of a kind takes chunks from queue k & 1 and clears the other one,
+    // which pass k - 1 finished with before a grid barrier and pass k + 1
+    // starts on after one
+    int npass = 0;
+    auto queue = [&](int kind) {
+        int* q = queues + 2 * kind;
+        if (tid == 0) q[(npass + 1) & 1] = 0;
+        return q + (npass & 1);
+    };
     grid.sync();
     // r = b_s = b_p - H_pl (H_ll + lambda I)^-1 b_l, x = 0
-    op_landmarks<kIdW>(P, jac, hdf, nullptr, true, ws, wsp, yst);
+    op_landmarks<kIdW>(P, jac, hdf, nullptr, true, ws, wsp, yst, queue(0));
     grid.sync();
-    op_pose_chunks(P, jp_pm, wsp, part);
+    op_pose_chunks(P, jp_pm, wsp, part, queue(1));
+    ++npass;
     grid.sync();
     double acc = 0.0;
     for_pose_sums(P, part, [&](int k, const double* tot) {
@@ -632,9 +653,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
         double rz = grid_sum(grid, acc, slots + ((red++) & 1) * kPcgMaxBlocks, sh);
         for (;;) {
             // q = S p
-            op_landmarks<kIdW>(P, jac, hdf, pdf, false, ws, wsp, yst);
+            op_landmarks<kIdW>(P, jac, hdf, pdf, false, ws, wsp, yst, queue(0));
             grid.sync();
-            op_pose_chunks(P, jp_pm, wsp, part);
+            op_pose_chunks(P, jp_pm, wsp, part, queue(1));
+            ++npass;
             grid.sync();
             acc = 0.0;
             for_pose_sums(P, part, [&](int k, const double* tot) {
@@ -697,10 +719,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pcg(DevProblem P, const ObsJac*
 
 size_t pcg_doubles(const DevProblem& P) {
     // r p q (FP64), rf uf zf (FP32, 2n doubles' room), the double-float p,
-    // chunk partials, the double-float landmark inverses and y, slots, ws
-    // (16 B each); in 8-byte units (the sum before ws is even: ws is 16-byte
-    // aligned)
-    return 6 * (size_t)P.n + 6 * (size_t)P.nopch + 12 * (size_t)P.L + 2 * (size_t)kPcgMaxBlocks + 4 * (size_t)P.M;
+    // chunk partials, the double-float landmark inverses and y, slots, four
+    // queue counters, ws (16 B each); in 8-byte units (the sum before ws is
+    // even: ws is 16-byte aligned)
+    return 6 * (size_t)P.n + 6 * (size_t)P.nopch + 12 * (size_t)P.L + 2 * (size_t)kPcgMaxBlocks + 2 + 4 * (size_t)P.M;
 }
 
 cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s) {
