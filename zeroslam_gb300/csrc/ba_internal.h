@@ -300,8 +300,9 @@ cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float
 // X = L^-1 and XT = X^T from the factor F and its diagonal-block inverses D.
 template <typename TX>
 cudaError_t launch_tri_inverse(int n, const TX* F, const TX* D, TX* X, TX* XT, LmState* st, cudaStream_t s);
-// x = X^T X bs, then FP64 refinement x += X^T X (bs - S x) until
-// ||bs - S x|| <= tol ||bs|| or refine_iters sweeps; work: 4n + 256 doubles.
+// Dense mixed solves (zs_dense_cholesky_solve): x = X^T X bs, then FP64
+// refinement x += X^T X (bs - S x) until ||bs - S x|| <= tol ||bs|| or
+// refine_iters sweeps; work: 4n + 256 doubles.
 template <typename TS, typename TX>
 cudaError_t launch_refine(int n, const TS* S, const TX* X, const TX* XT, const double* bs, double* x, double* work,
                           LmState* st, int refine_iters, double tol, cudaStream_t s);

@@ -1,4 +1,4 @@
-// Mixed-precision reduced solve after the FP32 factorisation S ~ L L^T:
+// Mixed-precision reduced solves after the FP32 factorisation S ~ L L^T:
 //
 // 1. k_tri_inverse: X = L^-1 by recursive 2 x 2 block inversion,
 //        inv([A 0; B C]) = [A^-1 0; -C^-1 (B A^-1)  C^-1],
@@ -7,10 +7,14 @@
 //    level is a set of independent 32 x 32 output tiles of GEMM work spread
 //    over all SMs. X^T is stored beside X so that both products below are
 //    row-wise; the lower triangle of X^T doubles as the scratch for B A^-1.
-// 2. k_refine: x = X^T X b_s, then FP64 iterative refinement
-//        r = b_s - S x (FP64 accumulation),  x += X^T X r
-//    until ||r|| <= tol ||b_s|| or the sweep limit, all GEMVs inside one
-//    cooperative launch with a deterministic grid-wide norm.
+//    (n >= 128 in FP32: the 64-wide k_tri_inverse64 of ba_chol_blk.cu.)
+// 2. k_pcg (bundle adjustment, mixed form): conjugate gradients on the exact
+//    Schur operator of the FP32 Jacobian, applied matrix-free in double-float,
+//    preconditioned by X^T X; see the section below.
+// 3. k_refine (dense solves, zs_dense_cholesky_solve): x = X^T X b_s, then
+//    FP64 iterative refinement r = b_s - S x, x += X^T X r until
+//    ||r|| <= tol ||b_s|| or the sweep limit, in one cooperative launch with a
+//    deterministic grid-wide norm.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -753,8 +757,6 @@ cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it,
 
 template cudaError_t launch_tri_inverse<float>(int, const float*, const float*, float*, float*, LmState*,
                                                cudaStream_t);
-template cudaError_t launch_refine<float, float>(int, const float*, const float*, const float*, const double*, double*,
-                                                double*, LmState*, int, double, cudaStream_t);
 template cudaError_t launch_refine<double, float>(int, const double*, const float*, const float*, const double*,
                                                  double*, double*, LmState*, int, double, cudaStream_t);
 

@@ -1082,7 +1082,6 @@ template void launch_schur<double>(const DevProblem&, DevWork&, const LmState*, 
 template void launch_schur<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 template void launch_backsub<double>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 template void launch_bs<double>(const DevProblem&, DevWork&, cudaStream_t);
-template void launch_backsub<float>(const DevProblem&, DevWork&, const LmState*, cudaStream_t);
 template void launch_bs<float>(const DevProblem&, DevWork&, cudaStream_t);
 template void launch_w<double>(const DevProblem&, DevWork&, cudaStream_t);
 template void launch_w<float>(const DevProblem&, DevWork&, cudaStream_t);
