@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--batch-windows", type=int, default=256)
     ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiable solve) timing")
+    ap.add_argument("--no-cull", action="store_true", help="skip the map-culling timing")
+    ap.add_argument("--cull-only", action="store_true", help="print the map-culling section alone")
     ap.add_argument("--batch-profile", action="store_true",
                     help="with --single batch-*: per-phase SM cycles of the window solves by keyframe range")
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
@@ -382,6 +384,83 @@ def adjoint_section(args, dist: Dist) -> dict:
             "observations": sc.M}
 
 
+# Per observation that reaches the cull's error pass: R X + t, projection and
+# distance in FP64, 35 operations (9 mul + 12 add for R X + t, 1 div + 4 mul +
+# 2 add for the projection, 2 sub + 2 mul + 2 add + 1 sqrt for the distance;
+# a division or square root counted once); bytes read per observation: frame
+# index 4 + float2 keypoint 8; per landmark: id 4 + location 24 + range 8 read,
+# flag 1 + mean 4 written.
+CULL_FP64_OPS_PER_OBS = 35
+CULL_BYTES_PER_OBS = 12
+CULL_BYTES_PER_LANDMARK = 41
+
+
+def cull_section(args, dist: Dist, peaks: dict, hbm_gbs: float, sc=None) -> dict:
+    """Map culling (map::cull) of the 1M-observation walk as a map at its
+    ground truth, with the cull's other branches made to occur
+    (scenes.cull_map) and both id generators at 0, so that every landmark
+    with observations reaches the error pass (zeroslam itself only looks at
+    the newest 500 landmarks; this is the throughput case): zs_map_cull from
+    host arrays (device time of the kernel, and end to end with the map's
+    host->device copies and the flags' and means' copies back), and
+    zs_ba_cull of the resident walk problem (frames from the resident poses,
+    nothing copied in but the ids). The oracle's C restatement of map::cull,
+    one host thread, is the CPU baseline."""
+    from zeroslam_gb300 import ba, scenes
+
+    sc = sc if sc is not None and sc.name.startswith("walk") else scenes.walk_scene(seed=1)
+    cm = scenes.cull_map(sc, seed=5, truth=True)
+    cm.landmark_id_generator = 0
+    cm.frame_id_generator = 0
+    steps = max(1, args.steps)
+    with ba.BundleAdjuster(precision=ba.FP64, device=dist.local) as h:
+        for _ in range(max(3, args.warmup)):
+            h.map_cull(cm)
+        dist.barrier()
+        dev, wall = [], []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            e, m, rep = h.map_cull(cm)
+            wall.append(time.perf_counter() - t0)
+            dev.append(rep.ms_device)
+        h.set_problem(sc)
+        lid = np.arange(sc.L, dtype=np.int32)
+        fid = np.arange(sc.K, dtype=np.int32)
+        for _ in range(3):
+            h.cull(lid, fid, 0, 0)
+        res = [h.cull(lid, fid, 0, 0)[2].ms_device for _ in range(steps)]
+    ms = dist.max(float(np.median(dev)))
+    e2e_ms = dist.max(float(np.median(wall)) * 1e3)
+    passes = int(rep.error_passes)
+    obs_in_pass = int(sum(int(cm.landmark_obs[l + 1] - cm.landmark_obs[l]) for l in np.flatnonzero(m >= 0)))
+    ops = CULL_FP64_OPS_PER_OBS * obs_in_pass
+    nbytes = CULL_BYTES_PER_OBS * cm.M + CULL_BYTES_PER_LANDMARK * cm.L
+    out = {"workload": f"walk map: F={cm.F} frames, L={cm.L} landmarks, M={cm.M} observations "
+                       f"({passes} landmarks / {obs_in_pass} observations in the error pass)",
+           "ms_device": ms, "landmarks_per_s": dist.world * cm.L / (ms * 1e-3),
+           "e2e": {"ms": e2e_ms, "landmarks_per_s": dist.world * cm.L / (e2e_ms * 1e-3),
+                   "h2d_bytes": int(cm.frame_pose.nbytes + cm.frame_intrinsics.nbytes + 4 * cm.L + 24 * cm.L +
+                                    8 * (cm.L + 1) + 8 * cm.M + 8 * cm.M),
+                   "d2h_bytes": int(5 * cm.L + 32)},
+           "resident_ms_device": dist.max(float(np.median(res))),
+           "erased": int(rep.erased),
+           "fp64": {"ops_per_obs": CULL_FP64_OPS_PER_OBS, "achieved_tops": ops / (ms * 1e-3) / 1e12,
+                    "peak_fma_tflops": peaks.get("fp64_tflops")},
+           "hbm": {"bytes": nbytes, "achieved_gbs": nbytes / (ms * 1e-3) / 1e9, "peak_gbs": hbm_gbs,
+                   "frac": nbytes / (ms * 1e-3) / 1e9 / hbm_gbs}}
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        from oracle.oracle import Oracle
+
+        o = Oracle()
+        t0 = time.perf_counter()
+        e_o, m_o, _ = o.map_cull(cm)
+        cpu_s = time.perf_counter() - t0
+        out["cpu_baseline"] = {"ms": cpu_s * 1e3, "landmarks_per_s": cm.L / cpu_s, "cores": 1, "kind": "port",
+                               "sample": "the whole map, once"}
+        out["parity"] = bool(np.array_equal(e_o, e) and np.array_equal(m_o.view(np.uint32), m.view(np.uint32)))
+    return out
+
+
 def profile_solve(sc, precision: int, iters: int, device: int) -> dict:
     from zeroslam_gb300 import ba
 
@@ -501,6 +580,7 @@ def ours_arm(args, dist: Dist):
     batch = None if args.no_batch else batch_section(args, dist)
     loop = None if args.no_loop else loop_section(args, dist)
     adjoint = None if args.no_adjoint else adjoint_section(args, dist)
+    cull = None if args.no_cull else cull_section(args, dist, peaks, hbm, sc)
 
     prof_m = profile_solve(sc, ba.MIXED, iters, device)
     prof_d = profile_solve(sc, ba.FP64, iters, device)
@@ -557,6 +637,7 @@ def ours_arm(args, dist: Dist):
         "batched_windows": batch,
         "loop_4m": loop,
         "adjoint": adjoint,
+        "map_cull": cull,
     }
     print(json.dumps(line), flush=True)
 
@@ -608,6 +689,16 @@ def main():
         single_solve(args)
         return
     dist = Dist()
+    if args.cull_only:
+        from zeroslam_gb300 import ba
+
+        f64, f32 = ba.pipe_peaks(dist.local)
+        mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        hbm = float(json.load(open(mp)).get("hbm_gbs", 6800.0)) if os.path.exists(mp) else 6800.0
+        out = cull_section(args, dist, {"fp64_tflops": f64, "fp32_tflops": f32}, hbm)
+        if dist.rank == 0:
+            print(json.dumps({"map_cull": out}), flush=True)
+        return
     if args.impl == "reference":
         reference_arm(args, dist)
     else:

@@ -242,6 +242,61 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
 /* Initial damping tau * min(clamp, max diagonal of H) at the current state. */
 int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda);
 
+/* ---- map culling: map::map::cull (source/map.hpp:269-323) ----
+ *
+ * For each landmark, in the reference's order: kept untouched when
+ * id + 500 < landmark_id_generator; erased when it has no observations;
+ * erased when it has at most 4 and the frame id of its last one + 7 <
+ * frame_id_generator; otherwise erased when none of its observations has a
+ * frame in the map, or when the float mean over those that have of
+ * |keypoint - projection| (5.991 where camera::pinhole::project fails) is
+ * >= 5.991. Decisions and means are the reference's bit for bit. The caller
+ * erases the flagged landmarks and their observation lists from its map, as
+ * cull() does. */
+typedef struct zs_map_cull_input {
+    int32_t num_frames;               /* F */
+    const double* frame_pose;         /* [F*12] frame::rotation (row-major 3x3) then frame::translation */
+    const double* frame_intrinsics;   /* [F*4] fx, fy, cx, cy of each frame's camera::pinhole */
+    int32_t num_landmarks;            /* L */
+    const int32_t* landmark_id;       /* [L] landmark::point::id */
+    const double* landmarks;          /* [L*3] landmark::point::location */
+    const int64_t* landmark_obs;      /* [L+1] landmark l's observations are [landmark_obs[l], landmark_obs[l+1]),
+                                         in the order of map::observations[id]; landmark_obs[0] = 0 */
+    const int32_t* obs_frame;         /* [M] index of the observing frame in the frame arrays, or -1 when that
+                                         frame is not in the map */
+    const int32_t* obs_frame_id;      /* [M] id of the observing frame (observation::first) */
+    const float* obs_keypoint;        /* [M*2] keypoint_pyramid[0][kp_index].x, .y of the observing frame */
+    int32_t landmark_id_generator;    /* landmark::point::id_generator */
+    int32_t frame_id_generator;       /* frame::frame::id_generator */
+} zs_map_cull_input;
+
+typedef struct zs_cull_report {
+    int64_t erased;       /* landmarks flagged for erasure */
+    int64_t error_passes; /* landmarks whose mean reprojection error was computed */
+    double ms_device;     /* device time of the cull kernels (CUDA events) */
+} zs_cull_report;
+
+/* Culls a map given as host arrays on h's device (h needs no problem).
+ * erase [L] (1 = erase), mean_error [L] (the mean compared with 5.991, -1
+ * where it is not computed) and rep may each be NULL. Returns ZS_OK, or
+ * ZS_ERR_INVALID for a frame index outside [-1, F) or decreasing ranges.
+ * Replaces map::map::cull, source/map.hpp:269-323. */
+int zs_map_cull(zs_ba_handle* h, const zs_map_cull_input* in, uint8_t* erase, float* mean_error,
+                zs_cull_report* rep);
+
+/* The same cull of the map that h's resident problem holds, at h's current
+ * state, without copying it back: frames are the problem's poses, with the
+ * rotation matrix and translation that map::optimise writes back into them
+ * (source/map.hpp:247-251), observations are the problem's, each landmark's
+ * in the problem's order, and every frame is in the map. landmark_id [L] and
+ * pose_frame_id [K] give the ids. It is map::optimise (every landmark and
+ * observation in the problem) followed by map::cull, with the cull's inputs
+ * never leaving the device. Single problems only (ZS_ERR_UNSUPPORTED after
+ * zs_ba_set_batch). */
+int zs_ba_cull(zs_ba_handle* h, const int32_t* landmark_id, const int32_t* pose_frame_id,
+               int32_t landmark_id_generator, int32_t frame_id_generator, uint8_t* erase, float* mean_error,
+               zs_cull_report* rep);
+
 /* Dense SPD solve on the device with the reference's pivot tests: factors the
  * row-major n x n matrix A = L L^T and solves L L^T x = b. L (n*n, lower, zero
  * above the diagonal) and x may be NULL. precision: ZS_PRECISION_FP64, or

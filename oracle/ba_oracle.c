@@ -622,3 +622,80 @@ out:
     free(delta); free(bk_pose); free(bk_lm);
     return success;
 }
+
+/* ---------------------------------------------------------------- map culling */
+
+/* The reference's cull constants, source/map.hpp:272,281-282,304,316. */
+#define CULL_AGE 500
+#define CULL_FEW_OBS 4
+#define CULL_RECENT 7
+#define CULL_ERROR 5.991f
+
+void zso_pose_rt(const double pose[7], double Rt[12]) {
+    const double q[4] = {pose[6], pose[3], pose[4], pose[5]};
+    qmatrix(q, Rt);
+    Rt[9] = pose[0];
+    Rt[10] = pose[1];
+    Rt[11] = pose[2];
+}
+
+/* One observation's error term of source/map.hpp:290-308: the frame maps the
+ * landmark (R X + t, the summation order of source/matrix.hpp:494-509),
+ * camera::pinhole::project (source/camera.hpp:91-111) and the Euclidean
+ * pixel distance (source/matrix.hpp:177-183) rounded to float; 5.991 when the
+ * point does not project. */
+static float cull_error(const double Rt[12], const double intr[4], const double X[3], const float kp[2]) {
+    double m[3];
+    for (int i = 0; i < 3; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += Rt[3 * i + k] * X[k];
+        m[i] = s + Rt[9 + i];
+    }
+    if (m[2] < 1.0e-12) return CULL_ERROR;
+    const double iz = 1.0 / m[2];
+    const double ux = m[0] * iz, uy = m[1] * iz;
+    const double px = intr[0] * ux + intr[2];
+    const double py = intr[1] * uy + intr[3];
+    const double dx = (double)kp[0] - px, dy = (double)kp[1] - py;
+    double ls = 0.0;
+    ls += dx * dx;
+    ls += dy * dy;
+    return (float)sqrt(ls);
+}
+
+/* map::cull, source/map.hpp:269-323, one landmark at a time. */
+long long zso_map_cull(const zso_cull_map* m, unsigned char* erase, float* mean_error) {
+    long long erased = 0;
+    for (int l = 0; l < m->num_landmarks; ++l) {
+        int e = 0;
+        float mean = -1.0f;
+        if (m->landmark_id[l] + CULL_AGE >= m->landmark_id_generator) {
+            const long long o0 = m->landmark_obs[l], o1 = m->landmark_obs[l + 1];
+            if (o1 <= o0) {
+                e = 1; /* no observations, map.hpp:277-280 and 281-287 */
+            } else if (o1 - o0 <= CULL_FEW_OBS && m->obs_frame_id[o1 - 1] + CULL_RECENT < m->frame_id_generator) {
+                e = 1;
+            } else {
+                float err = 0.0f;
+                long long processed = 0;
+                for (long long o = o0; o < o1; ++o) {
+                    const int f = m->obs_frame[o];
+                    if (f < 0) continue;
+                    err += cull_error(m->frame_pose + 12 * (long long)f, m->frame_intrinsics + 4 * (long long)f,
+                                      m->landmarks + 3 * (long long)l, m->obs_keypoint + 2 * o);
+                    ++processed;
+                }
+                if (processed == 0) {
+                    e = 1;
+                } else {
+                    mean = err / (float)processed;
+                    e = mean >= CULL_ERROR;
+                }
+            }
+        }
+        if (erase) erase[l] = (unsigned char)e;
+        if (mean_error) mean_error[l] = mean;
+        erased += e;
+    }
+    return erased;
+}

@@ -18,6 +18,7 @@
  *   source/matrix_decomposition_cholesky.hpp:26-95
  *   source/lie.hpp:188-204,247-264,284-294,337-362,446-450,521-531
  *   source/camera.hpp:91-142
+ *   source/map.hpp:247-251,269-323   frame write-back and map::cull
  * The reference stores H_pl in a hash map and sums the Schur products in
  * hash-iteration order; this restatement sums per landmark in ascending
  * landmark order, so results agree to rounding, not bit for bit.
@@ -93,6 +94,34 @@ double zso_initial_lambda(const zso_problem* p);
 
 /* Full Levenberg-Marquardt solve; returns the accepted-step count. */
 int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep);
+
+/* Map culling, source/map.hpp:269-323, over a map given as arrays (the layout
+ * of zs_map_cull_input in include/zeroslam_ba.h). */
+typedef struct zso_cull_map {
+    int num_frames;
+    const double* frame_pose;        /* [F*12] rotation (row-major) then translation */
+    const double* frame_intrinsics;  /* [F*4] fx fy cx cy */
+    int num_landmarks;
+    const int* landmark_id;          /* [L] */
+    const double* landmarks;         /* [L*3] */
+    const long long* landmark_obs;   /* [L+1] */
+    const int* obs_frame;            /* [M] frame index or -1 (frame not in the map) */
+    const int* obs_frame_id;         /* [M] */
+    const float* obs_keypoint;       /* [M*2] */
+    int landmark_id_generator;
+    int frame_id_generator;
+} zso_cull_map;
+
+/* erase[l] = 1 when map::cull erases landmark l; mean_error[l] = the float
+ * mean reprojection error it compares with 5.991, or -1 where the error pass
+ * does not run (old landmarks, landmarks erased before it). Either output
+ * may be NULL. Returns the number erased. */
+long long zso_map_cull(const zso_cull_map* m, unsigned char* erase, float* mean_error);
+
+/* Rotation matrix and translation written back to a frame from a
+ * [tx ty tz qx qy qz qw] vertex, source/map.hpp:247-251 with
+ * source/lie.hpp:188-204: Rt = (R row-major, t). */
+void zso_pose_rt(const double pose[7], double Rt[12]);
 
 #ifdef __cplusplus
 }

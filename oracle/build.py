@@ -59,7 +59,8 @@ def build_ref(force: bool = False) -> str | None:
     inc = os.path.join(REFERENCE_ROOT, "source")
     deps = [src] + [os.path.join(inc, f) for f in ("factor_graph.hpp", "camera.hpp", "lie.hpp", "matrix.hpp",
                                                    "matrix_sparse_block.hpp", "matrix_sparse_block_diagonal.hpp",
-                                                   "matrix_decomposition_cholesky.hpp", "math.hpp")]
+                                                   "matrix_decomposition_cholesky.hpp", "math.hpp", "map.hpp",
+                                                   "frame.hpp", "landmark.hpp", "feature.hpp", "image.hpp")]
     if force or _stale(REF_SO, deps):
         os.makedirs(REF_DIR, exist_ok=True)
         tmp = REF_SO + f".{os.getpid()}.tmp"

@@ -75,6 +75,28 @@ class _Arrays:
         return p
 
 
+class _CullMap(C.Structure):
+    _fields_ = [("num_frames", C.c_int), ("frame_pose", _dp), ("frame_intrinsics", _dp),
+                ("num_landmarks", C.c_int), ("landmark_id", _ip), ("landmarks", _dp),
+                ("landmark_obs", C.POINTER(C.c_longlong)), ("obs_frame", _ip), ("obs_frame_id", _ip),
+                ("obs_keypoint", C.POINTER(C.c_float)), ("landmark_id_generator", C.c_int),
+                ("frame_id_generator", C.c_int)]
+
+
+def _cull_arrays(cm) -> dict:
+    return dict(
+        frame_pose=np.ascontiguousarray(cm.frame_pose, dtype=np.float64),
+        frame_intrinsics=np.ascontiguousarray(cm.frame_intrinsics, dtype=np.float64),
+        frame_id=np.ascontiguousarray(cm.frame_id, dtype=np.int32),
+        landmark_id=np.ascontiguousarray(cm.landmark_id, dtype=np.int32),
+        landmarks=np.ascontiguousarray(cm.landmarks, dtype=np.float64),
+        landmark_obs=np.ascontiguousarray(cm.landmark_obs, dtype=np.int64),
+        obs_frame=np.ascontiguousarray(cm.obs_frame, dtype=np.int32),
+        obs_frame_id=np.ascontiguousarray(cm.obs_frame_id, dtype=np.int32),
+        obs_keypoint=np.ascontiguousarray(cm.obs_keypoint, dtype=np.float32),
+    )
+
+
 class Oracle:
     def __init__(self):
         self.lib = C.CDLL(_build.build_oracle())
@@ -99,6 +121,32 @@ class Oracle:
         L.zso_pose_plus.argtypes = [_dp, _dp]
         L.zso_loss.restype = None
         L.zso_loss.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+        L.zso_map_cull.restype = C.c_longlong
+        L.zso_map_cull.argtypes = [C.POINTER(_CullMap), _up, C.POINTER(C.c_float)]
+        L.zso_pose_rt.restype = None
+        L.zso_pose_rt.argtypes = [_dp, _dp]
+
+    def map_cull(self, cm):
+        """map::cull of a ``scenes.CullMap``: (erase uint8 [L], mean error float32 [L], erased)."""
+        a = _cull_arrays(cm)
+        m = _CullMap(a["frame_pose"].shape[0], _ptr(a["frame_pose"], _dp), _ptr(a["frame_intrinsics"], _dp),
+                     a["landmark_id"].shape[0], _ptr(a["landmark_id"], _ip), _ptr(a["landmarks"], _dp),
+                     _ptr(a["landmark_obs"], C.POINTER(C.c_longlong)), _ptr(a["obs_frame"], _ip),
+                     _ptr(a["obs_frame_id"], _ip), _ptr(a["obs_keypoint"], C.POINTER(C.c_float)),
+                     int(cm.landmark_id_generator), int(cm.frame_id_generator))
+        L = a["landmark_id"].shape[0]
+        erase = np.zeros(L, dtype=np.uint8)
+        mean = np.zeros(L, dtype=np.float32)
+        n = self.lib.zso_map_cull(C.byref(m), _ptr(erase, _up), _ptr(mean, C.POINTER(C.c_float)))
+        return erase, mean, int(n)
+
+    def pose_rt(self, poses):
+        """[K, 12] rotation and translation map::optimise writes back from [K, 7] poses."""
+        P = np.ascontiguousarray(poses, dtype=np.float64).reshape(-1, 7)
+        out = np.zeros((P.shape[0], 12))
+        for k in range(P.shape[0]):
+            self.lib.zso_pose_rt(_ptr(P[k], _dp), _ptr(out[k], _dp))
+        return out
 
     def chi2(self, scene) -> float:
         a = _Arrays(scene)
@@ -201,6 +249,34 @@ class Reference:
         L.zsref_pose_plus.argtypes = [_dp, _dp]
         L.zsref_loss.restype = None
         L.zsref_loss.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+        L.zsref_map_cull.restype = C.c_longlong
+        L.zsref_map_cull.argtypes = [C.c_int, _dp, _dp, _ip, C.c_int, _ip, _dp, C.POINTER(C.c_longlong), _ip, _ip,
+                                     C.POINTER(C.c_float), C.c_int, C.c_int, _up, _dp]
+        L.zsref_pose_rt.restype = None
+        L.zsref_pose_rt.argtypes = [_dp, _dp]
+
+    def map_cull(self, cm, timing: bool = False):
+        """Which landmarks zeroslam's map::cull erases from the map of a
+        ``scenes.CullMap``: (erase uint8 [L], erased[, seconds cull() took])."""
+        a = _cull_arrays(cm)
+        L = a["landmark_id"].shape[0]
+        erase = np.zeros(L, dtype=np.uint8)
+        secs = C.c_double(0.0)
+        n = self.lib.zsref_map_cull(a["frame_pose"].shape[0], _ptr(a["frame_pose"], _dp),
+                                    _ptr(a["frame_intrinsics"], _dp), _ptr(a["frame_id"], _ip), L,
+                                    _ptr(a["landmark_id"], _ip), _ptr(a["landmarks"], _dp),
+                                    _ptr(a["landmark_obs"], C.POINTER(C.c_longlong)), _ptr(a["obs_frame"], _ip),
+                                    _ptr(a["obs_frame_id"], _ip), _ptr(a["obs_keypoint"], C.POINTER(C.c_float)),
+                                    int(cm.landmark_id_generator), int(cm.frame_id_generator), _ptr(erase, _up),
+                                    C.byref(secs))
+        return (erase, int(n), secs.value) if timing else (erase, int(n))
+
+    def pose_rt(self, poses):
+        P = np.ascontiguousarray(poses, dtype=np.float64).reshape(-1, 7)
+        out = np.zeros((P.shape[0], 12))
+        for k in range(P.shape[0]):
+            self.lib.zsref_pose_rt(_ptr(P[k], _dp), _ptr(out[k], _dp))
+        return out
 
     @staticmethod
     def available() -> bool:

@@ -4,9 +4,11 @@
 // unmodified reference headers (source/factor_graph.hpp, camera.hpp, lie.hpp,
 // matrix*.hpp) into oracle/_ref/. It is used to pin the C restatement
 // (ba_oracle.c), to write the golden fixtures under tests/golden/, and as the
-// timed CPU baseline. Only the reference's public API is used.
+// timed CPU baseline. Only the reference's public API is used. zsref_map_cull
+// runs map::map::cull (source/map.hpp:269-323) on a map assembled from arrays.
 #include "factor_graph.hpp"
 #include "camera.hpp"
+#include "map.hpp"
 
 #include <chrono>
 #include <cstring>
@@ -158,6 +160,74 @@ void zsref_loss(int kind, double delta, double e2, double* rho3) {
     else if (kind == 3) factor_graph::loss_tukey(delta).compute(e2, rho);
     else factor_graph::loss_trivial().compute(e2, rho);
     for (int i = 0; i < 3; ++i) rho3[i] = rho[i];
+}
+
+// Assembles a map::map from arrays (frame f: id frame_id[f], rotation and
+// translation frame_pose[12 f..], camera frame_intr[4 f..], one keypoint per
+// observation it makes; observations whose obs_frame is -1 name a frame id
+// that is not in the map), sets both id generators, runs cull() and reports
+// which landmarks it erased (and, in cull_seconds, how long cull() took).
+// Landmarks without observations get an empty
+// observation list when their index is odd and none when it is even, so both
+// of cull()'s branches for them run.
+long long zsref_map_cull(int F, const double* frame_pose, const double* frame_intr, const int* frame_id, int L,
+                         const int* landmark_id, const double* lms, const long long* lm_obs, const int* obs_frame,
+                         const int* obs_frame_id, const float* obs_kp, int lm_gen, int frame_gen,
+                         unsigned char* erase, double* cull_seconds) {
+    map::map m;
+    std::vector<frame::frame> frames(static_cast<size_t>(F));
+    for (int f = 0; f < F; ++f) {
+        frame::frame& fr = frames[static_cast<size_t>(f)];
+        fr.id = frame_id[f];
+        for (int i = 0; i < 3; ++i) {
+            for (int k = 0; k < 3; ++k) fr.rotation[i][k] = frame_pose[12 * f + 3 * i + k];
+            fr.translation[i] = frame_pose[12 * f + 9 + i];
+        }
+        fr.camera = camera::pinhole(frame_intr + 4 * f, 4);
+        fr.keypoint_pyramid.resize(1);
+    }
+    std::vector<size_t> kp_index(static_cast<size_t>(lm_obs[L]), 0);
+    for (long long o = 0; o < lm_obs[L]; ++o) {
+        const int f = obs_frame[o];
+        if (f < 0) continue;
+        std::vector<feature::point>& kps = frames[static_cast<size_t>(f)].keypoint_pyramid[0];
+        kp_index[static_cast<size_t>(o)] = kps.size();
+        kps.push_back(feature::point{obs_kp[2 * o], obs_kp[2 * o + 1], 0.0f, 0.0f});
+    }
+    for (int f = 0; f < F; ++f) m.add_frame(frames[static_cast<size_t>(f)]);
+    for (int l = 0; l < L; ++l) {
+        landmark::point p;
+        p.id = landmark_id[l];
+        for (int i = 0; i < 3; ++i) p.location[i] = lms[3 * l + i];
+        m.add_landmark(p);
+        if (lm_obs[l + 1] == lm_obs[l] && (l & 1)) m.observations[p.id];
+        for (long long o = lm_obs[l]; o < lm_obs[l + 1]; ++o)
+            m.observations[p.id].push_back({obs_frame_id[o], kp_index[static_cast<size_t>(o)]});
+    }
+    landmark::point::id_generator = lm_gen;
+    frame::frame::id_generator = frame_gen;
+    const auto t0 = std::chrono::steady_clock::now();
+    m.cull();
+    const auto t1 = std::chrono::steady_clock::now();
+    if (cull_seconds) *cull_seconds = std::chrono::duration<double>(t1 - t0).count();
+    long long erased = 0;
+    for (int l = 0; l < L; ++l) {
+        erase[l] = m.landmarks.count(landmark_id[l]) == 0 ? 1 : 0;
+        erased += erase[l];
+    }
+    return erased;
+}
+
+// The rotation and translation map::optimise writes back to a frame from a
+// vertex_pose (source/map.hpp:247-251).
+void zsref_pose_rt(const double* pose7, double* Rt) {
+    const lie::se3<double> v(lie::so3<double>(pose7[6], pose7[3], pose7[4], pose7[5]),
+                             matrix::matrix<double, 3, 1>{{pose7[0], pose7[1], pose7[2]}});
+    const matrix::matrix<double, 3, 3> R = v.rotation().get_matrix();
+    for (int i = 0; i < 3; ++i) {
+        for (int k = 0; k < 3; ++k) Rt[3 * i + k] = R[i][k];
+        Rt[9 + i] = v.translation()[i];
+    }
 }
 
 }  // extern "C"

@@ -31,6 +31,45 @@ def scene_from_npz(d: dict, name: str = "golden"):
 
 
 SOLVE_FIXTURES = sorted(f for f in os.listdir(GOLDEN) if f.startswith("solve_") and f.endswith(".npz"))
+CULL_FIXTURES = sorted(f for f in os.listdir(GOLDEN) if f.startswith("cull_") and f.endswith(".npz"))
+
+
+def cull_from_npz(d: dict):
+    from zeroslam_gb300.scenes import CullMap
+
+    return CullMap(**{f: (d[f] if d[f].ndim else d[f].item()) for f in CullMap.__dataclass_fields__})
+
+
+def known_answer_cull_maps():
+    """The two cull cases of tests/map.test.cpp, as (name, map, erase):
+    :128-143, a landmark at the origin seen once by a default frame (zero
+    rotation and translation, so the point does not project) with the
+    keypoint (0, 0), is erased, under generator values that reach the error
+    pass (0, 0) and that reach the age rule (0, 100); :154-164, a landmark
+    (id 42) without observations is erased. Also: the same landmark seen by a
+    frame at the identity, keypoint on its projection (kept), and with an id
+    older than the newest 500 (kept without a look)."""
+    from zeroslam_gb300.scenes import CullMap
+
+    def one(R, kp, lm_id, lm_gen, frame_gen, X=(0.0, 0.0, 0.0), nobs=1):
+        return CullMap(frame_pose=np.array([list(R) + [0.0, 0.0, 0.0]]),
+                       frame_intrinsics=np.array([[1.0, 1.0, 0.5, 0.5]]),  # camera::pinhole() (camera.hpp:61-64)
+                       frame_id=np.array([0], dtype=np.int32), landmark_id=np.array([lm_id], dtype=np.int32),
+                       landmarks=np.array([X], dtype=np.float64),
+                       landmark_obs=np.array([0, nobs], dtype=np.int64),
+                       obs_frame=np.zeros(nobs, dtype=np.int32), obs_frame_id=np.zeros(nobs, dtype=np.int32),
+                       obs_keypoint=np.array([kp] * nobs, dtype=np.float32).reshape(nobs, 2),
+                       landmark_id_generator=lm_gen, frame_id_generator=frame_gen)
+
+    zero = [0.0] * 9
+    eye = [1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0]
+    return [
+        ("map_test_128_error_pass", one(zero, (0.0, 0.0), 0, 0, 0), 1),
+        ("map_test_128_age_rule", one(zero, (0.0, 0.0), 0, 0, 100), 1),
+        ("map_test_154_no_observations", one(zero, (0.0, 0.0), 42, 43, 0, nobs=0), 1),
+        ("projects_onto_keypoint", one(eye, (0.6, 0.7), 0, 0, 0, X=(0.1, 0.2, 1.0)), 0),
+        ("older_than_500", one(zero, (0.0, 0.0), 0, 501, 0), 0),
+    ]
 
 
 @pytest.fixture(scope="session")

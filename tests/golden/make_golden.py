@@ -16,6 +16,9 @@ Fixtures:
   pose_plus.npz    vertex_pose::plus (source/factor_graph.hpp:947-960)
   solve_*.npz      factor_graph::solve on whole problems: state before and after,
                    chi2 before / after and the accepted-step count
+  cull_*.npz       map::cull (source/map.hpp:269-323) on array maps: inputs and
+                   the landmarks it erased; the frame rotations and translations
+                   map::optimise writes back from vertex poses (map.hpp:247-251)
 """
 
 from __future__ import annotations
@@ -215,8 +218,23 @@ def write_solve(ref: Reference, name: str, sc: scenes.Scene, iterations: int, us
     print(f"solve_{name}: K={sc.K} L={sc.L} M={sc.M} accepted={acc} chi2 {c0:.6g} -> {c1:.6g}")
 
 
+def write_cull(ref: Reference):
+    """map::cull (source/map.hpp:269-323) on maps with every branch made to
+    occur (scenes.cull_map), and the frame rotations map::optimise writes
+    back (source/map.hpp:247-251)."""
+    for name, (K, L, seed) in {"arc": (8, 600, 61), "arc_b": (10, 900, 62)}.items():
+        sc = scenes.arc_scene(K, L, seed=seed)
+        cm = scenes.cull_map(sc, seed=seed, truth=True)
+        erase, n = ref.map_cull(cm)
+        d = {f: getattr(cm, f) for f in cm.__dataclass_fields__}
+        d.update(ref_erase=erase, pose=sc.poses, pose_rt=ref.pose_rt(sc.poses))
+        np.savez_compressed(os.path.join(HERE, f"cull_{name}.npz"), **d)
+        print(f"cull_{name}: F={cm.F} L={cm.L} M={cm.M} erased={n}")
+
+
 def main():
     ref = Reference()
+    write_cull(ref)
     rng = np.random.default_rng(20261203)
     write_edges(ref, rng)
     write_losses(ref)

@@ -4,7 +4,8 @@ tests/golden/ (written by tests/golden/make_golden.py from the reference)."""
 import numpy as np
 import pytest
 
-from conftest import SOLVE_FIXTURES, cost_tol, load_npz, rel_err, scene_from_npz, state_tol
+from conftest import (CULL_FIXTURES, SOLVE_FIXTURES, cost_tol, cull_from_npz, known_answer_cull_maps, load_npz,
+                      rel_err, scene_from_npz, state_tol)
 
 
 def test_edge_literals(oracle):
@@ -90,3 +91,26 @@ def test_solve_matches_reference(oracle, name):
         assert err1 < err0
     if name == "solve_negative_information.npz":
         assert np.all(np.isfinite(poses))
+
+
+@pytest.mark.parametrize("name", CULL_FIXTURES)
+def test_map_cull_matches_reference(oracle, name):
+    """map::cull decisions (source/map.hpp:269-323), landmark for landmark."""
+    g = load_npz(name)
+    cm = cull_from_npz(g)
+    erase, mean, n = oracle.map_cull(cm)
+    assert np.array_equal(erase, g["ref_erase"])
+    assert n == int(g["ref_erase"].sum())
+    ev = mean >= 0
+    # the fixture reaches every branch, and means on both sides of 5.991
+    assert (~ev & (erase == 0)).any() and (~ev & (erase == 1)).any()
+    assert (ev & (erase == 0)).any() and (ev & (erase == 1)).any()
+    assert (mean == np.float32(5.991)).any()
+    assert np.array_equal(oracle.pose_rt(g["pose"]), g["pose_rt"])
+
+
+@pytest.mark.parametrize("case", known_answer_cull_maps(), ids=lambda c: c[0])
+def test_map_cull_known_answers(oracle, case):
+    _, cm, want = case
+    erase, _, n = oracle.map_cull(cm)
+    assert int(erase[0]) == want and n == want

@@ -54,3 +54,20 @@ def test_random_cholesky_and_invert(oracle, reference):
     for _ in range(20):
         A = rng.normal(size=(3, 3))
         assert np.array_equal(oracle.invert3(A)[1], reference.invert3(A)[1])
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_map_cull_parity(oracle, reference, seed):
+    """map::cull run live on maps built by scenes.cull_map (every branch
+    made to occur) and on a plain walk map, against the restatement."""
+    from conftest import known_answer_cull_maps
+
+    sc = scenes.arc_scene(12, 1500, seed=70 + seed)
+    for cm in (scenes.cull_map(sc, seed=seed, truth=True), scenes.cull_map(sc, seed=seed)):
+        e, _, n = oracle.map_cull(cm)
+        er, nr = reference.map_cull(cm)
+        assert np.array_equal(e, er) and n == nr
+    for _, cm, want in known_answer_cull_maps():
+        er, nr = reference.map_cull(cm)
+        assert int(er[0]) == want
+    assert np.array_equal(oracle.pose_rt(sc.poses), reference.pose_rt(sc.poses))

@@ -83,6 +83,18 @@ class AdjointReport(C.Structure):
                 ("ms_total", C.c_double)]
 
 
+class MapCullInput(C.Structure):
+    _fields_ = [("num_frames", C.c_int32), ("frame_pose", _dp), ("frame_intrinsics", _dp),
+                ("num_landmarks", C.c_int32), ("landmark_id", _ip), ("landmarks", _dp),
+                ("landmark_obs", C.POINTER(C.c_int64)), ("obs_frame", _ip), ("obs_frame_id", _ip),
+                ("obs_keypoint", C.POINTER(C.c_float)), ("landmark_id_generator", C.c_int32),
+                ("frame_id_generator", C.c_int32)]
+
+
+class CullReport(C.Structure):
+    _fields_ = [("erased", C.c_int64), ("error_passes", C.c_int64), ("ms_device", C.c_double)]
+
+
 class ZsError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
@@ -100,7 +112,8 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
-                 "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile")
+                 "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
+                 "zs_ba_cull")
 
 
 def library_path() -> str:
@@ -158,6 +171,12 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_ba_get_window_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
     lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
+    lib.zs_map_cull.restype = C.c_int
+    lib.zs_map_cull.argtypes = [C.c_void_p, C.POINTER(MapCullInput), _up, C.POINTER(C.c_float),
+                                C.POINTER(CullReport)]
+    lib.zs_ba_cull.restype = C.c_int
+    lib.zs_ba_cull.argtypes = [C.c_void_p, _ip, _ip, C.c_int32, C.c_int32, _up, C.POINTER(C.c_float),
+                               C.POINTER(CullReport)]
     _LIB = lib
     return lib
 
@@ -341,6 +360,38 @@ class BundleAdjuster:
             raise ZsError(st, "zs_ba_adjoint")
         return (duv, dint, rep, v) if want_state else (duv, dint, rep)
 
+    def cull(self, landmark_id, pose_frame_id, landmark_id_generator: int, frame_id_generator: int):
+        """map::cull of the resident problem at the current state (zs_ba_cull):
+        (erase uint8 [L], mean error float32 [L], CullReport)."""
+        lid = np.ascontiguousarray(landmark_id, dtype=np.int32)
+        fid = np.ascontiguousarray(pose_frame_id, dtype=np.int32)
+        if lid.shape != (self.L,) or fid.shape != (self.K,):
+            raise ValueError("landmark_id must have L entries and pose_frame_id K")
+        erase = np.zeros(self.L, dtype=np.uint8)
+        mean = np.zeros(self.L, dtype=np.float32)
+        rep = CullReport()
+        st = self.lib.zs_ba_cull(self.h, _p(lid, _ip), _p(fid, _ip), int(landmark_id_generator),
+                                 int(frame_id_generator), _p(erase, _up), _p(mean, C.POINTER(C.c_float)),
+                                 C.byref(rep))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_cull")
+        return erase, mean, rep
+
+    def map_cull(self, cm):
+        """map::cull of a map given as arrays (zs_map_cull, ``scenes.CullMap``):
+        (erase uint8 [L], mean error float32 [L], CullReport)."""
+        inp, keep = cull_input(cm)
+        L = inp.num_landmarks
+        erase = np.zeros(L, dtype=np.uint8)
+        mean = np.zeros(L, dtype=np.float32)
+        rep = CullReport()
+        st = self.lib.zs_map_cull(self.h, C.byref(inp), _p(erase, _up), _p(mean, C.POINTER(C.c_float)),
+                                  C.byref(rep))
+        del keep
+        if st != ZS_OK:
+            raise ZsError(st, "zs_map_cull")
+        return erase, mean, rep
+
     def linear_step(self, lam: float, want_S: bool = True) -> dict:
         n = 6 * self.K
         S = np.zeros((n, n)) if want_S else None
@@ -351,6 +402,35 @@ class BundleAdjuster:
         if st not in (ZS_OK, ZS_ERR_CHOLESKY):
             raise ZsError(st, "zs_ba_linear_step")
         return dict(ok=(st == ZS_OK), S=S, bs=bs, delta=delta, b=b)
+
+
+def cull_input(cm):
+    """A MapCullInput over the arrays of a ``scenes.CullMap``; returns
+    (input, arrays that must stay alive while it is used)."""
+    k = dict(
+        frame_pose=np.ascontiguousarray(cm.frame_pose, dtype=np.float64),
+        frame_intrinsics=np.ascontiguousarray(cm.frame_intrinsics, dtype=np.float64),
+        landmark_id=np.ascontiguousarray(cm.landmark_id, dtype=np.int32),
+        landmarks=np.ascontiguousarray(cm.landmarks, dtype=np.float64),
+        landmark_obs=np.ascontiguousarray(cm.landmark_obs, dtype=np.int64),
+        obs_frame=np.ascontiguousarray(cm.obs_frame, dtype=np.int32),
+        obs_frame_id=np.ascontiguousarray(cm.obs_frame_id, dtype=np.int32),
+        obs_keypoint=np.ascontiguousarray(cm.obs_keypoint, dtype=np.float32),
+    )
+    inp = MapCullInput()
+    inp.num_frames = k["frame_pose"].shape[0]
+    inp.frame_pose = _p(k["frame_pose"], _dp)
+    inp.frame_intrinsics = _p(k["frame_intrinsics"], _dp)
+    inp.num_landmarks = k["landmark_id"].shape[0]
+    inp.landmark_id = _p(k["landmark_id"], _ip)
+    inp.landmarks = _p(k["landmarks"], _dp)
+    inp.landmark_obs = _p(k["landmark_obs"], C.POINTER(C.c_int64))
+    inp.obs_frame = _p(k["obs_frame"], _ip)
+    inp.obs_frame_id = _p(k["obs_frame_id"], _ip)
+    inp.obs_keypoint = _p(k["obs_keypoint"], C.POINTER(C.c_float))
+    inp.landmark_id_generator = int(cm.landmark_id_generator)
+    inp.frame_id_generator = int(cm.frame_id_generator)
+    return inp, k
 
 
 def dense_cholesky_solve(A, b, precision: int = FP64):

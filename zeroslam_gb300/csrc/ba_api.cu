@@ -362,6 +362,8 @@ struct zs_ba_handle {
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
     HostScratch hscratch;        // build_problem's host arrays (pinned, reused)
+    void* cull_buf = nullptr;    // map culling's device arrays (handle lifetime, grown on demand)
+    size_t cull_cap = 0;
     // batched windows
     bool batch = false;
     BatchDev B;
@@ -404,6 +406,63 @@ struct zs_ba_handle {
         has_problem = false;
     }
 };
+
+// Carves map culling's device arrays out of one handle-owned buffer.
+struct CullCarve {
+    char* base;
+    size_t off = 0;
+    explicit CullCarve(void* b) : base(static_cast<char*>(b)) {}
+    template <typename T>
+    T* take(size_t count) {
+        T* p = reinterpret_cast<T*>(base + off);
+        off += (count * sizeof(T) + 255) & ~size_t(255);
+        return p;
+    }
+    template <typename T>
+    static size_t bytes(size_t count) { return (count * sizeof(T) + 255) & ~size_t(255); }
+};
+
+static void cull_reserve(zs_ba_handle* h, size_t bytes) {
+    if (bytes <= h->cull_cap) return;
+    if (h->cull_buf) {
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+        ZS_CUDA(cudaFree(h->cull_buf));
+        h->cull_buf = nullptr;
+        h->cull_cap = 0;
+    }
+    const size_t cap = std::max(bytes, h->cull_cap + h->cull_cap / 2);
+    ZS_CUDA(cudaMalloc(&h->cull_buf, cap));
+    h->cull_cap = cap;
+}
+
+// Runs k_cull (after `pre`, which enqueues the inputs' copies and any kernel
+// they need), copies the outputs back and fills the report.
+template <typename Pre, typename Launch>
+static int cull_run(zs_ba_handle* h, CullArgs& a, uint8_t* erase, float* mean_error, zs_cull_report* rep,
+                    Pre&& pre, Launch&& launch) {
+    ZS_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), h->stream));
+    pre();
+    ZS_CUDA(cudaEventRecord(h->ev0, h->stream));
+    launch();
+    ZS_CUDA(cudaGetLastError());
+    ZS_CUDA(cudaEventRecord(h->ev1, h->stream));
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    if (erase && a.L > 0)
+        ZS_CUDA(cudaMemcpyAsync(erase, a.erase, (size_t)a.L, cudaMemcpyDeviceToHost, h->stream));
+    if (mean_error && a.L > 0)
+        ZS_CUDA(cudaMemcpyAsync(mean_error, a.mean, sizeof(float) * (size_t)a.L, cudaMemcpyDeviceToHost, h->stream));
+    ZS_CUDA(cudaMemcpyAsync(cnt, a.counters, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream));
+    ZS_CUDA(cudaStreamSynchronize(h->stream));
+    if (cnt[2]) return ZS_ERR_INVALID;
+    if (rep) {
+        float ms = 0.f;
+        ZS_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        rep->erased = (int64_t)cnt[0];
+        rep->error_passes = (int64_t)cnt[1];
+        rep->ms_device = ms;
+    }
+    return ZS_OK;
+}
 
 extern "C" {
 
@@ -492,6 +551,7 @@ void zs_ba_destroy(zs_ba_handle* h) {
     h->timer.destroy();
     h->release_problem();
     h->hscratch.release();
+    if (h->cull_buf) cudaFree(h->cull_buf);
     if (h->st) cudaFree(h->st);
     if (h->st_host) cudaFreeHost(h->st_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1239,6 +1299,122 @@ int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda) {
         return cuda_status(e.err);
     }
     return ZS_OK;
+}
+
+int zs_map_cull(zs_ba_handle* h, const zs_map_cull_input* in, uint8_t* erase, float* mean_error,
+                zs_cull_report* rep) {
+    if (!h || !in) return ZS_ERR_INVALID;
+    const int F = in->num_frames, L = in->num_landmarks;
+    if (F < 0 || L < 0) return ZS_ERR_INVALID;
+    if (L > 0 && (!in->landmark_id || !in->landmarks || !in->landmark_obs)) return ZS_ERR_INVALID;
+    if (F > 0 && (!in->frame_pose || !in->frame_intrinsics)) return ZS_ERR_INVALID;
+    const int64_t M = L > 0 ? in->landmark_obs[L] : 0;
+    if (L > 0 && (in->landmark_obs[0] != 0 || M < 0)) return ZS_ERR_INVALID;
+    if (M > 0 && (!in->obs_frame || !in->obs_frame_id || !in->obs_keypoint)) return ZS_ERR_INVALID;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        using C = CullCarve;
+        cull_reserve(h, C::bytes<unsigned long long>(4) + C::bytes<double>(12 * (size_t)F) +
+                            C::bytes<double>(4 * (size_t)F) + C::bytes<int32_t>(L) + C::bytes<double>(3 * (size_t)L) +
+                            C::bytes<int64_t>((size_t)L + 1) + 2 * C::bytes<int32_t>((size_t)M) +
+                            C::bytes<float2>((size_t)M) + C::bytes<uint8_t>(L) + C::bytes<float>(L));
+        C c(h->cull_buf);
+        CullArgs a;
+        a.L = L;
+        a.F = F;
+        a.M = M;
+        a.counters = c.take<unsigned long long>(4);
+        double* Rt = c.take<double>(12 * (size_t)F);
+        double* intr = c.take<double>(4 * (size_t)F);
+        int32_t* lm_id = c.take<int32_t>(L);
+        double* lm = c.take<double>(3 * (size_t)L);
+        int64_t* obs_ptr = c.take<int64_t>((size_t)L + 1);
+        int32_t* obs_frame = c.take<int32_t>((size_t)M);
+        int32_t* obs_frame_id = c.take<int32_t>((size_t)M);
+        float2* kp = c.take<float2>((size_t)M);
+        a.erase = c.take<uint8_t>(L);
+        a.mean = c.take<float>(L);
+        a.Rt = Rt;
+        a.intr = intr;
+        a.intr_stride = 4;
+        a.lm = lm;
+        a.lm_stride = 3;
+        a.lm_id = lm_id;
+        a.obs_frame = obs_frame;
+        a.obs_frame_id = obs_frame_id;
+        a.lm_gen = in->landmark_id_generator;
+        a.frame_gen = in->frame_id_generator;
+        auto h2d = [&](void* d, const void* src, size_t bytes) {
+            if (bytes) ZS_CUDA(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, h->stream));
+        };
+        return cull_run(h, a, erase, mean_error, rep, [&] {
+            h2d(Rt, in->frame_pose, sizeof(double) * 12 * (size_t)F);
+            h2d(intr, in->frame_intrinsics, sizeof(double) * 4 * (size_t)F);
+            h2d(lm_id, in->landmark_id, sizeof(int32_t) * (size_t)L);
+            h2d(lm, in->landmarks, sizeof(double) * 3 * (size_t)L);
+            if (L > 0) h2d(obs_ptr, in->landmark_obs, sizeof(int64_t) * ((size_t)L + 1));
+            h2d(obs_frame, in->obs_frame, sizeof(int32_t) * (size_t)M);
+            h2d(obs_frame_id, in->obs_frame_id, sizeof(int32_t) * (size_t)M);
+            h2d(kp, in->obs_keypoint, sizeof(float2) * (size_t)M);
+        }, [&] { launch_cull(a, obs_ptr, kp, h->stream); });
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+}
+
+int zs_ba_cull(zs_ba_handle* h, const int32_t* landmark_id, const int32_t* pose_frame_id,
+               int32_t landmark_id_generator, int32_t frame_id_generator, uint8_t* erase, float* mean_error,
+               zs_cull_report* rep) {
+    if (!h) return ZS_ERR_INVALID;
+    if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
+    if (h->batch) return ZS_ERR_UNSUPPORTED;
+    const DevProblem& P = h->P;
+    if ((P.L > 0 && !landmark_id) || (P.K > 0 && !pose_frame_id)) return ZS_ERR_INVALID;
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        using C = CullCarve;
+        cull_reserve(h, C::bytes<unsigned long long>(4) + C::bytes<double>(12 * (size_t)P.K) +
+                            C::bytes<double>(4) + C::bytes<int32_t>(P.L) + C::bytes<int32_t>(P.K) +
+                            C::bytes<uint8_t>(P.L) + C::bytes<float>(P.L));
+        C c(h->cull_buf);
+        CullArgs a;
+        a.L = P.L;
+        a.F = P.K;
+        a.M = P.M;
+        a.counters = c.take<unsigned long long>(4);
+        double* Rt = c.take<double>(12 * (size_t)P.K);
+        double* intr = c.take<double>(4);
+        int32_t* lm_id = c.take<int32_t>(P.L);
+        int32_t* frame_id = c.take<int32_t>(P.K);
+        a.erase = c.take<uint8_t>(P.L);
+        a.mean = c.take<float>(P.L);
+        a.Rt = Rt;
+        a.intr = intr;
+        a.intr_stride = 0;
+        a.lm = P.lm;
+        a.lm_stride = kLmStride;
+        a.lm_id = lm_id;
+        a.obs_frame = P.obs_pose;
+        a.obs_frame_id = nullptr;
+        a.frame_id = frame_id;
+        a.lm_gen = landmark_id_generator;
+        a.frame_gen = frame_id_generator;
+        const double in4[4] = {P.intr.fx, P.intr.fy, P.intr.cx, P.intr.cy};
+        return cull_run(h, a, erase, mean_error, rep, [&] {
+            ZS_CUDA(cudaMemcpyAsync(intr, in4, sizeof(in4), cudaMemcpyHostToDevice, h->stream));
+            if (P.L > 0)
+                ZS_CUDA(cudaMemcpyAsync(lm_id, landmark_id, sizeof(int32_t) * (size_t)P.L, cudaMemcpyHostToDevice,
+                                        h->stream));
+            if (P.K > 0)
+                ZS_CUDA(cudaMemcpyAsync(frame_id, pose_frame_id, sizeof(int32_t) * (size_t)P.K,
+                                        cudaMemcpyHostToDevice, h->stream));
+        }, [&] {
+            launch_pose_rt(P.K, P.pose, Rt, h->stream);
+            launch_cull(a, P.lm_ptr, P.obs_uv, h->stream);
+        });
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
 }
 
 int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b) {

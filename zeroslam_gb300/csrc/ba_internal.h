@@ -273,6 +273,36 @@ void launch_adj_dot(int64_t N, const double* x, const double* y, double* red, cu
 void launch_adj_copy(int64_t N, const double* src, double* dst, cudaStream_t s);
 void launch_adj_out(const DevProblem& P, const double* rec, const double* v, double* duv, double* red, cudaStream_t s);
 
+// ---- map culling (ba_cull.cu) ----
+// Inputs of k_cull: L landmarks (lm, lm_stride doubles apart, ids lm_id),
+// their observations (ranges obs_ptr, frame index obs_frame, -1 when the
+// frame is not in the map), F frames (Rt: 12 doubles each, rotation then
+// translation; intrinsics intr, intr_stride doubles apart: 4 per frame or 0
+// for one camera) and the frame id of each observation (obs_frame_id) or of
+// each frame (frame_id, used when obs_frame_id is null). Outputs: erase[L],
+// mean[L] (-1 where no error pass runs) and counters (erased, error passes,
+// invalid input), which the caller zeroes.
+struct CullArgs {
+    int L = 0, F = 0;
+    int64_t M = 0;  // observations: every range must lie in [0, M]
+    const double* Rt = nullptr;
+    const double* intr = nullptr;
+    int intr_stride = 0;
+    const double* lm = nullptr;
+    int lm_stride = 3;
+    const int32_t* lm_id = nullptr;
+    const int32_t* obs_frame = nullptr;
+    const int32_t* obs_frame_id = nullptr;
+    const int32_t* frame_id = nullptr;
+    int32_t lm_gen = 0, frame_gen = 0;
+    uint8_t* erase = nullptr;
+    float* mean = nullptr;
+    unsigned long long* counters = nullptr;
+};
+void launch_pose_rt(int K, const double* pose, double* Rt, cudaStream_t s);
+void launch_cull(const CullArgs& a, const int64_t* obs_ptr, const float2* kp, cudaStream_t s);
+void launch_cull(const CullArgs& a, const int32_t* obs_ptr, const double2* kp, cudaStream_t s);
+
 // ---- dense reduced system (ba_cholesky.cu) ----
 // launch_factor: S (n x n row-major, type TS) -> F = L (lower, type TF) and
 // D = the inverses of L's 32 x 32 diagonal blocks ([ceil(n/32) * 1024] TF);

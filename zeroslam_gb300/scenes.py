@@ -476,3 +476,118 @@ def adjoint_scene(K: int = 50, L: int = 10000, seed: int = 3) -> Scene:
 
 def loop_large_scene(seed: int = 4) -> Scene:
     return loop_scene(seed=seed)
+
+
+# ---------------------------------------------------------------- map culling
+
+@dataclass
+class CullMap:
+    """A zeroslam map as the arrays of ``zs_map_cull_input`` (include/zeroslam_ba.h):
+    frames (rotation and translation [F, 12], intrinsics [F, 4], ids [F]),
+    landmarks (ids [L], locations [L, 3]), each landmark's observations in
+    order (ranges ``landmark_obs`` [L+1]; observing frame index, -1 for a
+    frame not in the map; observing frame id; float32 keypoint [M, 2]) and
+    the two id generators."""
+    frame_pose: np.ndarray
+    frame_intrinsics: np.ndarray
+    frame_id: np.ndarray
+    landmark_id: np.ndarray
+    landmarks: np.ndarray
+    landmark_obs: np.ndarray
+    obs_frame: np.ndarray
+    obs_frame_id: np.ndarray
+    obs_keypoint: np.ndarray
+    landmark_id_generator: int
+    frame_id_generator: int
+
+    @property
+    def F(self) -> int:
+        return int(self.frame_pose.shape[0])
+
+    @property
+    def L(self) -> int:
+        return int(self.landmarks.shape[0])
+
+    @property
+    def M(self) -> int:
+        return int(self.obs_frame.shape[0])
+
+
+def frames_from_poses(poses: np.ndarray) -> np.ndarray:
+    """[K, 12] rotation (row-major) and translation of [K, 7] poses."""
+    q, t = unpack_poses(poses)
+    R = quat_to_matrix(q)
+    return np.ascontiguousarray(np.concatenate([R.reshape(-1, 9), t], axis=1))
+
+
+def cull_map(sc: Scene, seed: int = 0, frame_pose: np.ndarray | None = None, plain: bool = False,
+             truth: bool = False) -> CullMap:
+    """The map of a scene at its current state (``truth``: at its ground
+    truth, where the pixel errors are the observation noise), for map culling.
+
+    Each landmark's observations keep the scene's order. ``plain`` gives the
+    scene itself: every frame in the map, the scene's pixels rounded to
+    float32 (zeroslam's keypoints are float), one camera, every landmark and
+    frame recent. Otherwise every branch of the cull is made to occur, in
+    proportions drawn from ``seed``: half the landmark ids older than the
+    newest 500; landmarks cut to 1-4 observations, a frame id generator that
+    leaves most frames older than the newest 7; landmarks without
+    observations; observations whose frame is not in the map (and landmarks
+    with no frame in the map at all); landmarks moved behind a camera that
+    sees them; keypoints shifted by up to 10 px so that the mean errors
+    straddle 5.991; and intrinsics that differ between frames.
+    ``frame_pose`` overrides the frames' rotations and translations."""
+    K, L = sc.K, sc.L
+    order = np.argsort(sc.obs_landmark, kind="stable")
+    obs_lm = sc.obs_landmark[order].astype(np.int64)
+    obs_pose = sc.obs_pose[order].astype(np.int32)
+    uv = sc.obs_uv[order].astype(np.float64)
+    poses = sc.gt_poses if truth else sc.poses
+    X = np.array(sc.gt_landmarks if truth else sc.landmarks, dtype=np.float64, copy=True)
+    Rt = frames_from_poses(poses) if frame_pose is None else np.ascontiguousarray(frame_pose, dtype=np.float64)
+    intr = np.tile(np.asarray(sc.intrinsics, dtype=np.float64), (K, 1))
+    frame_id = np.arange(K, dtype=np.int32) + 10
+    landmark_id = np.arange(L, dtype=np.int32) + 1000
+    obs_frame = obs_pose.copy()
+    keep = np.ones(obs_lm.shape[0], dtype=bool)
+    if plain:
+        kp = uv.astype(np.float32)
+        counts = np.bincount(obs_lm, minlength=L)
+        ptr = np.zeros(L + 1, dtype=np.int64)
+        np.cumsum(counts, out=ptr[1:])
+        return CullMap(Rt, intr, frame_id, landmark_id, X, ptr, obs_frame, frame_id[obs_frame], kp,
+                       int(landmark_id[0]), int(frame_id[0]))
+    rng = np.random.default_rng(seed)
+    intr[:, 0] *= 1.0 + 0.01 * (np.arange(K) % 3)
+    # keypoints shifted per landmark: a third by up to 10 px
+    shift = np.where(rng.random(L) < 0.35, rng.uniform(0.0, 10.0, L), 0.0)
+    ang = rng.uniform(0.0, 2.0 * math.pi, L)
+    uv = uv + (shift[:, None] * np.stack([np.cos(ang), np.sin(ang)], 1))[obs_lm]
+    kp = uv.astype(np.float32)
+    counts = np.bincount(obs_lm, minlength=L)
+    first = np.zeros(L + 1, dtype=np.int64)
+    np.cumsum(counts, out=first[1:])
+    rank = np.arange(obs_lm.shape[0]) - first[obs_lm]
+    # 20% of the landmarks keep only their first 1-4 observations, 5% none
+    cut = rng.random(L)
+    nkeep = np.where(cut < 0.20, rng.integers(1, 5, L), np.where(cut < 0.25, 0, counts))
+    keep &= rank < nkeep[obs_lm]
+    # observations from frames that are not in the map: 5% of all, and every
+    # observation of 2% of the landmarks
+    gone = rng.random(obs_lm.shape[0]) < 0.05
+    gone |= (rng.random(L) < 0.02)[obs_lm]
+    obs_frame[gone] = -1
+    obs_frame_id = np.where(gone, 100000 + rng.integers(0, 1000, obs_lm.shape[0]), frame_id[obs_pose]).astype(np.int32)
+    # 3% of the landmarks behind the first camera that sees them (2 m along
+    # its optical axis backwards, from its centre)
+    back = np.flatnonzero((rng.random(L) < 0.03) & (counts > 0))
+    k0 = obs_pose[first[back]]
+    R = Rt[k0, :9].reshape(-1, 3, 3)
+    c = -np.einsum("nji,nj->ni", R, Rt[k0, 9:])
+    X[back] = c - 2.0 * R[:, 2, :]
+    obs_frame, obs_frame_id, kp, obs_lm = obs_frame[keep], obs_frame_id[keep], kp[keep], obs_lm[keep]
+    ptr = np.zeros(L + 1, dtype=np.int64)
+    np.cumsum(np.bincount(obs_lm, minlength=L), out=ptr[1:])
+    return CullMap(Rt, intr, frame_id, landmark_id, X, ptr, np.ascontiguousarray(obs_frame, dtype=np.int32),
+                   np.ascontiguousarray(obs_frame_id), np.ascontiguousarray(kp), 1000 + L // 2 + 500,
+                   int(frame_id[-1]) + 4)
