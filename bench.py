@@ -48,8 +48,8 @@ def parse():
     ap.add_argument("--batch-windows", type=int, default=256)
     ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiable solve) timing")
-    ap.add_argument("--no-cull", action="store_true", help="skip the map-culling timing")
-    ap.add_argument("--cull-only", action="store_true", help="print the map-culling section alone")
+    ap.add_argument("--no-cull", action="store_true", help="skip the map culling and map optimise timings")
+    ap.add_argument("--map-only", action="store_true", help="print the map culling and map optimise sections alone")
     ap.add_argument("--batch-profile", action="store_true",
                     help="with --single batch-*: per-phase SM cycles of the window solves by keyframe range")
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
@@ -461,6 +461,38 @@ def cull_section(args, dist: Dist, peaks: dict, hbm_gbs: float, sc=None) -> dict
     return out
 
 
+def scenes_walk():
+    from zeroslam_gb300 import scenes
+
+    return scenes.walk_scene(seed=1)
+
+
+def map_section(args, dist: Dist, sc=None) -> dict:
+    """map::optimise (zs_map_optimise) on the 1M-observation walk as a map:
+    the whole map (local_window 0, 20 Huber rounds) and the newest 20
+    frames' window (local_window 20, 10 rounds), mixed form. Host time of the
+    window selection and problem assembly, the solve's device time and the
+    call's wall time (selection, upload and structure analysis, solve,
+    read-back and write-back of the frames and landmarks)."""
+    from zeroslam_gb300 import ba, scenes
+
+    sc = sc if sc is not None and sc.name.startswith("walk") else scenes.walk_scene(seed=1)
+    cm = scenes.slam_map(sc)
+    out = {"workload": f"walk map: F={cm.F} frames, L={cm.L} landmarks, M={cm.M} observations, mixed form"}
+    with ba.BundleAdjuster(precision=ba.MIXED, device=dist.local) as h:
+        h.map_optimise(cm, 0, False, 2)
+        for name, lw, rounds in (("global", 0, 20), ("window20", 20, 10)):
+            dist.barrier()
+            t0 = time.perf_counter()
+            _, _, rep = h.map_optimise(cm, lw, False, rounds)
+            wall = dist.max(time.perf_counter() - t0)
+            out[name] = {"local_window": lw, "rounds": rounds, "wall_ms": wall * 1e3, "select_ms": rep.ms_select,
+                         "solve_ms": rep.solve.ms_total, "lm_iterations": rep.solve.iterations,
+                         "frames": rep.frames, "landmarks": rep.landmarks, "edges": rep.edges,
+                         "chi2": [rep.solve.chi2_initial, rep.solve.chi2_final]}
+    return out
+
+
 def profile_solve(sc, precision: int, iters: int, device: int) -> dict:
     from zeroslam_gb300 import ba
 
@@ -581,6 +613,7 @@ def ours_arm(args, dist: Dist):
     loop = None if args.no_loop else loop_section(args, dist)
     adjoint = None if args.no_adjoint else adjoint_section(args, dist)
     cull = None if args.no_cull else cull_section(args, dist, peaks, hbm, sc)
+    mapopt = None if args.no_cull else map_section(args, dist, sc)
 
     prof_m = profile_solve(sc, ba.MIXED, iters, device)
     prof_d = profile_solve(sc, ba.FP64, iters, device)
@@ -638,6 +671,7 @@ def ours_arm(args, dist: Dist):
         "loop_4m": loop,
         "adjoint": adjoint,
         "map_cull": cull,
+        "map_optimise": mapopt,
     }
     print(json.dumps(line), flush=True)
 
@@ -689,15 +723,17 @@ def main():
         single_solve(args)
         return
     dist = Dist()
-    if args.cull_only:
+    if args.map_only:
         from zeroslam_gb300 import ba
 
         f64, f32 = ba.pipe_peaks(dist.local)
         mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
         hbm = float(json.load(open(mp)).get("hbm_gbs", 6800.0)) if os.path.exists(mp) else 6800.0
-        out = cull_section(args, dist, {"fp64_tflops": f64, "fp32_tflops": f32}, hbm)
+        sc = scenes_walk()
+        out = cull_section(args, dist, {"fp64_tflops": f64, "fp32_tflops": f32}, hbm, sc)
+        mo = map_section(args, dist, sc)
         if dist.rank == 0:
-            print(json.dumps({"map_cull": out}), flush=True)
+            print(json.dumps({"map_cull": out, "map_optimise": mo}), flush=True)
         return
     if args.impl == "reference":
         reference_arm(args, dist)

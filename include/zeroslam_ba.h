@@ -242,6 +242,59 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
 /* Initial damping tau * min(clamp, max diagonal of H) at the current state. */
 int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda);
 
+/* ---- windowed bundle adjustment of a map: map::map::optimise (source/map.hpp:65-267) ----
+ *
+ * The map as arrays; frame_pose and landmarks are updated in place. With
+ * local_window > 0 the window is selected as the reference does (79-127):
+ * frames are fixed when their id is 0, 1 (maps of more than two frames) or
+ * below frame_id_generator - local_window; landmarks seen by a non-fixed
+ * frame are optimised with every frame that sees them within
+ * 2 * local_window of the newest frame. local_window <= 0 optimises the whole
+ * map (frames 0 and 1 fixed). With fix_landmarks, landmarks are fixed and
+ * edges to fixed frames are dropped (the tracking mode, pose-only). Each
+ * edge is a reprojection with loss_huber(sqrt(5.991)); frames are converted
+ * to vertex_pose as so3(rotation matrix) (lie.hpp:159-180), frames without
+ * edges leave the problem, and after `rounds` LM iterations (zs_ba_solve on
+ * h, with h's options) every selected frame gets back so3::get_matrix of its
+ * pose and every optimised landmark its location (239-252). The camera of
+ * frame 0 is used for every edge, as the reference uses the first frame's.
+ * Observations whose frame is not in the map (obs_frame -1) are skipped
+ * (the reference requires every observing frame to be in the map). */
+typedef struct zs_map_optimise_input {
+    int32_t num_frames;               /* F */
+    const int32_t* frame_id;          /* [F] frame::id */
+    double* frame_pose;               /* [F*12] rotation (row-major) then translation; updated */
+    const double* frame_intrinsics;   /* [F*4] fx, fy, cx, cy */
+    int32_t num_landmarks;            /* L */
+    const int32_t* landmark_id;       /* [L] */
+    double* landmarks;                /* [L*3] updated */
+    const int64_t* landmark_obs;      /* [L+1] observation ranges, map::observations order; [0] = 0 */
+    const int32_t* obs_frame;         /* [M] frame index, or -1 */
+    const float* obs_keypoint;        /* [M*2] */
+    int32_t frame_id_generator;       /* frame::frame::id_generator */
+} zs_map_optimise_input;
+
+#define ZS_MAP_OPTIMISED 0            /* the problem was solved and written back */
+#define ZS_MAP_NOTHING_TO_OPTIMISE 1  /* no frames, or no frame or landmark with an edge */
+#define ZS_MAP_ALL_FIXED 2            /* no non-fixed pose or landmark */
+
+typedef struct zs_map_optimise_report {
+    int32_t outcome;     /* ZS_MAP_* */
+    int32_t frames;      /* non-fixed poses in the problem (the reference's non_fixed_poses) */
+    int32_t landmarks;   /* non-fixed landmarks (non_fixed_landmarks) */
+    int32_t edges;       /* edges (non_fixed_edges) */
+    int32_t problem_poses;      /* poses in the problem, fixed included */
+    int32_t problem_landmarks;  /* landmarks in the problem */
+    double ms_select;    /* host time of the window selection and problem assembly */
+    zs_ba_report solve;  /* the solve (zeroed unless outcome == ZS_MAP_OPTIMISED) */
+} zs_map_optimise_report;
+
+/* Replaces map::map::optimise(local_window, fix_landmarks, rounds,
+ * use_relative_convergence), source/map.hpp:65-267. Returns ZS_OK (see
+ * rep->outcome), ZS_ERR_INVALID for bad arrays, or the solve's error. */
+int zs_map_optimise(zs_ba_handle* h, zs_map_optimise_input* map, int32_t local_window, int32_t fix_landmarks,
+                    int32_t rounds, int32_t use_relative, zs_map_optimise_report* rep);
+
 /* ---- map culling: map::map::cull (source/map.hpp:269-323) ----
  *
  * For each landmark, in the reference's order: kept untouched when

@@ -699,3 +699,35 @@ long long zso_map_cull(const zso_cull_map* m, unsigned char* erase, float* mean_
     }
     return erased;
 }
+
+/* so3 from a rotation matrix, source/lie.hpp:159-180 (the branch on the trace
+ * and, below it, on the largest diagonal entry, as written there). */
+void zso_rt_pose(const double Rt[12], double pose[7]) {
+    const double* R = Rt;
+    double q[4];
+    const double tr = R[0] + R[4] + R[8];
+    if (tr > 0) {
+        const double s = sqrt(tr + 1);
+        const double inv = 0.5 / s;
+        q[0] = 0.5 * s;
+        q[1] = (R[7] - R[5]) * inv;
+        q[2] = (R[2] - R[6]) * inv;
+        q[3] = (R[3] - R[1]) * inv;
+    } else {
+        const int i = (R[0] < R[4]) ? (1 + (R[4] < R[8])) : (2 * (R[0] < R[8]));
+        const int j = (i + 1) % 3, k = (j + 1) % 3;
+        const double s = sqrt(R[3 * i + i] - R[3 * j + j] - R[3 * k + k] + 1.0);
+        const double inv = 0.5 / s;
+        q[0] = (R[3 * j + k] - R[3 * k + j]) * inv;
+        q[1 + i] = 0.5 * s;
+        q[1 + j] = (R[3 * i + j] + R[3 * j + i]) * inv;
+        q[1 + k] = (R[3 * i + k] + R[3 * k + i]) * inv;
+    }
+    pose[0] = Rt[9];
+    pose[1] = Rt[10];
+    pose[2] = Rt[11];
+    pose[3] = q[1];
+    pose[4] = q[2];
+    pose[5] = q[3];
+    pose[6] = q[0];
+}

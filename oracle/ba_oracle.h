@@ -123,6 +123,11 @@ long long zso_map_cull(const zso_cull_map* m, unsigned char* erase, float* mean_
  * source/lie.hpp:188-204: Rt = (R row-major, t). */
 void zso_pose_rt(const double pose[7], double Rt[12]);
 
+/* The vertex_pose parameters [tx ty tz qx qy qz qw] map::optimise builds
+ * from a frame's rotation matrix and translation, source/map.hpp:131-135
+ * with the so3-from-matrix conversion of source/lie.hpp:159-180. */
+void zso_rt_pose(const double Rt[12], double pose[7]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -125,6 +125,105 @@ class Oracle:
         L.zso_map_cull.argtypes = [C.POINTER(_CullMap), _up, C.POINTER(C.c_float)]
         L.zso_pose_rt.restype = None
         L.zso_pose_rt.argtypes = [_dp, _dp]
+        L.zso_rt_pose.restype = None
+        L.zso_rt_pose.argtypes = [_dp, _dp]
+
+    def rt_pose(self, frame_pose):
+        """[F, 7] vertex_pose parameters map::optimise builds from [F, 12] frames."""
+        Rt = np.ascontiguousarray(frame_pose, dtype=np.float64).reshape(-1, 12)
+        out = np.zeros((Rt.shape[0], 7))
+        for f in range(Rt.shape[0]):
+            self.lib.zso_rt_pose(_ptr(Rt[f], _dp), _ptr(out[f], _dp))
+        return out
+
+    def map_optimise(self, cm, local_window: int, fix_landmarks: bool, rounds: int, use_relative: bool = False):
+        """map::map::optimise (source/map.hpp:65-267) restated over a
+        ``scenes.CullMap``: window selection (79-127), the graph (129-179,
+        frames in array order, landmarks in array order, each landmark's
+        edges in observation order), removal of poses without edges
+        (181-192), the two early returns (195-233), the solve with
+        loss_huber(sqrt(5.991)) (236) and the write-back (239-252).
+        Returns (frame_pose [F, 12], landmarks [L, 3], info); the inputs are
+        not modified."""
+        from zeroslam_gb300.scenes import Scene
+
+        F, L = cm.F, cm.L
+        fp = np.array(cm.frame_pose, dtype=np.float64, copy=True)
+        X = np.array(cm.landmarks, dtype=np.float64, copy=True)
+        info = {"status": 1, "frames": 0, "landmarks": 0, "edges": 0}
+        if F == 0:
+            return fp, X, info
+        fid = [int(v) for v in cm.frame_id]
+        ptr = cm.landmark_obs
+        below = int(cm.frame_id_generator) - 1 - local_window
+        fixed_below = below + 1
+
+        def is_fixed(i, windowed):
+            return i == 0 or (i == 1 and F > 2) or (windowed and i < fixed_below)
+
+        if local_window > 0:
+            active = [not is_fixed(i, True) for i in fid]
+            horizon = int(cm.frame_id_generator) - 1 - 2 * local_window
+            relevant = [False] * F
+            active_lm = [False] * L
+            for l in range(L):
+                obs = range(int(ptr[l]), int(ptr[l + 1]))
+                if any(cm.obs_frame[o] >= 0 and active[cm.obs_frame[o]] for o in obs):
+                    active_lm[l] = True
+                    for o in obs:
+                        if cm.obs_frame[o] >= 0 and cm.obs_frame_id[o] >= horizon:
+                            relevant[cm.obs_frame[o]] = True
+            relevant = [r or a for r, a in zip(relevant, active)]
+        else:
+            relevant = [True] * F
+            active_lm = [True] * L
+        pose_fixed = [is_fixed(fid[f], local_window > 0) for f in range(F)]
+        poses7 = self.rt_pose(fp)
+        lm_of, obs_pose, obs_lm, obs_uv = {}, [], [], []
+        for l in range(L):
+            if not active_lm[l]:
+                continue
+            for o in range(int(ptr[l]), int(ptr[l + 1])):
+                f = int(cm.obs_frame[o])
+                if f < 0 or not relevant[f]:
+                    continue
+                if pose_fixed[f] and fix_landmarks:
+                    continue
+                if l not in lm_of:
+                    lm_of[l] = len(lm_of)
+                obs_pose.append(f)
+                obs_lm.append(lm_of[l])
+                obs_uv.append([float(cm.obs_keypoint[o, 0]), float(cm.obs_keypoint[o, 1])])
+        has_edge = [False] * F
+        for f in obs_pose:
+            has_edge[f] = True
+        problem_frames = [f for f in range(F) if relevant[f] and has_edge[f]]
+        nf_poses = sum(1 for f in problem_frames if not pose_fixed[f])
+        nf_lms = 0 if fix_landmarks else len(lm_of)
+        info.update(frames=nf_poses, landmarks=nf_lms, edges=len(obs_pose))
+        if nf_poses == 0 and nf_lms == 0:
+            info["status"] = 2
+            return fp, X, info
+        if not any(relevant) or not lm_of:
+            info["status"] = 1
+            return fp, X, info
+        pidx = {f: i for i, f in enumerate(problem_frames)}
+        lms = sorted(lm_of, key=lambda l: lm_of[l])
+        sc = Scene(name="map", poses=poses7[problem_frames].copy(),
+                   pose_fixed=np.array([pose_fixed[f] for f in problem_frames], dtype=np.uint8),
+                   landmarks=X[lms].copy(), landmark_fixed=np.full(len(lms), int(bool(fix_landmarks)), dtype=np.uint8),
+                   obs_pose=np.array([pidx[f] for f in obs_pose], dtype=np.int32),
+                   obs_landmark=np.array(obs_lm, dtype=np.int32), obs_uv=np.array(obs_uv, dtype=np.float64),
+                   intrinsics=tuple(float(v) for v in cm.frame_intrinsics[0]), loss_kind=1,
+                   loss_delta=float(np.sqrt(5.991)))
+        P, Lm, rep = self.solve(sc, rounds, use_relative)
+        for f in range(F):
+            if relevant[f]:
+                fp[f] = self.pose_rt(P[pidx[f]] if f in pidx else poses7[f])[0]
+        X[lms] = Lm
+        info.update(status=0, accepted=rep.accepted, chi2_initial=rep.chi2_initial, chi2_final=rep.chi2_final,
+                    scene=sc, problem_frames=problem_frames, problem_landmarks=lms)
+        return fp, X, info
 
     def map_cull(self, cm):
         """map::cull of a ``scenes.CullMap``: (erase uint8 [L], mean error float32 [L], erased)."""
@@ -254,6 +353,31 @@ class Reference:
                                      C.POINTER(C.c_float), C.c_int, C.c_int, _up, _dp]
         L.zsref_pose_rt.restype = None
         L.zsref_pose_rt.argtypes = [_dp, _dp]
+        L.zsref_rt_pose.restype = None
+        L.zsref_rt_pose.argtypes = [_dp, _dp]
+        L.zsref_map_optimise.restype = None
+        L.zsref_map_optimise.argtypes = [C.c_int, _dp, _dp, _ip, C.c_int, _ip, _dp, C.POINTER(C.c_longlong), _ip,
+                                         C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+
+    def rt_pose(self, frame_pose):
+        Rt = np.ascontiguousarray(frame_pose, dtype=np.float64).reshape(-1, 12)
+        out = np.zeros((Rt.shape[0], 7))
+        for f in range(Rt.shape[0]):
+            self.lib.zsref_rt_pose(_ptr(Rt[f], _dp), _ptr(out[f], _dp))
+        return out
+
+    def map_optimise(self, cm, local_window: int, fix_landmarks: bool, rounds: int, use_relative: bool = False):
+        """zeroslam's map::optimise on the map of a ``scenes.CullMap`` (every
+        observing frame in the map): (frame_pose [F, 12], landmarks [L, 3])."""
+        a = _cull_arrays(cm)
+        fp = a["frame_pose"].copy()
+        X = a["landmarks"].copy()
+        self.lib.zsref_map_optimise(fp.shape[0], _ptr(fp, _dp), _ptr(a["frame_intrinsics"], _dp),
+                                    _ptr(a["frame_id"], _ip), X.shape[0], _ptr(a["landmark_id"], _ip), _ptr(X, _dp),
+                                    _ptr(a["landmark_obs"], C.POINTER(C.c_longlong)), _ptr(a["obs_frame"], _ip),
+                                    _ptr(a["obs_keypoint"], C.POINTER(C.c_float)), int(cm.frame_id_generator),
+                                    int(local_window), int(bool(fix_landmarks)), int(rounds), int(bool(use_relative)))
+        return fp, X
 
     def map_cull(self, cm, timing: bool = False):
         """Which landmarks zeroslam's map::cull erases from the map of a

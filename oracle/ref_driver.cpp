@@ -230,4 +230,73 @@ void zsref_pose_rt(const double* pose7, double* Rt) {
     }
 }
 
+// vertex_pose parameters of a frame, as map::optimise builds them
+// (source/map.hpp:131-135).
+void zsref_rt_pose(const double* Rt, double* pose7) {
+    matrix::matrix<double, 3, 3> R;
+    matrix::matrix<double, 3, 1> t;
+    for (int i = 0; i < 3; ++i) {
+        for (int k = 0; k < 3; ++k) R[i][k] = Rt[3 * i + k];
+        t[i] = Rt[9 + i];
+    }
+    const lie::se3<double> v(R, t);
+    pose7[0] = v.translation()[0];
+    pose7[1] = v.translation()[1];
+    pose7[2] = v.translation()[2];
+    pose7[3] = v.rotation().get_quaternion()[1];
+    pose7[4] = v.rotation().get_quaternion()[2];
+    pose7[5] = v.rotation().get_quaternion()[3];
+    pose7[6] = v.rotation().get_quaternion()[0];
+}
+
+// Assembles a map::map as zsref_map_cull does (every landmark gets an
+// observation list, empty or not, and every observing frame must be in the
+// map: map::optimise looks both up with at()), sets the frame id generator,
+// runs optimise(local_window, fix_landmarks, rounds, use_relative) and
+// copies the frames' rotations and translations and the landmarks back.
+void zsref_map_optimise(int F, double* frame_pose, const double* frame_intr, const int* frame_id, int L,
+                        const int* landmark_id, double* lms, const long long* lm_obs, const int* obs_frame,
+                        const float* obs_kp, int frame_gen, int local_window, int fix_landmarks, int rounds,
+                        int use_relative) {
+    map::map m;
+    std::vector<frame::frame> frames(static_cast<size_t>(F));
+    for (int f = 0; f < F; ++f) {
+        frame::frame& fr = frames[static_cast<size_t>(f)];
+        fr.id = frame_id[f];
+        for (int i = 0; i < 3; ++i) {
+            for (int k = 0; k < 3; ++k) fr.rotation[i][k] = frame_pose[12 * f + 3 * i + k];
+            fr.translation[i] = frame_pose[12 * f + 9 + i];
+        }
+        fr.camera = camera::pinhole(frame_intr + 4 * f, 4);
+        fr.keypoint_pyramid.resize(1);
+    }
+    std::vector<size_t> kp_index(static_cast<size_t>(lm_obs[L]), 0);
+    for (long long o = 0; o < lm_obs[L]; ++o) {
+        std::vector<feature::point>& kps = frames[static_cast<size_t>(obs_frame[o])].keypoint_pyramid[0];
+        kp_index[static_cast<size_t>(o)] = kps.size();
+        kps.push_back(feature::point{obs_kp[2 * o], obs_kp[2 * o + 1], 0.0f, 0.0f});
+    }
+    for (int f = 0; f < F; ++f) m.add_frame(frames[static_cast<size_t>(f)]);
+    for (int l = 0; l < L; ++l) {
+        landmark::point p;
+        p.id = landmark_id[l];
+        for (int i = 0; i < 3; ++i) p.location[i] = lms[3 * l + i];
+        m.add_landmark(p);
+        std::vector<map::map::observation<int, size_t>>& ob = m.observations[p.id];
+        for (long long o = lm_obs[l]; o < lm_obs[l + 1]; ++o)
+            ob.push_back({frame_id[obs_frame[o]], kp_index[static_cast<size_t>(o)]});
+    }
+    frame::frame::id_generator = frame_gen;
+    m.optimise(local_window, fix_landmarks != 0, rounds, use_relative != 0);
+    for (int f = 0; f < F; ++f) {
+        const frame::frame& fr = m.frames.at(frame_id[f]);
+        for (int i = 0; i < 3; ++i) {
+            for (int k = 0; k < 3; ++k) frame_pose[12 * f + 3 * i + k] = fr.rotation[i][k];
+            frame_pose[12 * f + 9 + i] = fr.translation[i];
+        }
+    }
+    for (int l = 0; l < L; ++l)
+        for (int i = 0; i < 3; ++i) lms[3 * l + i] = m.landmarks.at(landmark_id[l]).location[i];
+}
+
 }  // extern "C"

@@ -40,6 +40,23 @@ def cull_from_npz(d: dict):
     return CullMap(**{f: (d[f] if d[f].ndim else d[f].item()) for f in CullMap.__dataclass_fields__})
 
 
+MAP_OPTIMISE_CASES = {  # fixture case: (local_window, fix_landmarks, rounds), tests/golden/make_golden.py
+    "global_1": (0, False, 1),
+    "window4_1": (4, False, 1),
+    "tracking_50": (1, True, 50),
+}
+
+
+def map_state_cost(oracle, cm, info, frame_pose, landmarks) -> float:
+    """Robust cost of a map state on the problem map::optimise built (the
+    oracle's scene for that window)."""
+    sc = info["scene"].copy()
+    frames = [f for f in range(cm.F) if f in set(info["problem_frames"])]
+    sc.poses = oracle.rt_pose(frame_pose[frames])
+    sc.landmarks = landmarks[info["problem_landmarks"]]
+    return oracle.chi2(sc)
+
+
 def known_answer_cull_maps():
     """The two cull cases of tests/map.test.cpp, as (name, map, erase):
     :128-143, a landmark at the origin seen once by a default frame (zero

@@ -16,6 +16,9 @@ Fixtures:
   pose_plus.npz    vertex_pose::plus (source/factor_graph.hpp:947-960)
   solve_*.npz      factor_graph::solve on whole problems: state before and after,
                    chi2 before / after and the accepted-step count
+  map_optimise.npz map::optimise (source/map.hpp:65-267) on an array map: the
+                   frames and landmarks it writes back; the vertex poses it
+                   builds from the frames (so3 from a rotation matrix)
   cull_*.npz       map::cull (source/map.hpp:269-323) on array maps: inputs and
                    the landmarks it erased; the frame rotations and translations
                    map::optimise writes back from vertex poses (map.hpp:247-251)
@@ -232,9 +235,33 @@ def write_cull(ref: Reference):
         print(f"cull_{name}: F={cm.F} L={cm.L} M={cm.M} erased={n}")
 
 
+MAP_OPTIMISE_CASES = {  # name: (local_window, fix_landmarks, rounds)
+    "global_1": (0, False, 1),
+    "window4_1": (4, False, 1),
+    "tracking_50": (1, True, 50),
+}
+
+
+def write_map_optimise(ref: Reference):
+    """map::optimise (source/map.hpp:65-267) on the map of a light-noise arc
+    scene: a global and a windowed round, and the tracking mode (landmarks
+    fixed, edges to fixed frames dropped) to convergence."""
+    sc = scenes.arc_scene(12, 1000, seed=7, min_obs=2, **scenes.ADJOINT_INIT_NOISE)
+    cm = scenes.slam_map(sc)
+    d = {f: getattr(cm, f) for f in cm.__dataclass_fields__}
+    d["rt_pose"] = ref.rt_pose(cm.frame_pose)
+    for name, (lw, fixl, rounds) in MAP_OPTIMISE_CASES.items():
+        fp, X = ref.map_optimise(cm, lw, fixl, rounds)
+        d[f"{name}_frame_pose"] = fp
+        d[f"{name}_landmarks"] = X
+    np.savez_compressed(os.path.join(HERE, "map_optimise.npz"), **d)
+    print(f"map_optimise: F={cm.F} L={cm.L} M={cm.M}")
+
+
 def main():
     ref = Reference()
     write_cull(ref)
+    write_map_optimise(ref)
     rng = np.random.default_rng(20261203)
     write_edges(ref, rng)
     write_losses(ref)

@@ -4,7 +4,7 @@ tests/golden/ (written by tests/golden/make_golden.py from the reference)."""
 import numpy as np
 import pytest
 
-from conftest import (CULL_FIXTURES, SOLVE_FIXTURES, cost_tol, cull_from_npz, known_answer_cull_maps, load_npz,
+from conftest import (CULL_FIXTURES, MAP_OPTIMISE_CASES, SOLVE_FIXTURES, cost_tol, cull_from_npz, known_answer_cull_maps, load_npz,
                       rel_err, scene_from_npz, state_tol)
 
 
@@ -114,3 +114,20 @@ def test_map_cull_known_answers(oracle, case):
     _, cm, want = case
     erase, _, n = oracle.map_cull(cm)
     assert int(erase[0]) == want and n == want
+
+
+@pytest.mark.parametrize("case", sorted(MAP_OPTIMISE_CASES))
+def test_map_optimise_matches_reference(oracle, case):
+    """map::optimise (source/map.hpp:65-267): window selection, graph,
+    conversion of the frames, solve and write-back. One LM round agrees to
+    rounding; the tracking mode (fixed landmarks, 50 rounds) to 1e-9."""
+    g = load_npz("map_optimise.npz")
+    cm = cull_from_npz(g)
+    assert np.array_equal(oracle.rt_pose(cm.frame_pose), g["rt_pose"])
+    lw, fixl, rounds = MAP_OPTIMISE_CASES[case]
+    fp, X, info = oracle.map_optimise(cm, lw, fixl, rounds)
+    assert info["status"] == 0
+    tol = 1e-12 if rounds == 1 else 1e-6
+    assert rel_err(fp, g[f"{case}_frame_pose"]) < tol
+    assert rel_err(X, g[f"{case}_landmarks"]) < tol
+    assert rel_err(fp, cm.frame_pose) > 1e-6  # the frames moved

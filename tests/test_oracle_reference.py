@@ -71,3 +71,27 @@ def test_map_cull_parity(oracle, reference, seed):
         er, nr = reference.map_cull(cm)
         assert int(er[0]) == want
     assert np.array_equal(oracle.pose_rt(sc.poses), reference.pose_rt(sc.poses))
+
+
+def test_map_optimise_parity(oracle, reference):
+    """map::optimise live: one round of the global and windowed graphs to
+    rounding; ten rounds under the Huber loss by cost (the reference's vertex
+    order comes from hash sets, so weakly seen landmarks drift apart at the
+    level of the robust solve's rounding, as for multi-step robust solves);
+    the tracking mode to 1e-6."""
+    from conftest import map_state_cost
+
+    sc = scenes.arc_scene(12, 1200, seed=9, min_obs=2, **scenes.ADJOINT_INIT_NOISE)
+    cm = scenes.slam_map(sc)
+    assert np.array_equal(oracle.rt_pose(cm.frame_pose), reference.rt_pose(cm.frame_pose))
+    for lw in (0, 4):
+        fo, Xo, info = oracle.map_optimise(cm, lw, False, 1)
+        fr, Xr = reference.map_optimise(cm, lw, False, 1)
+        assert rel_err(fo, fr) < 1e-12 and rel_err(Xo, Xr) < 1e-12
+        fo, Xo, info = oracle.map_optimise(cm, lw, False, 10)
+        fr, Xr = reference.map_optimise(cm, lw, False, 10)
+        co, cr = map_state_cost(oracle, cm, info, fo, Xo), map_state_cost(oracle, cm, info, fr, Xr)
+        assert abs(co - cr) <= 1e-5 * cr
+    fo, Xo, _ = oracle.map_optimise(cm, 1, True, 50)
+    fr, Xr = reference.map_optimise(cm, 1, True, 50)
+    assert rel_err(fo, fr) < 1e-6 and np.array_equal(Xo, Xr)

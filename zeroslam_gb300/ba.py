@@ -91,6 +91,22 @@ class MapCullInput(C.Structure):
                 ("frame_id_generator", C.c_int32)]
 
 
+class MapOptimiseInput(C.Structure):
+    _fields_ = [("num_frames", C.c_int32), ("frame_id", _ip), ("frame_pose", _dp), ("frame_intrinsics", _dp),
+                ("num_landmarks", C.c_int32), ("landmark_id", _ip), ("landmarks", _dp),
+                ("landmark_obs", C.POINTER(C.c_int64)), ("obs_frame", _ip), ("obs_keypoint", C.POINTER(C.c_float)),
+                ("frame_id_generator", C.c_int32)]
+
+
+class MapOptimiseReport(C.Structure):
+    _fields_ = [("outcome", C.c_int32), ("frames", C.c_int32), ("landmarks", C.c_int32), ("edges", C.c_int32),
+                ("problem_poses", C.c_int32), ("problem_landmarks", C.c_int32), ("ms_select", C.c_double),
+                ("solve", Report)]
+
+
+MAP_OPTIMISED, MAP_NOTHING_TO_OPTIMISE, MAP_ALL_FIXED = 0, 1, 2
+
+
 class CullReport(C.Structure):
     _fields_ = [("erased", C.c_int64), ("error_passes", C.c_int64), ("ms_device", C.c_double)]
 
@@ -113,7 +129,7 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
                  "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
-                 "zs_ba_cull")
+                 "zs_ba_cull", "zs_map_optimise")
 
 
 def library_path() -> str:
@@ -174,6 +190,9 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_map_cull.restype = C.c_int
     lib.zs_map_cull.argtypes = [C.c_void_p, C.POINTER(MapCullInput), _up, C.POINTER(C.c_float),
                                 C.POINTER(CullReport)]
+    lib.zs_map_optimise.restype = C.c_int
+    lib.zs_map_optimise.argtypes = [C.c_void_p, C.POINTER(MapOptimiseInput), C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_int32, C.POINTER(MapOptimiseReport)]
     lib.zs_ba_cull.restype = C.c_int
     lib.zs_ba_cull.argtypes = [C.c_void_p, _ip, _ip, C.c_int32, C.c_int32, _up, C.POINTER(C.c_float),
                                C.POINTER(CullReport)]
@@ -376,6 +395,30 @@ class BundleAdjuster:
         if st != ZS_OK:
             raise ZsError(st, "zs_ba_cull")
         return erase, mean, rep
+
+    def map_optimise(self, cm, local_window: int, fix_landmarks: bool, rounds: int, use_relative: bool = False):
+        """map::optimise of a map given as arrays (zs_map_optimise, ``scenes.CullMap``):
+        (frame_pose [F, 12], landmarks [L, 3], MapOptimiseReport); the map is not modified.
+        The handle's problem becomes the map's window."""
+        fp = np.array(cm.frame_pose, dtype=np.float64, copy=True, order="C")
+        X = np.array(cm.landmarks, dtype=np.float64, copy=True, order="C")
+        fid = np.ascontiguousarray(cm.frame_id, dtype=np.int32)
+        intr = np.ascontiguousarray(cm.frame_intrinsics, dtype=np.float64)
+        lid = np.ascontiguousarray(cm.landmark_id, dtype=np.int32)
+        ptr = np.ascontiguousarray(cm.landmark_obs, dtype=np.int64)
+        of = np.ascontiguousarray(cm.obs_frame, dtype=np.int32)
+        kp = np.ascontiguousarray(cm.obs_keypoint, dtype=np.float32)
+        inp = MapOptimiseInput(fp.shape[0], _p(fid, _ip), _p(fp, _dp), _p(intr, _dp), X.shape[0], _p(lid, _ip),
+                               _p(X, _dp), _p(ptr, C.POINTER(C.c_int64)), _p(of, _ip),
+                               _p(kp, C.POINTER(C.c_float)), int(cm.frame_id_generator))
+        rep = MapOptimiseReport()
+        st = self.lib.zs_map_optimise(self.h, C.byref(inp), int(local_window), int(bool(fix_landmarks)),
+                                      int(rounds), int(bool(use_relative)), C.byref(rep))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_map_optimise")
+        if rep.outcome == MAP_OPTIMISED:
+            self.K, self.L, self.M = rep.problem_poses, rep.problem_landmarks, rep.edges
+        return fp, X, rep
 
     def map_cull(self, cm):
         """map::cull of a map given as arrays (zs_map_cull, ``scenes.CullMap``):

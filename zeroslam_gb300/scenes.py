@@ -591,3 +591,17 @@ def cull_map(sc: Scene, seed: int = 0, frame_pose: np.ndarray | None = None, pla
     return CullMap(Rt, intr, frame_id, landmark_id, X, ptr, np.ascontiguousarray(obs_frame, dtype=np.int32),
                    np.ascontiguousarray(obs_frame_id), np.ascontiguousarray(kp), 1000 + L // 2 + 500,
                    int(frame_id[-1]) + 4)
+
+
+def slam_map(sc: Scene) -> CullMap:
+    """A scene at its current state as a zeroslam map for map::optimise:
+    frame ids 0..K-1 (0 and 1 are the map's gauge, source/map.hpp:89,134),
+    landmark ids 0..L-1, one camera, float32 keypoints, every observing
+    frame in the map, both id generators one past the last id."""
+    cm = cull_map(sc, plain=True)
+    cm.frame_id = np.arange(sc.K, dtype=np.int32)
+    cm.obs_frame_id = cm.frame_id[cm.obs_frame].astype(np.int32)
+    cm.landmark_id = np.arange(sc.L, dtype=np.int32)
+    cm.landmark_id_generator = sc.L
+    cm.frame_id_generator = sc.K
+    return cm
