@@ -48,8 +48,9 @@ def parse():
     ap.add_argument("--batch-windows", type=int, default=256)
     ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiable solve) timing")
-    ap.add_argument("--no-cull", action="store_true", help="skip the map culling and map optimise timings")
-    ap.add_argument("--map-only", action="store_true", help="print the map culling and map optimise sections alone")
+    ap.add_argument("--no-cull", action="store_true", help="skip the map culling, map optimise and matching timings")
+    ap.add_argument("--map-only", action="store_true",
+                    help="print the map culling, map optimise and matching sections alone")
     ap.add_argument("--batch-profile", action="store_true",
                     help="with --single batch-*: per-phase SM cycles of the window solves by keyframe range")
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
@@ -461,6 +462,47 @@ def cull_section(args, dist: Dist, peaks: dict, hbm_gbs: float, sc=None) -> dict
     return out
 
 
+def match_section(args, dist: Dist) -> dict:
+    """Descriptor matching (zs_find_matches, feature::find_matches): two frames
+    of 2,000 descriptors with zeroslam's arguments (threshold 32, two
+    matches per descriptor, room for 2 max(n)), both directions as
+    slam::process_frame calls it; and 20,000 x 20,000 (a map-scale search).
+    Device time of the kernels and wall time of the call (host arrays in,
+    matches out). The oracle's C restatement (one core) times the small case."""
+    from zeroslam_gb300 import ba, scenes
+
+    out = {}
+    with ba.BundleAdjuster(device=dist.local) as h:
+        for name, n in (("frames_2000", 2000), ("map_20000", 20000)):
+            lhs, rhs = scenes.descriptor_pair(n, n, seed=7)
+            for _ in range(3):
+                h.find_matches(lhs, rhs, 32.0, 2, 2 * n)
+            dev, wall = [], []
+            for _ in range(max(1, args.steps)):
+                t0 = time.perf_counter()
+                m1, ms1 = h.find_matches(lhs, rhs, 32.0, 2, 2 * n, timing=True)
+                m2, ms2 = h.find_matches(rhs, lhs, 32.0, 2, 2 * n, timing=True)
+                wall.append(time.perf_counter() - t0)
+                dev.append(ms1 + ms2)
+            ms = dist.max(float(np.median(dev)))
+            pairs = 2 * n * n
+            out[name] = {"descriptors": n, "directions": 2, "ms_device": ms,
+                         "wall_ms": dist.max(float(np.median(wall)) * 1e3),
+                         "pairs_per_s": dist.world * pairs / (ms * 1e-3), "matches": [len(m1), len(m2)]}
+            if name == "frames_2000" and not args.no_cpu and dist.rank == 0 and dist.world == 1:
+                from oracle.oracle import Oracle
+
+                o = Oracle()
+                t0 = time.perf_counter()
+                a = o.find_matches(lhs, rhs, 32.0, 2, 2 * n)
+                b = o.find_matches(rhs, lhs, 32.0, 2, 2 * n)
+                cpu = time.perf_counter() - t0
+                out[name]["cpu_baseline"] = {"ms": cpu * 1e3, "cores": 1, "kind": "port",
+                                             "sample": "both directions, once"}
+                out[name]["parity"] = bool(np.array_equal(a, m1) and np.array_equal(b, m2))
+    return out
+
+
 def scenes_walk():
     from zeroslam_gb300 import scenes
 
@@ -614,6 +656,7 @@ def ours_arm(args, dist: Dist):
     adjoint = None if args.no_adjoint else adjoint_section(args, dist)
     cull = None if args.no_cull else cull_section(args, dist, peaks, hbm, sc)
     mapopt = None if args.no_cull else map_section(args, dist, sc)
+    matching = None if args.no_cull else match_section(args, dist)
 
     prof_m = profile_solve(sc, ba.MIXED, iters, device)
     prof_d = profile_solve(sc, ba.FP64, iters, device)
@@ -672,6 +715,7 @@ def ours_arm(args, dist: Dist):
         "adjoint": adjoint,
         "map_cull": cull,
         "map_optimise": mapopt,
+        "matching": matching,
     }
     print(json.dumps(line), flush=True)
 
@@ -732,8 +776,9 @@ def main():
         sc = scenes_walk()
         out = cull_section(args, dist, {"fp64_tflops": f64, "fp32_tflops": f32}, hbm, sc)
         mo = map_section(args, dist, sc)
+        mt = match_section(args, dist)
         if dist.rank == 0:
-            print(json.dumps({"map_cull": out, "map_optimise": mo}), flush=True)
+            print(json.dumps({"map_cull": out, "map_optimise": mo, "matching": mt}), flush=True)
         return
     if args.impl == "reference":
         reference_arm(args, dist)

@@ -21,6 +21,9 @@
  *                                 matrix::solve_cholesky                   source/matrix_decomposition_cholesky.hpp:26-95
  *   zs_ba_reset_state             vertex_base::restore                     source/factor_graph.hpp:135-137
  *   zs_ba_status_string           (stderr diagnostics of solve)           source/factor_graph.hpp:495,786
+ *   zs_map_optimise               map::map::optimise                       source/map.hpp:65-267
+ *   zs_map_cull / zs_ba_cull      map::map::cull                           source/map.hpp:269-323
+ *   zs_find_matches               feature::find_matches, distance<256>     source/feature.hpp:1133-1235
  *
  * Conventions: return values are status codes (0 = ok, negative = error);
  * nothing throws or aborts across this boundary. Host buffers stay owned by
@@ -241,6 +244,30 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
 
 /* Initial damping tau * min(clamp, max diagonal of H) at the current state. */
 int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda);
+
+/* ---- descriptor matching: feature::find_matches (source/feature.hpp:1190-1235) ---- */
+
+/* feature::match, field for field (size_t, size_t, float on LP64 hosts). */
+typedef struct zs_match {
+    uint64_t lhs_index;
+    uint64_t rhs_index;
+    float score;        /* the Hamming distance, as float */
+} zs_match;
+
+#define ZS_MATCH_MAX_K 8
+
+/* For each lhs descriptor in order (32 bytes each, the 256-bit
+ * feature::descriptor), the matches_count nearest rhs descriptors by Hamming
+ * distance (distance<256>) whose distance is below threshold, nearest first,
+ * equal distances in rhs order; lhs descriptors are taken while
+ * found + matches_count <= matches_size (the reference's capacity rule).
+ * Writes matches[0 .. *found) exactly as the reference does; entries from
+ * *found on are not written (the reference leaves scratch there). Host
+ * arrays; ms_device (may be NULL) receives the kernels' device time.
+ * matches_count > ZS_MATCH_MAX_K returns ZS_ERR_UNSUPPORTED. */
+int zs_find_matches(zs_ba_handle* h, const uint8_t* lhs, int64_t lhs_count, const uint8_t* rhs, int64_t rhs_count,
+                    float threshold, int64_t matches_count, zs_match* matches, int64_t matches_size, int64_t* found,
+                    double* ms_device);
 
 /* ---- windowed bundle adjustment of a map: map::map::optimise (source/map.hpp:65-267) ----
  *

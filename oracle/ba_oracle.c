@@ -731,3 +731,55 @@ void zso_rt_pose(const double Rt[12], double pose[7]) {
     pose[5] = q[3];
     pose[6] = q[0];
 }
+
+/* ---------------------------------------------------------------- matching */
+
+/* distance<256>, source/feature.hpp:1139-1187: the popcount of the XOR of
+ * the two 32-byte descriptors, counted per byte from a table of the 256
+ * byte values' bit counts. */
+static unsigned int hamming256(const unsigned char* a, const unsigned char* b) {
+    static unsigned char bits[256];
+    static int ready = 0;
+    if (!ready) {
+        for (int v = 0; v < 256; ++v) {
+            int c = 0;
+            for (int x = v; x; x >>= 1) c += x & 1;
+            bits[v] = (unsigned char)c;
+        }
+        ready = 1;
+    }
+    unsigned int d = 0;
+    for (int i = 0; i < 32; ++i) d += bits[a[i] ^ b[i]];
+    return d;
+}
+
+/* feature::find_matches, source/feature.hpp:1190-1235. */
+long long zso_find_matches(const unsigned char* lhs, long long n_lhs, const unsigned char* rhs, long long n_rhs,
+                           float threshold, long long k, zso_match* matches, long long size) {
+    if (k <= 0 || size <= 0) return 0;
+    long long count = 0;
+    for (long long i = 0; i < n_lhs; ++i) {
+        if (count + k > size) break;
+        for (long long m = 0; m < k; ++m) {
+            matches[count + m].lhs_index = (unsigned long long)i;
+            matches[count + m].rhs_index = 0;
+            matches[count + m].score = threshold;
+        }
+        for (long long j = 0; j < n_rhs; ++j) {
+            const float score = (float)hamming256(lhs + 32 * i, rhs + 32 * j);
+            for (long long m = 0; m < k; ++m) {
+                if (score < matches[count + m].score) {
+                    for (long long s = k - 1; s > m; --s) matches[count + s] = matches[count + s - 1];
+                    matches[count + m].score = score;
+                    matches[count + m].rhs_index = (unsigned long long)j;
+                    matches[count + m].lhs_index = (unsigned long long)i;
+                    break;
+                }
+            }
+        }
+        const long long save = count;
+        for (long long m = 0; m < k; ++m)
+            if (matches[save + m].score < threshold) ++count;
+    }
+    return count;
+}

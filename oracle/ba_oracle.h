@@ -19,6 +19,8 @@
  *   source/lie.hpp:188-204,247-264,284-294,337-362,446-450,521-531
  *   source/camera.hpp:91-142
  *   source/map.hpp:247-251,269-323   frame write-back and map::cull
+ *   source/lie.hpp:159-180           so3 from a rotation matrix (map::optimise)
+ *   source/feature.hpp:1133-1235     distance<256> and find_matches
  * The reference stores H_pl in a hash map and sums the Schur products in
  * hash-iteration order; this restatement sums per landmark in ascending
  * landmark order, so results agree to rounding, not bit for bit.
@@ -127,6 +129,19 @@ void zso_pose_rt(const double pose[7], double Rt[12]);
  * from a frame's rotation matrix and translation, source/map.hpp:131-135
  * with the so3-from-matrix conversion of source/lie.hpp:159-180. */
 void zso_rt_pose(const double Rt[12], double pose[7]);
+
+/* feature::find_matches with distance<256>, source/feature.hpp:1133-1235:
+ * for each lhs descriptor (32 bytes) in order, while count + k <= size, the
+ * k smallest Hamming distances to the rhs descriptors (scanned in order,
+ * strict improvement, so ties keep the earlier rhs) that are below the
+ * threshold. matches: [size] of (lhs, rhs, score). Returns the count. */
+typedef struct zso_match {
+    unsigned long long lhs_index;
+    unsigned long long rhs_index;
+    float score;
+} zso_match;
+long long zso_find_matches(const unsigned char* lhs, long long n_lhs, const unsigned char* rhs, long long n_rhs,
+                           float threshold, long long k, zso_match* matches, long long size);
 
 #ifdef __cplusplus
 }

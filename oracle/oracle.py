@@ -97,6 +97,18 @@ def _cull_arrays(cm) -> dict:
     )
 
 
+MATCH_DTYPE = np.dtype([("lhs_index", np.uint64), ("rhs_index", np.uint64), ("score", np.float32)], align=True)
+
+
+def _find_matches(fn, lhs, rhs, threshold, k, size):
+    lhs = np.ascontiguousarray(lhs, dtype=np.uint8).reshape(-1, 32)
+    rhs = np.ascontiguousarray(rhs, dtype=np.uint8).reshape(-1, 32)
+    out = np.zeros(max(int(size), 1), dtype=MATCH_DTYPE)
+    n = fn(_ptr(lhs, _up), lhs.shape[0], _ptr(rhs, _up), rhs.shape[0], float(threshold), int(k),
+           out.ctypes.data_as(C.c_void_p), int(size))
+    return out[:n].copy()
+
+
 class Oracle:
     def __init__(self):
         self.lib = C.CDLL(_build.build_oracle())
@@ -127,6 +139,13 @@ class Oracle:
         L.zso_pose_rt.argtypes = [_dp, _dp]
         L.zso_rt_pose.restype = None
         L.zso_rt_pose.argtypes = [_dp, _dp]
+        L.zso_find_matches.restype = C.c_longlong
+        L.zso_find_matches.argtypes = [_up, C.c_longlong, _up, C.c_longlong, C.c_float, C.c_longlong, C.c_void_p,
+                                       C.c_longlong]
+
+    def find_matches(self, lhs, rhs, threshold: float, k: int, size: int):
+        """feature::find_matches: structured array of (lhs_index, rhs_index, score)."""
+        return _find_matches(self.lib.zso_find_matches, lhs, rhs, threshold, k, size)
 
     def rt_pose(self, frame_pose):
         """[F, 7] vertex_pose parameters map::optimise builds from [F, 12] frames."""
@@ -355,6 +374,12 @@ class Reference:
         L.zsref_pose_rt.argtypes = [_dp, _dp]
         L.zsref_rt_pose.restype = None
         L.zsref_rt_pose.argtypes = [_dp, _dp]
+        L.zsref_find_matches.restype = C.c_longlong
+        L.zsref_find_matches.argtypes = [_up, C.c_longlong, _up, C.c_longlong, C.c_float, C.c_longlong, C.c_void_p,
+                                         C.c_longlong]
+
+    def find_matches(self, lhs, rhs, threshold: float, k: int, size: int):
+        return _find_matches(self.lib.zsref_find_matches, lhs, rhs, threshold, k, size)
         L.zsref_map_optimise.restype = None
         L.zsref_map_optimise.argtypes = [C.c_int, _dp, _dp, _ip, C.c_int, _ip, _dp, C.POINTER(C.c_longlong), _ip,
                                          C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]

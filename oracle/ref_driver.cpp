@@ -299,4 +299,15 @@ void zsref_map_optimise(int F, double* frame_pose, const double* frame_intr, con
         for (int i = 0; i < 3; ++i) lms[3 * l + i] = m.landmarks.at(landmark_id[l]).location[i];
 }
 
+// feature::find_matches on descriptor arrays (32 bytes each); matches holds
+// size entries of (lhs, rhs, score) laid out as feature::match.
+long long zsref_find_matches(const unsigned char* lhs, long long n_lhs, const unsigned char* rhs, long long n_rhs,
+                             float threshold, long long k, feature::match* matches, long long size) {
+    std::vector<feature::descriptor> l(static_cast<size_t>(n_lhs)), r(static_cast<size_t>(n_rhs));
+    for (long long i = 0; i < n_lhs; ++i) std::memcpy(l[static_cast<size_t>(i)].data, lhs + 32 * i, 32);
+    for (long long j = 0; j < n_rhs; ++j) std::memcpy(r[static_cast<size_t>(j)].data, rhs + 32 * j, 32);
+    return static_cast<long long>(feature::find_matches(l.data(), l.size(), r.data(), r.size(), threshold,
+                                                        static_cast<size_t>(k), matches, static_cast<size_t>(size)));
+}
+
 }  // extern "C"

@@ -57,6 +57,29 @@ def map_state_cost(oracle, cm, info, frame_pose, landmarks) -> float:
     return oracle.chi2(sc)
 
 
+def known_answer_descriptors():
+    """The matching cases of tests/feature.test.cpp: :763-778, every one-bit
+    descriptor (bit i of four little-endian 64-bit words) is at distance 1
+    from the zero descriptor; :780-808, two tables of ten descriptors whose
+    first four bytes are given (the rest zero), threshold 1, two matches per
+    lhs, room for 20: 12 matches (only equal descriptors match; {4,4,4,4}
+    twice in rhs gives two)."""
+    onehot = np.zeros((256, 32), dtype=np.uint8)
+    for i in range(256):
+        w = np.zeros(4, dtype="<u8")
+        w[i // 64] = np.uint64(1) << np.uint64(i % 64)
+        onehot[i] = np.frombuffer(w.tobytes(), dtype=np.uint8)
+    head_l = [(1, 2, 3, 4), (5, 6, 7, 8), (0, 0, 0, 0), (4, 4, 4, 4), (1, 1, 2, 2), (4, 3, 2, 1), (8, 7, 6, 5),
+              (8, 8, 8, 8), (4, 4, 4, 4), (3, 3, 4, 4)]
+    head_r = [(4, 3, 2, 1), (8, 7, 6, 5), (8, 8, 8, 8), (4, 4, 4, 4), (3, 3, 4, 4), (1, 2, 3, 4), (5, 6, 7, 8),
+              (0, 0, 0, 0), (4, 4, 4, 4), (1, 1, 2, 2)]
+    lhs = np.zeros((10, 32), dtype=np.uint8)
+    rhs = np.zeros((10, 32), dtype=np.uint8)
+    lhs[:, :4] = head_l
+    rhs[:, :4] = head_r
+    return onehot, (lhs, rhs, 1.0, 2, 20, 12)
+
+
 def known_answer_cull_maps():
     """The two cull cases of tests/map.test.cpp, as (name, map, erase):
     :128-143, a landmark at the origin seen once by a default frame (zero

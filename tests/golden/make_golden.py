@@ -19,6 +19,9 @@ Fixtures:
   map_optimise.npz map::optimise (source/map.hpp:65-267) on an array map: the
                    frames and landmarks it writes back; the vertex poses it
                    builds from the frames (so3 from a rotation matrix)
+  matches.npz      feature::find_matches (source/feature.hpp:1190-1235): two
+                   descriptor sets and the matches of several threshold / k /
+                   size cases
   cull_*.npz       map::cull (source/map.hpp:269-323) on array maps: inputs and
                    the landmarks it erased; the frame rotations and translations
                    map::optimise writes back from vertex poses (map.hpp:247-251)
@@ -258,10 +261,35 @@ def write_map_optimise(ref: Reference):
     print(f"map_optimise: F={cm.F} L={cm.L} M={cm.M}")
 
 
+MATCH_CASES = [  # (threshold, k, size): zeroslam's call (32, 2, 2 max(n)), ties and wide thresholds,
+    (32.0, 2, 1600),  # the capacity rule, k = 1 and the largest k
+    (32.0, 1, 1600),
+    (100.0, 3, 2400),
+    (32.5, 2, 301),
+    (130.0, 8, 6400),
+]
+
+
+def write_matches(ref: Reference):
+    """feature::find_matches (source/feature.hpp:1190-1235) on descriptor sets
+    with near copies (true matches around the threshold) and exact duplicate
+    rhs descriptors (ties)."""
+    lhs, rhs = scenes.descriptor_pair(700, 800, seed=3)
+    d = {"lhs": lhs, "rhs": rhs, "cases": np.array(MATCH_CASES, dtype=np.float64)}
+    for c, (thr, k, size) in enumerate(MATCH_CASES):
+        m = ref.find_matches(lhs, rhs, thr, k, size)
+        d[f"case{c}_lhs"] = m["lhs_index"]
+        d[f"case{c}_rhs"] = m["rhs_index"]
+        d[f"case{c}_score"] = m["score"]
+        print(f"matches case {c}: threshold {thr} k {k} size {size}: {len(m)} matches")
+    np.savez_compressed(os.path.join(HERE, "matches.npz"), **d)
+
+
 def main():
     ref = Reference()
     write_cull(ref)
     write_map_optimise(ref)
+    write_matches(ref)
     rng = np.random.default_rng(20261203)
     write_edges(ref, rng)
     write_losses(ref)

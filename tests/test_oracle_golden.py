@@ -4,7 +4,8 @@ tests/golden/ (written by tests/golden/make_golden.py from the reference)."""
 import numpy as np
 import pytest
 
-from conftest import (CULL_FIXTURES, MAP_OPTIMISE_CASES, SOLVE_FIXTURES, cost_tol, cull_from_npz, known_answer_cull_maps, load_npz,
+from conftest import (CULL_FIXTURES, MAP_OPTIMISE_CASES, SOLVE_FIXTURES, cost_tol, cull_from_npz, known_answer_cull_maps,
+                      known_answer_descriptors, load_npz,
                       rel_err, scene_from_npz, state_tol)
 
 
@@ -131,3 +132,21 @@ def test_map_optimise_matches_reference(oracle, case):
     assert rel_err(fp, g[f"{case}_frame_pose"]) < tol
     assert rel_err(X, g[f"{case}_landmarks"]) < tol
     assert rel_err(fp, cm.frame_pose) > 1e-6  # the frames moved
+
+
+def test_find_matches_matches_reference(oracle):
+    """feature::find_matches (source/feature.hpp:1190-1235), match for match."""
+    g = load_npz("matches.npz")
+    for c, (thr, k, size) in enumerate(g["cases"]):
+        m = oracle.find_matches(g["lhs"], g["rhs"], float(thr), int(k), int(size))
+        assert np.array_equal(m["lhs_index"], g[f"case{c}_lhs"])
+        assert np.array_equal(m["rhs_index"], g[f"case{c}_rhs"])
+        assert np.array_equal(m["score"], g[f"case{c}_score"])
+
+
+def test_find_matches_known_answers(oracle):
+    onehot, (lhs, rhs, thr, k, size, want) = known_answer_descriptors()
+    zero = np.zeros((1, 32), dtype=np.uint8)
+    m = oracle.find_matches(onehot, zero, 2.0, 1, 256)
+    assert len(m) == 256 and np.all(m["score"] == 1.0)
+    assert len(oracle.find_matches(lhs, rhs, thr, k, size)) == want

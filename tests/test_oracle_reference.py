@@ -95,3 +95,18 @@ def test_map_optimise_parity(oracle, reference):
     fo, Xo, _ = oracle.map_optimise(cm, 1, True, 50)
     fr, Xr = reference.map_optimise(cm, 1, True, 50)
     assert rel_err(fo, fr) < 1e-6 and np.array_equal(Xo, Xr)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_find_matches_parity(oracle, reference, seed):
+    from conftest import known_answer_descriptors
+
+    lhs, rhs = scenes.descriptor_pair(400, 500, seed=10 + seed)
+    for thr, k, size in [(32.0, 2, 1000), (64.0, 4, 1601), (128.0, 8, 4000), (float("nan"), 2, 100), (-1.0, 1, 100)]:
+        a = oracle.find_matches(lhs, rhs, thr, k, size)
+        b = reference.find_matches(lhs, rhs, thr, k, size)
+        assert np.array_equal(a, b)
+    onehot, (l, r, thr, k, size, want) = known_answer_descriptors()
+    assert len(reference.find_matches(l, r, thr, k, size)) == want
+    m = reference.find_matches(onehot, np.zeros((1, 32), dtype=np.uint8), 2.0, 1, 256)
+    assert len(m) == 256 and np.all(m["score"] == 1.0)

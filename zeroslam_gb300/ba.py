@@ -91,6 +91,9 @@ class MapCullInput(C.Structure):
                 ("frame_id_generator", C.c_int32)]
 
 
+MATCH_DTYPE = np.dtype([("lhs_index", np.uint64), ("rhs_index", np.uint64), ("score", np.float32)], align=True)
+
+
 class MapOptimiseInput(C.Structure):
     _fields_ = [("num_frames", C.c_int32), ("frame_id", _ip), ("frame_pose", _dp), ("frame_intrinsics", _dp),
                 ("num_landmarks", C.c_int32), ("landmark_id", _ip), ("landmarks", _dp),
@@ -129,7 +132,7 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
                  "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
-                 "zs_ba_cull", "zs_map_optimise")
+                 "zs_ba_cull", "zs_map_optimise", "zs_find_matches")
 
 
 def library_path() -> str:
@@ -190,6 +193,9 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_map_cull.restype = C.c_int
     lib.zs_map_cull.argtypes = [C.c_void_p, C.POINTER(MapCullInput), _up, C.POINTER(C.c_float),
                                 C.POINTER(CullReport)]
+    lib.zs_find_matches.restype = C.c_int
+    lib.zs_find_matches.argtypes = [C.c_void_p, _up, C.c_int64, _up, C.c_int64, C.c_float, C.c_int64, C.c_void_p,
+                                    C.c_int64, C.POINTER(C.c_int64), _dp]
     lib.zs_map_optimise.restype = C.c_int
     lib.zs_map_optimise.argtypes = [C.c_void_p, C.POINTER(MapOptimiseInput), C.c_int32, C.c_int32, C.c_int32,
                                     C.c_int32, C.POINTER(MapOptimiseReport)]
@@ -419,6 +425,21 @@ class BundleAdjuster:
         if rep.outcome == MAP_OPTIMISED:
             self.K, self.L, self.M = rep.problem_poses, rep.problem_landmarks, rep.edges
         return fp, X, rep
+
+    def find_matches(self, lhs, rhs, threshold: float, k: int, size: int, timing: bool = False):
+        """feature::find_matches on the device (zs_find_matches): a structured
+        array of (lhs_index, rhs_index, score) [, device ms]."""
+        lhs = np.ascontiguousarray(lhs, dtype=np.uint8).reshape(-1, 32)
+        rhs = np.ascontiguousarray(rhs, dtype=np.uint8).reshape(-1, 32)
+        out = np.zeros(max(int(size), 1), dtype=MATCH_DTYPE)
+        n = C.c_int64()
+        ms = C.c_double()
+        st = self.lib.zs_find_matches(self.h, _p(lhs, _up), lhs.shape[0], _p(rhs, _up), rhs.shape[0], float(threshold),
+                                      int(k), out.ctypes.data_as(C.c_void_p), int(size), C.byref(n), C.byref(ms))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_find_matches")
+        res = out[:n.value].copy()
+        return (res, ms.value) if timing else res
 
     def map_cull(self, cm):
         """map::cull of a map given as arrays (zs_map_cull, ``scenes.CullMap``):

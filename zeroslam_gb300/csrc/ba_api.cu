@@ -362,8 +362,8 @@ struct zs_ba_handle {
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
     HostScratch hscratch;        // build_problem's host arrays (pinned, reused)
-    void* cull_buf = nullptr;    // map culling's device arrays (handle lifetime, grown on demand)
-    size_t cull_cap = 0;
+    void* aux_buf = nullptr;     // device arrays of map culling and matching (handle lifetime, grown on demand)
+    size_t aux_cap = 0;
     // batched windows
     bool batch = false;
     BatchDev B;
@@ -407,11 +407,11 @@ struct zs_ba_handle {
     }
 };
 
-// Carves map culling's device arrays out of one handle-owned buffer.
-struct CullCarve {
+// Carves the device arrays of map culling and matching out of one handle-owned buffer.
+struct Carve {
     char* base;
     size_t off = 0;
-    explicit CullCarve(void* b) : base(static_cast<char*>(b)) {}
+    explicit Carve(void* b) : base(static_cast<char*>(b)) {}
     template <typename T>
     T* take(size_t count) {
         T* p = reinterpret_cast<T*>(base + off);
@@ -422,17 +422,17 @@ struct CullCarve {
     static size_t bytes(size_t count) { return (count * sizeof(T) + 255) & ~size_t(255); }
 };
 
-static void cull_reserve(zs_ba_handle* h, size_t bytes) {
-    if (bytes <= h->cull_cap) return;
-    if (h->cull_buf) {
+static void aux_reserve(zs_ba_handle* h, size_t bytes) {
+    if (bytes <= h->aux_cap) return;
+    if (h->aux_buf) {
         ZS_CUDA(cudaStreamSynchronize(h->stream));
-        ZS_CUDA(cudaFree(h->cull_buf));
-        h->cull_buf = nullptr;
-        h->cull_cap = 0;
+        ZS_CUDA(cudaFree(h->aux_buf));
+        h->aux_buf = nullptr;
+        h->aux_cap = 0;
     }
-    const size_t cap = std::max(bytes, h->cull_cap + h->cull_cap / 2);
-    ZS_CUDA(cudaMalloc(&h->cull_buf, cap));
-    h->cull_cap = cap;
+    const size_t cap = std::max(bytes, h->aux_cap + h->aux_cap / 2);
+    ZS_CUDA(cudaMalloc(&h->aux_buf, cap));
+    h->aux_cap = cap;
 }
 
 // Runs k_cull (after `pre`, which enqueues the inputs' copies and any kernel
@@ -551,7 +551,7 @@ void zs_ba_destroy(zs_ba_handle* h) {
     h->timer.destroy();
     h->release_problem();
     h->hscratch.release();
-    if (h->cull_buf) cudaFree(h->cull_buf);
+    if (h->aux_buf) cudaFree(h->aux_buf);
     if (h->st) cudaFree(h->st);
     if (h->st_host) cudaFreeHost(h->st_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1301,6 +1301,73 @@ int zs_ba_initial_lambda(zs_ba_handle* h, double* lambda) {
     return ZS_OK;
 }
 
+int zs_find_matches(zs_ba_handle* h, const uint8_t* lhs, int64_t lhs_count, const uint8_t* rhs, int64_t rhs_count,
+                    float threshold, int64_t matches_count, zs_match* matches, int64_t matches_size, int64_t* found,
+                    double* ms_device) {
+    if (!h || !found) return ZS_ERR_INVALID;
+    *found = 0;
+    if (ms_device) *ms_device = 0.0;
+    if (matches_count <= 0 || matches_size <= 0) return ZS_OK;  // feature.hpp:1200-1202
+    if (!matches || lhs_count < 0 || rhs_count < 0) return ZS_ERR_INVALID;
+    if (lhs_count > 0x3fffffff || rhs_count > 0x3fffffff) return ZS_ERR_INVALID;
+    if ((lhs_count > 0 && !lhs) || (rhs_count > 0 && !rhs)) return ZS_ERR_INVALID;
+    if (matches_count > ZS_MATCH_MAX_K) return ZS_ERR_UNSUPPORTED;
+    if (lhs_count == 0) return ZS_OK;
+    const int nl = (int)lhs_count, nr = (int)rhs_count, k = (int)matches_count;
+    // a distance d is kept when (float)d < threshold
+    int d_lim = 257;
+    for (int d = 0; d <= 256; ++d)
+        if (!((float)d < threshold)) {
+            d_lim = d;
+            break;
+        }
+    try {
+        ZS_CUDA(cudaSetDevice(h->device));
+        const int chunks = match_chunks(nl, nr);
+        using C = Carve;
+        aux_reserve(h, C::bytes<uint8_t>(32 * (size_t)nl) + C::bytes<uint8_t>(32 * (size_t)nr) +
+                           C::bytes<unsigned long long>(chunks > 1 ? (size_t)chunks * nl * k : 1) +
+                           C::bytes<unsigned long long>((size_t)nl * k));
+        C c(h->aux_buf);
+        uint8_t* dl = c.take<uint8_t>(32 * (size_t)nl);
+        uint8_t* dr = c.take<uint8_t>(32 * (size_t)nr);
+        unsigned long long* part = c.take<unsigned long long>(chunks > 1 ? (size_t)chunks * nl * k : 1);
+        unsigned long long* out = c.take<unsigned long long>((size_t)nl * k);
+        ZS_CUDA(cudaMemcpyAsync(dl, lhs, 32 * (size_t)nl, cudaMemcpyHostToDevice, h->stream));
+        if (nr > 0) ZS_CUDA(cudaMemcpyAsync(dr, rhs, 32 * (size_t)nr, cudaMemcpyHostToDevice, h->stream));
+        ZS_CUDA(cudaEventRecord(h->ev0, h->stream));
+        launch_match(dl, nl, dr, nr, k, d_lim, chunks, part, out, h->stream);
+        ZS_CUDA(cudaGetLastError());
+        ZS_CUDA(cudaEventRecord(h->ev1, h->stream));
+        std::vector<unsigned long long> keys((size_t)nl * k);
+        ZS_CUDA(cudaMemcpyAsync(keys.data(), out, sizeof(unsigned long long) * keys.size(), cudaMemcpyDeviceToHost,
+                                h->stream));
+        ZS_CUDA(cudaStreamSynchronize(h->stream));
+        if (ms_device) {
+            float ms = 0.f;
+            ZS_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+            *ms_device = ms;
+        }
+        // the reference's layout, feature.hpp:1204-1232
+        int64_t count = 0;
+        for (int i = 0; i < nl; ++i) {
+            if (count + k > matches_size) break;
+            for (int m = 0; m < k; ++m) {
+                const unsigned long long key = keys[(size_t)i * k + m];
+                if (key == ~0ull) break;
+                zs_match& o = matches[count++];
+                o.lhs_index = (uint64_t)i;
+                o.rhs_index = (uint64_t)(key & 0xffffffffull);
+                o.score = (float)(unsigned int)(key >> 32);
+            }
+        }
+        *found = count;
+    } catch (const CudaError& e) {
+        return cuda_status(e.err);
+    }
+    return ZS_OK;
+}
+
 int zs_map_cull(zs_ba_handle* h, const zs_map_cull_input* in, uint8_t* erase, float* mean_error,
                 zs_cull_report* rep) {
     if (!h || !in) return ZS_ERR_INVALID;
@@ -1313,12 +1380,12 @@ int zs_map_cull(zs_ba_handle* h, const zs_map_cull_input* in, uint8_t* erase, fl
     if (M > 0 && (!in->obs_frame || !in->obs_frame_id || !in->obs_keypoint)) return ZS_ERR_INVALID;
     try {
         ZS_CUDA(cudaSetDevice(h->device));
-        using C = CullCarve;
-        cull_reserve(h, C::bytes<unsigned long long>(4) + C::bytes<double>(12 * (size_t)F) +
+        using C = Carve;
+        aux_reserve(h, C::bytes<unsigned long long>(4) + C::bytes<double>(12 * (size_t)F) +
                             C::bytes<double>(4 * (size_t)F) + C::bytes<int32_t>(L) + C::bytes<double>(3 * (size_t)L) +
                             C::bytes<int64_t>((size_t)L + 1) + 2 * C::bytes<int32_t>((size_t)M) +
                             C::bytes<float2>((size_t)M) + C::bytes<uint8_t>(L) + C::bytes<float>(L));
-        C c(h->cull_buf);
+        C c(h->aux_buf);
         CullArgs a;
         a.L = L;
         a.F = F;
@@ -1372,11 +1439,11 @@ int zs_ba_cull(zs_ba_handle* h, const int32_t* landmark_id, const int32_t* pose_
     if ((P.L > 0 && !landmark_id) || (P.K > 0 && !pose_frame_id)) return ZS_ERR_INVALID;
     try {
         ZS_CUDA(cudaSetDevice(h->device));
-        using C = CullCarve;
-        cull_reserve(h, C::bytes<unsigned long long>(4) + C::bytes<double>(12 * (size_t)P.K) +
+        using C = Carve;
+        aux_reserve(h, C::bytes<unsigned long long>(4) + C::bytes<double>(12 * (size_t)P.K) +
                             C::bytes<double>(4) + C::bytes<int32_t>(P.L) + C::bytes<int32_t>(P.K) +
                             C::bytes<uint8_t>(P.L) + C::bytes<float>(P.L));
-        C c(h->cull_buf);
+        C c(h->aux_buf);
         CullArgs a;
         a.L = P.L;
         a.F = P.K;

@@ -303,6 +303,15 @@ void launch_pose_rt(int K, const double* pose, double* Rt, cudaStream_t s);
 void launch_cull(const CullArgs& a, const int64_t* obs_ptr, const float2* kp, cudaStream_t s);
 void launch_cull(const CullArgs& a, const int32_t* obs_ptr, const double2* kp, cudaStream_t s);
 
+// ---- descriptor matching (ba_match.cu) ----
+// Chunks of the rhs for n_lhs x n_rhs matching; launch_match writes, per lhs,
+// the k smallest keys (distance << 32 | rhs index) with distance < d_lim into
+// out [n_lhs * k] (~0 where fewer), using part [chunks * n_lhs * k] when
+// chunks > 1. lhs and rhs: 32-byte descriptors, 16-byte aligned.
+int match_chunks(int n_lhs, int n_rhs);
+void launch_match(const uint8_t* lhs, int n_lhs, const uint8_t* rhs, int n_rhs, int k, int d_lim, int chunks,
+                  unsigned long long* part, unsigned long long* out, cudaStream_t s);
+
 // ---- dense reduced system (ba_cholesky.cu) ----
 // launch_factor: S (n x n row-major, type TS) -> F = L (lower, type TF) and
 // D = the inverses of L's 32 x 32 diagonal blocks ([ceil(n/32) * 1024] TF);

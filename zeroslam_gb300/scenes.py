@@ -605,3 +605,29 @@ def slam_map(sc: Scene) -> CullMap:
     cm.landmark_id_generator = sc.L
     cm.frame_id_generator = sc.K
     return cm
+
+
+# ---------------------------------------------------------------- descriptors
+
+def descriptor_pair(n_lhs: int, n_rhs: int, seed: int = 0, near: float = 0.6, dup: float = 0.05):
+    """Two sets of 256-bit binary descriptors (uint8 [n, 32]) for matching.
+    rhs: uniform random bits, with a fraction ``dup`` of them exact copies of
+    other rhs descriptors (equal distances, so ties occur). lhs: a fraction
+    ``near`` are copies of a random rhs descriptor with 0-40 bits flipped
+    (true matches near zeroslam's threshold of 32), the rest uniform random
+    (distance ~128 to everything)."""
+    rng = np.random.default_rng(seed)
+    rhs = rng.integers(0, 256, size=(n_rhs, 32), dtype=np.uint8)
+    if n_rhs > 1:
+        d = np.flatnonzero(rng.random(n_rhs) < dup)
+        rhs[d] = rhs[rng.integers(0, n_rhs, d.size)]
+    lhs = rng.integers(0, 256, size=(n_lhs, 32), dtype=np.uint8)
+    if n_rhs > 0:
+        nr = np.flatnonzero(rng.random(n_lhs) < near)
+        lhs[nr] = rhs[rng.integers(0, n_rhs, nr.size)]
+        bits = np.unpackbits(lhs[nr], axis=1)
+        flips = rng.integers(0, 41, nr.size)
+        for row, f in enumerate(flips):
+            bits[row, rng.choice(256, size=f, replace=False)] ^= 1
+        lhs[nr] = np.packbits(bits, axis=1)
+    return lhs, rhs
