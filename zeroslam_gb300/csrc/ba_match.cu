@@ -6,7 +6,7 @@
 // and replacing only on a strict improvement, so equal distances keep the
 // earlier rhs. That is the k smallest keys (distance << 32 | rhs index), which
 // is what is computed here, in two launches:
-//   k_match_partial: a block holds 128 lhs descriptors (one per thread, in
+//   k_match_partial: a block holds 256 lhs descriptors (two per thread, in
 //     registers) and scans one chunk of the rhs through shared memory in
 //     tiles of 256 descriptors (every thread reads the same descriptor: a
 //     broadcast); XOR, a carry-save popcount of the 8 words, and an
@@ -23,7 +23,8 @@ namespace zs {
 
 namespace {
 
-constexpr int kMatchLhs = 128;   // lhs descriptors (threads) per block
+constexpr int kMatchLhs = 128;   // threads per block
+constexpr int kMatchPerBlock = 2 * kMatchLhs;  // lhs descriptors per block (two per thread)
 constexpr int kMatchTile = 256;  // rhs descriptors per shared-memory tile
 constexpr unsigned long long kNoKey = ~0ull;
 
@@ -70,20 +71,28 @@ __device__ __forceinline__ int popc8(unsigned x0, unsigned x1, unsigned x2, unsi
 }
 
 // part: [gridDim.y][n_lhs][K] keys, kNoKey where fewer than K were found.
+// Each thread holds two lhs descriptors (rows i and i + kMatchLhs of the
+// block's 2 kMatchLhs), so every shared-memory read of an rhs descriptor
+// serves two distances.
 template <int K>
 __global__ void __launch_bounds__(kMatchLhs) k_match_partial(const uint4* __restrict__ lhs, int n_lhs,
                                                              const uint4* __restrict__ rhs, int n_rhs, int chunk,
                                                              int d_lim, unsigned long long* __restrict__ part) {
     __shared__ uint4 s_rhs[2 * kMatchTile];
-    const int i = blockIdx.x * kMatchLhs + threadIdx.x;
-    uint4 a0 = make_uint4(0, 0, 0, 0), a1 = a0;
-    if (i < n_lhs) {
-        a0 = lhs[2 * (int64_t)i];
-        a1 = lhs[2 * (int64_t)i + 1];
+    const int i0 = blockIdx.x * kMatchPerBlock + threadIdx.x;
+    const int i1 = i0 + kMatchLhs;
+    uint4 a0 = make_uint4(0, 0, 0, 0), a1 = a0, c0 = a0, c1 = a0;
+    if (i0 < n_lhs) {
+        a0 = lhs[2 * (int64_t)i0];
+        a1 = lhs[2 * (int64_t)i0 + 1];
     }
-    unsigned long long best[K];
+    if (i1 < n_lhs) {
+        c0 = lhs[2 * (int64_t)i1];
+        c1 = lhs[2 * (int64_t)i1 + 1];
+    }
+    unsigned long long best[K], best1[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) best[k] = kNoKey;
+    for (int k = 0; k < K; ++k) best[k] = best1[k] = kNoKey;
     const int j0 = blockIdx.y * chunk;
     const int j1 = min(n_rhs, j0 + chunk);
     for (int t0 = j0; t0 < j1; t0 += kMatchTile) {
@@ -95,13 +104,22 @@ __global__ void __launch_bounds__(kMatchLhs) k_match_partial(const uint4* __rest
             const uint4 b0 = s_rhs[2 * r], b1 = s_rhs[2 * r + 1];
             const int d = popc8(a0.x ^ b0.x, a0.y ^ b0.y, a0.z ^ b0.z, a0.w ^ b0.w, a1.x ^ b1.x, a1.y ^ b1.y,
                                 a1.z ^ b1.z, a1.w ^ b1.w);
-            if (d < d_lim) insert_key<K>(best, ((unsigned long long)d << 32) | (unsigned int)(t0 + r));
+            const int e = popc8(c0.x ^ b0.x, c0.y ^ b0.y, c0.z ^ b0.z, c0.w ^ b0.w, c1.x ^ b1.x, c1.y ^ b1.y,
+                                c1.z ^ b1.z, c1.w ^ b1.w);
+            const unsigned j = (unsigned int)(t0 + r);
+            if (d < d_lim) insert_key<K>(best, ((unsigned long long)d << 32) | j);
+            if (e < d_lim) insert_key<K>(best1, ((unsigned long long)e << 32) | j);
         }
     }
-    if (i < n_lhs) {
-        unsigned long long* o = part + ((int64_t)blockIdx.y * n_lhs + i) * K;
+    if (i0 < n_lhs) {
+        unsigned long long* o = part + ((int64_t)blockIdx.y * n_lhs + i0) * K;
 #pragma unroll
         for (int k = 0; k < K; ++k) o[k] = best[k];
+    }
+    if (i1 < n_lhs) {
+        unsigned long long* o = part + ((int64_t)blockIdx.y * n_lhs + i1) * K;
+#pragma unroll
+        for (int k = 0; k < K; ++k) o[k] = best1[k];
     }
 }
 
@@ -130,7 +148,7 @@ template <int K>
 void launch_match_k(const uint8_t* lhs, int n_lhs, const uint8_t* rhs, int n_rhs, int d_lim, int chunks,
                     unsigned long long* part, unsigned long long* out, cudaStream_t s) {
     const int chunk = (n_rhs + chunks - 1) / chunks;
-    const dim3 grid((n_lhs + kMatchLhs - 1) / kMatchLhs, chunks);
+    const dim3 grid((n_lhs + kMatchPerBlock - 1) / kMatchPerBlock, chunks);
     unsigned long long* dst = chunks == 1 ? out : part;
     k_match_partial<K><<<grid, kMatchLhs, 0, s>>>(reinterpret_cast<const uint4*>(lhs), n_lhs,
                                                   reinterpret_cast<const uint4*>(rhs), n_rhs, chunk, d_lim, dst);
@@ -148,7 +166,7 @@ int match_chunks(int n_lhs, int n_rhs) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 152;
-    const int lhs_blocks = (n_lhs + kMatchLhs - 1) / kMatchLhs;
+    const int lhs_blocks = (n_lhs + kMatchPerBlock - 1) / kMatchPerBlock;
     const int want = (8 * sms + lhs_blocks - 1) / std::max(lhs_blocks, 1);  // ~8 blocks of 128 threads per SM
     const int most = std::max(1, (n_rhs + 63) / 64);                         // at least 64 rhs per chunk
     return std::max(1, std::min(want, most));
