@@ -9,7 +9,10 @@ checks run where the zeroslam source tree is (they skip elsewhere):
     vertices untouched when no GPU is usable (no CPU fallback);
   * zeroslam's own tests/factor_graph.test.cpp compiles unmodified against
     the drop-in (its solve sections need a GPU to pass);
-  * the drop-in's robust losses print bit-identical values to zeroslam's.
+  * the drop-in's robust losses print bit-identical values to zeroslam's;
+  * the map-level glue (include/zeroslam_gb300/map_glue.hpp) compiles against
+    zeroslam's map, frame, landmark and feature types and lays a map out as
+    the C ABI expects (tests/cpp/map_glue_test.cpp).
 """
 
 import os
@@ -64,3 +67,9 @@ def test_losses_match_reference(tmp_path):
     a = subprocess.run([mine], capture_output=True, text=True, check=True).stdout
     b = subprocess.run([ref], capture_output=True, text=True, check=True).stdout
     assert a == b and len(a.splitlines()) == 27
+
+
+def test_map_glue_host_checks(tmp_path):
+    exe = _compile(os.path.join(CPP, "map_glue_test.cpp"), str(tmp_path / "map_glue_test"))
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip().splitlines()[-1] == "OK", r.stderr
