@@ -92,3 +92,19 @@ def test_map_optimise_then_resident_cull(zs_lib, oracle):
     after.frame_pose, after.landmarks = fp, X
     e_o, m_o, n_o = oracle.map_cull(after)
     assert np.array_equal(e, e_o) and np.array_equal(m.view(np.uint32), m_o.view(np.uint32))
+
+
+def test_map_optimise_missing_frames(zs_lib, oracle):
+    """Observations whose frame is not in the map are skipped (zeroslam's
+    optimise requires every observing frame to be in the map): one round,
+    global and windowed, against the oracle's restatement."""
+    sc = scenes.arc_scene(12, 1200, seed=16, min_obs=2, **scenes.ADJOINT_INIT_NOISE)
+    cm = scenes.slam_map(sc)
+    cm.obs_frame = cm.obs_frame.copy()
+    cm.obs_frame[::9] = -1
+    for lw in (0, 4):
+        fo, Xo, info = oracle.map_optimise(cm, lw, False, 1)
+        with _ba() as h:
+            fp, X, rep = h.map_optimise(cm, lw, False, 1)
+        assert rep.edges == info["edges"] < int((cm.obs_frame >= 0).sum()) + 1
+        assert rel_err(fp, fo) < 1e-9 and rel_err(X, Xo) < 1e-9
