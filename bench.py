@@ -532,6 +532,24 @@ def map_section(args, dist: Dist, sc=None) -> dict:
                          "solve_ms": rep.solve.ms_total, "lm_iterations": rep.solve.iterations,
                          "frames": rep.frames, "landmarks": rep.landmarks, "edges": rep.edges,
                          "chi2": [rep.solve.chi2_initial, rep.solve.chi2_final]}
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        # one round of the whole map of a 30-keyframe, 6,000-landmark arc
+        # (167,607 edges) by the oracle (window selection, then its C solver)
+        # and by zs_map_optimise (FP64); zeroslam's own map::optimise builds its
+        # graph in time quadratic in the edges (~27 s for this map on one x86 core)
+        from oracle.oracle import Oracle
+
+        small = scenes.slam_map(scenes.arc_scene(30, 6000, seed=7, min_obs=2, **scenes.ADJOINT_INIT_NOISE))
+        t0 = time.perf_counter()
+        Oracle().map_optimise(small, 0, False, 1)
+        cpu_s = time.perf_counter() - t0
+        with ba.BundleAdjuster(precision=ba.FP64, device=dist.local) as h:
+            h.map_optimise(small, 0, False, 1)
+            t0 = time.perf_counter()
+            h.map_optimise(small, 0, False, 1)
+            gpu_s = time.perf_counter() - t0
+        out["cpu_baseline"] = {"workload": f"arc map: F={small.F}, L={small.L}, M={small.M}, one round, global",
+                               "ms": cpu_s * 1e3, "cores": 1, "kind": "port", "gpu_wall_ms": gpu_s * 1e3}
     return out
 
 
