@@ -329,7 +329,40 @@ def batch_section(args, dist: Dist) -> dict:
                     "bucket_windows": r["brep"]["bucket_windows"], "bucket_threads": r["brep"]["bucket_threads"]}
     out["mixed_over_fp64"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
     out["max_rel_cost_mixed_vs_fp64"] = float(np.max(np.abs(m["chi2"] - d["chi2"]) / d["chi2"]))
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        out["cpu_baseline"] = batch_cpu_baseline(wins, iters)
     return out
+
+
+def batch_cpu_baseline(wins, iters: int) -> dict:
+    """The windows as independent CPU solves, one window per host thread
+    across every host core (the reference's solver where it is built here,
+    else the oracle's C restatement; both release the interpreter lock while
+    they run): the first 4 x cores windows, wall time and the mean
+    single-core time per window."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import build as ob
+    from oracle.oracle import Oracle, Reference
+
+    kind = "reference" if os.path.exists(ob.REF_SO) and ob.reference_available() else "port"
+    impl = Reference() if kind == "reference" else Oracle()
+    cores = os.cpu_count() or 1
+    sample = wins[:min(len(wins), 4 * cores)]
+
+    def one(sc):
+        t0 = time.perf_counter()
+        impl.solve(sc, iters)
+        return time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        per = list(ex.map(one, sample))
+    wall = time.perf_counter() - t0
+    return {"value": len(sample) / wall, "unit": "windows/s", "cores": cores, "kind": kind,
+            "wall_s": wall, "single_core_s_per_window": float(np.mean(per)),
+            "sample": f"the first {len(sample)} of {len(wins)} windows, {iters} LM iterations each, "
+                      f"one window per host thread on {cores} threads"}
 
 
 def loop_section(args, dist: Dist) -> dict:
