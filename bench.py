@@ -384,7 +384,50 @@ def loop_section(args, dist: Dist) -> dict:
                     "obs_per_s": dist.sum(r["rep"]["attempts"] * sc.M) / sec}
     out["mixed_over_fp64"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
     out["mixed_rel_cost_vs_fp64"] = abs(m["chi2"] - d["chi2"]) / d["chi2"]
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        out["cpu_baseline"] = loop_cpu_estimate(sc)
     return out
+
+
+def loop_cpu_estimate(sc) -> dict:
+    """Seconds per LM iteration of the oracle's C restatement (one core) at
+    the loop scene, estimated from two bounded measurements, since a single
+    iteration takes about a minute there: the per-observation cost from one
+    iteration on the first 100 keyframes and the landmarks they see (minus
+    that run's dense factorisation), and the n = 6000 dense factorisation
+    from the n = 1200 one (n^3)."""
+    from oracle.oracle import Oracle
+    from zeroslam_gb300 import scenes
+
+    o = Oracle()
+    keep = sc.obs_pose < 100
+    lms = np.unique(sc.obs_landmark[keep])
+    remap = np.full(sc.L, -1, dtype=np.int64)
+    remap[lms] = np.arange(lms.size)
+    sub = scenes.Scene(name="loop_sample", poses=sc.poses[:100].copy(), pose_fixed=sc.pose_fixed[:100].copy(),
+                       landmarks=sc.landmarks[lms].copy(), landmark_fixed=sc.landmark_fixed[lms].copy(),
+                       obs_pose=sc.obs_pose[keep].copy(), obs_landmark=remap[sc.obs_landmark[keep]].astype(np.int32),
+                       obs_uv=sc.obs_uv[keep].copy())
+    rng = np.random.default_rng(0)
+
+    def chol_s(n):
+        G = rng.normal(size=(n, n))
+        A = G @ G.T + n * np.eye(n)
+        t0 = time.perf_counter()
+        o.cholesky(A)
+        return time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    o.solve(sub, 1)
+    t_sub = time.perf_counter() - t0
+    c600, c1200 = chol_s(6 * sub.K), chol_s(1200)
+    per_obs = max(0.0, t_sub - c600) / sub.M
+    chol = c1200 * (6 * sc.K / 1200.0) ** 3
+    est = per_obs * sc.M + chol
+    return {"value": 1.0 / est, "unit": "LM iters/s", "cores": 1, "kind": "port", "estimate": True,
+            "sample": f"one LM iteration on the first 100 keyframes (M={sub.M}): {t_sub:.2f} s, of which the "
+                      f"n=600 factorisation {c600:.2f} s; n=1200 factorisation {c1200:.2f} s, scaled by n^3 to "
+                      f"n={6 * sc.K}: {chol:.1f} s; estimate {per_obs * sc.M:.1f} s + {chol:.1f} s per iteration"}
 
 
 def adjoint_section(args, dist: Dist) -> dict:
