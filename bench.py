@@ -269,8 +269,18 @@ def run_solves(sc, precision: int, steps: int, warmup: int, iters: int, device: 
         reps.append(rep)
     dist.barrier()
     final_chi2 = h.chi2()
+    poses, lms = h.get_state()
     h.close()
-    return dict(ms=ms, iterations=it, launches=launches, chi2=final_chi2, rep=reps[-1].as_dict())
+    return dict(ms=ms, iterations=it, launches=launches, chi2=final_chi2, rep=reps[-1].as_dict(), poses=poses,
+                landmarks=lms)
+
+
+def rel_state(a: dict, b: dict) -> dict:
+    """Max-norm relative difference of two solves' final poses and landmarks."""
+    def rel(x, y):
+        return float(np.max(np.abs(x - y)) / max(float(np.max(np.abs(y))), 1e-300))
+
+    return {"poses": rel(a["poses"], b["poses"]), "landmarks": rel(a["landmarks"], b["landmarks"])}
 
 
 def batch_run(wins, precision: int, steps: int, warmup: int, iters: int, device: int, dist: Dist) -> dict:
@@ -384,6 +394,7 @@ def loop_section(args, dist: Dist) -> dict:
                     "obs_per_s": dist.sum(r["rep"]["attempts"] * sc.M) / sec}
     out["mixed_over_fp64"] = out["mixed"]["lm_iters_per_s"] / out["fp64"]["lm_iters_per_s"]
     out["mixed_rel_cost_vs_fp64"] = abs(m["chi2"] - d["chi2"]) / d["chi2"]
+    out["mixed_rel_state_vs_fp64"] = rel_state(m, d)
     if not args.no_cpu and dist.rank == 0 and dist.world == 1:
         out["cpu_baseline"] = loop_cpu_estimate(sc)
     return out
@@ -796,7 +807,8 @@ def ours_arm(args, dist: Dist):
                  "ms_per_step": max_ms_d / args.steps, "final_chi2": fp64["chi2"], "rep": fp64["rep"],
                  "roofline": roof_d, "profile_ms": prof_d["ms_phase"]},
         "mixed_over_fp64": value / value_d,
-        "mixed_final_chi2": mixed["chi2"], "mixed_rel_cost_vs_fp64": rel_cost, "mixed_rep": mixed["rep"],
+        "mixed_final_chi2": mixed["chi2"], "mixed_rel_cost_vs_fp64": rel_cost,
+        "mixed_rel_state_vs_fp64": rel_state(mixed, fp64), "mixed_rep": mixed["rep"],
         "profile_ms": prof_m["ms_phase"],
         "roofline": roof_m,
         "pipe_peaks": peaks,
