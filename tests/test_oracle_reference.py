@@ -110,3 +110,19 @@ def test_find_matches_parity(oracle, reference, seed):
     assert len(reference.find_matches(l, r, thr, k, size)) == want
     m = reference.find_matches(onehot, np.zeros((1, 32), dtype=np.uint8), 2.0, 1, 256)
     assert len(m) == 256 and np.all(m["score"] == 1.0)
+
+
+def test_solve_parity_k50_and_windows(oracle, reference):
+    """The oracle against the reference on a 50-keyframe scene (the
+    differentiable configuration's size) and on windows of the batched
+    configuration, over whole solves."""
+    sc = scenes.arc_scene(50, 1500, seed=51)
+    po, lo, rep = oracle.solve(sc, 3)
+    pr, lr, acc, c0, c1, _, _ = reference.solve(sc, 3)
+    assert rep.accepted == acc and abs(rep.chi2_final - c1) <= 1e-9 * c1
+    assert rel_err(po, pr) < 1e-8 and rel_err(lo, lr) < 1e-8
+    for w in (scenes.window_batch(256)[i] for i in (0, 2)):
+        po, lo, rep = oracle.solve(w, 10)
+        pr, lr, acc, c0, c1, _, _ = reference.solve(w, 10)
+        assert rep.accepted == acc and abs(rep.chi2_final - c1) <= 1e-9 * c1
+        assert rel_err(po, pr) < 1e-8
