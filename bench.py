@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-windows measurement")
     ap.add_argument("--batch-windows", type=int, default=256)
+    ap.add_argument("--batch-shard", action="store_true",
+                    help="with N ranks, split the windows over them by cost (default: every rank solves all)")
     ap.add_argument("--no-loop", action="store_true", help="skip the 4M-observation loop scene")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiable solve) timing")
     ap.add_argument("--no-cull", action="store_true", help="skip the map culling, map optimise and matching timings")
@@ -317,9 +319,11 @@ def batch_run(wins, precision: int, steps: int, warmup: int, iters: int, device:
 def batch_section(args, dist: Dist) -> dict:
     """256 independent windows (K in [5, 30], L in [200, 3000]), 10 LM
     iterations each, mixed and FP64, each a single graph launch."""
-    from zeroslam_gb300 import scenes
+    from zeroslam_gb300 import ba, scenes
 
     wins = scenes.window_batch(args.batch_windows)
+    if args.batch_shard and dist.world > 1:  # the windows split over the ranks, no exchange
+        wins = [wins[i] for i in ba.partition_windows(wins, dist.world)[dist.rank]]
     iters = 10
     m = batch_run(wins, 1, args.steps, args.warmup, iters, dist.local, dist)
     d = batch_run(wins, 0, args.steps, args.warmup, iters, dist.local, dist)

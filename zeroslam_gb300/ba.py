@@ -468,6 +468,27 @@ class BundleAdjuster:
         return dict(ok=(st == ZS_OK), S=S, bs=bs, delta=delta, b=b)
 
 
+def partition_windows(windows, parts: int) -> list:
+    """Splits independent windows over ``parts`` devices (one process per
+    GPU, no exchange between them): each window's cost is estimated as
+    M + n^3 (observations, and the dense reduced system of n = 6K), windows
+    are taken largest first and each goes to the part with the least cost so
+    far (ties to the lower part, then the lower window index), so every
+    process computes the same partition. Returns one ascending list of window
+    indices per part."""
+    if parts < 1:
+        raise ValueError("parts must be positive")
+    cost = [int(w.M) + (6 * int(w.K)) ** 3 for w in windows]
+    order = sorted(range(len(windows)), key=lambda i: (-cost[i], i))
+    load = [0] * parts
+    out = [[] for _ in range(parts)]
+    for i in order:
+        p = min(range(parts), key=lambda q: (load[q], q))
+        out[p].append(i)
+        load[p] += cost[i]
+    return [sorted(o) for o in out]
+
+
 def cull_input(cm):
     """A MapCullInput over the arrays of a ``scenes.CullMap``; returns
     (input, arrays that must stay alive while it is used)."""
