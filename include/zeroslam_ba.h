@@ -322,6 +322,17 @@ typedef struct zs_map_optimise_report {
 int zs_map_optimise(zs_ba_handle* h, zs_map_optimise_input* map, int32_t local_window, int32_t fix_landmarks,
                     int32_t rounds, int32_t use_relative, zs_map_optimise_report* rep);
 
+/* The window and graph zs_map_optimise would build, without a device or a
+ * handle (host work only): pose_frame [F] receives the frame index of each
+ * problem pose, landmark_index [L] the map landmark of each problem
+ * landmark, edge_obs [M] the observation (index into the map's observation
+ * arrays) of each edge, frame_written [F] 1 for the frames the optimise
+ * would write back; rep the counts and the outcome (ms_select and solve
+ * zero). Each output may be NULL. */
+int zs_map_optimise_plan(const zs_map_optimise_input* map, int32_t local_window, int32_t fix_landmarks,
+                         int32_t* pose_frame, int32_t* landmark_index, int64_t* edge_obs, uint8_t* frame_written,
+                         zs_map_optimise_report* rep);
+
 /* ---- map culling: map::map::cull (source/map.hpp:269-323) ----
  *
  * For each landmark, in the reference's order: kept untouched when

@@ -198,7 +198,7 @@ class Oracle:
             active_lm = [True] * L
         pose_fixed = [is_fixed(fid[f], local_window > 0) for f in range(F)]
         poses7 = self.rt_pose(fp)
-        lm_of, obs_pose, obs_lm, obs_uv = {}, [], [], []
+        lm_of, obs_pose, obs_lm, obs_uv, edge_obs = {}, [], [], [], []
         for l in range(L):
             if not active_lm[l]:
                 continue
@@ -212,6 +212,7 @@ class Oracle:
                     lm_of[l] = len(lm_of)
                 obs_pose.append(f)
                 obs_lm.append(lm_of[l])
+                edge_obs.append(o)
                 obs_uv.append([float(cm.obs_keypoint[o, 0]), float(cm.obs_keypoint[o, 1])])
         has_edge = [False] * F
         for f in obs_pose:
@@ -219,7 +220,9 @@ class Oracle:
         problem_frames = [f for f in range(F) if relevant[f] and has_edge[f]]
         nf_poses = sum(1 for f in problem_frames if not pose_fixed[f])
         nf_lms = 0 if fix_landmarks else len(lm_of)
-        info.update(frames=nf_poses, landmarks=nf_lms, edges=len(obs_pose))
+        info.update(frames=nf_poses, landmarks=nf_lms, edges=len(obs_pose), problem_frames=problem_frames,
+                    problem_landmarks=sorted(lm_of, key=lambda l: lm_of[l]), edge_obs=edge_obs,
+                    written=[bool(r) for r in relevant])
         if nf_poses == 0 and nf_lms == 0:
             info["status"] = 2
             return fp, X, info

@@ -132,7 +132,7 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
                  "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
-                 "zs_ba_cull", "zs_map_optimise", "zs_find_matches")
+                 "zs_ba_cull", "zs_map_optimise", "zs_find_matches", "zs_map_optimise_plan")
 
 
 def library_path() -> str:
@@ -196,6 +196,9 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_find_matches.restype = C.c_int
     lib.zs_find_matches.argtypes = [C.c_void_p, _up, C.c_int64, _up, C.c_int64, C.c_float, C.c_int64, C.c_void_p,
                                     C.c_int64, C.POINTER(C.c_int64), _dp]
+    lib.zs_map_optimise_plan.restype = C.c_int
+    lib.zs_map_optimise_plan.argtypes = [C.POINTER(MapOptimiseInput), C.c_int32, C.c_int32, _ip, _ip,
+                                         C.POINTER(C.c_int64), _up, C.POINTER(MapOptimiseReport)]
     lib.zs_map_optimise.restype = C.c_int
     lib.zs_map_optimise.argtypes = [C.c_void_p, C.POINTER(MapOptimiseInput), C.c_int32, C.c_int32, C.c_int32,
                                     C.c_int32, C.POINTER(MapOptimiseReport)]
@@ -487,6 +490,39 @@ def partition_windows(windows, parts: int) -> list:
         out[p].append(i)
         load[p] += cost[i]
     return [sorted(o) for o in out]
+
+
+def map_optimise_plan(cm, local_window: int, fix_landmarks: bool) -> dict:
+    """The window and graph map::optimise would build from a map
+    (zs_map_optimise_plan; host only, no device): problem poses as frame
+    indices, problem landmarks as map landmark indices, the edges as
+    observation indices, the frames written back, and the report."""
+    lib = load()
+    fid = np.ascontiguousarray(cm.frame_id, dtype=np.int32)
+    fp = np.ascontiguousarray(cm.frame_pose, dtype=np.float64)
+    intr = np.ascontiguousarray(cm.frame_intrinsics, dtype=np.float64)
+    lid = np.ascontiguousarray(cm.landmark_id, dtype=np.int32)
+    X = np.ascontiguousarray(cm.landmarks, dtype=np.float64)
+    ptr = np.ascontiguousarray(cm.landmark_obs, dtype=np.int64)
+    of = np.ascontiguousarray(cm.obs_frame, dtype=np.int32)
+    kp = np.ascontiguousarray(cm.obs_keypoint, dtype=np.float32)
+    inp = MapOptimiseInput(fp.shape[0], _p(fid, _ip), _p(fp, _dp), _p(intr, _dp), X.shape[0], _p(lid, _ip),
+                           _p(X, _dp), _p(ptr, C.POINTER(C.c_int64)), _p(of, _ip), _p(kp, C.POINTER(C.c_float)),
+                           int(cm.frame_id_generator))
+    F, L, M = fp.shape[0], X.shape[0], of.shape[0]
+    pose_frame = np.zeros(max(F, 1), dtype=np.int32)
+    lm_index = np.zeros(max(L, 1), dtype=np.int32)
+    edge_obs = np.zeros(max(M, 1), dtype=np.int64)
+    written = np.zeros(max(F, 1), dtype=np.uint8)
+    rep = MapOptimiseReport()
+    st = lib.zs_map_optimise_plan(C.byref(inp), int(local_window), int(bool(fix_landmarks)), _p(pose_frame, _ip),
+                                  _p(lm_index, _ip), _p(edge_obs, C.POINTER(C.c_int64)), _p(written, _up),
+                                  C.byref(rep))
+    if st != ZS_OK:
+        raise ZsError(st, "zs_map_optimise_plan")
+    return dict(report=rep, pose_frame=pose_frame[:rep.problem_poses].copy(),
+                landmark_index=lm_index[:rep.problem_landmarks].copy(), edge_obs=edge_obs[:rep.edges].copy(),
+                written=written[:F].astype(bool))
 
 
 def cull_input(cm):
