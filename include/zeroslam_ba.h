@@ -322,6 +322,14 @@ typedef struct zs_map_optimise_report {
 int zs_map_optimise(zs_ba_handle* h, zs_map_optimise_input* map, int32_t local_window, int32_t fix_landmarks,
                     int32_t rounds, int32_t use_relative, zs_map_optimise_report* rep);
 
+/* The conversions zs_map_optimise applies, host only: a frame's rotation
+ * matrix (row-major) and translation [12] to vertex_pose parameters
+ * [tx ty tz qx qy qz qw] as so3(rotation matrix) (source/lie.hpp:159-180,
+ * map.hpp:131-135), and back as so3::get_matrix (lie.hpp:188-204,
+ * map.hpp:247-251); both round as the reference does. */
+void zs_frame_to_pose(const double* frame_pose, double* pose);
+void zs_pose_to_frame(const double* pose, double* frame_pose);
+
 /* The window and graph zs_map_optimise would build, without a device or a
  * handle (host work only): pose_frame [F] receives the frame index of each
  * problem pose, landmark_index [L] the map landmark of each problem

@@ -56,3 +56,28 @@ def test_plan_outcomes(oracle):
     bad.obs_frame[0] = bad.F
     with pytest.raises(ba.ZsError):
         ba.map_optimise_plan(bad, 0, False)
+
+
+def _rotations(n, seed):
+    """Random rotations over the whole group (uniform unit quaternions), so
+    both branches of so3(rotation matrix) occur (trace <= 0 beyond 120 deg),
+    plus the half-turns about each axis."""
+    rng = np.random.default_rng(seed)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q = np.concatenate([q, [[0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1], [1, 0, 0, 0]]])
+    t = rng.normal(size=(q.shape[0], 3))
+    return scenes.pack_poses(q, t)
+
+
+def test_frame_pose_conversions_match_oracle(oracle):
+    """zs_frame_to_pose / zs_pose_to_frame, bit for bit with the oracle's
+    restatement (pinned to the reference in test_oracle_reference.py)."""
+    from zeroslam_gb300 import ba
+
+    poses = _rotations(500, 3)
+    frames = oracle.pose_rt(poses)
+    assert np.array_equal(ba.poses_to_frames(poses), frames)
+    tr = frames[:, 0] + frames[:, 4] + frames[:, 8]
+    assert (tr <= 0).sum() > 50 and (tr > 0).sum() > 50  # both branches
+    assert np.array_equal(ba.frames_to_poses(frames), oracle.rt_pose(frames))

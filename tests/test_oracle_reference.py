@@ -126,3 +126,18 @@ def test_solve_parity_k50_and_windows(oracle, reference):
         pr, lr, acc, c0, c1, _, _ = reference.solve(w, 10)
         assert rep.accepted == acc and abs(rep.chi2_final - c1) <= 1e-9 * c1
         assert rel_err(po, pr) < 1e-8
+
+
+def test_frame_pose_conversions_parity(oracle, reference):
+    """so3 from a rotation matrix and back (source/lie.hpp:159-204) over the
+    whole rotation group, both branches of the trace test, bit for bit."""
+    import numpy as np
+
+    rng = np.random.default_rng(5)
+    q = rng.normal(size=(400, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    poses = scenes.pack_poses(q, rng.normal(size=(400, 3)))
+    frames = reference.pose_rt(poses)
+    assert np.array_equal(oracle.pose_rt(poses), frames)
+    assert np.array_equal(oracle.rt_pose(frames), reference.rt_pose(frames))
+    assert (frames[:, 0] + frames[:, 4] + frames[:, 8] <= 0).sum() > 50

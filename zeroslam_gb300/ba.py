@@ -132,7 +132,8 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
                  "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
-                 "zs_ba_cull", "zs_map_optimise", "zs_find_matches", "zs_map_optimise_plan")
+                 "zs_ba_cull", "zs_map_optimise", "zs_find_matches", "zs_map_optimise_plan",
+                 "zs_frame_to_pose", "zs_pose_to_frame")
 
 
 def library_path() -> str:
@@ -196,6 +197,10 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_find_matches.restype = C.c_int
     lib.zs_find_matches.argtypes = [C.c_void_p, _up, C.c_int64, _up, C.c_int64, C.c_float, C.c_int64, C.c_void_p,
                                     C.c_int64, C.POINTER(C.c_int64), _dp]
+    lib.zs_frame_to_pose.restype = None
+    lib.zs_frame_to_pose.argtypes = [_dp, _dp]
+    lib.zs_pose_to_frame.restype = None
+    lib.zs_pose_to_frame.argtypes = [_dp, _dp]
     lib.zs_map_optimise_plan.restype = C.c_int
     lib.zs_map_optimise_plan.argtypes = [C.POINTER(MapOptimiseInput), C.c_int32, C.c_int32, _ip, _ip,
                                          C.POINTER(C.c_int64), _up, C.POINTER(MapOptimiseReport)]
@@ -490,6 +495,26 @@ def partition_windows(windows, parts: int) -> list:
         out[p].append(i)
         load[p] += cost[i]
     return [sorted(o) for o in out]
+
+
+def frames_to_poses(frame_pose) -> np.ndarray:
+    """[F, 7] vertex_pose parameters of [F, 12] frames (zs_frame_to_pose)."""
+    lib = load()
+    Rt = np.ascontiguousarray(frame_pose, dtype=np.float64).reshape(-1, 12)
+    out = np.zeros((Rt.shape[0], 7))
+    for f in range(Rt.shape[0]):
+        lib.zs_frame_to_pose(_p(Rt[f], _dp), _p(out[f], _dp))
+    return out
+
+
+def poses_to_frames(poses) -> np.ndarray:
+    """[K, 12] frames of [K, 7] poses (zs_pose_to_frame)."""
+    lib = load()
+    P = np.ascontiguousarray(poses, dtype=np.float64).reshape(-1, 7)
+    out = np.zeros((P.shape[0], 12))
+    for k in range(P.shape[0]):
+        lib.zs_pose_to_frame(_p(P[k], _dp), _p(out[k], _dp))
+    return out
 
 
 def map_optimise_plan(cm, local_window: int, fix_landmarks: bool) -> dict:

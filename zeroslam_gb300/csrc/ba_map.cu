@@ -74,6 +74,9 @@ void pose_to_rt(const double* p, double* Rt) {
 
 }  // namespace
 
+extern "C" void zs_frame_to_pose(const double* frame_pose, double* pose) { rt_to_pose(frame_pose, pose); }
+extern "C" void zs_pose_to_frame(const double* pose, double* frame_pose) { pose_to_rt(pose, frame_pose); }
+
 // The window and graph map::optimise builds from a map (map.hpp:65-233):
 // validation, window selection, the edges, removal of frames without edges
 // and the two early outcomes. Host-only: no device involved.
