@@ -225,6 +225,22 @@ int zs_ba_batch_solve_profile(zs_ba_handle* h, long long* out);
 /* Current state of one window ([K_w*7], [L_w*3]; either may be NULL). */
 int zs_ba_get_window_state(zs_ba_handle* h, int window, double* poses, double* landmarks);
 
+/* One attempt of the last zs_ba_solve: the values of the reference's verbose
+ * [GOOD] / [ BAD] lines (source/factor_graph.hpp:583-606). */
+typedef struct zs_ba_attempt {
+    int32_t iteration;  /* outer iteration, from 0 */
+    int32_t attempt;    /* attempt within the iteration (the reference's failure counter) */
+    int32_t solved;     /* 0: the damped linear solve failed (the reference's "Cholesky solver failed!") */
+    int32_t accepted;   /* 1: the step was kept */
+    double chi2;        /* cost at the attempted state (the current state's when not solved) */
+    double rho;         /* gain ratio (0 when not solved) */
+    double lambda;      /* damping after the attempt */
+} zs_ba_attempt;
+
+/* The attempts of the last zs_ba_solve on h, in order: *count receives their
+ * number, out the first min(count, capacity). */
+int zs_ba_get_history(zs_ba_handle* h, zs_ba_attempt* out, int32_t capacity, int32_t* count);
+
 /* Gradient of a scalar loss of the solved state with respect to the observed
  * pixels and the intrinsics, by the implicit-function theorem at the current
  * state (call after zs_ba_solve has converged). Inputs: a = dL/dx in the

@@ -21,6 +21,7 @@ STRUCTS = {  # C struct -> ctypes class in zeroslam_gb300.ba
     "zs_cull_report": "CullReport",
     "zs_map_optimise_input": "MapOptimiseInput",
     "zs_map_optimise_report": "MapOptimiseReport",
+    "zs_ba_attempt": "Attempt",
 }
 
 

@@ -251,3 +251,25 @@ def test_cauchy_tukey_losses(zs_lib, oracle, kind, precision):
     assert abs(r1.chi2_final - ro1.chi2_final) <= 1e-6 * ro1.chi2_final
     tol = 1e-5 if precision == 0 or kind == 2 else 1e-2
     assert abs(r.chi2_final - ro.chi2_final) <= tol * ro.chi2_final
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_solve_history(zs_lib, oracle, precision):
+    """zs_ba_get_history: one entry per attempt, consistent with the report
+    (attempts, accepted steps, failed solves, final cost and damping), and
+    the FP64 form's accept / reject sequence and costs as the oracle's."""
+    sc = scenes.arc_scene(15, 1500, seed=33, huber=True)
+    with _ba(zs_lib, precision) as h:
+        h.set_problem(sc)
+        r = h.solve(12)
+        hist = h.history()
+    assert len(hist) == r.attempts
+    assert sum(a["accepted"] for a in hist) == r.accepted
+    assert sum(not a["solved"] for a in hist) == r.cholesky_failures
+    assert [a["iteration"] for a in hist] == sorted(a["iteration"] for a in hist)
+    kept = [a["chi2"] for a in hist if a["accepted"]]
+    assert kept and kept[-1] == r.chi2_final and hist[-1]["lam"] == r.lambda_final
+    assert all(b < a for a, b in zip([r.chi2_initial] + kept, kept))  # accepted steps lower the cost
+    if precision == 0:
+        _, _, ro = oracle.solve(sc, 12)
+        assert (r.accepted, r.attempts) == (ro.accepted, ro.attempts)

@@ -78,6 +78,11 @@ class BatchReport(C.Structure):
         return d
 
 
+class Attempt(C.Structure):
+    _fields_ = [("iteration", C.c_int32), ("attempt", C.c_int32), ("solved", C.c_int32), ("accepted", C.c_int32),
+                ("chi2", C.c_double), ("rho", C.c_double), ("lambda", C.c_double)]
+
+
 class AdjointReport(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_residual", C.c_double),
                 ("ms_total", C.c_double)]
@@ -133,7 +138,7 @@ ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_b
                  "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
                  "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
                  "zs_ba_cull", "zs_map_optimise", "zs_find_matches", "zs_map_optimise_plan",
-                 "zs_frame_to_pose", "zs_pose_to_frame")
+                 "zs_frame_to_pose", "zs_pose_to_frame", "zs_ba_get_history")
 
 
 def library_path() -> str:
@@ -197,6 +202,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_find_matches.restype = C.c_int
     lib.zs_find_matches.argtypes = [C.c_void_p, _up, C.c_int64, _up, C.c_int64, C.c_float, C.c_int64, C.c_void_p,
                                     C.c_int64, C.POINTER(C.c_int64), _dp]
+    lib.zs_ba_get_history.restype = C.c_int
+    lib.zs_ba_get_history.argtypes = [C.c_void_p, C.POINTER(Attempt), C.c_int32, C.POINTER(C.c_int32)]
     lib.zs_frame_to_pose.restype = None
     lib.zs_frame_to_pose.argtypes = [_dp, _dp]
     lib.zs_pose_to_frame.restype = None
@@ -364,6 +371,19 @@ class BundleAdjuster:
         if v < 0:
             raise ZsError(v, "zs_ba_solve")
         return rep
+
+    def history(self) -> list:
+        """The last solve's attempts (zs_ba_get_history) as dicts."""
+        n = C.c_int32()
+        st = self.lib.zs_ba_get_history(self.h, None, 0, C.byref(n))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_get_history")
+        buf = (Attempt * max(n.value, 1))()
+        st = self.lib.zs_ba_get_history(self.h, buf, n.value, C.byref(n))
+        if st != ZS_OK:
+            raise ZsError(st, "zs_ba_get_history")
+        return [dict(iteration=a.iteration, attempt=a.attempt, solved=bool(a.solved), accepted=bool(a.accepted),
+                     chi2=a.chi2, rho=a.rho, lam=getattr(a, "lambda")) for a in buf[:n.value]]
 
     def chi2(self) -> float:
         out = C.c_double()

@@ -362,6 +362,7 @@ struct zs_ba_handle {
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
     HostScratch hscratch;        // build_problem's host arrays (pinned, reused)
+    std::vector<zs_ba_attempt> history;  // the last single-problem solve's attempts
     void* aux_buf = nullptr;     // device arrays of map culling and matching (handle lifetime, grown on demand)
     size_t aux_cap = 0;
     // batched windows
@@ -1139,6 +1140,7 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
                      lambda);
     const double legacy = o.legacy_stop * chi2;
     int success = 0;
+    h->history.clear();
     for (int it = 0; it < iterations; ++it) {
         r.iterations = it + 1;
         const double last = chi2;
@@ -1160,6 +1162,17 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
             read_state(h);
             r.attempts++;
             lambda = hs.lambda;
+            {
+                zs_ba_attempt a{};
+                a.iteration = it;
+                a.attempt = failures;
+                a.solved = hs.solve_ok ? 1 : 0;
+                a.accepted = hs.solve_ok && hs.good ? 1 : 0;
+                a.chi2 = hs.solve_ok ? hs.chi2_new : chi2;
+                a.rho = hs.solve_ok ? hs.rho : 0.0;
+                a.lambda = lambda;
+                h->history.push_back(a);
+            }
             if (!hs.solve_ok) {
                 r.cholesky_failures++;
                 if (sizeof(T) == 4) r.preconditioner_retries += hs.shifted;
@@ -1482,6 +1495,14 @@ int zs_ba_cull(zs_ba_handle* h, const int32_t* landmark_id, const int32_t* pose_
     } catch (const CudaError& e) {
         return cuda_status(e.err);
     }
+}
+
+int zs_ba_get_history(zs_ba_handle* h, zs_ba_attempt* out, int32_t capacity, int32_t* count) {
+    if (!h || !count || capacity < 0 || (capacity > 0 && !out)) return ZS_ERR_INVALID;
+    const int32_t n = (int32_t)h->history.size();
+    *count = n;
+    for (int32_t i = 0; i < n && i < capacity; ++i) out[i] = h->history[(size_t)i];
+    return ZS_OK;
 }
 
 int zs_ba_linear_step(zs_ba_handle* h, double lambda, double* S, double* bs, double* delta, double* b) {
