@@ -141,3 +141,15 @@ def test_frame_pose_conversions_parity(oracle, reference):
     assert np.array_equal(oracle.pose_rt(poses), frames)
     assert np.array_equal(oracle.rt_pose(frames), reference.rt_pose(frames))
     assert (frames[:, 0] + frames[:, 4] + frames[:, 8] <= 0).sum() > 50
+
+
+def test_map_cull_parity_large(oracle, reference):
+    """map::cull on an 844,142-observation map with every landmark in the
+    error pass (both id generators 0), landmark for landmark."""
+    sc = scenes.arc_scene(60, 20000, seed=99)
+    cm = scenes.cull_map(sc, seed=4, truth=True)
+    cm.landmark_id_generator = 0
+    cm.frame_id_generator = 0
+    e, _, n = oracle.map_cull(cm)
+    er, nr = reference.map_cull(cm)
+    assert cm.M > 800000 and n == nr > 0 and np.array_equal(e, er)
