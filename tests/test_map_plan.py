@@ -22,7 +22,7 @@ def _case_maps():
 @pytest.mark.parametrize("lw,fixl", [(0, False), (2, False), (4, False), (6, False), (1, True), (3, True),
                                      (0, True)])
 @pytest.mark.parametrize("which", ["map", "missing_frames"])
-def test_plan_matches_oracle(oracle, lw, fixl, which):
+def test_plan_matches_oracle(zs_lib, oracle, lw, fixl, which):
     from zeroslam_gb300 import ba
 
     cm = _case_maps()[which]
@@ -38,7 +38,7 @@ def test_plan_matches_oracle(oracle, lw, fixl, which):
         assert list(plan["written"]) == info["written"]
 
 
-def test_plan_outcomes(oracle):
+def test_plan_outcomes(zs_lib, oracle):
     from zeroslam_gb300 import ba
 
     cm = _case_maps()["map"]
@@ -70,7 +70,7 @@ def _rotations(n, seed):
     return scenes.pack_poses(q, t)
 
 
-def test_frame_pose_conversions_match_oracle(oracle):
+def test_frame_pose_conversions_match_oracle(zs_lib, oracle):
     """zs_frame_to_pose / zs_pose_to_frame, bit for bit with the oracle's
     restatement (pinned to the reference in test_oracle_reference.py)."""
     from zeroslam_gb300 import ba
