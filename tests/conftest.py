@@ -80,6 +80,33 @@ def known_answer_descriptors():
     return onehot, (lhs, rhs, 1.0, 2, 20, 12)
 
 
+def cull_boundary_maps():
+    """One-landmark maps at map::cull's boundaries (source/map.hpp:272-316):
+    a landmark id exactly 500 below the generator (looked at) and 501 below
+    (kept untouched); 4 observations whose last frame is exactly 7 and 8
+    below the frame generator, and 5 observations; depths exactly at and
+    just below 1e-12 (source/camera.hpp:98). Expected erase flags alongside."""
+    from zeroslam_gb300.scenes import CullMap
+
+    eye = [1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0]
+
+    def one(X, nobs, lm_id, lm_gen, last_frame_id, frame_gen):
+        return CullMap(frame_pose=np.array([eye + [0.0, 0.0, 0.0]]),
+                       frame_intrinsics=np.array([[1.0, 1.0, 0.5, 0.5]]),
+                       frame_id=np.array([last_frame_id], dtype=np.int32),
+                       landmark_id=np.array([lm_id], dtype=np.int32), landmarks=np.array([X], dtype=np.float64),
+                       landmark_obs=np.array([0, nobs], dtype=np.int64), obs_frame=np.zeros(nobs, dtype=np.int32),
+                       obs_frame_id=np.full(nobs, last_frame_id, dtype=np.int32),
+                       obs_keypoint=np.full((nobs, 2), 0.5, dtype=np.float32),
+                       landmark_id_generator=lm_gen, frame_id_generator=frame_gen)
+
+    behind, ahead = (0.0, 0.0, -1.0), (0.0, 0.0, 1.0)
+    return [(one(behind, 1, 100, 600, 0, 0), 1), (one(behind, 1, 100, 601, 0, 0), 0),
+            (one(ahead, 4, 0, 0, 10, 17), 0), (one(ahead, 4, 0, 0, 10, 18), 1), (one(ahead, 5, 0, 0, 10, 18), 0),
+            (one((0.0, 0.0, 1e-12), 1, 0, 0, 0, 0), 0),
+            (one((0.0, 0.0, float(np.nextafter(1e-12, 0.0))), 1, 0, 0, 0, 0), 1)]
+
+
 def known_answer_cull_maps():
     """The two cull cases of tests/map.test.cpp, as (name, map, erase):
     :128-143, a landmark at the origin seen once by a default frame (zero

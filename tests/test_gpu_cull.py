@@ -8,7 +8,7 @@ of a solve."""
 import numpy as np
 import pytest
 
-from conftest import CULL_FIXTURES, cull_from_npz, known_answer_cull_maps, load_npz
+from conftest import CULL_FIXTURES, cull_boundary_maps, cull_from_npz, known_answer_cull_maps, load_npz
 from zeroslam_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
@@ -116,3 +116,13 @@ def test_resident_cull_after_solve(zs_lib, oracle, precision):
         e_o, m_o, n_o = oracle.map_cull(cm)
         assert np.array_equal(e, e_o) and _same(m, m_o) and rep.erased == n_o
         assert 0 < n_o < sc.L
+
+
+def test_map_cull_boundaries(zs_lib, oracle):
+    """The cull's id, recency and depth boundaries: decisions and means as
+    the oracle's (pinned to the reference on the same maps)."""
+    with _ba() as h:
+        for cm, want in cull_boundary_maps():
+            e, m, _ = h.map_cull(cm)
+            e_o, m_o, _ = oracle.map_cull(cm)
+            assert int(e[0]) == int(e_o[0]) == want and _same(m, m_o)

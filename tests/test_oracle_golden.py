@@ -4,7 +4,8 @@ tests/golden/ (written by tests/golden/make_golden.py from the reference)."""
 import numpy as np
 import pytest
 
-from conftest import (CULL_FIXTURES, MAP_OPTIMISE_CASES, SOLVE_FIXTURES, cost_tol, cull_from_npz, known_answer_cull_maps,
+from conftest import (CULL_FIXTURES, MAP_OPTIMISE_CASES, SOLVE_FIXTURES, cost_tol, cull_boundary_maps, cull_from_npz,
+                      known_answer_cull_maps,
                       known_answer_descriptors, load_npz,
                       rel_err, scene_from_npz, state_tol)
 
@@ -150,3 +151,8 @@ def test_find_matches_known_answers(oracle):
     m = oracle.find_matches(onehot, zero, 2.0, 1, 256)
     assert len(m) == 256 and np.all(m["score"] == 1.0)
     assert len(oracle.find_matches(lhs, rhs, thr, k, size)) == want
+
+
+def test_map_cull_boundaries(oracle):
+    for cm, want in cull_boundary_maps():
+        assert int(oracle.map_cull(cm)[0][0]) == want

@@ -156,32 +156,15 @@ def test_map_cull_parity_large(oracle, reference):
 
 
 def test_map_cull_boundaries(oracle, reference):
-    """Boundaries of map::cull, oracle against the reference: a landmark id
-    exactly 500 below the generator (kept untouched) and 499 below (looked
-    at); 4 and 5 observations with the last frame exactly 7 and 8 below the
-    frame generator; depths exactly at and just below 1e-12; a NaN location."""
-    from zeroslam_gb300.scenes import CullMap
+    """map::cull's id, recency and depth boundaries and a NaN location,
+    oracle against the reference."""
+    from conftest import cull_boundary_maps
 
-    eye = [1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0]
-
-    def one(X, nobs, lm_id, lm_gen, last_frame_id, frame_gen, kp=(0.5, 0.5)):
-        return CullMap(frame_pose=np.array([eye + [0.0, 0.0, 0.0]]), frame_intrinsics=np.array([[1.0, 1.0, 0.5, 0.5]]),
-                       frame_id=np.array([last_frame_id], dtype=np.int32),
-                       landmark_id=np.array([lm_id], dtype=np.int32), landmarks=np.array([X], dtype=np.float64),
-                       landmark_obs=np.array([0, nobs], dtype=np.int64), obs_frame=np.zeros(nobs, dtype=np.int32),
-                       obs_frame_id=np.full(nobs, last_frame_id, dtype=np.int32),
-                       obs_keypoint=np.array([kp] * nobs, dtype=np.float32).reshape(nobs, 2),
-                       landmark_id_generator=lm_gen, frame_id_generator=frame_gen)
-
-    far = (0.0, 0.0, -1.0)  # behind the camera: the error pass erases it
-    cases = [one(far, 1, 100, 600, 0, 0), one(far, 1, 100, 601, 0, 0),
-             one((0.0, 0.0, 1.0), 4, 0, 0, 10, 17), one((0.0, 0.0, 1.0), 4, 0, 0, 10, 18),
-             one((0.0, 0.0, 1.0), 5, 0, 0, 10, 18),
-             one((0.0, 0.0, 1e-12), 1, 0, 0, 0, 0), one((0.0, 0.0, np.nextafter(1e-12, 0.0)), 1, 0, 0, 0, 0),
-             one((np.nan, 0.0, 1.0), 1, 0, 0, 0, 0)]
-    for cm in cases:
+    maps = [cm for cm, _ in cull_boundary_maps()]
+    nan = cull_boundary_maps()[2][0]
+    nan.landmarks = np.array([[np.nan, 0.0, 1.0]])
+    for cm in maps + [nan]:
         e, _, _ = oracle.map_cull(cm)
         er, _ = reference.map_cull(cm)
         assert np.array_equal(e, er)
-    got = [int(oracle.map_cull(cm)[0][0]) for cm in cases]
-    assert got == [1, 0, 0, 1, 0, 0, 1, 0]
+    assert int(oracle.map_cull(nan)[0][0]) == 0  # a NaN mean is not >= 5.991
