@@ -26,15 +26,10 @@ def test_reference_arm_line():
 def test_reference_arm_two_ranks():
     """Launched as the driver launches N > 1 (torchrun, 127.0.0.1): rank 0
     alone prints the line, the other rank exits 0 without work."""
-    import socket
-
-    with socket.socket() as s:
-        s.bind(("127.0.0.1", 0))
-        port = s.getsockname()[1]
-    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
-                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-                        "--workload", "arc", "--steps", "1", "--warmup", "3"], cwd=ROOT, capture_output=True,
-                       text=True, timeout=600)
+    # --standalone picks its own free rendezvous port on 127.0.0.1
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--standalone", "--local-addr", "127.0.0.1",
+                        "--nnodes=1", "--nproc-per-node", "2", "bench.py", "--impl", "reference", "--workload", "arc",
+                        "--steps", "1", "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1 and json.loads(lines[0])["impl"] == "reference"

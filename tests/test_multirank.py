@@ -43,8 +43,14 @@ def test_dist_two_ranks_gloo(tmp_path):
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
 
-    port = _free_port()
-    mp.start_processes(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    for attempt in range(3):  # a port taken between the probe and the rendezvous: try another
+        try:
+            mp.start_processes(_rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True,
+                               start_method="spawn")
+            break
+        except Exception:
+            if attempt == 2:
+                raise
     rows = [open(tmp_path / f"rank{r}.txt").read().split() for r in range(2)]
     for mx, sm, done, _ in rows:
         assert float(mx) == 2.0 and float(sm) == 30.0 and float(done) == 24.0
