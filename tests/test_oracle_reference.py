@@ -168,3 +168,19 @@ def test_map_cull_boundaries(oracle, reference):
         er, _ = reference.map_cull(cm)
         assert np.array_equal(e, er)
     assert int(oracle.map_cull(nan)[0][0]) == 0  # a NaN mean is not >= 5.991
+
+
+def test_find_matches_random_trials(oracle, reference):
+    """Small random trials over sizes, thresholds (including non-integers),
+    k and capacities, with descriptors drawn from few distinct values so that
+    ties are frequent; oracle and reference match for match."""
+    rng = np.random.default_rng(12)
+    for _ in range(40):
+        nl, nr = int(rng.integers(0, 40)), int(rng.integers(0, 40))
+        pool = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+        lhs = pool[rng.integers(0, 6, nl)] ^ (rng.random((nl, 32)) < 0.02).astype(np.uint8)
+        rhs = pool[rng.integers(0, 6, nr)] ^ (rng.random((nr, 32)) < 0.02).astype(np.uint8)
+        thr = float(rng.choice([0.0, 1.0, 5.5, 32.0, 129.0, 300.0]))
+        k = int(rng.integers(1, 9))
+        size = int(rng.integers(0, 3 * max(nl, 1) * k))
+        assert np.array_equal(oracle.find_matches(lhs, rhs, thr, k, size), reference.find_matches(lhs, rhs, thr, k, size))
