@@ -12,6 +12,13 @@ seeded. A step is one full 20-iteration solve from the initial state.
 
 Under torchrun each rank solves its own replica (independent problems, no
 collective): value = iterations of all ranks / max-over-ranks time.
+
+The same JSON line carries the other configurations and rows as sections:
+batched_windows (256 local windows, with a CPU baseline over every host
+core), loop_4m (the 4M-observation loop), adjoint (gradients of the solved
+state), map_cull (map::cull), map_optimise (map::optimise over map arrays)
+and matching (feature::find_matches). --map-only prints the last three
+alone; --no-batch / --no-loop / --no-adjoint / --no-cull skip sections.
 """
 
 from __future__ import annotations
