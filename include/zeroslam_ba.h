@@ -161,7 +161,12 @@ int zs_ba_reset_state(zs_ba_handle* h);
 
 /* Levenberg-Marquardt with Schur complement, `iterations` outer iterations,
  * stop rule as source/factor_graph.hpp:608-611. Returns the accepted-step
- * count (>= 0) or a negative status; `rep` may be NULL. */
+ * count (>= 0) or a negative status; `rep` may be NULL. A ZS_PRECISION_MIXED
+ * handle with a ZS_LOSS_TUKEY problem returns ZS_ERR_UNSUPPORTED: under that
+ * redescending loss the mixed form's rounding moves observations across the
+ * loss's threshold and the solve can settle in another nearby minimum than
+ * the FP64 one, so it cannot promise the mixed form's agreement with FP64
+ * (use a ZS_PRECISION_FP64 handle). */
 int zs_ba_solve(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* rep);
 
 /* Robust chi2 of the current state. */
@@ -434,9 +439,14 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, 
  * zs_dense_cholesky_solve; L and x may be NULL. Runs on the current device's
  * legacy default stream and returns after the result is copied back. The
  * first call on each device looks the workspace address up, so make that
- * first call before any stream capture. All calls share the one workspace:
+ * first call before any stream capture; the address is kept for the life of
+ * the process, so after a cudaDeviceReset of a device this entry point must
+ * not be called on that device again. All calls share the one workspace:
  * calls that overlap on the GPU (other host threads, other streams) race.
- * Returns ZS_OK or ZS_ERR_CHOLESKY. */
+ * Returns ZS_OK, ZS_ERR_CHOLESKY (a pivot or solve test failed),
+ * ZS_ERR_INVALID (null A or b, n <= 0 or n > ZS_NOALLOC_MAX_N) or
+ * ZS_ERR_CUDA / ZS_ERR_OUT_OF_MEMORY (a CUDA call failed; zs_last_error()
+ * names it). */
 int zs_dense_cholesky_solve_noalloc(const double* A, int n, const double* b, double* L, double* x);
 
 /* Measures the FP64 and FP32 fused multiply-add pipe peaks of `device` with

@@ -6,8 +6,62 @@
 #include "ba_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+
+/* ---------------------------------------------------------------- threads
+ * The restatement may spread its loops over host threads. Every floating-point
+ * value is still computed by the same operations in the same order as with one
+ * thread (threads own disjoint outputs; sums keep their serial order), so the
+ * results are bit-for-bit those of the serial restatement for any thread count. */
+
+static int g_threads = 1;
+
+void zso_set_threads(int n) { g_threads = n < 1 ? 1 : (n > 256 ? 256 : n); }
+int zso_get_threads(void) { return g_threads; }
+
+typedef void (*range_fn)(void* ctx, long long lo, long long hi);
+
+typedef struct range_job {
+    range_fn fn;
+    void* ctx;
+    long long lo, hi;
+} range_job;
+
+static void* range_run(void* a) {
+    range_job* j = (range_job*)a;
+    j->fn(j->ctx, j->lo, j->hi);
+    return NULL;
+}
+
+/* fn over [bounds[t], bounds[t+1]) for t < parts, one thread each (the caller
+ * runs part 0). */
+static void run_parts(range_fn fn, void* ctx, const long long* bounds, int parts) {
+    range_job jobs[256];
+    pthread_t tid[256];
+    int started[256];
+    for (int t = 0; t < parts; ++t) {
+        jobs[t].fn = fn; jobs[t].ctx = ctx; jobs[t].lo = bounds[t]; jobs[t].hi = bounds[t + 1];
+        started[t] = 0;
+    }
+    for (int t = 1; t < parts; ++t) started[t] = pthread_create(&tid[t], NULL, range_run, &jobs[t]) == 0;
+    range_run(&jobs[0]);
+    for (int t = 1; t < parts; ++t) {
+        if (started[t]) pthread_join(tid[t], NULL);
+        else range_run(&jobs[t]); /* no thread to be had: run the part here */
+    }
+}
+
+/* fn over [0, n) in g_threads equal contiguous parts (serial below min_n). */
+static void parallel_for(long long n, long long min_n, range_fn fn, void* ctx) {
+    int parts = g_threads;
+    if (n < min_n || parts <= 1) parts = 1;
+    if (parts > n) parts = (int)(n > 0 ? n : 1);
+    long long bounds[257];
+    for (int t = 0; t <= parts; ++t) bounds[t] = n * t / parts;
+    run_parts(fn, ctx, bounds, parts);
+}
 
 #define PENALTY 0.3 /* source/factor_graph.hpp:981 */
 
@@ -205,10 +259,10 @@ static double edge_chi2(const double r[2], const double* om) {
     return a * r[0] + b * r[1];
 }
 
-double zso_chi2(const zso_problem* p) {
-    /* get_current_chi, source/factor_graph.hpp:618-629 */
-    double total = 0.0;
-    for (long long o = 0; o < p->num_obs; ++o) {
+static void chi2_terms(void* ctx, long long lo, long long hi) {
+    const zso_problem* p = ((const zso_problem**)ctx)[0];
+    double* term = ((double**)ctx)[1];
+    for (long long o = lo; o < hi; ++o) {
         const double* pose = p->poses + 7LL * p->obs_pose[o];
         const double* X = p->landmarks + 3LL * p->obs_landmark[o];
         double r[2];
@@ -217,8 +271,20 @@ double zso_chi2(const zso_problem* p) {
         const double e2 = edge_chi2(r, om);
         double rho[3];
         zso_loss(p->loss_kind, p->loss_delta, e2, rho);
-        total += (p->loss_kind ? rho[0] : e2);
+        term[o] = p->loss_kind ? rho[0] : e2;
     }
+}
+
+double zso_chi2(const zso_problem* p) {
+    /* get_current_chi, source/factor_graph.hpp:618-629: the edges' robust
+     * terms (in parallel), then their sum in edge order */
+    double* term = malloc(((size_t)p->num_obs + 1) * sizeof(double));
+    if (!term) return NAN;
+    void* ctx[2] = {(void*)p, term};
+    parallel_for(p->num_obs, 4096, chi2_terms, ctx);
+    double total = 0.0;
+    for (long long o = 0; o < p->num_obs; ++o) total += term[o];
+    free(term);
     return total;
 }
 
@@ -245,24 +311,65 @@ int zso_invert3(const double a[9], double o[9]) {
     return 1;
 }
 
+typedef struct chol_ctx {
+    const double* A;
+    double* L;
+    int n, i0;
+} chol_ctx;
+
+/* Rows i0 + [lo, hi) of the factor, columns k < i0 (rows < i0 are final):
+ * the reference's formula for each entry, k outer so that each earlier row is
+ * read once per part. */
+static void chol_rows(void* c, long long lo, long long hi) {
+    const chol_ctx* x = (const chol_ctx*)c;
+    const int n = x->n;
+    for (int k = 0; k < x->i0; ++k) {
+        const double* Lk = x->L + (size_t)k * n;
+        for (long long r = lo; r < hi; ++r) {
+            const size_t i = (size_t)(x->i0 + r);
+            double* Li = x->L + i * n;
+            double v = x->A[i * n + k];
+            for (int j = 0; j < k; ++j) v -= Li[j] * Lk[j];
+            Li[k] = v / Lk[k];
+        }
+    }
+}
+
 int zso_cholesky(const double* A, int n, double* L) {
-    /* decompose_cholesky, source/matrix_decomposition_cholesky.hpp:26-59 */
+    /* decompose_cholesky, source/matrix_decomposition_cholesky.hpp:26-59: row
+     * by row, L_ik = (A_ik - sum_{j<k} L_ij L_kj) / L_kk, then the pivot
+     * A_ii - sum_{j<i} L_ij^2 must exceed 1e-14 max|A_ii|. Rows go in blocks of
+     * 64: the columns left of a block depend only on earlier rows and are
+     * formed for all its rows in parallel; the rest of the block follows row by
+     * row. Each entry is the same sequence of operations as in the serial
+     * loop; after a failed pivot the rows below it are zero, as there. */
     memset(L, 0, (size_t)n * n * sizeof(double));
     double scale = 0.0;
     for (int i = 0; i < n; ++i) scale = fmax(scale, fabs(A[(size_t)i * n + i]));
     const double eps = scale * 1e-14;
-    for (int i = 0; i < n; ++i) {
-        const double* Li = L + (size_t)i * n;
-        for (int k = 0; k < i; ++k) {
-            const double* Lk = L + (size_t)k * n;
-            double v = A[(size_t)i * n + k];
-            for (int j = 0; j < k; ++j) v -= Li[j] * Lk[j];
-            L[(size_t)i * n + k] = v / Lk[k];
+    const int B = 64;
+    for (int i0 = 0; i0 < n; i0 += B) {
+        const int i1 = i0 + B < n ? i0 + B : n;
+        if (i0 > 0) {
+            chol_ctx c = {A, L, n, i0};
+            parallel_for(i1 - i0, (long long)(n >= 512 ? 1 : B + 1), chol_rows, &c);
         }
-        double v = A[(size_t)i * n + i];
-        for (int j = 0; j < i; ++j) v -= Li[j] * Li[j];
-        if (!(v > eps)) return 0;
-        L[(size_t)i * n + i] = sqrt(v);
+        for (int i = i0; i < i1; ++i) {
+            double* Li = L + (size_t)i * n;
+            for (int k = i0; k < i; ++k) {
+                const double* Lk = L + (size_t)k * n;
+                double v = A[(size_t)i * n + k];
+                for (int j = 0; j < k; ++j) v -= Li[j] * Lk[j];
+                Li[k] = v / Lk[k];
+            }
+            double v = A[(size_t)i * n + i];
+            for (int j = 0; j < i; ++j) v -= Li[j] * Li[j];
+            if (!(v > eps)) {
+                if (i + 1 < n) memset(L + (size_t)(i + 1) * n, 0, (size_t)(n - i - 1) * n * sizeof(double));
+                return 0;
+            }
+            Li[i] = sqrt(v);
+        }
     }
     return 1;
 }
@@ -304,27 +411,22 @@ static void lin_free(lin* s) {
     free(s->hpp); free(s->hll); free(s->b); free(s->lm_ptr); free(s->blk_pose); free(s->hpl);
 }
 
-/* make_hessian, source/factor_graph.hpp:648-732. */
-static int linearise(const zso_problem* p, lin* s) {
-    const int K = p->num_poses, L = p->num_landmarks;
-    const long long M = p->num_obs;
-    const int n = 6 * K;
-    memset(s, 0, sizeof(*s));
-    s->K = K; s->L = L;
-    s->hpp = calloc((size_t)K * 36, sizeof(double));
-    s->hll = calloc((size_t)L * 9 + 1, sizeof(double));
-    s->b = calloc((size_t)n + 3 * (size_t)L + 1, sizeof(double));
-    s->lm_ptr = calloc((size_t)L + 1, sizeof(int));
-    double* hpl_obs = calloc((size_t)M * 18 + 1, sizeof(double));
-    if (!s->hpp || !s->hll || !s->b || !s->lm_ptr || !hpl_obs) { free(hpl_obs); lin_free(s); return 0; }
-    for (long long o = 0; o < M; ++o) {
+/* Per edge: r (2), J_p (12), J_l (6), the robust weight W (4), rho' and
+ * Omega r (2). */
+#define EDGE_TERMS 27
+
+static void edge_terms(void* ctx, long long lo, long long hi) {
+    const zso_problem* p = (const zso_problem*)((void**)ctx)[0];
+    double* et = (double*)((void**)ctx)[1];
+    for (long long o = lo; o < hi; ++o) {
+        double* e = et + EDGE_TERMS * o;
+        double* r = e;
+        double* W = e + 20;
         const int pi = p->obs_pose[o], li = p->obs_landmark[o];
-        const int pf = p->pose_fixed[pi], lf = p->landmark_fixed[li];
-        double r[2], Jp[12], Jl[6];
-        zso_edge(p->poses + 7LL * pi, p->landmarks + 3LL * li, p->obs_uv + 2 * o, p->intrinsics, r, Jp, Jl);
+        zso_edge(p->poses + 7LL * pi, p->landmarks + 3LL * li, p->obs_uv + 2 * o, p->intrinsics, r, e + 2, e + 14);
         const double* om = p->obs_info ? p->obs_info + 4 * o : IDENT2;
         /* edge_base::robust_info, source/factor_graph.hpp:254-269 */
-        double W[4] = {om[0], om[1], om[2], om[3]};
+        for (int i = 0; i < 4; ++i) W[i] = om[i];
         double drho = 1.0;
         if (p->loss_kind) {
             const double e2 = edge_chi2(r, om);
@@ -341,36 +443,94 @@ static int linearise(const zso_problem* p, lin* s) {
                 W[3] += 2.0 * rho[2] * we1 * we1;
             }
         }
+        e[24] = drho;
         /* Omega r for the gradient (the non-robust information scaled by drho). */
-        const double orr[2] = {om[0] * r[0] + om[1] * r[1], om[2] * r[0] + om[3] * r[1]};
-        if (!pf) {
-            double JtW[12]; /* 6x2 */
-            for (int a = 0; a < 6; ++a) {
-                JtW[a * 2 + 0] = Jp[0 * 6 + a] * W[0] + Jp[1 * 6 + a] * W[2];
-                JtW[a * 2 + 1] = Jp[0 * 6 + a] * W[1] + Jp[1 * 6 + a] * W[3];
-            }
-            double* H = s->hpp + 36LL * pi;
-            for (int a = 0; a < 6; ++a)
-                for (int c = 0; c < 6; ++c) H[a * 6 + c] += JtW[a * 2] * Jp[c] + JtW[a * 2 + 1] * Jp[6 + c];
-            if (!lf) {
-                double* B = hpl_obs + 18 * o;
-                for (int a = 0; a < 6; ++a)
-                    for (int c = 0; c < 3; ++c) B[a * 3 + c] = JtW[a * 2] * Jl[c] + JtW[a * 2 + 1] * Jl[3 + c];
-            }
-            for (int a = 0; a < 6; ++a) s->b[6 * pi + a] -= drho * (Jp[a] * orr[0] + Jp[6 + a] * orr[1]);
-        }
-        if (!lf) {
-            double JtW[6]; /* 3x2 */
-            for (int a = 0; a < 3; ++a) {
-                JtW[a * 2 + 0] = Jl[0 * 3 + a] * W[0] + Jl[1 * 3 + a] * W[2];
-                JtW[a * 2 + 1] = Jl[0 * 3 + a] * W[1] + Jl[1 * 3 + a] * W[3];
-            }
-            double* H = s->hll + 9LL * li;
-            for (int a = 0; a < 3; ++a)
-                for (int c = 0; c < 3; ++c) H[a * 3 + c] += JtW[a * 2] * Jl[c] + JtW[a * 2 + 1] * Jl[3 + c];
-            for (int a = 0; a < 3; ++a) s->b[n + 3 * li + a] -= drho * (Jl[a] * orr[0] + Jl[3 + a] * orr[1]);
-        }
+        e[25] = om[0] * r[0] + om[1] * r[1];
+        e[26] = om[2] * r[0] + om[3] * r[1];
     }
+}
+
+typedef struct lin_ctx {
+    const zso_problem* p;
+    lin* s;
+    const double* et;
+    double* hpl_obs;
+} lin_ctx;
+
+/* H_pp, b_p and the per-edge H_pl blocks of the poses in [k0, k1): each
+ * pose's sums over its edges in edge order. */
+static void lin_pose_sums(void* ctx, long long k0, long long k1) {
+    const lin_ctx* x = (const lin_ctx*)ctx;
+    const zso_problem* p = x->p;
+    for (long long o = 0; o < p->num_obs; ++o) {
+        const int pi = p->obs_pose[o], li = p->obs_landmark[o];
+        if (pi < k0 || pi >= k1 || p->pose_fixed[pi]) continue;
+        const double* e = x->et + EDGE_TERMS * o;
+        const double *Jp = e + 2, *Jl = e + 14, *W = e + 20, *orr = e + 25;
+        const double drho = e[24];
+        double JtW[12]; /* 6x2 */
+        for (int a = 0; a < 6; ++a) {
+            JtW[a * 2 + 0] = Jp[0 * 6 + a] * W[0] + Jp[1 * 6 + a] * W[2];
+            JtW[a * 2 + 1] = Jp[0 * 6 + a] * W[1] + Jp[1 * 6 + a] * W[3];
+        }
+        double* H = x->s->hpp + 36LL * pi;
+        for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 6; ++c) H[a * 6 + c] += JtW[a * 2] * Jp[c] + JtW[a * 2 + 1] * Jp[6 + c];
+        if (!p->landmark_fixed[li]) {
+            double* B = x->hpl_obs + 18 * o;
+            for (int a = 0; a < 6; ++a)
+                for (int c = 0; c < 3; ++c) B[a * 3 + c] = JtW[a * 2] * Jl[c] + JtW[a * 2 + 1] * Jl[3 + c];
+        }
+        for (int a = 0; a < 6; ++a) x->s->b[6 * pi + a] -= drho * (Jp[a] * orr[0] + Jp[6 + a] * orr[1]);
+    }
+}
+
+/* H_ll and b_l of the landmarks in [l0, l1), each summed in edge order. */
+static void lin_landmark_sums(void* ctx, long long l0, long long l1) {
+    const lin_ctx* x = (const lin_ctx*)ctx;
+    const zso_problem* p = x->p;
+    const int n = 6 * p->num_poses;
+    for (long long o = 0; o < p->num_obs; ++o) {
+        const int li = p->obs_landmark[o];
+        if (li < l0 || li >= l1 || p->landmark_fixed[li]) continue;
+        const double* e = x->et + EDGE_TERMS * o;
+        const double *Jl = e + 14, *W = e + 20, *orr = e + 25;
+        const double drho = e[24];
+        double JtW[6]; /* 3x2 */
+        for (int a = 0; a < 3; ++a) {
+            JtW[a * 2 + 0] = Jl[0 * 3 + a] * W[0] + Jl[1 * 3 + a] * W[2];
+            JtW[a * 2 + 1] = Jl[0 * 3 + a] * W[1] + Jl[1 * 3 + a] * W[3];
+        }
+        double* H = x->s->hll + 9LL * li;
+        for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) H[a * 3 + c] += JtW[a * 2] * Jl[c] + JtW[a * 2 + 1] * Jl[3 + c];
+        for (int a = 0; a < 3; ++a) x->s->b[n + 3 * li + a] -= drho * (Jl[a] * orr[0] + Jl[3 + a] * orr[1]);
+    }
+}
+
+/* make_hessian, source/factor_graph.hpp:648-732: per-edge terms (in
+ * parallel), then every pose's and landmark's sums in edge order. */
+static int linearise(const zso_problem* p, lin* s) {
+    const int K = p->num_poses, L = p->num_landmarks;
+    const long long M = p->num_obs;
+    const int n = 6 * K;
+    memset(s, 0, sizeof(*s));
+    s->K = K; s->L = L;
+    s->hpp = calloc((size_t)K * 36, sizeof(double));
+    s->hll = calloc((size_t)L * 9 + 1, sizeof(double));
+    s->b = calloc((size_t)n + 3 * (size_t)L + 1, sizeof(double));
+    s->lm_ptr = calloc((size_t)L + 1, sizeof(int));
+    double* hpl_obs = calloc((size_t)M * 18 + 1, sizeof(double));
+    if (!s->hpp || !s->hll || !s->b || !s->lm_ptr || !hpl_obs) { free(hpl_obs); lin_free(s); return 0; }
+    /* per-edge terms (in parallel), then the sums in edge order */
+    double* et = malloc(((size_t)M + 1) * EDGE_TERMS * sizeof(double));
+    if (!et) { free(hpl_obs); lin_free(s); return 0; }
+    void* ectx[2] = {(void*)p, et};
+    parallel_for(M, 4096, edge_terms, ectx);
+    lin_ctx c = {p, s, et, hpl_obs};
+    parallel_for(K, 64, lin_pose_sums, &c);
+    parallel_for(L, 1024, lin_landmark_sums, &c);
+    free(et);
     /* Group the pose-landmark blocks by landmark, one block per distinct pose
      * (duplicate observations of a pair add up, as the hash map does). */
     int* cnt = calloc((size_t)L + 1, sizeof(int));
@@ -416,6 +576,63 @@ static int linearise(const zso_problem* p, lin* s) {
     return 1;
 }
 
+typedef struct schur_ctx {
+    const struct lin* s;
+    const double* Wb;
+    double* S;
+} schur_ctx;
+
+/* The Schur products W_a H_b^T of every landmark whose row pose a lies in
+ * [p0, p1), added to S in landmark order. */
+static void schur_rows(void* c, long long p0, long long p1) {
+    const schur_ctx* x = (const schur_ctx*)c;
+    const struct lin* s = x->s;
+    const int n = 6 * s->K;
+    for (int l = 0; l < s->L; ++l)
+        for (int ka = s->lm_ptr[l]; ka < s->lm_ptr[l + 1]; ++ka) {
+            const int ia = s->blk_pose[ka];
+            if (ia < p0 || ia >= p1) continue;
+            const double* W = x->Wb + 18LL * ka;
+            for (int kb = s->lm_ptr[l]; kb < s->lm_ptr[l + 1]; ++kb) {
+                const double* H = s->hpl + 18LL * kb;
+                const int ib = s->blk_pose[kb];
+                for (int a = 0; a < 6; ++a) {
+                    double* row = x->S + (size_t)(6 * ia + a) * n + 6 * ib;
+                    for (int c = 0; c < 6; ++c)
+                        row[c] += W[a * 3] * H[c * 3] + W[a * 3 + 1] * H[c * 3 + 1] + W[a * 3 + 2] * H[c * 3 + 2];
+                }
+            }
+        }
+}
+
+/* Pose ranges of about equal Schur work (blocks x landmark degree) per thread. */
+static int schur_parts(const struct lin* s, long long* bounds) {
+    int parts = g_threads;
+    if (parts > s->K) parts = s->K > 0 ? s->K : 1;
+    if ((long long)s->nblk < 20000) parts = 1;
+    bounds[0] = 0;
+    if (parts == 1) {
+        bounds[1] = s->K;
+        return 1;
+    }
+    double* w = calloc((size_t)s->K + 1, sizeof(double));
+    double total = 0.0;
+    for (int l = 0; l < s->L; ++l) {
+        const int d = s->lm_ptr[l + 1] - s->lm_ptr[l];
+        for (int k = s->lm_ptr[l]; k < s->lm_ptr[l + 1]; ++k) w[s->blk_pose[k]] += d;
+        total += (double)d * d;
+    }
+    int t = 1;
+    double acc = 0.0;
+    for (int k = 0; k < s->K && t < parts; ++k) {
+        acc += w[k];
+        if (acc >= total * t / parts) bounds[t++] = k + 1;
+    }
+    while (t <= parts) bounds[t++] = s->K;
+    free(w);
+    return parts;
+}
+
 /* solve_linear_system, source/factor_graph.hpp:736-806. */
 static int solve_system(const zso_problem* p, const lin* s, double lambda, double* S_out, double* bs_out,
                         double* delta) {
@@ -455,21 +672,14 @@ static int solve_system(const zso_problem* p, const lin* s, double lambda, doubl
             double* t = bs + 6LL * s->blk_pose[k];
             for (int a = 0; a < 6; ++a) t[a] -= W[a * 3] * bl[0] + W[a * 3 + 1] * bl[1] + W[a * 3 + 2] * bl[2];
         }
-    /* C = sum_l W_l H_l^T accumulated into S, then S = (H_pp + lambda I) - C */
-    for (int l = 0; l < L; ++l)
-        for (int ka = s->lm_ptr[l]; ka < s->lm_ptr[l + 1]; ++ka) {
-            const double* W = Wb + 18LL * ka;
-            const int ia = s->blk_pose[ka];
-            for (int kb = s->lm_ptr[l]; kb < s->lm_ptr[l + 1]; ++kb) {
-                const double* H = s->hpl + 18LL * kb;
-                const int ib = s->blk_pose[kb];
-                for (int a = 0; a < 6; ++a) {
-                    double* row = S + (size_t)(6 * ia + a) * n + 6 * ib;
-                    for (int c = 0; c < 6; ++c)
-                        row[c] += W[a * 3] * H[c * 3] + W[a * 3 + 1] * H[c * 3 + 1] + W[a * 3 + 2] * H[c * 3 + 2];
-                }
-            }
-        }
+    /* C = sum_l W_l H_l^T accumulated into S, then S = (H_pp + lambda I) - C;
+     * threads own pose rows of C (each entry's sum keeps landmark order) */
+    {
+        schur_ctx c = {s, Wb, S};
+        long long bounds[257];
+        const int parts = schur_parts(s, bounds);
+        run_parts(schur_rows, &c, bounds, parts);
+    }
     for (size_t i = 0; i < (size_t)n * n; ++i) S[i] = -S[i];
     for (int k = 0; k < K; ++k)
         for (int a = 0; a < 6; ++a)
@@ -536,91 +746,133 @@ int zso_linear_step(const zso_problem* p, double lambda, double* S, double* bs, 
     return ok;
 }
 
-int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep) {
-    /* factor_graph::solve, source/factor_graph.hpp:489-615 */
+/* factor_graph::solve, source/factor_graph.hpp:489-615, as a state machine:
+ * zso_lm_begin (:494-536), zso_lm_iteration (one pass of the outer loop,
+ * :538-611) and zso_lm_end; zso_solve runs them in sequence. */
+struct zso_lm {
+    zso_problem* p;
+    lin s;
+    int use_relative, it, success, stopped, have_lin;
+    double nu, chi2, lambda, legacy;
+    double *delta, *bk_pose, *bk_lm;
     zso_report rr;
-    memset(&rr, 0, sizeof(rr));
+};
+
+zso_lm* zso_lm_begin(zso_problem* p, int use_relative) {
+    zso_lm* m = calloc(1, sizeof(zso_lm));
+    if (!m) return NULL;
+    m->p = p;
+    m->use_relative = use_relative;
     const int K = p->num_poses, L = p->num_landmarks, n = 6 * K;
     const size_t nall = (size_t)n + 3 * (size_t)L;
     if (p->num_obs == 0 || (K == 0 && L == 0)) {
-        if (rep) *rep = rr;
-        return 0;
+        m->stopped = 1;
+        return m;
     }
-    lin s;
-    if (!linearise(p, &s)) return 0;
-    double nu = 2.0;
-    double chi2 = zso_chi2(p);
-    rr.chi2_initial = chi2;
-    double lambda = 1e-5 * max_diag(&s);
+    if (!linearise(p, &m->s)) {
+        m->stopped = 1;
+        return m;
+    }
+    m->have_lin = 1;
+    m->nu = 2.0;
+    m->chi2 = zso_chi2(p);
+    m->rr.chi2_initial = m->chi2;
+    m->lambda = 1e-5 * max_diag(&m->s);
+    m->legacy = 1e-10 * m->chi2;
+    m->delta = calloc(nall + 1, sizeof(double));
+    m->bk_pose = malloc(((size_t)K * 7 + 1) * sizeof(double));
+    m->bk_lm = malloc(((size_t)L * 3 + 1) * sizeof(double));
+    return m;
+}
+
+int zso_lm_iteration(zso_lm* m) {
+    if (!m || m->stopped) return 0;
+    zso_problem* p = m->p;
+    const int K = p->num_poses, L = p->num_landmarks, n = 6 * K;
+    const size_t nall = (size_t)n + 3 * (size_t)L;
     const int max_failures = 10;
-    const double legacy = 1e-10 * chi2;
-    double* delta = calloc(nall + 1, sizeof(double));
-    double* bk_pose = malloc(((size_t)K * 7 + 1) * sizeof(double));
-    double* bk_lm = malloc(((size_t)L * 3 + 1) * sizeof(double));
-    int success = 0;
-    for (int it = 0; it < iterations; ++it) {
-        rr.iterations = it + 1;
-        const double last = chi2;
-        int failures = 0;
-        while (failures < max_failures) {
-            rr.attempts++;
-            if (!solve_system(p, &s, lambda, NULL, NULL, delta)) {
-                rr.chol_failures++;
-                memset(delta, 0, nall * sizeof(double));
-                lambda *= nu;
-                nu *= 2.0;
-                ++failures;
-                if (!isfinite(lambda)) break;
-                continue;
-            }
-            /* update_states, source/factor_graph.hpp:809-830 */
-            memcpy(bk_pose, p->poses, (size_t)K * 7 * sizeof(double));
-            memcpy(bk_lm, p->landmarks, (size_t)L * 3 * sizeof(double));
-            for (int k = 0; k < K; ++k)
-                if (!p->pose_fixed[k]) zso_pose_plus(p->poses + 7LL * k, delta + 6LL * k);
-            for (int l = 0; l < L; ++l)
-                if (!p->landmark_fixed[l])
-                    for (int c = 0; c < 3; ++c) p->landmarks[3LL * l + c] += delta[n + 3 * l + c];
-            double scale = 0.0;
-            for (size_t i = 0; i < nall; ++i) scale += delta[i] * (lambda * delta[i] + s.b[i]);
-            scale += 1e-3;
-            const double chi_new = zso_chi2(p);
-            const double rho = (chi2 - chi_new) / scale;
-            int good = 0;
-            if (rho > 0 && isfinite(chi_new)) {
-                double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
-                alpha = fmin(alpha, 2.0 / 3.0);
-                lambda *= fmax(1.0 / 3.0, alpha);
-                nu = 2.0;
-                chi2 = chi_new;
-                good = 1;
-                ++success;
-            } else {
-                lambda *= nu;
-                nu *= 2.0;
-            }
-            if (!isfinite(lambda)) break;
-            if (good) {
-                lin_free(&s);
-                if (!linearise(p, &s)) { success = -1; goto out; }
-                break;
-            }
-            /* rollback_states, source/factor_graph.hpp:833-846 */
-            memcpy(p->poses, bk_pose, (size_t)K * 7 * sizeof(double));
-            memcpy(p->landmarks, bk_lm, (size_t)L * 3 * sizeof(double));
+    m->rr.iterations = m->it + 1;
+    const double last = m->chi2;
+    int failures = 0;
+    while (failures < max_failures) {
+        m->rr.attempts++;
+        if (!solve_system(p, &m->s, m->lambda, NULL, NULL, m->delta)) {
+            m->rr.chol_failures++;
+            memset(m->delta, 0, nall * sizeof(double));
+            m->lambda *= m->nu;
+            m->nu *= 2.0;
             ++failures;
+            if (!isfinite(m->lambda)) break;
+            continue;
         }
-        const double thr = use_relative ? 1e-6 * fmax(last, 1e-12) : legacy;
-        if (failures >= max_failures || (last - chi2) < thr || !isfinite(lambda)) break;
+        /* update_states, source/factor_graph.hpp:809-830 */
+        memcpy(m->bk_pose, p->poses, (size_t)K * 7 * sizeof(double));
+        memcpy(m->bk_lm, p->landmarks, (size_t)L * 3 * sizeof(double));
+        for (int k = 0; k < K; ++k)
+            if (!p->pose_fixed[k]) zso_pose_plus(p->poses + 7LL * k, m->delta + 6LL * k);
+        for (int l = 0; l < L; ++l)
+            if (!p->landmark_fixed[l])
+                for (int c = 0; c < 3; ++c) p->landmarks[3LL * l + c] += m->delta[n + 3 * l + c];
+        double scale = 0.0;
+        for (size_t i = 0; i < nall; ++i) scale += m->delta[i] * (m->lambda * m->delta[i] + m->s.b[i]);
+        scale += 1e-3;
+        const double chi_new = zso_chi2(p);
+        const double rho = (m->chi2 - chi_new) / scale;
+        int good = 0;
+        if (rho > 0 && isfinite(chi_new)) {
+            double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
+            alpha = fmin(alpha, 2.0 / 3.0);
+            m->lambda *= fmax(1.0 / 3.0, alpha);
+            m->nu = 2.0;
+            m->chi2 = chi_new;
+            good = 1;
+            ++m->success;
+        } else {
+            m->lambda *= m->nu;
+            m->nu *= 2.0;
+        }
+        if (!isfinite(m->lambda)) break;
+        if (good) {
+            lin_free(&m->s);
+            m->have_lin = 0;
+            if (!linearise(p, &m->s)) {
+                m->success = -1;
+                m->stopped = 1;
+                return 0;
+            }
+            m->have_lin = 1;
+            break;
+        }
+        /* rollback_states, source/factor_graph.hpp:833-846 */
+        memcpy(p->poses, m->bk_pose, (size_t)K * 7 * sizeof(double));
+        memcpy(p->landmarks, m->bk_lm, (size_t)L * 3 * sizeof(double));
+        ++failures;
     }
-    lin_free(&s);
-out:
-    rr.accepted = success;
-    rr.chi2_final = chi2;
-    rr.lambda_final = lambda;
-    if (rep) *rep = rr;
-    free(delta); free(bk_pose); free(bk_lm);
+    ++m->it;
+    const double thr = m->use_relative ? 1e-6 * fmax(last, 1e-12) : m->legacy;
+    if (failures >= max_failures || (last - m->chi2) < thr || !isfinite(m->lambda)) m->stopped = 1;
+    return !m->stopped;
+}
+
+int zso_lm_end(zso_lm* m, zso_report* rep) {
+    if (!m) return 0;
+    m->rr.accepted = m->success;
+    m->rr.chi2_final = m->chi2;
+    m->rr.lambda_final = m->lambda;
+    if (rep) *rep = m->rr;
+    const int success = m->success;
+    if (m->have_lin) lin_free(&m->s);
+    free(m->delta); free(m->bk_pose); free(m->bk_lm);
+    free(m);
     return success;
+}
+
+int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep) {
+    zso_lm* m = zso_lm_begin(p, use_relative);
+    if (!m) return 0;
+    for (int it = 0; it < iterations; ++it)
+        if (!zso_lm_iteration(m)) break;
+    return zso_lm_end(m, rep);
 }
 
 /* ---------------------------------------------------------------- map culling */

@@ -71,6 +71,12 @@ void zso_loss(int kind, double delta, double e2, double rho[3]);
 /* Sum of robust chi2 over all edges at the current state. */
 double zso_chi2(const zso_problem* p);
 
+/* Host threads the restatement may use for its loops (default 1). Results
+ * are bit-for-bit the same for every thread count: threads own disjoint
+ * outputs and every sum keeps its serial order. */
+void zso_set_threads(int n);
+int zso_get_threads(void);
+
 /* 3x3 inverse with zeroslam's |det| > 1e-12 * max|a|^3 test; out = 0 and
  * returns 0 when singular. */
 int zso_invert3(const double A[9], double out[9]);
@@ -96,6 +102,17 @@ double zso_initial_lambda(const zso_problem* p);
 
 /* Full Levenberg-Marquardt solve; returns the accepted-step count. */
 int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep);
+
+/* The same solve one outer iteration at a time (zso_solve is begin, up to
+ * `iterations` calls of zso_lm_iteration, end): zso_lm_begin linearises and
+ * sets the initial damping (source/factor_graph.hpp:494-536);
+ * zso_lm_iteration runs one pass of the outer loop (:538-611) and returns 0
+ * once a stop rule has fired; zso_lm_end fills the report, frees the state and
+ * returns the accepted-step count. p is updated in place. */
+typedef struct zso_lm zso_lm;
+zso_lm* zso_lm_begin(zso_problem* p, int use_relative);
+int zso_lm_iteration(zso_lm* m);
+int zso_lm_end(zso_lm* m, zso_report* rep);
 
 /* Map culling, source/map.hpp:269-323, over a map given as arrays (the layout
  * of zs_map_cull_input in include/zeroslam_ba.h). */

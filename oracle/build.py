@@ -4,13 +4,14 @@
   ``oracle/_build/libzsoracle.so`` with the system C compiler. It runs on any
   host (x86-64 here, aarch64 on the GPU host).
 * ``build_ref()`` compiles ``ref_driver.cpp`` against the unmodified
-  zeroslam headers where they lie (``<reference>/source``) into
+  zeroslam headers where they lie (``$ZS_REFERENCE_ROOT/source``) into
   ``oracle/_ref/libzsref.so``, with the reference's release flags
   (-O3 -DNDEBUG -std=c++17 -fno-exceptions -fno-rtti, CMakeLists.txt:17-43).
   Nothing is copied out of the reference tree. When the reference tree is
   absent this is a no-op.
 
-Run ``python oracle/build.py`` to build both.
+Run ``ZS_REFERENCE_ROOT=<zeroslam checkout> python oracle/build.py`` to build
+both (without the variable only the restatement is built).
 """
 
 from __future__ import annotations
@@ -24,7 +25,25 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libzsoracle.so")
 REF_SO = os.path.join(REF_DIR, "libzsref.so")
-REFERENCE_ROOT = os.environ.get("ZS_REFERENCE_ROOT", "/root/reference")
+# The zeroslam source tree to build the reference driver against: the
+# ZS_REFERENCE_ROOT environment variable, else the tree of the last build in
+# this checkout (recorded in oracle/_ref, which is not version-controlled),
+# else none (no reference build; the tests that need the tree skip).
+ROOT_RECORD = os.path.join(REF_DIR, "reference_root")
+
+
+def _reference_root() -> str:
+    env = os.environ.get("ZS_REFERENCE_ROOT", "")
+    if env:
+        return env
+    try:
+        with open(ROOT_RECORD) as f:
+            return f.read().strip()
+    except OSError:
+        return ""
+
+
+REFERENCE_ROOT = _reference_root()
 
 
 def _stale(target: str, sources: list[str]) -> bool:
@@ -42,14 +61,14 @@ def build_oracle(force: bool = False) -> str:
         tmp = ORACLE_SO + f".{os.getpid()}.tmp"
         # -ffp-contract=off keeps the restatement's rounding the same on hosts
         # with and without fused multiply-add.
-        subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off",
+        subprocess.check_call(["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
                                "-o", tmp, src, "-lm"])
         os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 
 
 def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REFERENCE_ROOT, "source", "factor_graph.hpp"))
+    return bool(REFERENCE_ROOT) and os.path.isfile(os.path.join(REFERENCE_ROOT, "source", "factor_graph.hpp"))
 
 
 def build_ref(force: bool = False) -> str | None:
@@ -67,6 +86,8 @@ def build_ref(force: bool = False) -> str | None:
         subprocess.check_call(["g++", "-O3", "-DNDEBUG", "-std=c++17", "-fno-exceptions", "-fno-rtti", "-fPIC",
                                "-shared", "-I", inc, "-o", tmp, src])
         os.replace(tmp, REF_SO)
+    with open(ROOT_RECORD, "w") as f:
+        f.write(REFERENCE_ROOT + "\n")
     return REF_SO
 
 

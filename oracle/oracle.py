@@ -109,14 +109,31 @@ def _find_matches(fn, lhs, rhs, threshold, k, size):
     return out[:n].copy()
 
 
+def default_threads() -> int:
+    """Host threads for the restatement's loops: every core, at most 16
+    (its results do not depend on the count)."""
+    return max(1, min(16, os.cpu_count() or 1))
+
+
 class Oracle:
-    def __init__(self):
+    def __init__(self, threads: int | None = None):
         self.lib = C.CDLL(_build.build_oracle())
         L = self.lib
+        L.zso_set_threads.restype = None
+        L.zso_set_threads.argtypes = [C.c_int]
+        L.zso_get_threads.restype = C.c_int
+        L.zso_get_threads.argtypes = []
+        self.set_threads(default_threads() if threads is None else threads)
         L.zso_chi2.restype = C.c_double
         L.zso_chi2.argtypes = [C.POINTER(_Problem)]
         L.zso_solve.restype = C.c_int
         L.zso_solve.argtypes = [C.POINTER(_Problem), C.c_int, C.c_int, C.POINTER(Report)]
+        L.zso_lm_begin.restype = C.c_void_p
+        L.zso_lm_begin.argtypes = [C.POINTER(_Problem), C.c_int]
+        L.zso_lm_iteration.restype = C.c_int
+        L.zso_lm_iteration.argtypes = [C.c_void_p]
+        L.zso_lm_end.restype = C.c_int
+        L.zso_lm_end.argtypes = [C.c_void_p, C.POINTER(Report)]
         L.zso_linear_step.restype = C.c_int
         L.zso_linear_step.argtypes = [C.POINTER(_Problem), C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]
         L.zso_initial_lambda.restype = C.c_double
@@ -142,6 +159,14 @@ class Oracle:
         L.zso_find_matches.restype = C.c_longlong
         L.zso_find_matches.argtypes = [_up, C.c_longlong, _up, C.c_longlong, C.c_float, C.c_longlong, C.c_void_p,
                                        C.c_longlong]
+
+    def set_threads(self, n: int) -> None:
+        """Host threads of the restatement's loops (process-wide)."""
+        self.lib.zso_set_threads(int(n))
+
+    @property
+    def threads(self) -> int:
+        return int(self.lib.zso_get_threads())
 
     def find_matches(self, lhs, rhs, threshold: float, k: int, size: int):
         """feature::find_matches: structured array of (lhs_index, rhs_index, score)."""
@@ -282,6 +307,11 @@ class Oracle:
         self.lib.zso_solve(C.byref(p), int(iterations), int(bool(use_relative)), C.byref(rep))
         return a.poses, a.landmarks, rep
 
+    def stepwise(self, scene, use_relative: bool = False) -> "StepwiseSolve":
+        """The solve of ``solve`` one outer LM iteration at a time (for timing
+        a solve iteration by iteration)."""
+        return StepwiseSolve(self, scene, use_relative)
+
     def initial_lambda(self, scene) -> float:
         a = _Arrays(scene)
         p = a.struct()
@@ -342,6 +372,35 @@ class Oracle:
         rho = np.zeros(3)
         self.lib.zso_loss(int(kind), float(delta), float(e2), _ptr(rho, _dp))
         return rho
+
+
+class StepwiseSolve:
+    """Oracle.solve split into its parts: construction linearises and sets the
+    initial damping (zso_lm_begin), ``iteration()`` runs one outer LM
+    iteration and returns False once a stop rule has fired, ``finish()``
+    returns (poses, landmarks, Report)."""
+
+    def __init__(self, oracle: "Oracle", scene, use_relative: bool = False):
+        self.lib = oracle.lib
+        self.a = _Arrays(scene)
+        self.p = self.a.struct()
+        self.m = self.lib.zso_lm_begin(C.byref(self.p), int(bool(use_relative)))
+        if not self.m:
+            raise MemoryError("zso_lm_begin")
+
+    def iteration(self) -> bool:
+        return bool(self.lib.zso_lm_iteration(self.m))
+
+    def finish(self):
+        rep = Report()
+        self.lib.zso_lm_end(self.m, C.byref(rep))
+        self.m = None
+        return self.a.poses, self.a.landmarks, rep
+
+    def __del__(self):
+        if getattr(self, "m", None):
+            self.lib.zso_lm_end(self.m, None)
+            self.m = None
 
 
 class Reference:

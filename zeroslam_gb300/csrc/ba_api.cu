@@ -510,6 +510,14 @@ static int cuda_status(cudaError_t e) {
 
 const char* zs_last_error(void) { return g_last_error; }
 
+}  // extern "C"
+
+namespace zs {
+int record_cuda_error(cudaError_t e) { return cuda_status(e); }
+}  // namespace zs
+
+extern "C" {
+
 int zs_ba_create(zs_ba_handle** out, const zs_ba_options* opt) {
     if (!out) return ZS_ERR_INVALID;
     *out = nullptr;
@@ -1254,6 +1262,14 @@ int linear_step_impl(zs_ba_handle* h, double lambda, double* S, double* bs, doub
     return h->st_host->solve_ok ? ZS_OK : ZS_ERR_CHOLESKY;
 }
 
+// The mixed form under Tukey's redescending loss is not offered: its FP32
+// Jacobian moves the step by ~1e-5 relative, which moves observations across
+// the loss's threshold (weight 0 beyond it) within a few iterations, and the
+// solve then settles in a different nearby minimum than the FP64 one (about
+// 4e-3 relative in cost after five iterations on a 10-keyframe arc) instead of
+// meeting the mixed form's 1e-6 agreement.
+bool mixed_tukey(const zs_ba_handle* h) { return h->tsize == 4 && h->P.loss.kind == ZS_LOSS_TUKEY; }
+
 }  // namespace
 
 extern "C" {
@@ -1263,6 +1279,7 @@ int zs_ba_solve(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report*
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
     if (h->batch) return ZS_ERR_UNSUPPORTED;  // zs_ba_solve_batch
+    if (mixed_tukey(h)) return ZS_ERR_UNSUPPORTED;
     // source/factor_graph.hpp:494-499: nothing to do without edges or vertices
     if (h->P.M == 0 || (h->P.K == 0 && h->P.L == 0)) return 0;
     if (iterations < 0) return ZS_ERR_INVALID;
@@ -2100,6 +2117,7 @@ int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_r
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
     if (!h->batch) return ZS_ERR_INVALID;
+    if (mixed_tukey(h)) return ZS_ERR_UNSUPPORTED;
     if (iterations < 0) return ZS_ERR_INVALID;
     try {
         ZS_CUDA(cudaSetDevice(h->device));

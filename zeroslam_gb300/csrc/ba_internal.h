@@ -161,6 +161,11 @@ struct WinCtl {
     double chi2_initial;
 };
 
+// Records e as this host thread's zs_last_error() text, clears CUDA's
+// last-error state and returns the status for it (ZS_ERR_CUDA or
+// ZS_ERR_OUT_OF_MEMORY). Defined with the C ABI (ba_api.cu).
+int record_cuda_error(cudaError_t e);
+
 // ---- kernels (ba_kernels.cu) ----
 template <typename T>
 void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s);

@@ -32,9 +32,15 @@ __device__ __align__(256) double g_scratch[kScratchDoubles];
 
 // Device address of g_scratch per device ordinal. In host code the symbol
 // g_scratch is only a host-side stand-in, so the address is looked up with
-// cudaGetSymbolAddress, once per device, with that device current.
+// cudaGetSymbolAddress, once per device, with that device current. The
+// cached address belongs to the device's current context: a caller that
+// resets a device (cudaDeviceReset) must not call this entry point on that
+// device again in the same process.
 constexpr int kMaxDevices = 64;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// A CUDA failure: recorded as zs_last_error() like every other entry point's.
+int fail(cudaError_t e) { return zs::record_cuda_error(e); }
 
 }  // namespace
 
@@ -42,16 +48,14 @@ extern "C" int zs_dense_cholesky_solve_noalloc(const double* A, int n, const dou
     if (!A || !b || n <= 0) return ZS_ERR_INVALID;
     if (n > kMaxN) return ZS_ERR_INVALID;  // beyond the fixed workspace
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        cudaGetLastError();
-        return ZS_ERR_CUDA;
-    }
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(e);
+    if (dev < 0 || dev >= kMaxDevices) return fail(cudaErrorInvalidDevice);
     if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
-            cudaGetLastError();
-            return ZS_ERR_CUDA;
-        }
+        e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess) return fail(e);
+        if (!p) return fail(cudaErrorInvalidSymbol);
         g_scratch_ptr[dev] = static_cast<double*>(p);
     }
     double* base = g_scratch_ptr[dev];
@@ -69,24 +73,18 @@ extern "C" int zs_dense_cholesky_solve_noalloc(const double* A, int n, const dou
     std::memset(&init, 0, sizeof(init));
     init.solve_ok = 1;
     cudaStream_t s = 0;
-    if (cudaMemcpyAsync(st, &init, sizeof(init), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(dA, A, nn * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(db, b, n * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess) {
-        cudaGetLastError();
-        return ZS_ERR_CUDA;
-    }
-    if (zs::launch_reduced_solve<double, double>(n, dA, dF, dD, db, dx, dwork, st, 0, 0.0, s) != cudaSuccess) {
-        cudaGetLastError();
-        return ZS_ERR_CUDA;
-    }
+    if ((e = cudaMemcpyAsync(st, &init, sizeof(init), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dA, A, nn * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(db, b, n * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return fail(e);
+    if ((e = zs::launch_reduced_solve<double, double>(n, dA, dF, dD, db, dx, dwork, st, 0, 0.0, s)) != cudaSuccess)
+        return fail(e);
     zs::LmState out;
-    if (cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        (x && cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
-        (L && cudaMemcpyAsync(L, dF, nn * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        cudaGetLastError();
-        return ZS_ERR_CUDA;
-    }
+    if ((e = cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (x && (e = cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+        (L && (e = cudaMemcpyAsync(L, dF, nn * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return fail(e);
     if (L)
         for (int i = 0; i < n; ++i)
             for (int j = i + 1; j < n; ++j) L[(size_t)i * n + j] = 0.0;
