@@ -10,7 +10,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_line():
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "arc", "--steps", "1",
+    """Each step is one timed LM iteration of a whole-scene CPU solve: with
+    more steps than one solve's iterations, a new solve starts, and the line
+    reports exactly the steps it timed."""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "arc", "--steps", "13",
                         "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
@@ -20,7 +23,12 @@ def test_reference_arm_line():
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "LM iters/s"
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["cpu_baseline"]["kind"] in ("reference", "port") and line["cpu_baseline"]["cores"] >= 1
-    assert "workload" in line["config"]
+    assert "workload" in line["config"] and line["config"]["iterations"] == 10
+    assert line["steps"] == 13 and line["warmup"] == 3
+    per = line["seconds_per_iteration"]
+    assert 0 < per["min"] <= per["median"] <= per["max"]
+    assert abs(line["value"] * line["ms_per_step"] * 1e-3 - 1.0) < 1e-9
+    assert "from 2 solve(s)" in line["cpu_baseline"]["sample"]
 
 
 def test_reference_arm_two_ranks():
