@@ -185,15 +185,17 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
     pipe = peaks["fp64_tflops"] if precision == 0 else peaks["fp32_tflops"]
     pipe_name = "fp64" if precision == 0 else "fp32"
     rs = 20 if precision else 18  # H_pl / W record length (floats padded to 80 bytes)
-    # mixed form: the reduced solve is X = L^-1 (reads F, writes X and X^T) and
-    # conjugate gradients on the matrix-free Schur operator: 1 application for
-    # b_s, one per iteration, half of one for the landmark back-substitution;
-    # 224 bytes per observation each (the 112-byte Jacobian record, J_p v
-    # stashed and read back, the weighted residual scattered pose-major, the
-    # pose-major J_p and that residual read back), plus X and X^T per iteration
+    # mixed form: the reduced solve is conjugate gradients on the matrix-free
+    # Schur operator: 1 application for b_s, one per iteration, half of one for
+    # the landmark back-substitution; 224 bytes per observation each (the
+    # 112-byte Jacobian record, J_p v stashed and read back, the weighted
+    # residual scattered pose-major, the pose-major J_p and that residual read
+    # back), plus X and X^T per iteration (the preconditioner X = L^-1 is formed
+    # with the factor, in the factor phase: n^3/3 + n^3/3 flops)
     cg_it = prof.get("refine_sweeps", 0) / max(1, prof.get("attempts", 1))
     trisolve_bytes = (n * n * s * 2 if precision == 0 else
-                      10.0 * n * n + (1.5 + cg_it) * 224.0 * M + cg_it * 4.0 * n * n + 144.0 * L)
+                      (1.5 + cg_it) * 224.0 * M + cg_it * 4.0 * n * n + 144.0 * L)
+    factor_flops = n ** 3 / 3.0 if precision == 0 else 2.0 * n ** 3 / 3.0
     work = {
         # bytes: read observation + write H_pl, and H_ll / H_pp / b once
         # (mixed form: also the 112-byte Jacobian record and the 48-byte
@@ -204,7 +206,7 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
         # segment sums, one 288-byte record per pose pair and 512 triples, are
         # left out); memory-bound on the L1/L2 latency of the record gathers
         "schur": ("hbm", M * 2 * rs * s + T * 8, T * 216.0 + M * 36.0),
-        "factor": (pipe_name, None, n ** 3 / 3.0),
+        "factor": (pipe_name, None, factor_flops),
         "trisolve": ("hbm", trisolve_bytes, None),
         "update": ("hbm", M * 18 * s + L * 48 + K * 112, None),
         "cost": ("hbm", M * 24 + L * 32 + K * 64, None),
@@ -235,9 +237,9 @@ def phase_roofline(sc, prof: dict, precision: int, peaks: dict, hbm_gbs: float) 
 def phase_traffic(sc, precision: int, phase: str, cg_it: float = 0.0):
     """DRAM bytes per launch of the phase's main kernel from the committed ncu
     capture (profiles/traffic_walk_1M_mixed.json), for the scene it was taken on.
-    The reduced solve (trisolve) is X = L^-1 plus the conjugate-gradient launch,
-    whose captured launch made 3 operator applications; its bytes are scaled to
-    the average attempt's 1 + cg_it applications."""
+    The reduced solve (trisolve) is the conjugate-gradient launch, whose
+    captured launch made 3 operator applications; its bytes are scaled to the
+    average attempt's 1.5 + cg_it applications."""
     path = os.path.join(ROOT, "profiles", "traffic_walk_1M_mixed.json")
     if precision != 1 or sc.M != 1019227 or not os.path.exists(path):
         return None
@@ -250,10 +252,9 @@ def phase_traffic(sc, precision: int, phase: str, cg_it: float = 0.0):
     nbytes = e["dram_read"] + e["dram_write"]
     out = {"kernel": k, "source": "profiles/traffic_walk_1M_mixed.json (one ncu capture)"}
     if phase == "trisolve":
-        x = t["kernels"]["k_tri_inverse64"]
-        nbytes = nbytes * (1.0 + cg_it) / 3.0 + x["dram_read"] + x["dram_write"]
-        out["kernel"] = "k_tri_inverse64 + k_pcg"
-        out["scaled"] = f"k_pcg bytes x (1 + {cg_it:.2f}) / 3 operator applications"
+        apps = t["kernels"][k].get("applications", 3.0)
+        nbytes = nbytes * (1.5 + cg_it) / apps
+        out["scaled"] = f"k_pcg bytes x (1.5 + {cg_it:.2f}) / {apps:g} operator applications"
     out["bytes_per_launch"] = nbytes
     return out
 

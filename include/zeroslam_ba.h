@@ -420,8 +420,10 @@ int zs_ba_cull(zs_ba_handle* h, const int32_t* landmark_id, const int32_t* pose_
 /* Dense SPD solve on the device with the reference's pivot tests: factors the
  * row-major n x n matrix A = L L^T and solves L L^T x = b. L (n*n, lower, zero
  * above the diagonal) and x may be NULL. precision: ZS_PRECISION_FP64, or
- * ZS_PRECISION_MIXED (FP32 factor + FP64 refinement of x).
- * Returns ZS_OK or ZS_ERR_CHOLESKY. */
+ * ZS_PRECISION_MIXED (the mixed solve's preconditioner: FP32 factor and its
+ * inverse, then FP64 refinement of x).
+ * Returns ZS_OK, ZS_ERR_CHOLESKY, ZS_ERR_TIMEOUT (mixed: a bounded wait between
+ * the factor's tile tasks ran out; nothing hangs) or a CUDA status. */
 int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, double* x, int precision);
 
 /* Largest n accepted by zs_dense_cholesky_solve_noalloc. */

@@ -854,6 +854,14 @@ int zso_lm_iteration(zso_lm* m) {
     return !m->stopped;
 }
 
+void zso_lm_report(const zso_lm* m, zso_report* rep) {
+    if (!m || !rep) return;
+    *rep = m->rr;
+    rep->accepted = m->success;
+    rep->chi2_final = m->chi2;
+    rep->lambda_final = m->lambda;
+}
+
 int zso_lm_end(zso_lm* m, zso_report* rep) {
     if (!m) return 0;
     m->rr.accepted = m->success;

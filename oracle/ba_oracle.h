@@ -108,11 +108,14 @@ int zso_solve(zso_problem* p, int iterations, int use_relative, zso_report* rep)
  * sets the initial damping (source/factor_graph.hpp:494-536);
  * zso_lm_iteration runs one pass of the outer loop (:538-611) and returns 0
  * once a stop rule has fired; zso_lm_end fills the report, frees the state and
- * returns the accepted-step count. p is updated in place. */
+ * returns the accepted-step count; zso_lm_report reads the report so far.
+ * p is updated in place. */
 typedef struct zso_lm zso_lm;
 zso_lm* zso_lm_begin(zso_problem* p, int use_relative);
 int zso_lm_iteration(zso_lm* m);
 int zso_lm_end(zso_lm* m, zso_report* rep);
+/* The report of the iterations run so far (the solve continues). */
+void zso_lm_report(const zso_lm* m, zso_report* rep);
 
 /* Map culling, source/map.hpp:269-323, over a map given as arrays (the layout
  * of zs_map_cull_input in include/zeroslam_ba.h). */

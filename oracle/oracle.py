@@ -134,6 +134,8 @@ class Oracle:
         L.zso_lm_iteration.argtypes = [C.c_void_p]
         L.zso_lm_end.restype = C.c_int
         L.zso_lm_end.argtypes = [C.c_void_p, C.POINTER(Report)]
+        L.zso_lm_report.restype = None
+        L.zso_lm_report.argtypes = [C.c_void_p, C.POINTER(Report)]
         L.zso_linear_step.restype = C.c_int
         L.zso_linear_step.argtypes = [C.POINTER(_Problem), C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]
         L.zso_initial_lambda.restype = C.c_double
@@ -377,8 +379,9 @@ class Oracle:
 class StepwiseSolve:
     """Oracle.solve split into its parts: construction linearises and sets the
     initial damping (zso_lm_begin), ``iteration()`` runs one outer LM
-    iteration and returns False once a stop rule has fired, ``finish()``
-    returns (poses, landmarks, Report)."""
+    iteration and returns False once a stop rule has fired, ``report()``
+    reads the Report so far and ``finish()`` returns (poses, landmarks,
+    Report)."""
 
     def __init__(self, oracle: "Oracle", scene, use_relative: bool = False):
         self.lib = oracle.lib
@@ -390,6 +393,12 @@ class StepwiseSolve:
 
     def iteration(self) -> bool:
         return bool(self.lib.zso_lm_iteration(self.m))
+
+    def report(self):
+        """The Report of the iterations run so far."""
+        rep = Report()
+        self.lib.zso_lm_report(self.m, C.byref(rep))
+        return rep
 
     def finish(self):
         rep = Report()

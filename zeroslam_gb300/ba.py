@@ -613,6 +613,15 @@ def dense_cholesky_solve(A, b, precision: int = FP64):
     return st == ZS_OK, Lm, x
 
 
+def dense_cholesky_status(A, b, precision: int = FP64) -> int:
+    """The status zs_dense_cholesky_solve returns for A x = b (no results)."""
+    lib = load()
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(A.shape[0])
+    return int(lib.zs_dense_cholesky_solve(_p(A, _dp), A.shape[0], _p(b, _dp), None, _p(x, _dp), int(precision)))
+
+
 def pipe_peaks(device: int = 0):
     """(fp64_tflops, fp32_tflops) measured by an FMA-chain microbenchmark."""
     lib = load()

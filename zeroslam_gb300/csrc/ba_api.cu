@@ -961,6 +961,9 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
             W.X = dalloc<char>(ts * (size_t)n * n, own);
             W.XT = dalloc<char>(ts * (size_t)n * n, own);
             W.pcg = dalloc<double>(pcg_doubles(P), own);
+            W.dag_flags = dalloc<int>((size_t)dag_flag_ints(n), own);
+            W.dag_epoch = 0;
+            ZS_CUDA(cudaMemsetAsync(W.dag_flags, 0, sizeof(int) * (size_t)dag_flag_ints(n), s));
         }
     }
     W.delta = dalloc<double>((size_t)n + 3 * (size_t)L, own);
@@ -1094,19 +1097,18 @@ void system_solve(zs_ba_handle* h) {
     }
     {
         PhaseScope ps(h->timer, ZS_PHASE_FACTOR, s);
-        if constexpr (sizeof(T) == 4)  // the conjugate-gradient preconditioner
-            ZS_CUDA(launch_factor_preconditioner(P.n, W.S, (float*)W.F, (float*)W.D, h->st, kPreconditionerShift, s));
+        if constexpr (sizeof(T) == 4)  // the conjugate-gradient preconditioner: L and X = L^-1
+            ZS_CUDA(launch_preconditioner(P.n, W.S, (float*)W.F, (float*)W.X, (float*)W.XT, h->st,
+                                          kPreconditionerShift, W.dag_flags, &W.dag_epoch, s));
         else
             ZS_CUDA((launch_factor<double, T>(P.n, W.S, (T*)W.F, (T*)W.D, h->st, s)));
     }
     {
         PhaseScope ps(h->timer, ZS_PHASE_TRISOLVE, s);
         if constexpr (sizeof(T) == 4) {
-            // mixed form: explicit L^-1, then conjugate gradients on the FP64
-            // Schur operator preconditioned by X^T X; it also writes b_s and
-            // the landmark back-substitution
-            ZS_CUDA((launch_tri_inverse<float>(P.n, (const float*)W.F, (const float*)W.D, (float*)W.X,
-                                               (float*)W.XT, h->st, s)));
+            // mixed form: conjugate gradients on the FP64 Schur operator
+            // preconditioned by X^T X; it also writes b_s and the landmark
+            // back-substitution
             ZS_CUDA(launch_pcg(P, W, h->st, std::max(0, h->opt.refine_iterations), h->opt.refine_tolerance, s));
         } else {
             ZS_CUDA((launch_solve_refine<double, double>(P.n, W.S, (const double*)W.F, (const double*)W.D, W.bs,
@@ -1169,6 +1171,12 @@ int solve_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report*
             }
             read_state(h);
             r.attempts++;
+            if (hs.timeout) {  // a bounded device wait ran out: the solve stops with the state restored
+                std::snprintf(g_last_error, sizeof(g_last_error), "a dependency wait of the preconditioner ran out");
+                r.status = ZS_ERR_TIMEOUT;
+                if (rep) *rep = r;
+                return ZS_ERR_TIMEOUT;
+            }
             lambda = hs.lambda;
             {
                 zs_ba_attempt a{};
@@ -1259,6 +1267,7 @@ int linear_step_impl(zs_ba_handle* h, double lambda, double* S, double* bs, doub
     if (delta && nall > 0) ZS_CUDA(cudaMemcpyAsync(delta, W.delta, nall * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (b && nall > 0) ZS_CUDA(cudaMemcpyAsync(b, W.b, nall * sizeof(double), cudaMemcpyDeviceToHost, s));
     ZS_CUDA(cudaStreamSynchronize(s));
+    if (h->st_host->timeout) return ZS_ERR_TIMEOUT;
     return h->st_host->solve_ok ? ZS_OK : ZS_ERR_CHOLESKY;
 }
 
@@ -1720,11 +1729,14 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
             }
         } else {
             float* dF = dalloc<float>(nn, owned);
-            float* dD = dalloc<float>(1024 * (size_t)((n + 31) / 32), owned);
             float* dX = dalloc<float>(nn, owned);
             float* dXT = dalloc<float>(nn, owned);
-            ZS_CUDA((launch_factor<double, float>(n, dA, dF, dD, st, s)));
-            ZS_CUDA((launch_tri_inverse<float>(n, dF, dD, dX, dXT, st, s)));
+            int* flags = dalloc<int>((size_t)dag_flag_ints(n), owned);
+            int epoch = 0;
+            ZS_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)dag_flag_ints(n), s));
+            // the factor as the mixed solve forms it, without the shifted retry
+            // (st->skip_factor stays 0, so the solve test applies)
+            ZS_CUDA((launch_factor_dag(n, dA, dF, dX, dXT, st, flags, &epoch, s)));
             ZS_CUDA((launch_refine<double, float>(n, dA, dX, dXT, db, dx, dwork, st, 10, 1e-14, s)));
             if (Lout) {
                 std::vector<float> tmp(nn);
@@ -1742,7 +1754,7 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
             for (int i = 0; i < n; ++i)
                 for (int j = 0; j < n; ++j) Lout[(size_t)i * n + j] = (j <= i) ? Lh[(size_t)i * n + j] : 0.0;
         }
-        status = out.solve_ok ? ZS_OK : ZS_ERR_CHOLESKY;
+        status = out.timeout ? ZS_ERR_TIMEOUT : (out.solve_ok ? ZS_OK : ZS_ERR_CHOLESKY);
     } catch (const CudaError& e) {
         status = cuda_status(e.err);
     }

@@ -569,6 +569,33 @@ cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float
     return cudaGetLastError();
 }
 
+cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, LmState* st, int* flags,
+                              int* epoch, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t nn = (int64_t)n * n;
+    k_diag_max<double><<<1, kThreads, 0, s>>>(n, S, st, 1e-14, 0); note_launch();
+    k_convert<double, float><<<grid_for(nn), kThreads, 0, s>>>(nn, S, F); note_launch();
+    cudaError_t e = launch_chol_inverse_dag(n, F, X, XT, st, flags, epoch, s);
+    if (e != cudaSuccess) return e;
+    k_check_solve_eps<float><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, LmState* st, double mu,
+                                  int* flags, int* epoch, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t nn = (int64_t)n * n;
+    cudaError_t e = launch_factor_dag(n, S, F, X, XT, st, flags, epoch, s);
+    if (e != cudaSuccess) return e;
+    k_retry_arm<<<1, 32, 0, s>>>(st); note_launch();
+    k_convert_shift<<<std::min<int64_t>(grid_for(nn), 4096), kThreads, 0, s>>>(n, S, F, mu, st); note_launch();
+    e = launch_chol_inverse_dag(n, F, X, XT, st, flags, epoch, s);
+    if (e != cudaSuccess) return e;
+    k_check_solve_eps<float><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
+    k_retry_disarm<<<1, 32, 0, s>>>(st); note_launch();
+    return cudaGetLastError();
+}
+
 template <typename TS, typename TF>
 cudaError_t launch_solve_refine(int n, const TS* S, const TF* F, const TF* D, const double* bs, double* x,
                                 double* work, LmState* st, int refine_iters, double tol, cudaStream_t s) {

@@ -117,6 +117,8 @@ struct DevWork {
     double* work = nullptr;    // [4n + 256] triangular-solve and refinement vectors
     void* X = nullptr;         // mixed form: [n*n] L^-1 (lower)
     void* XT = nullptr;        // mixed form: [n*n] (L^-1)^T (upper; lower used as scratch)
+    int* dag_flags = nullptr;  // mixed form: [dag_flag_ints(n)] tile flags of the preconditioner's launch
+    int dag_epoch = 0;         // mixed form: epoch of its last launch (host side)
     double* delta = nullptr;   // [n + 3L]
     double* red = nullptr;     // [kReduceBlocks * 4] reduction partials
     int32_t* ired = nullptr;   // [kReduceBlocks]
@@ -141,6 +143,7 @@ struct LmState {
     int32_t refine_sweeps;  // refinement sweeps of the last reduced solve
     int32_t skip_factor;    // mixed form: the factor kernels return at once (no retry armed)
     int32_t shifted;        // mixed form: the last preconditioner factor needed the diagonal shift
+    int32_t timeout;        // a bounded device wait ran out (the launch gave up; solve_ok = 0)
 };
 
 // Per-window LM control of a batched solve (source/factor_graph.hpp:538-611
@@ -339,6 +342,28 @@ cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double*
 // st->shifted.
 cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float* D, LmState* st, double mu,
                                          cudaStream_t s);
+
+// ---- mixed form: the preconditioner (ba_chol_dag.cu) ----
+// F (n x n FP32, the matrix) -> L in F's lower triangle (zeros above the
+// diagonal inside the 64 x 64 diagonal tiles), X = L^-1 (lower, with its
+// diagonal) and XT = X^T (upper), in one cooperative launch of per-tile
+// tasks with dependency flags; pivot test d > st->eps_factor. A failed pivot
+// sets st->solve_ok = 0; a wait that runs out also sets st->timeout. flags:
+// dag_flag_ints(n) ints, zero before the first launch that uses them; *epoch
+// advances per launch. Returns at once when st->skip_factor is set.
+int dag_flag_ints(int n);
+cudaError_t launch_chol_inverse_dag(int n, float* F, float* X, float* XT, LmState* st, int* flags, int* epoch,
+                                    cudaStream_t s);
+// eps from S's diagonal, F = S in FP32, the factor and inverse, and the
+// reference's solve test on L's diagonal.
+cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, LmState* st, int* flags,
+                              int* epoch, cudaStream_t s);
+// The whole preconditioner of an attempt: eps from S's diagonal, F = S in
+// FP32, the factor and inverse; when that fails, once more on
+// S + mu diag(S) (st->shifted); then the reference's solve test on L's
+// diagonal (source/matrix_decomposition_cholesky.hpp:74,80,89).
+cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, LmState* st, double mu,
+                                  int* flags, int* epoch, cudaStream_t s);
 
 // ---- mixed form (ba_inverse.cu) ----
 // X = L^-1 and XT = X^T from the factor F and its diagonal-block inverses D.

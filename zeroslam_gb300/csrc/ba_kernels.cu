@@ -100,14 +100,18 @@ __global__ void __launch_bounds__(kThreads) k_pose_aux(DevProblem P, double* aux
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 3 : 0) k_linearize(DevProblem P, T* __restrict__ hpl, T* __restrict__ lm_part,
                                                         T* __restrict__ pose_part, const double* __restrict__ aux,
                                                         ObsJac* __restrict__ jac, float4* __restrict__ jp_pm) {
     constexpr int RS = RecStride<T>::value;
     // threads in pose-major order: the large records (H_pl, pose partials)
-    // are written coalesced and neighbouring threads share the pose's data
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= P.M) return;
+    // are written coalesced and neighbouring threads share the pose's data.
+    // In the mixed form every lane of a warp takes part in the pose sums
+    // below: a lane past the last observation repeats it and adds nothing.
+    const int64_t q_id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool valid = q_id < P.M;
+    if (sizeof(T) == 8 && !valid) return;
+    const int64_t q = valid ? q_id : P.M - 1;
     const int64_t o = P.pose_obs[q];
     const int pi = P.obs_pose[o], li = P.obs_lm[o];
     const double* xp = P.lm + (int64_t)li * kLmStride;
@@ -227,10 +231,12 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
     const T g0 = (T)(drho * orr0), g1 = (T)(drho * orr1);
     const bool pf = P.pose_fixed[pi] != 0, lf = P.lm_fixed[li] != 0;
 
-    T* hb = hpl + q * RS;
     T prec[kPoseRec];
+    T hrec[18];
 #pragma unroll
     for (int k = 0; k < kPoseRec; ++k) prec[k] = T(0);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) hrec[k] = T(0);
     if (!pf) {
         T A0[6], A1[6];  // (J_p^T W) columns
 #pragma unroll
@@ -249,39 +255,62 @@ __global__ void __launch_bounds__(kThreads) k_linearize(DevProblem P, T* __restr
 #pragma unroll
             for (int a = 0; a < 6; ++a)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) hb[a * 3 + c] = A0[a] * Jl[c] + A1[a] * Jl[3 + c];
-        } else {
-#pragma unroll
-            for (int k = 0; k < 18; ++k) hb[k] = T(0);
+                for (int c = 0; c < 3; ++c) hrec[a * 3 + c] = A0[a] * Jl[c] + A1[a] * Jl[3 + c];
         }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 18; ++k) hb[k] = T(0);
     }
-    store_rec(pose_part + q * kPoseRec, prec);
+    if (valid) {
+        T* hb = hpl + q * RS;
+#pragma unroll
+        for (int k = 0; k < 18; ++k) hb[k] = hrec[k];
+    }
+    if constexpr (sizeof(T) == 8) store_rec(pose_part + q * kPoseRec, prec);
     if constexpr (sizeof(T) == 4) {
         // mixed form: the Jacobian record (H_ll and b are its FP64 Gram sums)
-        float4* d = reinterpret_cast<float4*>(jac + o);
-        const df g0 = df_from_double(drho * orr0), g1 = df_from_double(drho * orr1);
-        d[0] = make_float4(g0.hi, g0.lo, g1.hi, g1.lo);
-        float jp[12], jl[6];
+        if (valid) {
+            float4* d = reinterpret_cast<float4*>(jac + o);
+            const df g0 = df_from_double(drho * orr0), g1 = df_from_double(drho * orr1);
+            d[0] = make_float4(g0.hi, g0.lo, g1.hi, g1.lo);
+            float jp[12], jl[6];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) jp[k] = pf ? 0.f : (float)Jp[k];
+            for (int k = 0; k < 12; ++k) jp[k] = pf ? 0.f : (float)Jp[k];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) jl[k] = lf ? 0.f : (float)Jl[k];
-        if (jp_pm) {  // J_p is read only by the single problem's conjugate-gradient operator
-            const float4 j0 = make_float4(jp[0], jp[1], jp[2], jp[3]), j1 = make_float4(jp[4], jp[5], jp[6], jp[7]),
-                         j2 = make_float4(jp[8], jp[9], jp[10], jp[11]);
-            d[1] = j0;
-            d[2] = j1;
-            d[3] = j2;
-            jp_pm[3 * q] = j0;  // pose-major copy for the operator's pose pass
-            jp_pm[3 * q + 1] = j1;
-            jp_pm[3 * q + 2] = j2;
+            for (int k = 0; k < 6; ++k) jl[k] = lf ? 0.f : (float)Jl[k];
+            if (jp_pm) {  // J_p is read only by the single problem's conjugate-gradient operator
+                const float4 j0 = make_float4(jp[0], jp[1], jp[2], jp[3]), j1 = make_float4(jp[4], jp[5], jp[6], jp[7]),
+                             j2 = make_float4(jp[8], jp[9], jp[10], jp[11]);
+                d[1] = j0;
+                d[2] = j1;
+                d[3] = j2;
+                jp_pm[3 * q] = j0;  // pose-major copy for the operator's pose pass
+                jp_pm[3 * q + 1] = j1;
+                jp_pm[3 * q + 2] = j2;
+            }
+            d[4] = make_float4(jl[0], jl[1], jl[2], jl[3]);
+            d[5] = make_float4(jl[4], jl[5], (float)W00, (float)W01);
+            d[6] = make_float4((float)W10, (float)W11, 0.f, 0.f);
         }
-        d[4] = make_float4(jl[0], jl[1], jl[2], jl[3]);
-        d[5] = make_float4(jl[4], jl[5], (float)W00, (float)W01);
-        d[6] = make_float4((float)W10, (float)W11, 0.f, 0.f);
+        // The pose sums, warp by warp: a segmented inclusive scan over the
+        // warp's lanes keyed by pose (pose-major order, so each pose's lanes
+        // are contiguous); the last lane of each pose's run stores the run's
+        // 27 sums at its position, and k_reduce_pose_runs adds a pose's runs.
+        const int lane = threadIdx.x & 31;
+        const int key = valid ? pi : 0x7fffffff;
+        if (!valid) {
+#pragma unroll
+            for (int k = 0; k < kPoseRec; ++k) prec[k] = T(0);
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int ko = __shfl_up_sync(0xffffffffu, key, off);
+            const bool take = lane >= off && ko == key;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                const T v = __shfl_up_sync(0xffffffffu, prec[k], off);
+                if (take) prec[k] += v;
+            }
+        }
+        const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+        if (valid && (lane == 31 || kn != key || q + 1 == P.M)) store_rec(pose_part + q * kPoseRec, prec);
         return;
     } else {
     T lrec[kLmRec];
@@ -519,6 +548,59 @@ __global__ void __launch_bounds__(kThreads) k_reduce_pose(DevProblem P, const T*
     }
 }
 
+// Mixed form: H_pp and b_p of pose k (a CTA per pose) from the runs that
+// k_linearize stored: within each 32-position warp chunk of the pose's
+// pose-major range, the run's sums sit at its last position. Threads take
+// the chunks in turn and add in FP64; the warps' totals meet in a fixed
+// order.
+__global__ void __launch_bounds__(kThreads) k_reduce_pose_runs(DevProblem P, const float* __restrict__ pose_part,
+                                                               double* hpp, double* b) {
+    constexpr int NW = kThreads / 32;
+    __shared__ double sh[NW][28];
+    const int k = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double acc[27];
+#pragma unroll
+    for (int c = 0; c < 27; ++c) acc[c] = 0.0;
+    const int s0 = P.pose_ptr[k], e = P.pose_ptr[k + 1];
+    if (e > s0) {
+        const int c0 = s0 >> 5, c1 = (e - 1) >> 5;
+        for (int c = c0 + threadIdx.x; c <= c1; c += blockDim.x) {
+            const int tail = min(e, 32 * c + 32) - 1;
+            const float4* r = reinterpret_cast<const float4*>(pose_part + (int64_t)tail * kPoseRec);
+#pragma unroll
+            for (int i = 0; i < 7; ++i) {
+                const float4 t = __ldg(r + i);
+                acc[4 * i] += (double)t.x;
+                acc[4 * i + 1] += (double)t.y;
+                acc[4 * i + 2] += (double)t.z;
+                if (4 * i + 3 < 27) acc[4 * i + 3] += (double)t.w;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 27; ++c) {
+        double v = acc[c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) sh[warp][c] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        const int c = threadIdx.x;
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) v += sh[w][c];
+        if (c < 21) {
+            const int a = kUp6[c][0], d = kUp6[c][1];
+            hpp[(int64_t)k * 36 + a * 6 + d] = v;
+            hpp[(int64_t)k * 36 + d * 6 + a] = v;
+        } else {
+            b[6LL * k + (c - 21)] = v;
+        }
+    }
+}
+
 // Damped 3x3 landmark inverses (landmark_inverse).
 __global__ void __launch_bounds__(kThreads) k_invert(DevProblem P, const double* __restrict__ hll, double* hinv,
                                                      float* hinv_f, const LmState* st) {
@@ -657,6 +739,81 @@ __global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevPr
             for (int k = 0; k < 32; ++k) v1 += r[k][32 + lane];
             out[32 + lane] = v1;
         }
+    }
+}
+
+// The FP32 (mixed form) version of k_schur_segments with the records staged
+// through shared memory: per round the warp first copies its 32 triples' W
+// and H_pl records (80 bytes each) with 16-byte loads in which consecutive
+// lanes read consecutive 16-byte pieces of the same records (five lanes per
+// record, so one warp-wide load touches about seven records' cache lines
+// instead of 32 scattered ones), then each lane multiplies its own triple's
+// records out of shared memory (an 80-byte record stride puts the 128-bit
+// reads of eight consecutive lanes in distinct bank groups). The sums and
+// their order are k_schur_segments<float>'s.
+constexpr int kSchurStagedThreads = 256;
+
+__global__ void __launch_bounds__(kSchurStagedThreads) k_schur_segments_staged(DevProblem P,
+                                                                               const float* __restrict__ W,
+                                                                               const float* __restrict__ hpl,
+                                                                               double* __restrict__ part,
+                                                                               const WinCtl* __restrict__ ctl) {
+    constexpr int RS = 20;          // floats per record (18 used)
+    constexpr int Q = RS / 4;       // 16-byte pieces per record
+    constexpr int NW = kSchurStagedThreads / 32;
+    __shared__ float4 sw[NW][32 * Q];
+    __shared__ float4 sh[NW][32 * Q];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (g >= P.nsegs) return;
+    if (ctl && P.pose_win && !ctl[P.pose_win[P.pair_i[P.seg_pair[g]]]].active) return;
+    float acc[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = 0.f;
+    const int64_t t0 = P.seg_ptr[g], t1 = P.seg_ptr[g + 1];
+    float4* ws = sw[wib];
+    float4* hs = sh[wib];
+    const float4* W4 = reinterpret_cast<const float4*>(W);
+    const float4* H4 = reinterpret_cast<const float4*>(hpl);
+    for (int64_t base = t0; base < t1; base += 32) {
+        const int cnt = (t1 - base) < 32 ? (int)(t1 - base) : 32;
+        const int2 tr = lane < cnt ? P.triples[base + lane] : make_int2(0, 0);
+        // cooperative copy: piece e = 32 k + lane of the round's 32 records
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const int e = 32 * k + lane;
+            const int r = e / Q, c = e - r * Q;
+            const int px = __shfl_sync(0xffffffffu, tr.x, r);
+            const int py = __shfl_sync(0xffffffffu, tr.y, r);
+            if (r < cnt) {
+                ws[e] = __ldg(W4 + (int64_t)px * Q + c);
+                hs[e] = __ldg(H4 + (int64_t)py * Q + c);
+            }
+        }
+        __syncwarp();
+        if (lane < cnt) {
+            float wv[RS], hv[RS];
+#pragma unroll
+            for (int c = 0; c < Q; ++c) {
+                const float4 a = ws[lane * Q + c], b = hs[lane * Q + c];
+                wv[4 * c] = a.x; wv[4 * c + 1] = a.y; wv[4 * c + 2] = a.z; wv[4 * c + 3] = a.w;
+                hv[4 * c] = b.x; hv[4 * c + 1] = b.y; hv[4 * c + 2] = b.z; hv[4 * c + 3] = b.w;
+            }
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int d = 0; d < 6; ++d)
+                    acc[a * 6 + d] += wv[a * 3] * hv[d * 3] + wv[a * 3 + 1] * hv[d * 3 + 1] + wv[a * 3 + 2] * hv[d * 3 + 2];
+        }
+        __syncwarp();
+    }
+    double* out = part + g * 36;
+#pragma unroll
+    for (int e = 0; e < 36; ++e) {
+        float v = acc[e];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (e == lane || e == 32 + lane) out[e] = (double)v;
     }
 }
 
@@ -945,7 +1102,10 @@ __global__ void k_decide(LmState* st) {
 }
 
 __global__ void k_set_solve_ok(LmState* st, int v) {
-    if (threadIdx.x == 0) st->solve_ok = v;
+    if (threadIdx.x == 0) {
+        st->solve_ok = v;
+        st->timeout = 0;
+    }
 }
 
 // ------------------------------------------------------------------ launchers
@@ -980,7 +1140,10 @@ void launch_linearize(const DevProblem& P, DevWork& W, cudaStream_t s) {
         note_launch();
     }
     if (P.K > 0) {
-        k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b);
+        if constexpr (sizeof(T) == 4)
+            k_reduce_pose_runs<<<P.K, kThreads, 0, s>>>(P, (const float*)W.pose_part, W.hpp, W.b);
+        else
+            k_reduce_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.pose_part, W.hpp, W.b);
         note_launch();
     }
 }
@@ -1000,9 +1163,16 @@ void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStr
 template <typename T>
 void launch_schur_pairs(const DevProblem& P, DevWork& W, const WinCtl* ctl, cudaStream_t s) {
     if (P.npairs > 0) {
-        constexpr int nt = schur_seg_threads<T>();
-        const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
-        k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
+        if constexpr (sizeof(T) == 4) {
+            constexpr int nt = kSchurStagedThreads;
+            const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
+            k_schur_segments_staged<<<(int)blocks, nt, 0, s>>>(P, (const float*)W.W, (const float*)W.hpl, W.partial,
+                                                                ctl);
+        } else {
+            constexpr int nt = schur_seg_threads<T>();
+            const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
+            k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
+        }
         note_launch();
         k_schur_assemble<<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, W.partial, W.S, ctl);
         note_launch();
