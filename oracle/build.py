@@ -61,7 +61,7 @@ def build_oracle(force: bool = False) -> str:
         tmp = ORACLE_SO + f".{os.getpid()}.tmp"
         # -ffp-contract=off keeps the restatement's rounding the same on hosts
         # with and without fused multiply-add.
-        subprocess.check_call(["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
+        subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
                                "-o", tmp, src, "-lm"])
         os.replace(tmp, ORACLE_SO)
     return ORACLE_SO

@@ -742,81 +742,6 @@ __global__ void __launch_bounds__(schur_seg_threads<T>()) k_schur_segments(DevPr
     }
 }
 
-// The FP32 (mixed form) version of k_schur_segments with the records staged
-// through shared memory: per round the warp first copies its 32 triples' W
-// and H_pl records (80 bytes each) with 16-byte loads in which consecutive
-// lanes read consecutive 16-byte pieces of the same records (five lanes per
-// record, so one warp-wide load touches about seven records' cache lines
-// instead of 32 scattered ones), then each lane multiplies its own triple's
-// records out of shared memory (an 80-byte record stride puts the 128-bit
-// reads of eight consecutive lanes in distinct bank groups). The sums and
-// their order are k_schur_segments<float>'s.
-constexpr int kSchurStagedThreads = 256;
-
-__global__ void __launch_bounds__(kSchurStagedThreads) k_schur_segments_staged(DevProblem P,
-                                                                               const float* __restrict__ W,
-                                                                               const float* __restrict__ hpl,
-                                                                               double* __restrict__ part,
-                                                                               const WinCtl* __restrict__ ctl) {
-    constexpr int RS = 20;          // floats per record (18 used)
-    constexpr int Q = RS / 4;       // 16-byte pieces per record
-    constexpr int NW = kSchurStagedThreads / 32;
-    __shared__ float4 sw[NW][32 * Q];
-    __shared__ float4 sh[NW][32 * Q];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (g >= P.nsegs) return;
-    if (ctl && P.pose_win && !ctl[P.pose_win[P.pair_i[P.seg_pair[g]]]].active) return;
-    float acc[36];
-#pragma unroll
-    for (int e = 0; e < 36; ++e) acc[e] = 0.f;
-    const int64_t t0 = P.seg_ptr[g], t1 = P.seg_ptr[g + 1];
-    float4* ws = sw[wib];
-    float4* hs = sh[wib];
-    const float4* W4 = reinterpret_cast<const float4*>(W);
-    const float4* H4 = reinterpret_cast<const float4*>(hpl);
-    for (int64_t base = t0; base < t1; base += 32) {
-        const int cnt = (t1 - base) < 32 ? (int)(t1 - base) : 32;
-        const int2 tr = lane < cnt ? P.triples[base + lane] : make_int2(0, 0);
-        // cooperative copy: piece e = 32 k + lane of the round's 32 records
-#pragma unroll
-        for (int k = 0; k < Q; ++k) {
-            const int e = 32 * k + lane;
-            const int r = e / Q, c = e - r * Q;
-            const int px = __shfl_sync(0xffffffffu, tr.x, r);
-            const int py = __shfl_sync(0xffffffffu, tr.y, r);
-            if (r < cnt) {
-                ws[e] = __ldg(W4 + (int64_t)px * Q + c);
-                hs[e] = __ldg(H4 + (int64_t)py * Q + c);
-            }
-        }
-        __syncwarp();
-        if (lane < cnt) {
-            float wv[RS], hv[RS];
-#pragma unroll
-            for (int c = 0; c < Q; ++c) {
-                const float4 a = ws[lane * Q + c], b = hs[lane * Q + c];
-                wv[4 * c] = a.x; wv[4 * c + 1] = a.y; wv[4 * c + 2] = a.z; wv[4 * c + 3] = a.w;
-                hv[4 * c] = b.x; hv[4 * c + 1] = b.y; hv[4 * c + 2] = b.z; hv[4 * c + 3] = b.w;
-            }
-#pragma unroll
-            for (int a = 0; a < 6; ++a)
-#pragma unroll
-                for (int d = 0; d < 6; ++d)
-                    acc[a * 6 + d] += wv[a * 3] * hv[d * 3] + wv[a * 3 + 1] * hv[d * 3 + 1] + wv[a * 3 + 2] * hv[d * 3 + 2];
-        }
-        __syncwarp();
-    }
-    double* out = part + g * 36;
-#pragma unroll
-    for (int e = 0; e < 36; ++e) {
-        float v = acc[e];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (e == lane || e == 32 + lane) out[e] = (double)v;
-    }
-}
-
 // S_ij -= the pair's segment sums, added in FP64 in segment order: diagonal
 // pairs subtract from the H_pp + lambda I block written by k_s_init,
 // off-diagonal pairs write both blocks. With windows the pair's window S
@@ -1163,16 +1088,9 @@ void launch_invert_w(const DevProblem& P, DevWork& W, const LmState* st, cudaStr
 template <typename T>
 void launch_schur_pairs(const DevProblem& P, DevWork& W, const WinCtl* ctl, cudaStream_t s) {
     if (P.npairs > 0) {
-        if constexpr (sizeof(T) == 4) {
-            constexpr int nt = kSchurStagedThreads;
-            const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
-            k_schur_segments_staged<<<(int)blocks, nt, 0, s>>>(P, (const float*)W.W, (const float*)W.hpl, W.partial,
-                                                                ctl);
-        } else {
-            constexpr int nt = schur_seg_threads<T>();
-            const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
-            k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
-        }
+        constexpr int nt = schur_seg_threads<T>();
+        const int64_t blocks = (P.nsegs * 32 + nt - 1) / nt;
+        k_schur_segments<T><<<(int)blocks, nt, 0, s>>>(P, (const T*)W.W, (const T*)W.hpl, W.partial, ctl);
         note_launch();
         k_schur_assemble<<<grid_for((int64_t)P.npairs * 36), kThreads, 0, s>>>(P, W.partial, W.S, ctl);
         note_launch();
