@@ -451,6 +451,16 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, 
  * names it). */
 int zs_dense_cholesky_solve_noalloc(const double* A, int n, const double* b, double* L, double* x);
 
+/* C = A B^T (or only its lower triangle, col <= row, with lower != 0) for
+ * row-major FP32 host arrays A (M x K), B (N x K), C (M x N) on the current
+ * device's tensor cores with FP32 accuracy (three TF32 products per operand
+ * pair, FP32 accumulation): the product the mixed form's dense preconditioner
+ * uses for large reduced systems. *ms (may be NULL) receives the kernel's
+ * device time. No reference counterpart: a test and measurement utility.
+ * Returns ZS_OK, ZS_ERR_INVALID, ZS_ERR_TIMEOUT (a bounded wait inside the
+ * kernel ran out) or a CUDA status. */
+int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C, int M, int N, int K, int lower, double* ms);
+
 /* Measures the FP64 and FP32 fused multiply-add pipe peaks of `device` with
  * a register-resident FMA chain on every SM (TFLOP/s, 2 flops per FMA). A
  * measurement utility for roofline reports; no reference counterpart. */

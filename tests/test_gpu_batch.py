@@ -161,12 +161,14 @@ def test_batch_huber_windows(zs_lib, oracle):
     """Local windows as map::optimise builds them, with loss_huber(sqrt(5.991))
     (source/map.hpp:74): the FP64 batch against the oracle window by window
     after one iteration (1e-9). After five, the FP64 batch, the mixed batch
-    and the single-problem FP64 solve all within 1e-3 of the oracle's cost:
-    under Huber the outliers' second-order term is switched by the sign of
-    rho' + 2 rho'' e^2, zero in exact arithmetic, so states that differ in
-    the last bits (the dense solves sum in different orders) take different
-    branches and the paths separate (measured up to 1.9e-4 after five
-    iterations on these small windows)."""
+    and the single-problem FP64 solve all lower the cost and stay within 5% of
+    the oracle's: under Huber the outliers' second-order term is switched by
+    the sign of rho' + 2 rho'' e^2, zero in exact arithmetic, so states that
+    differ in the last bits (the dense solves sum in different orders; the
+    host's libm and the device's sin and cos round differently) take
+    different branches and the paths separate into nearby minima (measured:
+    up to 1.9e-4 on most windows, 2.8e-2 on one, where the oracle built on
+    aarch64 and on x86-64 themselves end 2.9e-2 apart)."""
     wins = _small_batch(6, seed=9)
     for w in wins:
         w.loss_kind, w.loss_delta = 1, float(np.sqrt(5.991))
@@ -181,5 +183,5 @@ def test_batch_huber_windows(zs_lib, oracle):
             h.set_problem(sc)
             rs = h.solve(5)
         for c in (reps[w].chi2_final, reps_m[w].chi2_final, rs.chi2_final):
-            assert abs(c - ro.chi2_final) <= 1e-3 * ro.chi2_final, (w, c, ro.chi2_final)
+            assert abs(c - ro.chi2_final) <= 5e-2 * ro.chi2_final, (w, c, ro.chi2_final)
             assert c < ro.chi2_initial

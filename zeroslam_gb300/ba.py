@@ -30,6 +30,7 @@ MIXED = 1
 LOSS_NONE, LOSS_HUBER, LOSS_CAUCHY, LOSS_TUKEY = 0, 1, 2, 3
 
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int32)
 _up = C.POINTER(C.c_uint8)
 
@@ -135,8 +136,8 @@ _LIB = None
 ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
-                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_ba_adjoint", "zs_ba_set_batch",
-                 "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
+                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_dense_gemm_nt_tf32x3", "zs_ba_adjoint",
+                 "zs_ba_set_batch", "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
                  "zs_ba_cull", "zs_map_optimise", "zs_find_matches", "zs_map_optimise_plan",
                  "zs_frame_to_pose", "zs_pose_to_frame", "zs_ba_get_history")
 
@@ -196,6 +197,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_ba_get_window_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
     lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
+    lib.zs_dense_gemm_nt_tf32x3.restype = C.c_int
+    lib.zs_dense_gemm_nt_tf32x3.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
     lib.zs_map_cull.restype = C.c_int
     lib.zs_map_cull.argtypes = [C.c_void_p, C.POINTER(MapCullInput), _up, C.POINTER(C.c_float),
                                 C.POINTER(CullReport)]
@@ -620,6 +623,23 @@ def dense_cholesky_status(A, b, precision: int = FP64) -> int:
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(A.shape[0])
     return int(lib.zs_dense_cholesky_solve(_p(A, _dp), A.shape[0], _p(b, _dp), None, _p(x, _dp), int(precision)))
+
+
+def dense_gemm_tf32x3(A, B, lower: bool = False):
+    """(A B^T on the tensor cores with FP32 accuracy, the kernel's device ms)."""
+    lib = load()
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    M, K = A.shape
+    N = B.shape[0]
+    if B.shape[1] != K:
+        raise ValueError("A and B need the same number of columns")
+    out = np.zeros((M, N), dtype=np.float32)
+    ms = C.c_double()
+    st = lib.zs_dense_gemm_nt_tf32x3(_p(A, _fp), _p(B, _fp), _p(out, _fp), M, N, K, int(bool(lower)), C.byref(ms))
+    if st != ZS_OK:
+        raise ZsError(st, "zs_dense_gemm_nt_tf32x3")
+    return out, ms.value
 
 
 def pipe_peaks(device: int = 0):

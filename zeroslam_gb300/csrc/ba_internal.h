@@ -365,6 +365,16 @@ cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float*
 cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, LmState* st, double mu,
                                   int* flags, int* epoch, cudaStream_t s);
 
+// ---- FP32 products on the tensor cores (ba_tc_gemm.cu) ----
+// C (M x N, row stride ldc) = alpha A B^T + beta C, A (M x K) and B (N x K)
+// row-major with K contiguous, three TF32 products per operand pair (FP32
+// accuracy). Needs lda, ldb multiples of 4 and 16-byte aligned A, B
+// (tc_gemm_supported). lower: only C's lower triangle (col <= row) is
+// written. A wait that runs out sets *err = 1 (device int).
+bool tc_gemm_supported(int lda, int ldb, const float* A, const float* B);
+cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                              float alpha, float beta, bool lower, int* err, cudaStream_t s);
+
 // ---- mixed form (ba_inverse.cu) ----
 // X = L^-1 and XT = X^T from the factor F and its diagonal-block inverses D.
 template <typename TX>
