@@ -186,10 +186,10 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
     return true;
 }
 
-// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows) in
-// place: L_jj into F (zeros above the diagonal), L_jj^-1 into X's tile
-// (zeros above the diagonal) and its transpose into XT's. Returns 0 when a
-// pivot fails its test (uniform).
+// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows):
+// L_jj stays in sm.T (store_diag_factor writes it out), L_jj^-1 goes into
+// X's tile (zeros above the diagonal) and its transpose into XT's. Returns 0
+// when a pivot fails its test (uniform).
 __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float eps, Smem& sm) {
     const int n = d.n, k0 = kP * jb;
     const int nbw = (kb + 31) >> 5;
@@ -250,21 +250,31 @@ __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float e
         }
         __syncthreads();
     }
-    // L_jj and its inverse out (row-major, zeros above the diagonal), the
-    // inverse's transpose into XT
+    // the inverse out (row-major, zeros above the diagonal) and its transpose
+    // into XT: what the other tiles wait for (L_jj itself follows the flag)
+    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
+        const int i = e >> 6, j = e & 63;
+        if (i >= kb || j >= kb) continue;
+        d.X[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? Inv[i * kPL + j] : 0.f;
+        d.XT[(int64_t)(k0 + i) * n + k0 + j] = i <= j ? Inv[j * kPL + i] : 0.f;
+    }
+    return 1;
+}
+
+// L_jj (row-major, zeros above the diagonal) into F from the factored tiles.
+// No task reads F's diagonal tiles; the solve test after the launch does.
+__device__ void store_diag_factor(const Dag& d, int jb, int kb, const Smem& sm) {
+    const int n = d.n, k0 = kP * jb;
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
         if (i >= kb || j >= kb) continue;
         float l = 0.f;
         if (j <= i) {
-            const float* Tb = tile_at(T, i >> 5, j >> 5);
+            const float* Tb = tile_at(sm.T, i >> 5, j >> 5);
             l = (j == i) ? Tb[(i & 31) * (kLd + 1)] : Tb[(i & 31) * kLd + (j & 31)];
         }
         d.F[(int64_t)(k0 + i) * n + k0 + j] = l;
-        d.X[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? Inv[i * kPL + j] : 0.f;
-        d.XT[(int64_t)(k0 + i) * n + k0 + j] = i <= j ? Inv[j * kPL + i] : 0.f;
     }
-    return 1;
 }
 
 // acc (the owner's 4 x 4 block of a 64 x 64 tile) into a shared-memory tile,
@@ -284,6 +294,11 @@ __device__ __forceinline__ void acc_to_smem(const float acc[4][4], float* S, boo
 // L tile (i, j), i >= j.
 __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
     const int n = d.n, N = d.N;
+    const int ri = tile_len(d, i), cj = tile_len(d, j);
+    // the tile's S values, copied while the sums run (sm.inv is free until
+    // the diagonal factor)
+    load_block(d.F, n, kP * i, kP * j, cj, sm.inv);
+    cp_async_commit();
     float acc[4][4];
     zero_acc(acc);
     const bool ok = accumulate(d, j, [&](int k, const float*& ma, int& ra, int& ca, const float*& mb, int& rb,
@@ -295,17 +310,18 @@ __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
         fb = d.flagL + j * N + k;
     }, sm, acc);
     if (!ok) return false;
+    cp_async_wait_none();
+    __syncthreads();
     // C = S_ij - acc into a[0]
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const int ri = tile_len(d, i), cj = tile_len(d, j);
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const int r = ty + 16 * a, c = tx + 16 * b;
-            const float s = (r < ri && c < cj) ? ldcg(d.F + (int64_t)(kP * i + r) * n + kP * j + c) : 0.f;
-            acc[a][b] = s - acc[a][b];
+            acc[a][b] = sm.inv[r * kPL + c] - acc[a][b];
         }
+    __syncthreads();
     acc_to_smem(acc, sm.a[0], false);
     __syncthreads();
     if (i == j) {
@@ -330,6 +346,8 @@ __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
             }
     }
     publish(d, d.flagL + i * N + j, task);
+    if (i == j) store_diag_factor(d, j, cj, sm);
+    __syncthreads();
     return true;
 }
 
