@@ -481,11 +481,6 @@ static int cluster_size() {
     return c;
 }
 
-// The mixed form's 64-wide-panel factorisation (ba_chol_blk.cu) for n >= 128;
-// D serves as its 64 x 64 scratch before k_diag_inverses fills it.
-cudaError_t launch_chol_blk(int n, float* F, float* Li, LmState* st, cudaStream_t s);
-constexpr int kBlkMinN = 128;
-
 template <typename TS, typename TF>
 cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
@@ -499,17 +494,11 @@ cudaError_t launch_factor(int n, const TS* S, TF* F, TF* D, LmState* st, cudaStr
     int blocks = sms;  // one CTA per SM, all co-resident
     if (blocks > nblk * (nblk + 1) / 2 + 1) blocks = nblk * (nblk + 1) / 2 + 1;
     if (blocks < 1) blocks = 1;
-    cudaError_t e;
-    if (sizeof(TF) == 4 && n >= kBlkMinN) {
-        e = launch_chol_blk(n, reinterpret_cast<float*>(F), reinterpret_cast<float*>(D), st, s);
-        if (e != cudaSuccess) return e;
-    } else {
-        int nn_i = n;
-        void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
-        e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<TF>, dim3(blocks), dim3(kThreads), args, 0, s);
-        if (e != cudaSuccess) return e;
-        note_launch();
-    }
+    int nn_i = n;
+    void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<TF>, dim3(blocks), dim3(kThreads), args, 0, s);
+    if (e != cudaSuccess) return e;
+    note_launch();
     k_check_solve_eps<TF><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
     k_diag_inverses<TF><<<nblk, kThreads, 0, s>>>(n, F, D, st); note_launch();
     return cudaGetLastError();
@@ -536,37 +525,6 @@ __global__ void __launch_bounds__(kThreads) k_convert_shift(int n, const double*
         const double v = S[i];
         F[i] = (float)(i / n == i % n ? v + mu * fabs(v) : v);
     }
-}
-
-cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float* D, LmState* st, double mu,
-                                         cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    cudaError_t e = launch_factor<double, float>(n, S, F, D, st, s);
-    if (e != cudaSuccess) return e;
-    k_retry_arm<<<1, 32, 0, s>>>(st); note_launch();
-    k_convert_shift<<<std::min<int64_t>(grid_for((int64_t)n * n), 4096), kThreads, 0, s>>>(n, S, F, mu, st);
-    note_launch();
-    const int nblk = (n + kNB - 1) / kNB;
-    if (n >= kBlkMinN) {
-        e = launch_chol_blk(n, F, D, st, s);
-        if (e != cudaSuccess) return e;
-    } else {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        int blocks = sms;
-        if (blocks > nblk * (nblk + 1) / 2 + 1) blocks = nblk * (nblk + 1) / 2 + 1;
-        if (blocks < 1) blocks = 1;
-        int nn_i = n;
-        void* args[] = {(void*)&nn_i, (void*)&F, (void*)&st};
-        e = cudaLaunchCooperativeKernel((const void*)k_chol_coop<float>, dim3(blocks), dim3(kThreads), args, 0, s);
-        if (e != cudaSuccess) return e;
-        note_launch();
-    }
-    k_check_solve_eps<float><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
-    k_diag_inverses<float><<<nblk, kThreads, 0, s>>>(n, F, D, st); note_launch();
-    k_retry_disarm<<<1, 32, 0, s>>>(st); note_launch();
-    return cudaGetLastError();
 }
 
 cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, LmState* st, int* flags,
@@ -639,8 +597,6 @@ cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double*
     template cudaError_t launch_reduced_solve<TS, TF>(int, const TS*, TF*, TF*, const double*, double*, double*, \
                                                       LmState*, int, double, cudaStream_t);
 ZS_INST(double, double)
-ZS_INST(float, float)
-ZS_INST(double, float)
 #undef ZS_INST
 
 }  // namespace zs

@@ -116,7 +116,7 @@ struct DevWork {
     double* bs = nullptr;      // [n]
     double* work = nullptr;    // [4n + 256] triangular-solve and refinement vectors
     void* X = nullptr;         // mixed form: [n*n] L^-1 (lower)
-    void* XT = nullptr;        // mixed form: [n*n] (L^-1)^T (upper; lower used as scratch)
+    void* XT = nullptr;        // mixed form: [n*n] (L^-1)^T (upper)
     int* dag_flags = nullptr;  // mixed form: [dag_flag_ints(n)] tile flags of the preconditioner's launch
     int dag_epoch = 0;         // mixed form: epoch of its last launch (host side)
     double* delta = nullptr;   // [n + 3L]
@@ -336,12 +336,6 @@ template <typename TS, typename TF>
 cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double* bs, double* x, double* work,
                                  LmState* st, int refine_iters, double tol, cudaStream_t s);
 
-// Mixed form: launch_factor, then, when it failed, one more factorisation of
-// S + mu diag(S) (the factor is the conjugate-gradient preconditioner only,
-// and the FP32-formed S may be indefinite where the exact S is not). Sets
-// st->shifted.
-cudaError_t launch_factor_preconditioner(int n, const double* S, float* F, float* D, LmState* st, double mu,
-                                         cudaStream_t s);
 
 // ---- mixed form: the preconditioner (ba_chol_dag.cu) ----
 // F (n x n FP32, the matrix) -> L in F's lower triangle (zeros above the
@@ -376,9 +370,6 @@ cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, cons
                               float alpha, float beta, bool lower, int* err, cudaStream_t s);
 
 // ---- mixed form (ba_inverse.cu) ----
-// X = L^-1 and XT = X^T from the factor F and its diagonal-block inverses D.
-template <typename TX>
-cudaError_t launch_tri_inverse(int n, const TX* F, const TX* D, TX* X, TX* XT, LmState* st, cudaStream_t s);
 // Dense mixed solves (zs_dense_cholesky_solve): x = X^T X bs, then FP64
 // refinement x += X^T X (bs - S x) until ||bs - S x|| <= tol ||bs|| or
 // refine_iters sweeps; work: 4n + 256 doubles.

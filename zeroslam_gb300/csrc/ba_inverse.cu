@@ -1,17 +1,10 @@
-// Mixed-precision reduced solves after the FP32 factorisation S ~ L L^T:
-//
-// 1. k_tri_inverse: X = L^-1 by recursive 2 x 2 block inversion,
-//        inv([A 0; B C]) = [A^-1 0; -C^-1 (B A^-1)  C^-1],
-//    from the 32 x 32 diagonal-block inverses D_k up, doubling the block
-//    size each level (log2(n/32) levels, two grid barriers per level). Every
-//    level is a set of independent 32 x 32 output tiles of GEMM work spread
-//    over all SMs. X^T is stored beside X so that both products below are
-//    row-wise; the lower triangle of X^T doubles as the scratch for B A^-1.
-//    (n >= 128 in FP32: the 64-wide k_tri_inverse64 of ba_chol_blk.cu.)
-// 2. k_pcg (bundle adjustment, mixed form): conjugate gradients on the exact
+// Mixed-precision reduced solves with the preconditioner X = L^-1 of the
+// FP32 factor S ~ L L^T (formed with the factor by k_chol_inverse_dag,
+// ba_chol_dag.cu; X^T is stored beside X so that both products are row-wise):
+// 1. k_pcg (bundle adjustment, mixed form): conjugate gradients on the exact
 //    Schur operator of the FP32 Jacobian, applied matrix-free in double-float,
 //    preconditioned by X^T X; see the section below.
-// 3. k_refine (dense solves, zs_dense_cholesky_solve): x = X^T X b_s, then
+// 2. k_refine (dense solves, zs_dense_cholesky_solve): x = X^T X b_s, then
 //    FP64 iterative refinement r = b_s - S x, x += X^T X r until
 //    ||r|| <= tol ||b_s|| or the sweep limit, in one cooperative launch with a
 //    deterministic grid-wide norm.
@@ -26,115 +19,9 @@ namespace cg = cooperative_groups;
 
 namespace zs {
 
-constexpr int kB = 32;
-
-cudaError_t launch_tri_inverse64(int n, const float* F, const float* D, float* X, float* XT, LmState* st,
-                                 cudaStream_t s);
-
 template <typename T>
 __device__ __forceinline__ T ldc(const T* p) {
     return __ldcg(p);
-}
-
-// acc (r, c4..c4+3) += sum over k-blocks m in [m0, m1) of
-// A[rowA0 + r, 32m + kk] * B[32m + kk, colB0 + c4 + q], zero outside n.
-// A and B may have been written earlier in this launch (read through L2).
-template <typename T>
-__device__ void tile_gemm(int n, const T* A, int rowA0, const T* B, int colB0, int m0, int m1, T (*sa)[kB + 1],
-                          T (*sb)[kB + 1], T acc[4]) {
-    const int r = threadIdx.x / 8, c4 = (threadIdx.x % 8) * 4;
-    for (int m = m0; m < m1; ++m) {
-        T va[4], vb[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * kThreads;
-            const int rr = e / kB, cc = e % kB;
-            const int ar = rowA0 + rr, ac = m * kB + cc;
-            va[q] = (ar < n && ac < n) ? ldc(A + (int64_t)ar * n + ac) : T(0);
-            const int br = m * kB + rr, bc = colB0 + cc;
-            vb[q] = (br < n && bc < n) ? ldc(B + (int64_t)br * n + bc) : T(0);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * kThreads;
-            sa[e / kB][e % kB] = va[q];
-            sb[e / kB][e % kB] = vb[q];
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int kk = 0; kk < kB; ++kk) {
-            const T av = sa[r][kk];
-            acc[0] += av * sb[kk][c4];
-            acc[1] += av * sb[kk][c4 + 1];
-            acc[2] += av * sb[kk][c4 + 2];
-            acc[3] += av * sb[kk][c4 + 3];
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kThreads, 1) k_tri_inverse(int n, const T* __restrict__ F, const T* __restrict__ D,
-                                                             T* X, T* XT, const LmState* st) {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ T sa[kB][kB + 1];
-    __shared__ T sb[kB][kB + 1];
-    if (!__ldcg(&st->solve_ok)) return;  // written by an earlier launch: uniform
-    const int nblk = (n + kB - 1) / kB;
-    // level 0: diagonal blocks X_kk = D_k (and their transposes)
-    for (int k = blockIdx.x; k < nblk; k += gridDim.x) {
-        for (int e = threadIdx.x; e < kB * kB; e += blockDim.x) {
-            const int r = e / kB, c = e % kB;
-            const int gr = k * kB + r, gc = k * kB + c;
-            if (gr < n && gc < n) {
-                const T v = D[(int64_t)k * kB * kB + e];
-                X[(int64_t)gr * n + gc] = v;
-                XT[(int64_t)gc * n + gr] = v;
-            }
-        }
-    }
-    grid.sync();
-    const int r = threadIdx.x / 8, c4 = (threadIdx.x % 8) * 4;
-    for (int s = 1; s < nblk; s *= 2) {
-        const int npairs = (nblk + 2 * s - 1) / (2 * s);
-        const int ntask = npairs * s * s;
-        // step 1: T_ij = sum_{m=j}^{a_end-1} L_im X_mj -> XT[rows of i, cols of j] (lower scratch)
-        for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
-            const int p = t / (s * s), w = t % (s * s);
-            const int a0 = p * 2 * s, c0 = a0 + s;
-            const int i = c0 + w / s, j = a0 + w % s;
-            if (i >= nblk) continue;
-            T acc[4] = {T(0), T(0), T(0), T(0)};
-            tile_gemm<T>(n, F, i * kB, X, j * kB, j, c0, sa, sb, acc);
-            const int row = i * kB + r;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int col = j * kB + c4 + q;
-                if (row < n && col < n) XT[(int64_t)row * n + col] = acc[q];
-            }
-        }
-        grid.sync();
-        // step 2: X_ij = - sum_{m=c0}^{i} X_im T_mj
-        for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
-            const int p = t / (s * s), w = t % (s * s);
-            const int a0 = p * 2 * s, c0 = a0 + s;
-            const int i = c0 + w / s, j = a0 + w % s;
-            if (i >= nblk) continue;
-            T acc[4] = {T(0), T(0), T(0), T(0)};
-            tile_gemm<T>(n, X, i * kB, XT, j * kB, c0, i + 1, sa, sb, acc);
-            const int row = i * kB + r;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int col = j * kB + c4 + q;
-                if (row < n && col < n) {
-                    X[(int64_t)row * n + col] = -acc[q];
-                    XT[(int64_t)col * n + row] = -acc[q];
-                }
-            }
-        }
-        grid.sync();
-    }
 }
 
 __device__ inline double wsum(double v) {
@@ -238,20 +125,6 @@ static int sm_count() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return sms > 0 ? sms : 1;
-}
-
-template <typename TX>
-cudaError_t launch_tri_inverse(int n, const TX* F, const TX* D, TX* X, TX* XT, LmState* st, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    if (sizeof(TX) == 4 && n >= 128)  // 64-wide blocks, asynchronous tile loads (ba_chol_blk.cu)
-        return launch_tri_inverse64(n, reinterpret_cast<const float*>(F), reinterpret_cast<const float*>(D),
-                                    reinterpret_cast<float*>(X), reinterpret_cast<float*>(XT), st, s);
-    int nn = n;
-    void* args[] = {(void*)&nn, (void*)&F, (void*)&D, (void*)&X, (void*)&XT, (void*)&st};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_tri_inverse<TX>, dim3(sm_count()), dim3(kThreads), args,
-                                                0, s);
-    if (e == cudaSuccess) note_launch();
-    return e;
 }
 
 template <typename TS, typename TX>
@@ -755,8 +628,6 @@ cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it,
     return e;
 }
 
-template cudaError_t launch_tri_inverse<float>(int, const float*, const float*, float*, float*, LmState*,
-                                               cudaStream_t);
 template cudaError_t launch_refine<double, float>(int, const double*, const float*, const float*, const double*,
                                                  double*, double*, LmState*, int, double, cudaStream_t);
 
