@@ -187,6 +187,57 @@ __global__ void __launch_bounds__(kThreads) k_adj_axpby(int64_t N, double alpha,
     if (i < N) y[i] = alpha * x[i] + beta * y[i];
 }
 
+// ---- the conjugate-gradient loop's scalars on the device ----
+// The host enqueues iterations in batches and reads c->done once per batch;
+// every update below is skipped once done is set, so iterations enqueued past
+// the stop change nothing. The sums over the kReduceBlocks partials run in
+// block order on one thread: the same values a host-side sum gives.
+__device__ __forceinline__ double cg_sum(const double* red) {
+    double t = 0.0;
+    for (int i = 0; i < kReduceBlocks; ++i) t += red[i];
+    return t;
+}
+
+// pAp = -(p . q) with q = -H p; stop (done = 2) unless pAp > 0, else alpha.
+__global__ void k_adj_cg_pap(const double* __restrict__ red, AdjCg* c) {
+    if (threadIdx.x || c->done) return;
+    const double pAp = -cg_sum(red);
+    if (!(pAp > 0.0)) {
+        c->done = 2;
+        return;
+    }
+    c->alpha = c->rz / pAp;
+}
+
+// |r| after the update: one more iteration done; stop at the tolerance
+// (done = 1) or at the iteration limit (done = 3).
+__global__ void k_adj_cg_rn(const double* __restrict__ red, AdjCg* c) {
+    if (threadIdx.x || c->done) return;
+    c->rn = sqrt(cg_sum(red));
+    c->it += 1;
+    if (c->rn <= c->tol * c->anorm) c->done = 1;
+    else if (c->it >= c->max_it) c->done = 3;
+}
+
+// r . z of the new preconditioned residual: beta and the new rz.
+__global__ void k_adj_cg_rz(const double* __restrict__ red, AdjCg* c) {
+    if (threadIdx.x || c->done) return;
+    const double rz_new = cg_sum(red);
+    c->beta = rz_new / c->rz;
+    c->rz = rz_new;
+}
+
+// y = alpha x + 1 y (which = 0) or y = 1 x + beta y (which = 1), with the
+// coefficient from c; nothing once c->done.
+__global__ void __launch_bounds__(kThreads) k_adj_cg_axpby(int64_t N, const AdjCg* __restrict__ c, int which,
+                                                           const double* __restrict__ x, double* y) {
+    if (c->done) return;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double alpha = which == 0 ? c->alpha : 1.0, beta = which == 0 ? 1.0 : c->beta;
+    y[i] = alpha * x[i] + beta * y[i];
+}
+
 // Fixed-shape partial dot products x . y into red[blockIdx.x].
 __global__ void __launch_bounds__(kThreads) k_adj_dot(int64_t N, const double* __restrict__ x,
                                                       const double* __restrict__ y, double* red) {
@@ -312,6 +363,25 @@ void launch_adj_dot(int64_t N, const double* x, const double* y, double* red, cu
 void launch_adj_copy(int64_t N, const double* src, double* dst, cudaStream_t s) {
     if (N > 0) {
         k_adj_copy<<<grid_for(N), kThreads, 0, s>>>(N, src, dst);
+        note_launch();
+    }
+}
+
+void launch_adj_cg_pap(const double* red, AdjCg* c, cudaStream_t s) {
+    k_adj_cg_pap<<<1, 32, 0, s>>>(red, c);
+    note_launch();
+}
+void launch_adj_cg_rn(const double* red, AdjCg* c, cudaStream_t s) {
+    k_adj_cg_rn<<<1, 32, 0, s>>>(red, c);
+    note_launch();
+}
+void launch_adj_cg_rz(const double* red, AdjCg* c, cudaStream_t s) {
+    k_adj_cg_rz<<<1, 32, 0, s>>>(red, c);
+    note_launch();
+}
+void launch_adj_cg_axpby(int64_t N, const AdjCg* c, int which, const double* x, double* y, cudaStream_t s) {
+    if (N > 0) {
+        k_adj_cg_axpby<<<grid_for(N), kThreads, 0, s>>>(N, c, which, x, y);
         note_launch();
     }
 }

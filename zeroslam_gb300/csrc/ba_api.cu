@@ -967,7 +967,8 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
         }
     }
     W.delta = dalloc<double>((size_t)n + 3 * (size_t)L, own);
-    W.red = dalloc<double>(std::max<size_t>(kReduceBlocks * 4, (size_t)P.nochunks), own);
+    // (+16: the adjoint loop's device scalars, AdjCg, after the partial sums)
+    W.red = dalloc<double>(std::max<size_t>(kReduceBlocks * 4 + 16, (size_t)P.nochunks), own);
     W.ired = dalloc<int32_t>(kReduceBlocks, own);
     ZS_CUDA(cudaMemsetAsync(W.hll_inv, 0, sizeof(double) * 9 * (size_t)std::max(L, 1), s));
     ZS_CUDA(cudaMemsetAsync(W.delta, 0, sizeof(double) * std::max<size_t>(1, (size_t)n + 3 * (size_t)L), s));
@@ -1629,26 +1630,41 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
                 if (h->opt.verbose)
                     std::fprintf(stderr, "zs adjoint: |a| %.6e  r.Mr %.6e  |M^-1 a| %.6e\n", anorm, rz,
                                  std::sqrt(dot(z, z)));
-                while (it < max_it) {
-                    launch_adj_residual(P, h->adj_rec, pv, zero, h->adj_part, q, s);  // q = -H p
-                    const double pAp = -dot(pv, q);
-                    if (h->opt.verbose) std::fprintf(stderr, "zs adjoint: it %3d  p.Hp %.6e", it, pAp);
-                    if (!(pAp > 0.0)) {  // H not positive definite along p
-                        if (h->opt.verbose) std::fprintf(stderr, "\n");
-                        break;
+                // The iterations run with their scalars on the device
+                // (AdjCg): the host enqueues kAdjBatch of them at a time and
+                // reads the stop flag once per batch; iterations enqueued past
+                // the stop change nothing.
+                AdjCg c0{};
+                c0.rz = rz;
+                c0.anorm = anorm;
+                c0.tol = 1e-13;
+                c0.max_it = max_it;
+                AdjCg* cg = reinterpret_cast<AdjCg*>(W.red + kReduceBlocks * 4);
+                ZS_CUDA(cudaMemcpyAsync(cg, &c0, sizeof(AdjCg), cudaMemcpyHostToDevice, s));
+                double* red2 = W.red + kReduceBlocks;  // the loop's partial sums
+                AdjCg ch = c0;
+                constexpr int kAdjBatch = 8;
+                while (!ch.done) {
+                    for (int b = 0; b < kAdjBatch; ++b) {
+                        launch_adj_residual(P, h->adj_rec, pv, zero, h->adj_part, q, s);  // q = -H p
+                        launch_adj_dot(N, pv, q, red2, s);
+                        launch_adj_cg_pap(red2, cg, s);                // alpha = rz / p.Hp
+                        launch_adj_cg_axpby(N, cg, 0, pv, v, s);       // v += alpha p
+                        launch_adj_cg_axpby(N, cg, 0, q, r, s);        // r -= alpha H p
+                        launch_adj_dot(N, r, r, red2, s);
+                        launch_adj_cg_rn(red2, cg, s);                 // |r|, stop test
+                        precondition(r, z);
+                        launch_adj_dot(N, r, z, red2, s);
+                        launch_adj_cg_rz(red2, cg, s);                 // beta, rz
+                        launch_adj_cg_axpby(N, cg, 1, z, pv, s);       // p = z + beta p
                     }
-                    const double alpha = rz / pAp;
-                    launch_adj_axpby(N, alpha, pv, 1.0, v, s);  // v += alpha p
-                    launch_adj_axpby(N, alpha, q, 1.0, r, s);   // r -= alpha H p
-                    ++it;
-                    rn = std::sqrt(dot(r, r));
-                    if (h->opt.verbose) std::fprintf(stderr, "  |r|/|a| %.6e\n", rn / anorm);
-                    if (rn <= 1e-13 * anorm) break;
-                    precondition(r, z);
-                    const double rz_new = dot(r, z);
-                    launch_adj_axpby(N, 1.0, z, rz_new / rz, pv, s);  // p = z + beta p
-                    rz = rz_new;
+                    ZS_CUDA(cudaMemcpyAsync(&ch, cg, sizeof(AdjCg), cudaMemcpyDeviceToHost, s));
+                    ZS_CUDA(cudaStreamSynchronize(s));
+                    if (h->opt.verbose)
+                        std::fprintf(stderr, "zs adjoint: it %3d  |r|/|a| %.6e  done %d\n", ch.it, ch.rn / anorm,
+                                     ch.done);
                 }
+                it = ch.it;
                 // the true residual of the returned v
                 launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, r, s);
                 rn = std::sqrt(dot(r, r));

@@ -32,7 +32,6 @@
 
 #include "ba_internal.h"
 #include "ba_tile64.cuh"
-#include "ba_tiles.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -72,11 +71,8 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 struct Smem {
     float a[2][kTileFloats];
     float b[2][kTileFloats];
-    float T[3 * kTile];  // the diagonal tile as three 32 x 32 tiles (ba_tiles.cuh)
     float inv[kTileFloats];
     float dinv[kP];
-    float epsr[kP];
-    int flag;
 };
 
 // Thread 0 waits for *f == epoch; false when the launch was aborted (or this
@@ -186,70 +182,88 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
     return true;
 }
 
-// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows):
-// L_jj stays in sm.T (store_diag_factor writes it out), L_jj^-1 goes into
-// X's tile (zeros above the diagonal) and its transpose into XT's. Returns 0
+__device__ __forceinline__ void bar_pair() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
+// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows;
+// rows and columns from kb on are an identity block) with its inverse, in
+// warps 0 and 1 while the other warps wait:
+// * factor: thread r of the pair holds row r in registers; per column c the
+//   rows write their current entry c (unscaled) to a shared column, one
+//   64-thread barrier, then every row r > c takes
+//   A_rj -= (A_rc / A_cc) A_jc for c < j <= r with 1 / A_cc = rsqrt(A_cc)^2,
+//   and scales its entry to L_rc = A_rc rsqrt(A_cc) (the pivot test is the
+//   reference's d > eps on the unscaled A_cc);
+// * inverse: thread j of the pair solves L x = e_j for column j of L^-1 by
+//   forward substitution, right-looking (x_m = acc_m / L_mm, then
+//   acc_i -= L_im x_m), reading L's columns from shared memory.
+// L^T stays in sm.a[1] (store_diag_factor writes L out), L^-1 goes into X's
+// tile (zeros above the diagonal) and its transpose into XT's. Returns 0
 // when a pivot fails its test (uniform).
 __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float eps, Smem& sm) {
     const int n = d.n, k0 = kP * jb;
-    const int nbw = (kb + 31) >> 5;
-    float* T = sm.T;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* Lt = sm.a[1];      // Lt[k * kPL + r] = L_rk
+    float* colbuf = sm.b[0];  // two 64-float columns, alternating
     float* Inv = sm.inv;
-    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
-        const int i = e >> 6, j = e & 63;
-        if (j > i || (i >> 5) >= nbw) continue;
-        const float v = (i < kb && j < kb) ? C[i * kPL + j] : (i == j ? 1.f : 0.f);
-        tile_at(T, i >> 5, j >> 5)[(i & 31) * kLd + (j & 31)] = v;
-    }
-    if (threadIdx.x < kP) sm.epsr[threadIdx.x] = eps;
-    __syncthreads();
-    if (!cta_cholesky<float>(T, nbw, kb, sm.epsr, sm.dinv, &sm.flag)) return 0;
-    // the inverse [Xa 0; -Xc Lb Xa  Xc] from the 32 x 32 tile inverses
-    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
-        const int r = e >> 6, c = e & 63;
-        float v = 0.f;
-        if ((r >> 5) == (c >> 5) && (r >> 5) < nbw) {
-            const int b = r >> 5, rr = r & 31, cc = c & 31;
-            v = rr == cc ? sm.dinv[r] : (cc < rr ? tile_at(T, b, b)[cc * kLd + rr] : 0.f);
-        }
-        Inv[r * kPL + c] = v;
-    }
-    __syncthreads();
-    if (nbw == 2) {
-        float w[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
+    int fail = 0;
+    if (warp < 2) {
+        const int r = 32 * warp + lane;
+        float row[kP];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int e = threadIdx.x + q * blockDim.x;
-                w[q] = fmaf(tile_at(T, 1, 0)[(e >> 5) * kLd + m], Inv[m * kPL + (e & 31)], w[q]);
+        for (int k = 0; k < kP; ++k) row[k] = (r < kb && k < kb) ? C[r * kPL + k] : (r == k ? 1.f : 0.f);
+#pragma unroll
+        for (int c = 0; c < kP; ++c) {
+            float* col = colbuf + (c & 1) * kP;
+            if (r >= c) col[r] = row[c];
+            bar_pair();
+            const float dc = col[c];
+            if (c < kb && !(dc > eps)) fail = 1;
+            const float rs = rsqrtf(dc);
+            const float l = row[c] * rs;
+            if (r > c) {
+                const float a = l * rs;
+#pragma unroll
+                for (int g = (c + 1) >> 2; g < kP / 4; ++g) {
+                    const float4 v = reinterpret_cast<const float4*>(col)[g];
+                    const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int j = 4 * g + t;
+                        if (j > c && j <= r) row[j] = fmaf(-a, vv[t], row[j]);
+                    }
+                }
+            }
+            if (r >= c) row[c] = l;
+            if (r == c) sm.dinv[c] = rs;
+        }
+#pragma unroll
+        for (int k = 0; k < kP; ++k) Lt[k * kPL + r] = k <= r ? row[k] : 0.f;
+    }
+    if (__syncthreads_or(fail)) return 0;
+    if (warp < 2) {
+        const int j = 32 * warp + lane;
+        float acc[kP];
+#pragma unroll
+        for (int i = 0; i < kP; ++i) acc[i] = i == j ? 1.f : 0.f;
+#pragma unroll
+        for (int m = 0; m < kP; ++m) {
+            const float x = acc[m] * sm.dinv[m];  // zero for m < j
+            acc[m] = x;
+#pragma unroll
+            for (int g = (m + 1) >> 2; g < kP / 4; ++g) {
+                const float4 v = reinterpret_cast<const float4*>(Lt + m * kPL)[g];
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int i = 4 * g + t;
+                    if (i > m) acc[i] = fmaf(-vv[t], x, acc[i]);
+                }
             }
         }
-        __syncthreads();
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * blockDim.x;
-            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = w[q];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = 0.f;
-#pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int e = threadIdx.x + q * blockDim.x;
-                w[q] = fmaf(Inv[(32 + (e >> 5)) * kPL + 32 + m], Inv[(32 + m) * kPL + (e & 31)], w[q]);
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * blockDim.x;
-            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = -w[q];
-        }
-        __syncthreads();
+        for (int i = 0; i < kP; ++i) Inv[i * kPL + j] = acc[i];  // L^-1[i][j] (zero for i < j)
     }
+    __syncthreads();
     // the inverse out (row-major, zeros above the diagonal) and its transpose
     // into XT: what the other tiles wait for (L_jj itself follows the flag)
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
@@ -261,19 +275,14 @@ __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float e
     return 1;
 }
 
-// L_jj (row-major, zeros above the diagonal) into F from the factored tiles.
+// L_jj (row-major, zeros above the diagonal) into F from L^T in sm.a[1].
 // No task reads F's diagonal tiles; the solve test after the launch does.
 __device__ void store_diag_factor(const Dag& d, int jb, int kb, const Smem& sm) {
     const int n = d.n, k0 = kP * jb;
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
         if (i >= kb || j >= kb) continue;
-        float l = 0.f;
-        if (j <= i) {
-            const float* Tb = tile_at(sm.T, i >> 5, j >> 5);
-            l = (j == i) ? Tb[(i & 31) * (kLd + 1)] : Tb[(i & 31) * kLd + (j & 31)];
-        }
-        d.F[(int64_t)(k0 + i) * n + k0 + j] = l;
+        d.F[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? sm.a[1][j * kPL + i] : 0.f;
     }
 }
 

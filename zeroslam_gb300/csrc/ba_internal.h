@@ -280,6 +280,15 @@ void launch_adj_axpby(int64_t N, double alpha, const double* x, double beta, dou
 void launch_adj_dot(int64_t N, const double* x, const double* y, double* red, cudaStream_t s);
 void launch_adj_copy(int64_t N, const double* src, double* dst, cudaStream_t s);
 void launch_adj_out(const DevProblem& P, const double* rec, const double* v, double* duv, double* red, cudaStream_t s);
+// Scalars of the adjoint's conjugate-gradient loop, kept on the device.
+struct AdjCg {
+    double rz, alpha, beta, rn, anorm, tol;
+    int32_t it, max_it, done, pad;  // done: 1 converged, 2 H not positive along p, 3 iteration limit
+};
+void launch_adj_cg_pap(const double* red, AdjCg* c, cudaStream_t s);
+void launch_adj_cg_rn(const double* red, AdjCg* c, cudaStream_t s);
+void launch_adj_cg_rz(const double* red, AdjCg* c, cudaStream_t s);
+void launch_adj_cg_axpby(int64_t N, const AdjCg* c, int which, const double* x, double* y, cudaStream_t s);
 
 // ---- map culling (ba_cull.cu) ----
 // Inputs of k_cull: L landmarks (lm, lm_stride doubles apart, ids lm_id),

@@ -15,10 +15,19 @@
 //               buffer at the same offsets: the swizzled layout is kept);
 //               after the last step they read the accumulator out of tensor
 //               memory (tcgen05.ld, one 32-lane quarter per warp) and write C;
-//   warp 1      allocates 128 tensor-memory columns (the 128 x 128 FP32
-//               accumulator); one thread issues the tcgen05.mma (kind::tf32,
-//               M = N = 128, K = 8) instructions, 12 per K step, and commits
-//               each stage back to the producer.
+//   warp 1      allocates 512 tensor-memory columns; one thread issues the
+//               tcgen05.mma (kind::tf32, M = N = 128, K = 8) instructions,
+//               12 per K step, and commits each stage back to the producer.
+// The tensor core adds each product into its FP32 accumulator with
+// truncation, so an accumulator that takes thousands of products drifts by
+// ~0.5 ulp of its value per product. The leading products A_hi B_hi
+// therefore go into one of two 128-column accumulators per chunk of
+// kChunkKb K steps (128 values of K); after each chunk warps 2..5 add that
+// accumulator into a fourth region in FP32 (rounded to nearest) while the
+// next chunk goes into the other one. The small correction products go into
+// their own accumulator (their drift is 2^-11 of the result's), read once.
+// Tensor memory: columns [0, 128) and [128, 256) the chunk accumulators,
+// [256, 384) the corrections, [384, 512) the promoted sum.
 // Every wait on an mbarrier is bounded: when one runs out the kernel records
 // the error (*err = 1), lets its own copies and products finish (bounded),
 // frees its tensor memory and returns.
@@ -39,6 +48,8 @@ constexpr int kTcThreads = 192;
 constexpr uint32_t kBoxFloats = kBM * kBK;          // 4096 floats = 16 KB, one operand box
 constexpr uint32_t kBoxBytes = kBoxFloats * 4;
 constexpr long long kWaitLimit = 1ll << 24;         // polls of one mbarrier phase (well over a second)
+constexpr int kChunkKb = 4;                          // K steps per promoted chunk
+constexpr uint32_t kColCorr = 256, kColSum = 384, kTmemCols = 512;
 constexpr size_t kTcSmem = 4ull * kStages * kBoxBytes + 256 + 1024;  // boxes, barriers, alignment slack
 
 struct TcArgs {
@@ -142,6 +153,48 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+// 32 consecutive columns of this thread's TMEM lane from registers.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float v[32]) {
+    uint32_t r[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r[j] = __float_as_uint(v[j]);
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+        "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+        "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+        "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+        : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// Warps 2..5: chunk ch's accumulator (columns 128 (ch & 1)) into the sum
+// (columns [384, 512)) in FP32, this warp's 32 lanes, then one arrival per
+// thread on drained[ch & 1]. The first chunk is copied.
+__device__ bool drain_chunk(int ch, uint32_t tmem, uint64_t* chunk_done, uint64_t* drained, int warp, int lane,
+                            int* err) {
+    const int b = ch & 1;
+    if (!mbar_wait(chunk_done + b, (ch >> 1) & 1, err)) return false;
+    tc_fence_after();
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+#pragma unroll 1
+    for (int c = 0; c < kBN / 32; ++c) {
+        float v[32], acc[32];
+        tmem_ld32(lane_base + 128u * b + 32 * c, v);
+        if (ch > 0) {
+            tmem_ld32(lane_base + kColSum + 32 * c, acc);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] += acc[j];
+        }
+        tmem_st32(lane_base + kColSum + 32 * c, v);
+    }
+    tc_fence_before();
+    (void)lane;
+    mbar_arrive(drained + b);
+    return true;
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_constant__ CUtensorMap ta,
                                                               const __grid_constant__ CUtensorMap tb, TcArgs g) {
     extern __shared__ uint8_t smem_raw[];
@@ -155,7 +208,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
     uint64_t* conv = bars + kStages;       // a stage is split (128 arrivals)
     uint64_t* empty = bars + 2 * kStages;  // a stage's products are done (commit)
     uint64_t* done = bars + 3 * kStages;   // all products are done (commit)
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    uint64_t* chunk_done = done + 1;       // [2] a chunk accumulator's products are done (commit)
+    uint64_t* drained = done + 3;          // [2] a chunk accumulator was added into the sum (128 arrivals)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 5);
     volatile int* s_err = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int row0 = blockIdx.y * kBM, col0 = blockIdx.x * kBN;
@@ -170,12 +225,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
             mbar_init(empty + s, 1);
         }
         mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(chunk_done + b, 1);
+            mbar_init(drained + b, 128);
+        }
         *s_err = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(128)
+                     "r"(kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -204,6 +263,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
         if (lane == 0) {
             for (int kb = 0; kb < nk; ++kb) {
                 const int s = kb % kStages, r = kb / kStages;
+                const int ch = kb / kChunkKb, b = ch & 1;
+                const bool chunk_first = kb % kChunkKb == 0;
+                // a chunk accumulator is reused once the chunk before last was added into the sum
+                if (chunk_first && ch >= 2 && !mbar_wait(drained + b, ((ch >> 1) - 1) & 1, g.err)) {
+                    *s_err = 1;
+                    break;
+                }
                 if (!mbar_wait(conv + s, r & 1, g.err)) {
                     *s_err = 1;
                     break;
@@ -212,14 +278,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
                 tc_fence_after();
                 const uint64_t ah = smem_desc(a_hi + s * kBoxFloats), al = smem_desc(a_lo + s * kBoxFloats);
                 const uint64_t bh = smem_desc(b_hi + s * kBoxFloats), bl = smem_desc(b_lo + s * kBoxFloats);
+                const uint32_t acc_main = tmem + 128u * b, acc_corr = tmem + kColCorr;
 #pragma unroll
                 for (int ks = 0; ks < kBK / 8; ++ks) {
                     const uint64_t o = (uint64_t)(ks * 32) >> 4;  // 8 TF32 values = 32 bytes along the row
-                    tc_mma(tmem, ah + o, bh + o, (kb | ks) != 0);
-                    tc_mma(tmem, ah + o, bl + o, 1);
-                    tc_mma(tmem, al + o, bh + o, 1);
+                    tc_mma(acc_main, ah + o, bh + o, !(chunk_first && ks == 0));
+                    tc_mma(acc_corr, ah + o, bl + o, (kb | ks) != 0);
+                    tc_mma(acc_corr, al + o, bh + o, 1);
                 }
                 tc_commit(empty + s);
+                if (kb % kChunkKb == kChunkKb - 1 || kb == nk - 1) tc_commit(chunk_done + b);
             }
             tc_commit(done);  // arrives once every product issued so far has completed
         }
@@ -251,15 +319,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
             // the products read shared memory through the async proxy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(conv + s);
+            // after the last step of chunk ch, the previous chunk's accumulator
+            // (its products were issued a chunk earlier) goes into the sum
+            if ((kb % kChunkKb == kChunkKb - 1 || kb == nk - 1) && kb / kChunkKb >= 1 &&
+                !drain_chunk(kb / kChunkKb - 1, tmem, chunk_done, drained, warp, lane, g.err)) {
+                *s_err = 1;
+                break;
+            }
         }
+        const int nch = (nk + kChunkKb - 1) / kChunkKb;
+        if (!*s_err && !drain_chunk(nch - 1, tmem, chunk_done, drained, warp, lane, g.err)) *s_err = 1;
         if (mbar_wait(done, 0, g.err) && !*s_err) {
             tc_fence_after();
             const int q = warp & 3;  // this warp's 32-lane quarter of tensor memory
             const int row = row0 + 32 * q + lane;
+            const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
 #pragma unroll 1
             for (int c = 0; c < kBN / 32; ++c) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * c, v);
+                float v[32], w[32];
+                tmem_ld32(lane_base + kColSum + 32 * c, v);
+                tmem_ld32(lane_base + kColCorr + 32 * c, w);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] += w[j];
                 if (row < g.M) {
                     float* crow = g.C + (int64_t)row * g.ldc;
 #pragma unroll
@@ -285,7 +366,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
     }
 }
 
