@@ -182,86 +182,91 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
     return true;
 }
 
-__device__ __forceinline__ void bar_pair() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+// The lower triangle of a 64 x 64 tile (diagonal included, 2080 entries,
+// packed row by row) shared out over the CTA: thread t owns entries
+// t + 256 q, q < kOwn.
+constexpr int kTri = kP * (kP + 1) / 2;
+constexpr int kOwn = (kTri + t64::kThreads - 1) / t64::kThreads;
+
+__device__ __forceinline__ void tri_entry(int e, int& i, int& j) {
+    i = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+    while ((i + 1) * (i + 2) / 2 <= e) ++i;
+    while (i * (i + 1) / 2 > e) --i;
+    j = e - i * (i + 1) / 2;
+}
 
 // Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows;
-// rows and columns from kb on are an identity block) with its inverse, in
-// warps 0 and 1 while the other warps wait:
-// * factor: thread r of the pair holds row r in registers; per column c the
-//   rows write their current entry c (unscaled) to a shared column, one
-//   64-thread barrier, then every row r > c takes
-//   A_rj -= (A_rc / A_cc) A_jc for c < j <= r with 1 / A_cc = rsqrt(A_cc)^2,
-//   and scales its entry to L_rc = A_rc rsqrt(A_cc) (the pivot test is the
-//   reference's d > eps on the unscaled A_cc);
-// * inverse: thread j of the pair solves L x = e_j for column j of L^-1 by
-//   forward substitution, right-looking (x_m = acc_m / L_mm, then
-//   acc_i -= L_im x_m), reading L's columns from shared memory.
-// L^T stays in sm.a[1] (store_diag_factor writes L out), L^-1 goes into X's
-// tile (zeros above the diagonal) and its transpose into XT's. Returns 0
-// when a pivot fails its test (uniform).
+// rows and columns from kb on are an identity block) and inverts the factor,
+// the whole CTA working with the tile's entries in registers (kOwn per
+// thread) and one barrier per column:
+// * factor, right-looking and unscaled: at column c every entry (i, j) with
+//   j > c takes A_ij -= A_ic A_jc / A_cc, the column-c entries (final by
+//   then) read from a shared column that their owners filled at the step
+//   before; afterwards L_ij = A_ij / sqrt(A_jj). The pivot test is the
+//   reference's d > eps on A_cc;
+// * inverse, right-looking over the rows of X = L^-1: with row k of X final,
+//   every entry (i, j), i > k >= j, takes x_ij -= L_ik X_kj, and the entries
+//   of row k + 1 are final after it (X_ii = 1 / L_ii).
+// L stays in sm.a[1] (row-major; store_diag_factor writes it out), X goes
+// into X's tile (zeros above the diagonal) and its transpose into XT's.
+// Returns 0 when a pivot fails its test (uniform).
 __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float eps, Smem& sm) {
     const int n = d.n, k0 = kP * jb;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* Lt = sm.a[1];      // Lt[k * kPL + r] = L_rk
-    float* colbuf = sm.b[0];  // two 64-float columns, alternating
-    float* Inv = sm.inv;
-    int fail = 0;
-    if (warp < 2) {
-        const int r = 32 * warp + lane;
-        float row[kP];
+    float* Lm = sm.a[1];
+    float* col = sm.b[0];  // two 64-float columns, alternating
+    float* Xs = sm.inv;
+    int ei[kOwn], ej[kOwn];
+    float a[kOwn];
 #pragma unroll
-        for (int k = 0; k < kP; ++k) row[k] = (r < kb && k < kb) ? C[r * kPL + k] : (r == k ? 1.f : 0.f);
-#pragma unroll
-        for (int c = 0; c < kP; ++c) {
-            float* col = colbuf + (c & 1) * kP;
-            if (r >= c) col[r] = row[c];
-            bar_pair();
-            const float dc = col[c];
-            if (c < kb && !(dc > eps)) fail = 1;
-            const float rs = rsqrtf(dc);
-            const float l = row[c] * rs;
-            if (r > c) {
-                const float a = l * rs;
-#pragma unroll
-                for (int g = (c + 1) >> 2; g < kP / 4; ++g) {
-                    const float4 v = reinterpret_cast<const float4*>(col)[g];
-                    const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) {
-                        const int j = 4 * g + t;
-                        if (j > c && j <= r) row[j] = fmaf(-a, vv[t], row[j]);
-                    }
-                }
-            }
-            if (r >= c) row[c] = l;
-            if (r == c) sm.dinv[c] = rs;
+    for (int q = 0; q < kOwn; ++q) {
+        const int e = threadIdx.x + t64::kThreads * q;
+        ei[q] = -1;
+        ej[q] = 0;
+        a[q] = 0.f;
+        if (e < kTri) {
+            tri_entry(e, ei[q], ej[q]);
+            const int i = ei[q], j = ej[q];
+            a[q] = (i < kb && j < kb) ? C[i * kPL + j] : (i == j ? 1.f : 0.f);
+            if (j == 0) col[i] = a[q];
         }
-#pragma unroll
-        for (int k = 0; k < kP; ++k) Lt[k * kPL + r] = k <= r ? row[k] : 0.f;
     }
-    if (__syncthreads_or(fail)) return 0;
-    if (warp < 2) {
-        const int j = 32 * warp + lane;
-        float acc[kP];
+    for (int c = 0; c < kP; ++c) {
+        __syncthreads();
+        const float* cc = col + (c & 1) * kP;
+        float* nc = col + ((c + 1) & 1) * kP;
+        const float dc = cc[c];
+        if (c < kb && !(dc > eps)) return 0;  // every thread reads the same pivot: uniform
+        const float inv = __frcp_rn(dc);
+        if (threadIdx.x == 0) sm.dinv[c] = rsqrtf(dc);
 #pragma unroll
-        for (int i = 0; i < kP; ++i) acc[i] = i == j ? 1.f : 0.f;
-#pragma unroll
-        for (int m = 0; m < kP; ++m) {
-            const float x = acc[m] * sm.dinv[m];  // zero for m < j
-            acc[m] = x;
-#pragma unroll
-            for (int g = (m + 1) >> 2; g < kP / 4; ++g) {
-                const float4 v = reinterpret_cast<const float4*>(Lt + m * kPL)[g];
-                const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const int i = 4 * g + t;
-                    if (i > m) acc[i] = fmaf(-vv[t], x, acc[i]);
-                }
+        for (int q = 0; q < kOwn; ++q) {
+            const int i = ei[q], j = ej[q];
+            if (j > c) {
+                a[q] = fmaf(-(cc[i] * inv), cc[j], a[q]);
+                if (j == c + 1) nc[i] = a[q];
             }
         }
+    }
+    __syncthreads();
+    // L = A diag(A_jj)^-1/2 (lower), and the inverse's first row
+    float x[kOwn];
 #pragma unroll
-        for (int i = 0; i < kP; ++i) Inv[i * kPL + j] = acc[i];  // L^-1[i][j] (zero for i < j)
+    for (int q = 0; q < kOwn; ++q) {
+        const int i = ei[q], j = ej[q];
+        x[q] = i == j ? 1.f : 0.f;
+        if (i >= 0) {
+            Lm[i * kPL + j] = a[q] * sm.dinv[j];
+            if (i == 0) Xs[0] = sm.dinv[0];
+        }
+    }
+    for (int k = 0; k < kP - 1; ++k) {
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kOwn; ++q) {
+            const int i = ei[q], j = ej[q];
+            if (i > k && j <= k) x[q] = fmaf(-Lm[i * kPL + k], Xs[k * kPL + j], x[q]);
+            if (i == k + 1) Xs[i * kPL + j] = x[q] * sm.dinv[i];  // 1 / L_ii = A_ii^-1/2
+        }
     }
     __syncthreads();
     // the inverse out (row-major, zeros above the diagonal) and its transpose
@@ -269,20 +274,20 @@ __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float e
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
         if (i >= kb || j >= kb) continue;
-        d.X[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? Inv[i * kPL + j] : 0.f;
-        d.XT[(int64_t)(k0 + i) * n + k0 + j] = i <= j ? Inv[j * kPL + i] : 0.f;
+        d.X[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? Xs[i * kPL + j] : 0.f;
+        d.XT[(int64_t)(k0 + i) * n + k0 + j] = i <= j ? Xs[j * kPL + i] : 0.f;
     }
     return 1;
 }
 
-// L_jj (row-major, zeros above the diagonal) into F from L^T in sm.a[1].
+// L_jj (row-major, zeros above the diagonal) into F from sm.a[1].
 // No task reads F's diagonal tiles; the solve test after the launch does.
 __device__ void store_diag_factor(const Dag& d, int jb, int kb, const Smem& sm) {
     const int n = d.n, k0 = kP * jb;
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
         if (i >= kb || j >= kb) continue;
-        d.F[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? sm.a[1][j * kPL + i] : 0.f;
+        d.F[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? sm.a[1][i * kPL + j] : 0.f;
     }
 }
 
