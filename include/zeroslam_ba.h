@@ -461,6 +461,20 @@ int zs_dense_cholesky_solve_noalloc(const double* A, int n, const double* b, dou
  * kernel ran out) or a CUDA status. */
 int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C, int M, int N, int K, int lower, double* ms);
 
+/* The mixed form's FP32 preconditioner on a row-major n x n host matrix S:
+ * the factor S = L L^T and X = L^-1 (both lower triangular; the upper
+ * triangles of L and X come back zero; either may be NULL). form 0: as the
+ * mixed solve chooses; 1: the dataflow kernel alone (64 x 64 tiles, any n);
+ * 2: the blocked form (panels of 256 columns, the diagonal blocks by the
+ * dataflow kernel and all other work as tensor-core products; needs
+ * n % 4 == 0, else ZS_ERR_INVALID; the solves take it from n = 3072 on). *ms (may be NULL)
+ * receives the device time of the factor and inverse. No reference
+ * counterpart beyond matrix::decompose_cholesky
+ * (source/matrix_decomposition_cholesky.hpp:26-61): a test and measurement
+ * utility. Returns ZS_OK, ZS_ERR_CHOLESKY (a pivot was not positive),
+ * ZS_ERR_INVALID, ZS_ERR_TIMEOUT or a CUDA status. */
+int zs_dense_chol_inverse_f32(const float* S, int n, float* L, float* X, int form, double* ms);
+
 /* Measures the FP64 and FP32 fused multiply-add pipe peaks of `device` with
  * a register-resident FMA chain on every SM (TFLOP/s, 2 flops per FMA). A
  * measurement utility for roofline reports; no reference counterpart. */

@@ -136,7 +136,7 @@ _LIB = None
 ABI_FUNCTIONS = ("zs_ba_default_options", "zs_ba_create", "zs_ba_destroy", "zs_ba_set_problem", "zs_ba_set_state",
                  "zs_ba_get_state", "zs_ba_reset_state", "zs_ba_solve", "zs_ba_chi2", "zs_ba_linear_step",
                  "zs_ba_initial_lambda", "zs_dense_cholesky_solve", "zs_pipe_peaks", "zs_ba_status_string",
-                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_dense_gemm_nt_tf32x3", "zs_ba_adjoint",
+                 "zs_last_error", "zs_dense_cholesky_solve_noalloc", "zs_dense_gemm_nt_tf32x3", "zs_dense_chol_inverse_f32", "zs_ba_adjoint",
                  "zs_ba_set_batch", "zs_ba_solve_batch", "zs_ba_get_window_state", "zs_ba_batch_solve_profile", "zs_map_cull",
                  "zs_ba_cull", "zs_map_optimise", "zs_find_matches", "zs_map_optimise_plan",
                  "zs_frame_to_pose", "zs_pose_to_frame", "zs_ba_get_history")
@@ -199,6 +199,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
     lib.zs_dense_gemm_nt_tf32x3.restype = C.c_int
     lib.zs_dense_gemm_nt_tf32x3.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
+    lib.zs_dense_chol_inverse_f32.restype = C.c_int
+    lib.zs_dense_chol_inverse_f32.argtypes = [_fp, C.c_int, _fp, _fp, C.c_int, _dp]
     lib.zs_map_cull.restype = C.c_int
     lib.zs_map_cull.argtypes = [C.c_void_p, C.POINTER(MapCullInput), _up, C.POINTER(C.c_float),
                                 C.POINTER(CullReport)]
@@ -640,6 +642,22 @@ def dense_gemm_tf32x3(A, B, lower: bool = False):
     if st != ZS_OK:
         raise ZsError(st, "zs_dense_gemm_nt_tf32x3")
     return out, ms.value
+
+
+def dense_chol_inverse_f32(S, form: int = 0):
+    """(status, L, X = L^-1, device ms) of the mixed form's FP32
+    preconditioner on the symmetric matrix S; form 0 as the solve chooses,
+    1 the dataflow kernel alone, 2 the blocked tensor-core form."""
+    lib = load()
+    S = np.ascontiguousarray(S, dtype=np.float32)
+    n = S.shape[0]
+    L = np.zeros((n, n), dtype=np.float32)
+    X = np.zeros((n, n), dtype=np.float32)
+    ms = C.c_double()
+    st = lib.zs_dense_chol_inverse_f32(_p(S, _fp), n, _p(L, _fp), _p(X, _fp), int(form), C.byref(ms))
+    if st not in (ZS_OK, ZS_ERR_CHOLESKY):
+        raise ZsError(st, "zs_dense_chol_inverse_f32")
+    return st, L, X, ms.value
 
 
 def pipe_peaks(device: int = 0):

@@ -374,6 +374,10 @@ struct zs_ba_handle {
     int bgraph_iters = -1, bgraph_rel = -1;
     long long bbody_launches = 0, bpro_launches = 0;
     float tune_us[kBatchBuckets] = {0};
+    // the blocked preconditioner's streams (mixed form, large n), kept for the
+    // handle's lifetime and sized for the largest n seen
+    TcStreams tcs;
+    int tcs_n = 0;
 
     void release_graph() {
         if (bexec) cudaGraphExecDestroy(bexec);
@@ -961,6 +965,14 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
             W.X = dalloc<char>(ts * (size_t)n * n, own);
             W.XT = dalloc<char>(ts * (size_t)n * n, own);
             W.pcg = dalloc<double>(pcg_doubles(P), own);
+            if (chol_tc_applies(n)) {
+                W.tc_scratch = dalloc<float>((size_t)chol_tc_scratch_floats(n), own);
+                if (h->tcs_n < n) {
+                    ZS_CUDA(h->tcs.init(n));
+                    h->tcs_n = n;
+                }
+                W.tc_streams = &h->tcs;
+            }
             W.dag_flags = dalloc<int>((size_t)dag_flag_ints(n), own);
             W.dag_epoch = 0;
             ZS_CUDA(cudaMemsetAsync(W.dag_flags, 0, sizeof(int) * (size_t)dag_flag_ints(n), s));
@@ -1099,8 +1111,8 @@ void system_solve(zs_ba_handle* h) {
     {
         PhaseScope ps(h->timer, ZS_PHASE_FACTOR, s);
         if constexpr (sizeof(T) == 4)  // the conjugate-gradient preconditioner: L and X = L^-1
-            ZS_CUDA(launch_preconditioner(P.n, W.S, (float*)W.F, (float*)W.X, (float*)W.XT, h->st,
-                                          kPreconditionerShift, W.dag_flags, &W.dag_epoch, s));
+            ZS_CUDA(launch_preconditioner(P.n, W.S, (float*)W.F, (float*)W.X, (float*)W.XT, W.tc_scratch,
+                                          W.tc_streams, h->st, kPreconditionerShift, W.dag_flags, &W.dag_epoch, s));
         else
             ZS_CUDA((launch_factor<double, T>(P.n, W.S, (T*)W.F, (T*)W.D, h->st, s)));
     }
@@ -1752,7 +1764,10 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* Lou
             ZS_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)dag_flag_ints(n), s));
             // the factor as the mixed solve forms it, without the shifted retry
             // (st->skip_factor stays 0, so the solve test applies)
-            ZS_CUDA((launch_factor_dag(n, dA, dF, dX, dXT, st, flags, &epoch, s)));
+            float* scratch = chol_tc_applies(n) ? dalloc<float>((size_t)chol_tc_scratch_floats(n), owned) : nullptr;
+            TcStreams tcs;
+            if (scratch) ZS_CUDA(tcs.init(n));
+            ZS_CUDA((launch_factor_dag(n, dA, dF, dX, dXT, scratch, scratch ? &tcs : nullptr, st, flags, &epoch, s)));
             ZS_CUDA((launch_refine<double, float>(n, dA, dX, dXT, db, dx, dwork, st, 10, 1e-14, s)));
             if (Lout) {
                 std::vector<float> tmp(nn);

@@ -16,9 +16,14 @@
 // runs without grid-wide barriers, and X follows the factor a few tiles
 // behind. Tasks are numbered column block by column block (L tiles of
 // column c, then X tiles of row c); task t belongs to CTA t mod G, which
-// takes its tasks in increasing order. Every dependency of a task has a
-// smaller number, and all CTAs are co-resident (cooperative launch), so the
-// lowest unfinished task can always proceed.
+// takes its tasks in increasing order. Up to kFuseMaxN tile columns the task
+// of L tile (c + 1, c) also factors diagonal tile c + 1 (task_LD), so the
+// chain passes one flag per column. Every dependency of a task has a smaller number, and all CTAs are
+// co-resident (cooperative launch), so the lowest unfinished task can always
+// proceed.
+//
+// The matrix may be the n x n block of a larger one (row stride ld): the
+// blocked form of ba_chol_tc.cu runs this kernel on its diagonal blocks.
 //
 // Flags hold the launch's epoch (the host advances it per launch), so they
 // need no clearing. A wait gives up after a bounded number of polls: it then
@@ -32,6 +37,7 @@
 
 #include "ba_internal.h"
 #include "ba_tile64.cuh"
+#include "ba_tiles.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -47,6 +53,7 @@ constexpr long long kSpinLimit = 1ll << 20;
 
 struct Dag {
     int n, N;
+    int ld;  // row stride of F, X and XT (the matrix may be a block of a larger one)
     float* F;
     float* X;
     float* XT;
@@ -56,7 +63,14 @@ struct Dag {
     int* abort;  // epoch once the launch has given up
     int epoch;
     int stall;   // a task whose flag is never published (failure-path tests), else -1
+    int fuse;    // task (c, 1) also factors diagonal tile c + 1 (task_LD)
 };
+
+// Up to this many tile columns the fused task of the diagonal chain pays:
+// there the chain bounds the launch. Beyond it the launch is bound by its
+// work, and the fused task's doubled sums on one CTA cost more than the
+// flag it saves (measured: n = 1200 faster fused, n >= 3000 slower).
+constexpr int kFuseMaxN = 32;
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
     int v;
@@ -71,8 +85,11 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 struct Smem {
     float a[2][kTileFloats];
     float b[2][kTileFloats];
+    float T[3 * kTile];  // the diagonal tile as three 32 x 32 tiles (ba_tiles.cuh)
     float inv[kTileFloats];
     float dinv[kP];
+    float epsr[kP];
+    int flag;
 };
 
 // Thread 0 waits for *f == epoch; false when the launch was aborted (or this
@@ -131,13 +148,13 @@ __device__ void abort_launch(const Dag& d) {
 
 __device__ __forceinline__ int tile_len(const Dag& d, int b) { return min(kP, d.n - kP * b); }
 
-// acc += sum over terms q in [0, nq) of A_q B_q^T, where term q's operand
-// tiles are (M_a rows ra_q, cols ca_q) and (M_b rows rb_q, cols cb_q), both
-// with kk_q valid columns, ready once both of its flags are published. The
-// next term's tiles are copied while the current term is multiplied when its
-// flags are already set. Returns false when the launch was aborted.
-template <typename Term>
-__device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[4][4]) {
+// mul(A_q, B_q, kk_q) for terms q in [0, nq), where term q's operand tiles
+// are (M_a rows ra_q, cols ca_q) and (M_b rows rb_q, cols cb_q), both with
+// kk_q valid columns, ready once both of its flags are published. The next
+// term's tiles are copied while the current term is multiplied when its flags
+// are already set. Returns false when the launch was aborted.
+template <typename Term, typename Mul>
+__device__ bool accumulate_with(const Dag& d, int nq, Term term, Smem& sm, Mul mul) {
     if (nq <= 0) return true;
     struct Op {
         const float* ma;
@@ -148,8 +165,8 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
         const int* fb;
     };
     auto issue = [&](const Op& o, int buf) {
-        load_block(o.ma, d.n, o.ra, o.ca, o.kk, sm.a[buf]);
-        if (o.mb != o.ma || o.rb != o.ra || o.cb != o.ca) load_block(o.mb, d.n, o.rb, o.cb, o.kk, sm.b[buf]);
+        load_block(o.ma, d.n, d.ld, o.ra, o.ca, o.kk, sm.a[buf]);
+        if (o.mb != o.ma || o.rb != o.ra || o.cb != o.ca) load_block(o.mb, d.n, d.ld, o.rb, o.cb, o.kk, sm.b[buf]);
         cp_async_commit();
     };
     Op cur;
@@ -171,7 +188,7 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
         else cp_async_wait_none();
         __syncthreads();
         const bool same = cur.mb == cur.ma && cur.rb == cur.ra && cur.cb == cur.ca;
-        tile_nt_acc(sm.a[buf], same ? sm.a[buf] : sm.b[buf], cur.kk, acc);
+        mul(sm.a[buf], same ? sm.a[buf] : sm.b[buf], cur.kk);
         __syncthreads();
         if (q + 1 < nq && !pre) {
             if (!wait_flag(d, nxt.fa) || !wait_flag(d, nxt.fb)) return false;
@@ -182,112 +199,101 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
     return true;
 }
 
-// The lower triangle of a 64 x 64 tile (diagonal included, 2080 entries,
-// packed row by row) shared out over the CTA: thread t owns entries
-// t + 256 q, q < kOwn.
-constexpr int kTri = kP * (kP + 1) / 2;
-constexpr int kOwn = (kTri + t64::kThreads - 1) / t64::kThreads;
-
-__device__ __forceinline__ void tri_entry(int e, int& i, int& j) {
-    i = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
-    while ((i + 1) * (i + 2) / 2 <= e) ++i;
-    while (i * (i + 1) / 2 > e) --i;
-    j = e - i * (i + 1) / 2;
+// acc += sum over the terms of A_q B_q^T (accumulate_with).
+template <typename Term>
+__device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[4][4]) {
+    return accumulate_with(d, nq, term, sm,
+                           [&](const float* A, const float* B, int kk) { tile_nt_acc(A, B, kk, acc); });
 }
 
-// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows;
-// rows and columns from kb on are an identity block) and inverts the factor,
-// the whole CTA working with the tile's entries in registers (kOwn per
-// thread) and one barrier per column:
-// * factor, right-looking and unscaled: at column c every entry (i, j) with
-//   j > c takes A_ij -= A_ic A_jc / A_cc, the column-c entries (final by
-//   then) read from a shared column that their owners filled at the step
-//   before; afterwards L_ij = A_ij / sqrt(A_jj). The pivot test is the
-//   reference's d > eps on A_cc;
-// * inverse, right-looking over the rows of X = L^-1: with row k of X final,
-//   every entry (i, j), i > k >= j, takes x_ij -= L_ik X_kj, and the entries
-//   of row k + 1 are final after it (X_ii = 1 / L_ii).
-// L stays in sm.a[1] (row-major; store_diag_factor writes it out), X goes
-// into X's tile (zeros above the diagonal) and its transpose into XT's.
-// Returns 0 when a pivot fails its test (uniform).
+// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows):
+// L_jj stays in sm.T (store_diag_factor writes it out), L_jj^-1 goes into
+// X's tile (zeros above the diagonal) and its transpose into XT's. Returns 0
+// when a pivot fails its test (uniform).
 __device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float eps, Smem& sm) {
-    const int n = d.n, k0 = kP * jb;
-    float* Lm = sm.a[1];
-    float* col = sm.b[0];  // two 64-float columns, alternating
-    float* Xs = sm.inv;
-    int ei[kOwn], ej[kOwn];
-    float a[kOwn];
-#pragma unroll
-    for (int q = 0; q < kOwn; ++q) {
-        const int e = threadIdx.x + t64::kThreads * q;
-        ei[q] = -1;
-        ej[q] = 0;
-        a[q] = 0.f;
-        if (e < kTri) {
-            tri_entry(e, ei[q], ej[q]);
-            const int i = ei[q], j = ej[q];
-            a[q] = (i < kb && j < kb) ? C[i * kPL + j] : (i == j ? 1.f : 0.f);
-            if (j == 0) col[i] = a[q];
-        }
+    const int ld = d.ld, k0 = kP * jb;
+    const int nbw = (kb + 31) >> 5;
+    float* T = sm.T;
+    float* Inv = sm.inv;
+    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
+        const int i = e >> 6, j = e & 63;
+        if (j > i || (i >> 5) >= nbw) continue;
+        const float v = (i < kb && j < kb) ? C[i * kPL + j] : (i == j ? 1.f : 0.f);
+        tile_at(T, i >> 5, j >> 5)[(i & 31) * kLd + (j & 31)] = v;
     }
-    for (int c = 0; c < kP; ++c) {
-        __syncthreads();
-        const float* cc = col + (c & 1) * kP;
-        float* nc = col + ((c + 1) & 1) * kP;
-        const float dc = cc[c];
-        if (c < kb && !(dc > eps)) return 0;  // every thread reads the same pivot: uniform
-        const float inv = __frcp_rn(dc);
-        if (threadIdx.x == 0) sm.dinv[c] = rsqrtf(dc);
+    if (threadIdx.x < kP) sm.epsr[threadIdx.x] = eps;
+    __syncthreads();
+    if (!cta_cholesky<float>(T, nbw, kb, sm.epsr, sm.dinv, &sm.flag)) return 0;
+    // the inverse [Xa 0; -Xc Lb Xa  Xc] from the 32 x 32 tile inverses
+    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
+        const int r = e >> 6, c = e & 63;
+        float v = 0.f;
+        if ((r >> 5) == (c >> 5) && (r >> 5) < nbw) {
+            const int b = r >> 5, rr = r & 31, cc = c & 31;
+            v = rr == cc ? sm.dinv[r] : (cc < rr ? tile_at(T, b, b)[cc * kLd + rr] : 0.f);
+        }
+        Inv[r * kPL + c] = v;
+    }
+    __syncthreads();
+    if (nbw == 2) {
+        float w[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
 #pragma unroll
-        for (int q = 0; q < kOwn; ++q) {
-            const int i = ei[q], j = ej[q];
-            if (j > c) {
-                a[q] = fmaf(-(cc[i] * inv), cc[j], a[q]);
-                if (j == c + 1) nc[i] = a[q];
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * blockDim.x;
+                w[q] = fmaf(tile_at(T, 1, 0)[(e >> 5) * kLd + m], Inv[m * kPL + (e & 31)], w[q]);
             }
         }
-    }
-    __syncthreads();
-    // L = A diag(A_jj)^-1/2 (lower), and the inverse's first row
-    float x[kOwn];
-#pragma unroll
-    for (int q = 0; q < kOwn; ++q) {
-        const int i = ei[q], j = ej[q];
-        x[q] = i == j ? 1.f : 0.f;
-        if (i >= 0) {
-            Lm[i * kPL + j] = a[q] * sm.dinv[j];
-            if (i == 0) Xs[0] = sm.dinv[0];
-        }
-    }
-    for (int k = 0; k < kP - 1; ++k) {
         __syncthreads();
 #pragma unroll
-        for (int q = 0; q < kOwn; ++q) {
-            const int i = ei[q], j = ej[q];
-            if (i > k && j <= k) x[q] = fmaf(-Lm[i * kPL + k], Xs[k * kPL + j], x[q]);
-            if (i == k + 1) Xs[i * kPL + j] = x[q] * sm.dinv[i];  // 1 / L_ii = A_ii^-1/2
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * blockDim.x;
+            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = w[q];
         }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = 0.f;
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = threadIdx.x + q * blockDim.x;
+                w[q] = fmaf(Inv[(32 + (e >> 5)) * kPL + 32 + m], Inv[(32 + m) * kPL + (e & 31)], w[q]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = threadIdx.x + q * blockDim.x;
+            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = -w[q];
+        }
+        __syncthreads();
     }
-    __syncthreads();
     // the inverse out (row-major, zeros above the diagonal) and its transpose
     // into XT: what the other tiles wait for (L_jj itself follows the flag)
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
         if (i >= kb || j >= kb) continue;
-        d.X[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? Xs[i * kPL + j] : 0.f;
-        d.XT[(int64_t)(k0 + i) * n + k0 + j] = i <= j ? Xs[j * kPL + i] : 0.f;
+        d.X[(int64_t)(k0 + i) * ld + k0 + j] = j <= i ? Inv[i * kPL + j] : 0.f;
+        d.XT[(int64_t)(k0 + i) * ld + k0 + j] = i <= j ? Inv[j * kPL + i] : 0.f;
     }
     return 1;
 }
 
-// L_jj (row-major, zeros above the diagonal) into F from sm.a[1].
+// L_jj (row-major, zeros above the diagonal) into F from the factored tiles.
 // No task reads F's diagonal tiles; the solve test after the launch does.
 __device__ void store_diag_factor(const Dag& d, int jb, int kb, const Smem& sm) {
-    const int n = d.n, k0 = kP * jb;
+    const int ld = d.ld, k0 = kP * jb;
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
         if (i >= kb || j >= kb) continue;
-        d.F[(int64_t)(k0 + i) * n + k0 + j] = j <= i ? sm.a[1][i * kPL + j] : 0.f;
+        float l = 0.f;
+        if (j <= i) {
+            const float* Tb = tile_at(sm.T, i >> 5, j >> 5);
+            l = (j == i) ? Tb[(i & 31) * (kLd + 1)] : Tb[(i & 31) * kLd + (j & 31)];
+        }
+        d.F[(int64_t)(k0 + i) * ld + k0 + j] = l;
     }
 }
 
@@ -307,11 +313,11 @@ __device__ __forceinline__ void acc_to_smem(const float acc[4][4], float* S, boo
 
 // L tile (i, j), i >= j.
 __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
-    const int n = d.n, N = d.N;
+    const int n = d.n, ld = d.ld, N = d.N;
     const int ri = tile_len(d, i), cj = tile_len(d, j);
     // the tile's S values, copied while the sums run (sm.inv is free until
     // the diagonal factor)
-    load_block(d.F, n, kP * i, kP * j, cj, sm.inv);
+    load_block(d.F, n, ld, kP * i, kP * j, cj, sm.inv);
     cp_async_commit();
     float acc[4][4];
     zero_acc(acc);
@@ -346,7 +352,7 @@ __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
     } else {
         // L_ij = C L_jj^-T: out[r][c] = sum_m C[r][m] (L_jj^-1)[c][m]
         if (!wait_flag(d, d.flagL + j * N + j)) return false;
-        load_block(d.X, n, kP * j, kP * j, cj, sm.b[0]);
+        load_block(d.X, n, ld, kP * j, kP * j, cj, sm.b[0]);
         cp_async_wait_all();
         __syncthreads();
         float out[4][4];
@@ -356,7 +362,7 @@ __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const int r = ty + 16 * a, c = tx + 16 * b;
-                if (r < ri && c < cj) d.F[(int64_t)(kP * i + r) * n + kP * j + c] = out[a][b];
+                if (r < ri && c < cj) d.F[(int64_t)(kP * i + r) * ld + kP * j + c] = out[a][b];
             }
     }
     publish(d, d.flagL + i * N + j, task);
@@ -365,9 +371,94 @@ __device__ bool task_L(const Dag& d, int i, int j, int task, Smem& sm) {
     return true;
 }
 
+// L tile (j + 1, j) and then the diagonal tile j + 1, in one task: the
+// diagonal chain's step from L_jj to L_{j+1,j+1} stays inside one CTA (one
+// flag wait and one tile load instead of two of each). The sums of both
+// tiles share their L_{j+1,k} operand tiles:
+//   C_L = S_{j+1,j} - sum_{k<j} L_{j+1,k} L_jk^T,   L_{j+1,j} = C_L L_jj^-T
+//   C_D = S_{j+1,j+1} - sum_{k<j} L_{j+1,k} L_{j+1,k}^T - L_{j+1,j} L_{j+1,j}^T
+// and C_D is factored as task_L factors a diagonal tile.
+__device__ bool task_LD(const Dag& d, int j, int task, Smem& sm) {
+    const int n = d.n, ld = d.ld, N = d.N, i = j + 1;
+    const int ri = tile_len(d, i), cj = tile_len(d, j);
+    load_block(d.F, n, ld, kP * i, kP * j, cj, sm.inv);  // S_ij, copied while the sums run
+    cp_async_commit();
+    float accL[4][4], accD[4][4];
+    zero_acc(accL);
+    zero_acc(accD);
+    const bool ok = accumulate_with(
+        d, j,
+        [&](int k, const float*& ma, int& ra, int& ca, const float*& mb, int& rb, int& cb, int& kk, const int*& fa,
+            const int*& fb) {
+            ma = d.F; ra = kP * i; ca = kP * k;
+            mb = d.F; rb = kP * j; cb = kP * k;
+            kk = tile_len(d, k);
+            fa = d.flagL + i * N + k;
+            fb = d.flagL + j * N + k;
+        },
+        sm,
+        [&](const float* A, const float* B, int kk) {
+            tile_nt_acc(A, B, kk, accL);
+            tile_nt_acc(A, A, kk, accD);
+        });
+    if (!ok) return false;
+    cp_async_wait_none();
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    // C_L into a[0]
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int r = ty + 16 * a, c = tx + 16 * b;
+            accL[a][b] = sm.inv[r * kPL + c] - accL[a][b];
+        }
+    __syncthreads();
+    acc_to_smem(accL, sm.a[0], false);
+    // S_ii into sm.inv while L_jj is awaited
+    load_block(d.F, n, ld, kP * i, kP * i, ri, sm.inv);
+    cp_async_commit();
+    if (!wait_flag(d, d.flagL + j * N + j)) return false;
+    load_block(d.X, n, ld, kP * j, kP * j, cj, sm.b[0]);
+    cp_async_wait_all();
+    __syncthreads();
+    // L_ij = C_L L_jj^-T, out to F, kept in a[1]
+    float out[4][4];
+    tile_nt(sm.a[0], sm.b[0], cj, out);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int r = ty + 16 * a, c = tx + 16 * b;
+            if (r < ri && c < cj) d.F[(int64_t)(kP * i + r) * ld + kP * j + c] = out[a][b];
+        }
+    acc_to_smem(out, sm.a[1], false);
+    publish(d, d.flagL + i * N + j, task);  // (its barrier also orders a[1])
+    // C_D = S_ii - accD - L_ij L_ij^T into a[0]
+    tile_nt(sm.a[1], sm.a[1], cj, out);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int r = ty + 16 * a, c = tx + 16 * b;
+            accD[a][b] = sm.inv[r * kPL + c] - accD[a][b] - out[a][b];
+        }
+    __syncthreads();
+    acc_to_smem(accD, sm.a[0], false);
+    __syncthreads();
+    if (!factor_diag(d, i, ri, sm.a[0], (float)__ldcg(&d.st->eps_factor), sm)) {
+        abort_launch(d);
+        return false;
+    }
+    publish(d, d.flagL + i * N + i, task);
+    store_diag_factor(d, i, ri, sm);
+    __syncthreads();
+    return true;
+}
+
 // X tile (i, j), i > j, and its transpose.
 __device__ bool task_X(const Dag& d, int i, int j, int task, Smem& sm) {
-    const int n = d.n, N = d.N;
+    const int n = d.n, ld = d.ld, N = d.N;
     float acc[4][4];
     zero_acc(acc);
     // acc = sum_{m=j}^{i-1} L_im X_mj with X_mj^T = XT tile (j, m)
@@ -385,7 +476,7 @@ __device__ bool task_X(const Dag& d, int i, int j, int task, Smem& sm) {
     // X_ij = -L_ii^-1 acc: out[r][c] = sum_t (L_ii^-1)[r][t] acc^T[c][t]
     const int ri = tile_len(d, i), cj = tile_len(d, j);
     acc_to_smem(acc, sm.b[0], true);
-    load_block(d.X, n, kP * i, kP * i, ri, sm.a[0]);
+    load_block(d.X, n, ld, kP * i, kP * i, ri, sm.a[0]);
     cp_async_wait_all();
     __syncthreads();
     float out[4][4];
@@ -397,7 +488,7 @@ __device__ bool task_X(const Dag& d, int i, int j, int task, Smem& sm) {
         for (int b = 0; b < 4; ++b) {
             const int r = ty + 16 * a, c = tx + 16 * b;
             out[a][b] = -out[a][b];
-            if (r < ri && c < cj) d.X[(int64_t)(kP * i + r) * n + kP * j + c] = out[a][b];
+            if (r < ri && c < cj) d.X[(int64_t)(kP * i + r) * ld + kP * j + c] = out[a][b];
         }
     // XT tile (j, i) = X_ij^T, staged so that its rows are written contiguously
     __syncthreads();
@@ -405,7 +496,7 @@ __device__ bool task_X(const Dag& d, int i, int j, int task, Smem& sm) {
     __syncthreads();
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int c = e >> 6, r = e & 63;
-        if (r < ri && c < cj) d.XT[(int64_t)(kP * j + c) * n + kP * i + r] = sm.a[1][c * kPL + r];
+        if (r < ri && c < cj) d.XT[(int64_t)(kP * j + c) * ld + kP * i + r] = sm.a[1][c * kPL + r];
     }
     publish(d, d.flagX + i * N + j, task);
     return true;
@@ -419,7 +510,12 @@ __global__ void __launch_bounds__(t64::kThreads, 1) k_chol_inverse_dag(Dag d) {
     const int tasks = N * N;
     for (int t = blockIdx.x; t < tasks; t += gridDim.x) {
         const int c = t / N, r = t % N;
-        const bool ok = (r < N - c) ? task_L(d, c + r, c, t, sm) : task_X(d, c, r - (N - c), t, sm);
+        bool ok = true;
+        if (r >= N - c) ok = task_X(d, c, r - (N - c), t, sm);
+        else if (!d.fuse) ok = task_L(d, c + r, c, t, sm);
+        else if (r == 1) ok = task_LD(d, c, t, sm);     // L_{c+1,c} and L_{c+1,c+1}
+        else if (r > 1 || c == 0) ok = task_L(d, c + r, c, t, sm);
+        // (fused, r == 0, c > 0: the diagonal tile c came with task (c - 1, 1))
         if (!ok) return;
     }
 }
@@ -438,6 +534,11 @@ int dag_flag_ints(int n) {
 
 cudaError_t launch_chol_inverse_dag(int n, float* F, float* X, float* XT, LmState* st, int* flags, int* epoch,
                                     cudaStream_t s) {
+    return launch_chol_inverse_dag_ld(n, n, F, X, XT, st, flags, epoch, s);
+}
+
+cudaError_t launch_chol_inverse_dag_ld(int n, int ld, float* F, float* X, float* XT, LmState* st, int* flags,
+                                       int* epoch, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     static const int stall = stall_task_from_env();
     int dev = 0, sms = 0, per_sm = 0;
@@ -454,6 +555,7 @@ cudaError_t launch_chol_inverse_dag(int n, float* F, float* X, float* XT, LmStat
     if (blocks > N * N) blocks = N * N;
     Dag d;
     d.n = n;
+    d.ld = ld;
     d.N = N;
     d.F = F;
     d.X = X;
@@ -464,6 +566,7 @@ cudaError_t launch_chol_inverse_dag(int n, float* F, float* X, float* XT, LmStat
     d.abort = flags + 2 * N * N;
     d.epoch = ++*epoch;
     d.stall = stall;
+    d.fuse = N <= kFuseMaxN;
     void* args[] = {(void*)&d};
     e = cudaLaunchCooperativeKernel((const void*)k_chol_inverse_dag, dim3(blocks), dim3(t64::kThreads), args, smem,
                                     s);

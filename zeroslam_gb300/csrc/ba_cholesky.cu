@@ -527,27 +527,48 @@ __global__ void __launch_bounds__(kThreads) k_convert_shift(int n, const double*
     }
 }
 
-cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, LmState* st, int* flags,
-                              int* epoch, cudaStream_t s) {
+static cudaError_t launch_chol_inverse(int n, float* F, float* X, float* XT, float* scratch, TcStreams* ts,
+                                       LmState* st, int* flags, int* epoch, cudaStream_t s) {
+    if (scratch && ts && chol_tc_applies(n) && tc_gemm_supported(n, n, F, X))
+        return launch_chol_inverse_tc(n, F, X, XT, scratch, st, flags, epoch, *ts, s);
+    return launch_chol_inverse_dag(n, F, X, XT, st, flags, epoch, s);
+}
+
+cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, float* scratch, TcStreams* ts,
+                              LmState* st, int* flags, int* epoch, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int64_t nn = (int64_t)n * n;
     k_diag_max<double><<<1, kThreads, 0, s>>>(n, S, st, 1e-14, 0); note_launch();
     k_convert<double, float><<<grid_for(nn), kThreads, 0, s>>>(nn, S, F); note_launch();
-    cudaError_t e = launch_chol_inverse_dag(n, F, X, XT, st, flags, epoch, s);
+    cudaError_t e = launch_chol_inverse(n, F, X, XT, scratch, ts, st, flags, epoch, s);
     if (e != cudaSuccess) return e;
     k_check_solve_eps<float><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, LmState* st, double mu,
-                                  int* flags, int* epoch, cudaStream_t s) {
+cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, float* scratch,
+                                  TcStreams* ts, LmState* st, double mu, int* flags, int* epoch, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int64_t nn = (int64_t)n * n;
-    cudaError_t e = launch_factor_dag(n, S, F, X, XT, st, flags, epoch, s);
+    cudaError_t e = launch_factor_dag(n, S, F, X, XT, scratch, ts, st, flags, epoch, s);
     if (e != cudaSuccess) return e;
     k_retry_arm<<<1, 32, 0, s>>>(st); note_launch();
+    if (scratch && ts && chol_tc_applies(n)) {
+        // The blocked form's retry would be some 200 launches that return at
+        // once; the host reads the arm flag instead (one synchronisation,
+        // against milliseconds of factorisation) and launches the retry only
+        // when it is armed.
+        int32_t armed = 0;
+        if ((e = cudaMemcpyAsync(&armed, &st->shifted, sizeof(armed), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(s)) != cudaSuccess)
+            return e;
+        if (!armed) {
+            k_retry_disarm<<<1, 32, 0, s>>>(st); note_launch();
+            return cudaGetLastError();
+        }
+    }
     k_convert_shift<<<std::min<int64_t>(grid_for(nn), 4096), kThreads, 0, s>>>(n, S, F, mu, st); note_launch();
-    e = launch_chol_inverse_dag(n, F, X, XT, st, flags, epoch, s);
+    e = launch_chol_inverse(n, F, X, XT, scratch, ts, st, flags, epoch, s);
     if (e != cudaSuccess) return e;
     k_check_solve_eps<float><<<1, kThreads, 0, s>>>(n, F, st); note_launch();
     k_retry_disarm<<<1, 32, 0, s>>>(st); note_launch();

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "ba_common.cuh"
 
 namespace zs {
@@ -95,6 +97,8 @@ static_assert(sizeof(ObsJac) == 112, "ObsJac is seven 16-byte vectors");
 
 // Working arrays of one precision (T = double for the plain form, float for
 // the mixed form).
+struct TcStreams;
+
 struct DevWork {
     void* hpl = nullptr;       // [M*RS] T, RS = 18 (double) or 20 (float, padded); pose-major positions
     void* W = nullptr;         // [M*RS] T, pose-major positions
@@ -119,6 +123,8 @@ struct DevWork {
     void* XT = nullptr;        // mixed form: [n*n] (L^-1)^T (upper)
     int* dag_flags = nullptr;  // mixed form: [dag_flag_ints(n)] tile flags of the preconditioner's launch
     int dag_epoch = 0;         // mixed form: epoch of its last launch (host side)
+    float* tc_scratch = nullptr;  // mixed form at large n: panels of the blocked preconditioner
+    TcStreams* tc_streams = nullptr;  // and its streams (owned by the handle)
     double* delta = nullptr;   // [n + 3L]
     double* red = nullptr;     // [kReduceBlocks * 4] reduction partials
     int32_t* ired = nullptr;   // [kReduceBlocks]
@@ -357,26 +363,55 @@ cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double*
 int dag_flag_ints(int n);
 cudaError_t launch_chol_inverse_dag(int n, float* F, float* X, float* XT, LmState* st, int* flags, int* epoch,
                                     cudaStream_t s);
-// eps from S's diagonal, F = S in FP32, the factor and inverse, and the
-// reference's solve test on L's diagonal.
-cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, LmState* st, int* flags,
-                              int* epoch, cudaStream_t s);
+// The same for the n x n block at F, X, XT of matrices with row stride ld.
+cudaError_t launch_chol_inverse_dag_ld(int n, int ld, float* F, float* X, float* XT, LmState* st, int* flags,
+                                       int* epoch, cudaStream_t s);
+// Blocked form for large n (ba_chol_tc.cu): panels of kPanel columns, the
+// diagonal blocks by the dataflow kernel and the rest on the tensor cores.
+// It applies from kTcMinN on with n % 4 == 0; scratch holds
+// chol_tc_scratch_floats(n) floats (16-byte aligned).
+constexpr int kPanel = 256;
+constexpr int kTcMinN = 3072;
+bool chol_tc_applies(int n);
+int chol_tc_scratch_floats(int n);
+// The blocked form's streams (high priority: the factorisation's chain and
+// the work beside it; low: the bulk of the products) and its events, for
+// matrices up to n.
+struct TcStreams {
+    cudaStream_t hi = nullptr, mid = nullptr, lo = nullptr;
+    std::vector<cudaEvent_t> ev;
+    cudaError_t init(int n);
+    void release();
+    static int panels_of(int n);
+    ~TcStreams();
+};
+// Enqueued after everything before it on s; s waits for all of it.
+cudaError_t launch_chol_inverse_tc(int n, float* F, float* X, float* XT, float* scratch, LmState* st, int* flags,
+                                   int* epoch, TcStreams& ts, cudaStream_t s);
+// eps from S's diagonal, F = S in FP32, the factor and inverse (blocked when
+// scratch and ts are given and chol_tc_applies(n), else the dataflow kernel
+// alone),
+// and the reference's solve test on L's diagonal.
+cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float* XT, float* scratch, TcStreams* ts,
+                              LmState* st, int* flags, int* epoch, cudaStream_t s);
 // The whole preconditioner of an attempt: eps from S's diagonal, F = S in
 // FP32, the factor and inverse; when that fails, once more on
 // S + mu diag(S) (st->shifted); then the reference's solve test on L's
 // diagonal (source/matrix_decomposition_cholesky.hpp:74,80,89).
-cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, LmState* st, double mu,
-                                  int* flags, int* epoch, cudaStream_t s);
+cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, float* scratch,
+                                  TcStreams* ts, LmState* st, double mu, int* flags, int* epoch, cudaStream_t s);
 
 // ---- FP32 products on the tensor cores (ba_tc_gemm.cu) ----
 // C (M x N, row stride ldc) = alpha A B^T + beta C, A (M x K) and B (N x K)
 // row-major with K contiguous, three TF32 products per operand pair (FP32
 // accuracy). Needs lda, ldb multiples of 4 and 16-byte aligned A, B
 // (tc_gemm_supported). lower: only C's lower triangle (col <= row) is
-// written. A wait that runs out sets *err = 1 (device int).
+// written. A wait that runs out sets *err = 1 (device int). With st, the
+// launch returns at once when st->skip_factor is set or st->solve_ok clear,
+// and a wait that runs out also clears st->solve_ok.
 bool tc_gemm_supported(int lda, int ldb, const float* A, const float* B);
 cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                              float alpha, float beta, bool lower, int* err, cudaStream_t s);
+                              float alpha, float beta, bool lower, int* err, cudaStream_t s, LmState* st = nullptr);
 
 // ---- mixed form (ba_inverse.cu) ----
 // Dense mixed solves (zs_dense_cholesky_solve): x = X^T X bs, then FP64

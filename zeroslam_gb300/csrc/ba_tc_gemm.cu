@@ -59,6 +59,7 @@ struct TcArgs {
     float alpha, beta;
     int lower;  // write only C's lower triangle (col <= row); tiles above it are skipped
     int* err;
+    LmState* st;  // optional: return at once when the factorisation is skipped or has failed
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
 
     const int row0 = blockIdx.y * kBM, col0 = blockIdx.x * kBN;
     if (g.lower && col0 > row0 + kBM - 1) return;  // a tile above the diagonal (uniform, before any setup)
+    if (g.st && (__ldcg(&g.st->skip_factor) || !__ldcg(&g.st->solve_ok))) return;  // written by earlier launches
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nk = (g.K + kBK - 1) / kBK;
 
@@ -331,27 +333,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
         if (!*s_err && !drain_chunk(nch - 1, tmem, chunk_done, drained, warp, lane, g.err)) *s_err = 1;
         if (mbar_wait(done, 0, g.err) && !*s_err) {
             tc_fence_after();
+            // Every product has completed, so no copy or product touches the
+            // operand boxes any more: each warp stages its 32 x 32 blocks in
+            // a_hi (33-float rows, conflict-free both ways) and writes C a
+            // row at a time, 32 consecutive columns per warp instruction.
             const int q = warp & 3;  // this warp's 32-lane quarter of tensor memory
-            const int row = row0 + 32 * q + lane;
             const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+            float* stage = a_hi + q * 32 * 33;
 #pragma unroll 1
             for (int c = 0; c < kBN / 32; ++c) {
                 float v[32], w[32];
                 tmem_ld32(lane_base + kColSum + 32 * c, v);
                 tmem_ld32(lane_base + kColCorr + 32 * c, w);
 #pragma unroll
-                for (int j = 0; j < 32; ++j) v[j] += w[j];
-                if (row < g.M) {
-                    float* crow = g.C + (int64_t)row * g.ldc;
+                for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = v[j] + w[j];
+                __syncwarp();
+                const int col = col0 + 32 * c + lane;
+                // the 32 old values first, all loads in flight together
+                float old[32];
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int col = col0 + 32 * c + j;
-                        if (col < g.N && (!g.lower || col <= row)) {
-                            const float old = g.beta != 0.f ? crow[col] : 0.f;
-                            crow[col] = g.alpha * v[j] + g.beta * old;
-                        }
-                    }
+                for (int r = 0; r < 32; ++r) {
+                    const int row = row0 + 32 * q + r;
+                    old[r] = (g.beta != 0.f && row < g.M && col < g.N && (!g.lower || col <= row))
+                                 ? __ldcg(g.C + (int64_t)row * g.ldc + col)
+                                 : 0.f;
                 }
+#pragma unroll
+                for (int r = 0; r < 32; ++r) {
+                    const int row = row0 + 32 * q + r;
+                    if (row < g.M && col < g.N && (!g.lower || col <= row))
+                        g.C[(int64_t)row * g.ldc + col] = g.alpha * stage[r * 33 + lane] + g.beta * old[r];
+                }
+                __syncwarp();
             }
         }
     }
@@ -362,6 +375,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
             mbar_wait(full + kb % kStages, (kb / kStages) & 1, g.err);
     }
     if (warp == 1 && lane == 0 && *s_err) mbar_wait(done, 0, g.err);
+    if (threadIdx.x == 0 && *s_err && g.st) g.st->solve_ok = 0;
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
@@ -407,14 +421,14 @@ bool tc_gemm_supported(int lda, int ldb, const float* A, const float* B) {
 }
 
 cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                              float alpha, float beta, bool lower, int* err, cudaStream_t s) {
+                              float alpha, float beta, bool lower, int* err, cudaStream_t s, LmState* st) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     if (K <= 0 || !tc_gemm_supported(lda, ldb, A, B)) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     if (!make_map(&ta, A, M, K, lda) || !make_map(&tb, B, N, K, ldb)) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
     if (e != cudaSuccess) return e;
-    TcArgs g{M, N, K, C, ldc, alpha, beta, lower ? 1 : 0, err};
+    TcArgs g{M, N, K, C, ldc, alpha, beta, lower ? 1 : 0, err, st};
     const dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
     k_tc_gemm_nt<<<grid, kTcThreads, kTcSmem, s>>>(ta, tb, g);
     note_launch();

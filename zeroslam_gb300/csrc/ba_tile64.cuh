@@ -67,13 +67,13 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 // Rows r0 .. r0 + 64 (clipped to n), columns c0 .. c0 + kk of the row-major
-// n x n matrix M into S[row][m] (zero outside). With n % 4 == 0 (16-byte
-// rows) and c0 % 4 == 0: 16-byte asynchronous copies, four per thread, all in
-// flight together; the caller commits / waits and synchronises before
-// reading S. Otherwise plain L2 loads, complete on return (after the
-// caller's barrier).
-__device__ __forceinline__ void load_block(const float* M, int n, int r0, int c0, int kk, float* S) {
-    if ((n & 3) == 0) {
+// matrix M (row stride ld) into S[row][m] (zero outside). With ld % 4 == 0
+// (16-byte rows), c0 % 4 == 0 and M 16-byte aligned: 16-byte asynchronous
+// copies, four per thread, all in flight together; the caller commits / waits
+// and synchronises before reading S. Otherwise plain L2 loads, complete on
+// return (after the caller's barrier).
+__device__ __forceinline__ void load_block(const float* M, int n, int ld, int r0, int c0, int kk, float* S) {
+    if ((ld & 3) == 0) {
 #pragma unroll
         for (int q = 0; q < (kP * kP / 4) / kThreads; ++q) {
             const int e = threadIdx.x + q * kThreads;
@@ -81,7 +81,7 @@ __device__ __forceinline__ void load_block(const float* M, int n, int r0, int c0
             const int row = r0 + r;
             int bytes = (row < n) ? 4 * min(4, kk - c4) : 0;
             if (bytes < 0) bytes = 0;
-            const float* src = bytes > 0 ? M + (int64_t)row * n + c0 + c4 : M;
+            const float* src = bytes > 0 ? M + (int64_t)row * ld + c0 + c4 : M;
             cp_async16(S + r * kPL + c4, src, bytes);
         }
     } else {
@@ -90,7 +90,7 @@ __device__ __forceinline__ void load_block(const float* M, int n, int r0, int c0
         for (int q = 0; q < (kP * kP) / kThreads; ++q) {
             const int e = threadIdx.x + q * kThreads;
             const int r = e >> 6, m = e & 63;
-            v[q] = (r0 + r < n && m < kk) ? ldcg(M + (int64_t)(r0 + r) * n + c0 + m) : 0.f;
+            v[q] = (r0 + r < n && m < kk) ? ldcg(M + (int64_t)(r0 + r) * ld + c0 + m) : 0.f;
         }
 #pragma unroll
         for (int q = 0; q < (kP * kP) / kThreads; ++q) {
@@ -98,6 +98,11 @@ __device__ __forceinline__ void load_block(const float* M, int n, int r0, int c0
             S[(e >> 6) * kPL + (e & 63)] = v[q];
         }
     }
+}
+
+// The square case: an n x n matrix with row stride n.
+__device__ __forceinline__ void load_block(const float* M, int n, int r0, int c0, int kk, float* S) {
+    load_block(M, n, n, r0, c0, kk, S);
 }
 
 }  // namespace t64
