@@ -451,15 +451,18 @@ int zs_dense_cholesky_solve(const double* A, int n, const double* b, double* L, 
  * names it). */
 int zs_dense_cholesky_solve_noalloc(const double* A, int n, const double* b, double* L, double* x);
 
-/* C = A B^T (or only its lower triangle, col <= row, with lower != 0) for
- * row-major FP32 host arrays A (M x K), B (N x K), C (M x N) on the current
- * device's tensor cores with FP32 accuracy (three TF32 products per operand
- * pair, FP32 accumulation): the product the mixed form's dense preconditioner
- * uses for large reduced systems. *ms (may be NULL) receives the kernel's
- * device time. No reference counterpart: a test and measurement utility.
- * Returns ZS_OK, ZS_ERR_INVALID, ZS_ERR_TIMEOUT (a bounded wait inside the
- * kernel ran out) or a CUDA status. */
-int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C, int M, int N, int K, int lower, double* ms);
+/* C = A B^T (or only its lower triangle, col <= row, with lower != 0 and
+ * M >= N) for row-major FP32 host arrays A (M x K), B (N x K), C (M x N) on
+ * the current device's tensor cores with FP32 accuracy (three TF32 products
+ * per operand pair, FP32 accumulation): the product the mixed form's dense
+ * preconditioner uses for large reduced systems. max_ctas > 0 caps the grid
+ * (each CTA then walks several 128 x 128 tiles of C); 0: a CTA per tile.
+ * *ms (may be NULL) receives the kernel's device time. No reference
+ * counterpart: a test and measurement utility. Returns ZS_OK,
+ * ZS_ERR_INVALID, ZS_ERR_TIMEOUT (a bounded wait inside the kernel ran out)
+ * or a CUDA status. */
+int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C, int M, int N, int K, int lower, int max_ctas,
+                            double* ms);
 
 /* The mixed form's FP32 preconditioner on a row-major n x n host matrix S:
  * the factor S = L L^T and X = L^-1 (both lower triangular; the upper

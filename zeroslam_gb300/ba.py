@@ -198,7 +198,7 @@ def load(path: str | None = None) -> C.CDLL:
     lib.zs_dense_cholesky_solve_noalloc.restype = C.c_int
     lib.zs_dense_cholesky_solve_noalloc.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
     lib.zs_dense_gemm_nt_tf32x3.restype = C.c_int
-    lib.zs_dense_gemm_nt_tf32x3.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
+    lib.zs_dense_gemm_nt_tf32x3.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
     lib.zs_dense_chol_inverse_f32.restype = C.c_int
     lib.zs_dense_chol_inverse_f32.argtypes = [_fp, C.c_int, _fp, _fp, C.c_int, _dp]
     lib.zs_map_cull.restype = C.c_int
@@ -627,8 +627,9 @@ def dense_cholesky_status(A, b, precision: int = FP64) -> int:
     return int(lib.zs_dense_cholesky_solve(_p(A, _dp), A.shape[0], _p(b, _dp), None, _p(x, _dp), int(precision)))
 
 
-def dense_gemm_tf32x3(A, B, lower: bool = False):
-    """(A B^T on the tensor cores with FP32 accuracy, the kernel's device ms)."""
+def dense_gemm_tf32x3(A, B, lower: bool = False, max_ctas: int = 0):
+    """(A B^T on the tensor cores with FP32 accuracy, the kernel's device ms);
+    max_ctas > 0 caps the grid (each CTA walks several tiles)."""
     lib = load()
     A = np.ascontiguousarray(A, dtype=np.float32)
     B = np.ascontiguousarray(B, dtype=np.float32)
@@ -638,7 +639,8 @@ def dense_gemm_tf32x3(A, B, lower: bool = False):
         raise ValueError("A and B need the same number of columns")
     out = np.zeros((M, N), dtype=np.float32)
     ms = C.c_double()
-    st = lib.zs_dense_gemm_nt_tf32x3(_p(A, _fp), _p(B, _fp), _p(out, _fp), M, N, K, int(bool(lower)), C.byref(ms))
+    st = lib.zs_dense_gemm_nt_tf32x3(_p(A, _fp), _p(B, _fp), _p(out, _fp), M, N, K, int(bool(lower)), int(max_ctas),
+                                     C.byref(ms))
     if st != ZS_OK:
         raise ZsError(st, "zs_dense_gemm_nt_tf32x3")
     return out, ms.value

@@ -42,6 +42,7 @@
 #include <algorithm>
 
 #include "ba_internal.h"
+#include "ba_tile64.cuh"
 
 namespace zs {
 
@@ -95,9 +96,75 @@ __global__ void __launch_bounds__(256) k_copy_block(int rows, int cols, const fl
     }
 }
 
+// C (M x N) = alpha A B^T + beta C on the FP32 pipe, a CTA per 64 x 64 tile
+// of C (lower: tiles above the diagonal skipped, entries above it kept), K in
+// chunks of 64 double-buffered through shared memory by 16-byte
+// asynchronous copies: the small products on the blocked form's chain
+// (256 x 256 x 256), where a tensor-core tile's fixed costs (tensor-memory
+// allocation, the pipeline's fill, the promotion of its partial sums) exceed
+// the arithmetic. A, B 16-byte aligned with lda, ldb multiples of 4.
+constexpr size_t kGemm64Smem = 4 * sizeof(float) * t64::kTileFloats;
+
+__global__ void __launch_bounds__(t64::kThreads) k_gemm_nt64(int M, int N, int K, const float* __restrict__ A, int lda,
+                                                             const float* __restrict__ B, int ldb, float* C, int ldc,
+                                                             float alpha, float beta, int lower, const LmState* st) {
+    extern __shared__ __align__(16) float g64[];
+    if (__ldcg(&st->skip_factor) || !__ldcg(&st->solve_ok)) return;
+    const int row0 = blockIdx.y * t64::kP, col0 = blockIdx.x * t64::kP;
+    if (lower && col0 > row0 + t64::kP - 1) return;
+    float* sa[2] = {g64, g64 + t64::kTileFloats};
+    float* sb[2] = {g64 + 2 * t64::kTileFloats, g64 + 3 * t64::kTileFloats};
+    float acc[4][4];
+    t64::zero_acc(acc);
+    const int nk = (K + t64::kP - 1) / t64::kP;
+    auto issue = [&](int q, int buf) {
+        const int kk = min(t64::kP, K - q * t64::kP);
+        t64::load_block(A, M, lda, row0, q * t64::kP, kk, sa[buf]);
+        t64::load_block(B, N, ldb, col0, q * t64::kP, kk, sb[buf]);
+        t64::cp_async_commit();
+    };
+    issue(0, 0);
+    for (int q = 0; q < nk; ++q) {
+        const int buf = q & 1;
+        if (q + 1 < nk) {
+            issue(q + 1, buf ^ 1);
+            t64::cp_async_wait_one();
+        } else {
+            t64::cp_async_wait_none();
+        }
+        __syncthreads();
+        t64::tile_nt_acc(sa[buf], sb[buf], min(t64::kP, K - q * t64::kP), acc);
+        __syncthreads();
+    }
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int r = row0 + ty + 16 * a, c = col0 + tx + 16 * b;
+            if (r < M && c < N && (!lower || c <= r)) {
+                float* cp = C + (int64_t)r * ldc + c;
+                *cp = alpha * acc[a][b] + (beta != 0.f ? beta * *cp : 0.f);
+            }
+        }
+}
+
 unsigned grid_of(int64_t items) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((items + 255) / 256, 4096)); }
 
 }  // namespace
+
+cudaError_t launch_gemm_nt64(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                             float alpha, float beta, bool lower, const LmState* st, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return cudaSuccess;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_gemm_nt64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemm64Smem);
+    if (attr != cudaSuccess) return attr;
+    const dim3 grid((N + t64::kP - 1) / t64::kP, (M + t64::kP - 1) / t64::kP);
+    k_gemm_nt64<<<grid, t64::kThreads, kGemm64Smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta, lower ? 1 : 0,
+                                                          st);
+    note_launch();
+    return cudaGetLastError();
+}
 
 int chol_tc_scratch_floats(int n) { return 3 * n * kPanel; }
 
@@ -144,6 +211,12 @@ cudaError_t launch_chol_inverse_tc(int n, float* F, float* X, float* XT, float* 
     cudaEvent_t fork = G[panels], join = G[panels + 1];
     cudaStream_t hi = ts.hi, mid = ts.mid, lo = ts.lo;
     int* err = &st->timeout;
+    // the bulk stream's products leave 16 SMs to the dataflow launches of the
+    // chain (measured at n = 6000: 4.46 ms against 4.80 with no cap)
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int lo_cap = sms > 32 ? sms - 16 : 0;
     cudaError_t e;
 #define ZS_TRY(x)                               \
     do {                                        \
@@ -171,16 +244,17 @@ cudaError_t launch_chol_inverse_tc(int n, float* F, float* X, float* XT, float* 
         float* P = Pb[k & 1];
         float* F22 = F + (size_t)(o + b) * n + o + b;  // the trailing block
         // hi, the chain: the diagonal block, the top rows of P = S_21 X_kk^T
-        // (L_21's rows of the next panel) and the next diagonal block's update
+        // (L_21's rows of the next panel) and the next diagonal block's
+        // update, the last two as FP32-pipe tiles (k_gemm_nt64)
         ZS_TRY(launch_chol_inverse_dag_ld(b, n, Fkk, Xkk, XT + (size_t)o * n + o, st, flags, epoch, hi));
         if (m > 0) {
             if (k >= 2) ZS_TRY(cudaStreamWaitEvent(hi, G[k - 2], 0));  // P[k & 1] is free
             if (k >= 1) ZS_TRY(cudaStreamWaitEvent(hi, M[k - 1], 0));  // S_21 is final
-            ZS_TRY(launch_tc_gemm_nt(bn, b, b, S21, n, Xkk, n, P, kPanel, 1.f, 0.f, false, err, hi, st));
+            ZS_TRY(launch_gemm_nt64(bn, b, b, S21, n, Xkk, n, P, kPanel, 1.f, 0.f, false, st, hi));
             k_copy_block<<<grid_of((int64_t)bn * b / 4), 256, 0, hi>>>(bn, b, P, kPanel, S21, n, st);
             note_launch();
             if (k >= 2) ZS_TRY(cudaStreamWaitEvent(hi, R[k - 2], 0));
-            ZS_TRY(launch_tc_gemm_nt(bn, bn, b, P, kPanel, P, kPanel, F22, n, -1.f, 1.f, true, err, hi, st));
+            ZS_TRY(launch_gemm_nt64(bn, bn, b, P, kPanel, P, kPanel, F22, n, -1.f, 1.f, true, st, hi));
         }
         ZS_TRY(cudaEventRecord(E[k], hi));
         // mid, beside the next dataflow launch: the rest of P, the next
@@ -207,17 +281,18 @@ cudaError_t launch_chol_inverse_tc(int n, float* F, float* X, float* XT, float* 
         if (r2 > 0) {
             float* Pz = P + (size_t)(bn + bn2) * kPanel;
             ZS_TRY(launch_tc_gemm_nt(r2, r2, b, Pz, kPanel, Pz, kPanel, F22 + (size_t)(bn + bn2) * (n + 1), n, -1.f,
-                                     1.f, true, err, lo, st));
+                                     1.f, true, err, lo, st, lo_cap));
         }
         ZS_TRY(cudaEventRecord(R[k], lo));
         if (o > 0) {
             // Q = Y^T[0:o, k] X_kk^T, then into XT
-            ZS_TRY(launch_tc_gemm_nt(o, b, b, XT + o, n, Xkk, n, Q, kPanel, 1.f, 0.f, false, err, lo, st));
+            ZS_TRY(launch_tc_gemm_nt(o, b, b, XT + o, n, Xkk, n, Q, kPanel, 1.f, 0.f, false, err, lo, st, lo_cap));
             k_copy_block<<<grid_of((int64_t)o * b / 4), 256, 0, lo>>>(o, b, Q, kPanel, XT + o, n, st);
             note_launch();
         }
         if (m > 0)  // Y^T[0:o+b, o+b:n] -= XT[0:o+b, k] P^T
-            ZS_TRY(launch_tc_gemm_nt(o + b, m, b, XT + o, n, P, kPanel, XT + o + b, n, -1.f, 1.f, false, err, lo, st));
+            ZS_TRY(launch_tc_gemm_nt(o + b, m, b, XT + o, n, P, kPanel, XT + o + b, n, -1.f, 1.f, false, err, lo, st,
+                                     lo_cap));
         ZS_TRY(cudaEventRecord(G[k], lo));
     }
     ZS_TRY(cudaStreamWaitEvent(hi, G[panels - 1], 0));

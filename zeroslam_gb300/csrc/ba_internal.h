@@ -363,6 +363,12 @@ cudaError_t launch_reduced_solve(int n, const TS* S, TF* F, TF* D, const double*
 int dag_flag_ints(int n);
 cudaError_t launch_chol_inverse_dag(int n, float* F, float* X, float* XT, LmState* st, int* flags, int* epoch,
                                     cudaStream_t s);
+// C (M x N) = alpha A B^T + beta C on the FP32 pipe in 64 x 64 tiles (small
+// products; lower: only C's lower triangle); returns at once when
+// st->skip_factor is set or st->solve_ok clear. A, B 16-byte aligned, lda,
+// ldb multiples of 4.
+cudaError_t launch_gemm_nt64(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                             float alpha, float beta, bool lower, const LmState* st, cudaStream_t s);
 // The same for the n x n block at F, X, XT of matrices with row stride ld.
 cudaError_t launch_chol_inverse_dag_ld(int n, int ld, float* F, float* X, float* XT, LmState* st, int* flags,
                                        int* epoch, cudaStream_t s);
@@ -406,12 +412,15 @@ cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, fl
 // row-major with K contiguous, three TF32 products per operand pair (FP32
 // accuracy). Needs lda, ldb multiples of 4 and 16-byte aligned A, B
 // (tc_gemm_supported). lower: only C's lower triangle (col <= row) is
-// written. A wait that runs out sets *err = 1 (device int). With st, the
-// launch returns at once when st->skip_factor is set or st->solve_ok clear,
-// and a wait that runs out also clears st->solve_ok.
+// written (C square or taller than wide). A wait that runs out sets *err = 1
+// (device int). With st, the launch returns at once when st->skip_factor is
+// set or st->solve_ok clear, and a wait that runs out also clears
+// st->solve_ok. max_ctas > 0 caps the grid (each CTA walks several tiles),
+// leaving the other SMs to concurrent streams.
 bool tc_gemm_supported(int lda, int ldb, const float* A, const float* B);
 cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                              float alpha, float beta, bool lower, int* err, cudaStream_t s, LmState* st = nullptr);
+                              float alpha, float beta, bool lower, int* err, cudaStream_t s, LmState* st = nullptr,
+                              int max_ctas = 0);
 
 // ---- mixed form (ba_inverse.cu) ----
 // Dense mixed solves (zs_dense_cholesky_solve): x = X^T X bs, then FP64

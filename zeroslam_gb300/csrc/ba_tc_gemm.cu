@@ -7,8 +7,11 @@
 // low bits of the lo parts, about 2^-21 relative per product).
 //
 // A (M x K) and B (N x K) are row-major with K contiguous ("K-major"), row
-// strides lda, ldb multiples of 4 floats, bases 16-byte aligned. Per CTA one
-// 128 x 128 tile of C:
+// strides lda, ldb multiples of 4 floats, bases 16-byte aligned. A CTA walks
+// 128 x 128 tiles of C (tile blockIdx.x, then every gridDim.x-th; with a grid
+// capped below the SM count the rest of the GPU stays free for other
+// streams), keeping its tensor memory and its ring of stages from tile to
+// tile. Per tile:
 //   warp 0      TMA producer: 128 x 32 FP32 boxes of A and B per K step
 //               (cp.async.bulk.tensor, 128-byte swizzle) into a 3-stage ring;
 //   warps 2..5  split each landed box into hi (in place) and lo (a second
@@ -50,7 +53,8 @@ constexpr uint32_t kBoxBytes = kBoxFloats * 4;
 constexpr long long kWaitLimit = 1ll << 24;         // polls of one mbarrier phase (well over a second)
 constexpr int kChunkKb = 4;                          // K steps per promoted chunk
 constexpr uint32_t kColCorr = 256, kColSum = 384, kTmemCols = 512;
-constexpr size_t kTcSmem = 4ull * kStages * kBoxBytes + 256 + 1024;  // boxes, barriers, alignment slack
+constexpr uint32_t kStageFloats = 4 * 32 * 33;       // the epilogue's staging blocks
+constexpr size_t kTcSmem = 4ull * kStages * kBoxBytes + 4ull * kStageFloats + 256 + 1024;  // + barriers, alignment
 
 struct TcArgs {
     int M, N, K;
@@ -170,11 +174,12 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float v[32]) {
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-// Warps 2..5: chunk ch's accumulator (columns 128 (ch & 1)) into the sum
-// (columns [384, 512)) in FP32, this warp's 32 lanes, then one arrival per
-// thread on drained[ch & 1]. The first chunk is copied.
-__device__ bool drain_chunk(int ch, uint32_t tmem, uint64_t* chunk_done, uint64_t* drained, int warp, int lane,
-                            int* err) {
+// Warps 2..5: chunk ch's accumulator (columns 128 (ch & 1); ch counts the
+// CTA's chunks over all its tiles) into the sum (columns [384, 512)) in FP32,
+// this warp's 32 lanes, then one arrival per thread on drained[ch & 1]. A
+// tile's first chunk is copied.
+__device__ bool drain_chunk(int ch, bool first, uint32_t tmem, uint64_t* chunk_done, uint64_t* drained, int warp,
+                            int lane, int* err) {
     const int b = ch & 1;
     if (!mbar_wait(chunk_done + b, (ch >> 1) & 1, err)) return false;
     tc_fence_after();
@@ -183,7 +188,7 @@ __device__ bool drain_chunk(int ch, uint32_t tmem, uint64_t* chunk_done, uint64_
     for (int c = 0; c < kBN / 32; ++c) {
         float v[32], acc[32];
         tmem_ld32(lane_base + 128u * b + 32 * c, v);
-        if (ch > 0) {
+        if (!first) {
             tmem_ld32(lane_base + kColSum + 32 * c, acc);
 #pragma unroll
             for (int j = 0; j < 32; ++j) v[j] += acc[j];
@@ -196,6 +201,32 @@ __device__ bool drain_chunk(int ch, uint32_t tmem, uint64_t* chunk_done, uint64_
     return true;
 }
 
+// Tile idx of C in the launch's order (row-major over tile rows); with
+// lower, only tiles on or below the diagonal (tile column <= tile row) are
+// counted (C square or taller than wide).
+__device__ __forceinline__ void tile_coords(int idx, int ntn, bool lower, int& ti, int& tj) {
+    if (!lower) {
+        ti = idx / ntn;
+        tj = idx - ti * ntn;
+        return;
+    }
+    const int tri = ntn * (ntn + 1) / 2;
+    if (idx < tri) {
+        ti = (int)((sqrtf(8.f * (float)idx + 1.f) - 1.f) * 0.5f);
+        while ((ti + 1) * (ti + 2) / 2 <= idx) ++ti;
+        while (ti * (ti + 1) / 2 > idx) --ti;
+        tj = idx - ti * (ti + 1) / 2;
+    } else {
+        ti = ntn + (idx - tri) / ntn;
+        tj = (idx - tri) % ntn;
+    }
+}
+
+__device__ __forceinline__ int tile_count(int ntm, int ntn, bool lower) {
+    if (!lower) return ntm * ntn;
+    return ntn * (ntn + 1) / 2 + (ntm > ntn ? (ntm - ntn) * ntn : 0);
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_constant__ CUtensorMap ta,
                                                               const __grid_constant__ CUtensorMap tb, TcArgs g) {
     extern __shared__ uint8_t smem_raw[];
@@ -204,21 +235,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
     float* b_hi = a_hi + kStages * kBoxFloats;
     float* a_lo = b_hi + kStages * kBoxFloats;
     float* b_lo = a_lo + kStages * kBoxFloats;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(b_lo + kStages * kBoxFloats);
+    float* stg = b_lo + kStages * kBoxFloats;  // the epilogue's staging blocks, [4][32][33]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stg + kStageFloats);
     uint64_t* full = bars;                 // a stage's boxes landed (TMA bytes)
     uint64_t* conv = bars + kStages;       // a stage is split (128 arrivals)
     uint64_t* empty = bars + 2 * kStages;  // a stage's products are done (commit)
-    uint64_t* done = bars + 3 * kStages;   // all products are done (commit)
+    uint64_t* done = bars + 3 * kStages;   // all products of a tile are done (commit)
     uint64_t* chunk_done = done + 1;       // [2] a chunk accumulator's products are done (commit)
     uint64_t* drained = done + 3;          // [2] a chunk accumulator was added into the sum (128 arrivals)
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 5);
+    uint64_t* tmem_free = done + 5;        // a tile's epilogue has read tensor memory (128 arrivals)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 6);
     volatile int* s_err = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
-    const int row0 = blockIdx.y * kBM, col0 = blockIdx.x * kBN;
-    if (g.lower && col0 > row0 + kBM - 1) return;  // a tile above the diagonal (uniform, before any setup)
     if (g.st && (__ldcg(&g.st->skip_factor) || !__ldcg(&g.st->solve_ok))) return;  // written by earlier launches
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nk = (g.K + kBK - 1) / kBK;
+    const int nch = (nk + kChunkKb - 1) / kChunkKb;  // promoted chunks per tile
+    const int ntm = (g.M + kBM - 1) / kBM, ntn = (g.N + kBN - 1) / kBN;
+    const bool lower = g.lower != 0;
+    const int ntiles = tile_count(ntm, ntn, lower);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -231,6 +266,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
             mbar_init(chunk_done + b, 1);
             mbar_init(drained + b, 128);
         }
+        mbar_init(tmem_free, 128);
         *s_err = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -245,136 +281,172 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm_nt(const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    int issued = 0;  // producer: K steps whose boxes were requested
+    // Every role walks the CTA's tiles in the same order and counts K steps
+    // (gk) and chunks (gch) over all of them, so that the ring's stages and
+    // the barriers' phases continue from tile to tile.
+    int issued = 0;   // producer: K steps whose boxes were requested
+    int commits = 0;  // MMA issuer: tiles whose products were committed to done
     if (warp == 0) {
         if (lane == 0) {
-            for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % kStages, r = kb / kStages;
-                if (kb >= kStages && !mbar_wait(empty + s, (r - 1) & 1, g.err)) {
-                    *s_err = 1;
-                    break;
+            int gk = 0;
+            for (int t = blockIdx.x; t < ntiles && !*s_err; t += gridDim.x) {
+                int ti, tj;
+                tile_coords(t, ntn, lower, ti, tj);
+                for (int kb = 0; kb < nk; ++kb, ++gk) {
+                    const int s = gk % kStages, r = gk / kStages;
+                    if (gk >= kStages && !mbar_wait(empty + s, (r - 1) & 1, g.err)) {
+                        *s_err = 1;
+                        break;
+                    }
+                    if (*s_err) break;
+                    mbar_expect_tx(full + s, 2 * kBoxBytes);
+                    tma_load_2d(a_hi + s * kBoxFloats, &ta, kb * kBK, ti * kBM, full + s);
+                    tma_load_2d(b_hi + s * kBoxFloats, &tb, kb * kBK, tj * kBN, full + s);
+                    ++issued;
                 }
-                if (*s_err) break;
-                mbar_expect_tx(full + s, 2 * kBoxBytes);
-                tma_load_2d(a_hi + s * kBoxFloats, &ta, kb * kBK, row0, full + s);
-                tma_load_2d(b_hi + s * kBoxFloats, &tb, kb * kBK, col0, full + s);
-                ++issued;
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % kStages, r = kb / kStages;
-                const int ch = kb / kChunkKb, b = ch & 1;
-                const bool chunk_first = kb % kChunkKb == 0;
-                // a chunk accumulator is reused once the chunk before last was added into the sum
-                if (chunk_first && ch >= 2 && !mbar_wait(drained + b, ((ch >> 1) - 1) & 1, g.err)) {
+            int gk = 0, gch = 0;
+            for (int t = blockIdx.x; t < ntiles && !*s_err; t += gridDim.x, gch += nch) {
+                // the previous tile's epilogue has read the sum and the corrections
+                if (commits > 0 && !mbar_wait(tmem_free, (commits - 1) & 1, g.err)) {
                     *s_err = 1;
                     break;
                 }
-                if (!mbar_wait(conv + s, r & 1, g.err)) {
-                    *s_err = 1;
-                    break;
+                tc_fence_after();
+                for (int kb = 0; kb < nk; ++kb, ++gk) {
+                    const int s = gk % kStages, r = gk / kStages;
+                    const int ch = gch + kb / kChunkKb, b = ch & 1;
+                    const bool chunk_first = kb % kChunkKb == 0;
+                    // a chunk accumulator is reused once the chunk before last was added into the sum
+                    if (chunk_first && ch >= 2 && !mbar_wait(drained + b, ((ch >> 1) - 1) & 1, g.err)) {
+                        *s_err = 1;
+                        break;
+                    }
+                    if (!mbar_wait(conv + s, r & 1, g.err)) {
+                        *s_err = 1;
+                        break;
+                    }
+                    if (*s_err) break;
+                    tc_fence_after();
+                    const uint64_t ah = smem_desc(a_hi + s * kBoxFloats), al = smem_desc(a_lo + s * kBoxFloats);
+                    const uint64_t bh = smem_desc(b_hi + s * kBoxFloats), bl = smem_desc(b_lo + s * kBoxFloats);
+                    const uint32_t acc_main = tmem + 128u * b, acc_corr = tmem + kColCorr;
+#pragma unroll
+                    for (int ks = 0; ks < kBK / 8; ++ks) {
+                        const uint64_t o = (uint64_t)(ks * 32) >> 4;  // 8 TF32 values = 32 bytes along the row
+                        tc_mma(acc_main, ah + o, bh + o, !(chunk_first && ks == 0));
+                        tc_mma(acc_corr, ah + o, bl + o, (kb | ks) != 0);
+                        tc_mma(acc_corr, al + o, bh + o, 1);
+                    }
+                    tc_commit(empty + s);
+                    if (kb % kChunkKb == kChunkKb - 1 || kb == nk - 1) tc_commit(chunk_done + b);
                 }
                 if (*s_err) break;
-                tc_fence_after();
-                const uint64_t ah = smem_desc(a_hi + s * kBoxFloats), al = smem_desc(a_lo + s * kBoxFloats);
-                const uint64_t bh = smem_desc(b_hi + s * kBoxFloats), bl = smem_desc(b_lo + s * kBoxFloats);
-                const uint32_t acc_main = tmem + 128u * b, acc_corr = tmem + kColCorr;
-#pragma unroll
-                for (int ks = 0; ks < kBK / 8; ++ks) {
-                    const uint64_t o = (uint64_t)(ks * 32) >> 4;  // 8 TF32 values = 32 bytes along the row
-                    tc_mma(acc_main, ah + o, bh + o, !(chunk_first && ks == 0));
-                    tc_mma(acc_corr, ah + o, bl + o, (kb | ks) != 0);
-                    tc_mma(acc_corr, al + o, bh + o, 1);
-                }
-                tc_commit(empty + s);
-                if (kb % kChunkKb == kChunkKb - 1 || kb == nk - 1) tc_commit(chunk_done + b);
+                tc_commit(done);  // arrives once every product issued so far has completed
+                ++commits;
             }
-            tc_commit(done);  // arrives once every product issued so far has completed
+            if (*s_err) {
+                // let every product issued so far finish before the memory is freed
+                tc_commit(done);
+                mbar_wait(done, commits & 1, g.err);
+            }
         }
     } else {
-        // warps 2..5: split the landed boxes, then the epilogue
+        // warps 2..5: split the landed boxes, promote the chunks, then the epilogue
         const int ct = threadIdx.x - 64;
-        for (int kb = 0; kb < nk; ++kb) {
-            const int s = kb % kStages, r = kb / kStages;
-            if (!mbar_wait(full + s, r & 1, g.err)) {
-                *s_err = 1;
-                break;
-            }
-            float4* ah4 = reinterpret_cast<float4*>(a_hi + s * kBoxFloats);
-            float4* al4 = reinterpret_cast<float4*>(a_lo + s * kBoxFloats);
-            float4* bh4 = reinterpret_cast<float4*>(b_hi + s * kBoxFloats);
-            float4* bl4 = reinterpret_cast<float4*>(b_lo + s * kBoxFloats);
+        const int q = warp & 3;  // this warp's 32-lane quarter of tensor memory
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+        float* st = stg + q * 32 * 33;
+        int gk = 0, gch = 0, tiles = 0;
+        for (int t = blockIdx.x; t < ntiles && !*s_err; t += gridDim.x, gch += nch, ++tiles) {
+            int ti, tj;
+            tile_coords(t, ntn, lower, ti, tj);
+            const int row0 = ti * kBM, col0 = tj * kBN;
+            for (int kb = 0; kb < nk; ++kb, ++gk) {
+                const int s = gk % kStages, r = gk / kStages;
+                if (!mbar_wait(full + s, r & 1, g.err)) {
+                    *s_err = 1;
+                    break;
+                }
+                float4* ah4 = reinterpret_cast<float4*>(a_hi + s * kBoxFloats);
+                float4* al4 = reinterpret_cast<float4*>(a_lo + s * kBoxFloats);
+                float4* bh4 = reinterpret_cast<float4*>(b_hi + s * kBoxFloats);
+                float4* bl4 = reinterpret_cast<float4*>(b_lo + s * kBoxFloats);
 #pragma unroll
-            for (int i = 0; i < (int)(kBoxFloats / 4) / 128; ++i) {
-                const int e = ct + 128 * i;
-                float4 v = ah4[e], h;
-                h.x = tf32_round(v.x); h.y = tf32_round(v.y); h.z = tf32_round(v.z); h.w = tf32_round(v.w);
-                ah4[e] = h;
-                al4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-                v = bh4[e];
-                h.x = tf32_round(v.x); h.y = tf32_round(v.y); h.z = tf32_round(v.z); h.w = tf32_round(v.w);
-                bh4[e] = h;
-                bl4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                for (int i = 0; i < (int)(kBoxFloats / 4) / 128; ++i) {
+                    const int e = ct + 128 * i;
+                    float4 v = ah4[e], h;
+                    h.x = tf32_round(v.x); h.y = tf32_round(v.y); h.z = tf32_round(v.z); h.w = tf32_round(v.w);
+                    ah4[e] = h;
+                    al4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                    v = bh4[e];
+                    h.x = tf32_round(v.x); h.y = tf32_round(v.y); h.z = tf32_round(v.z); h.w = tf32_round(v.w);
+                    bh4[e] = h;
+                    bl4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                }
+                // the products read shared memory through the async proxy
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(conv + s);
+                // after the last step of chunk c, the previous chunk's accumulator
+                // (its products were issued a chunk earlier) goes into the sum
+                const int c = kb / kChunkKb;
+                if ((kb % kChunkKb == kChunkKb - 1 || kb == nk - 1) && c >= 1 &&
+                    !drain_chunk(gch + c - 1, c == 1, tmem, chunk_done, drained, warp, lane, g.err)) {
+                    *s_err = 1;
+                    break;
+                }
             }
-            // the products read shared memory through the async proxy
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(conv + s);
-            // after the last step of chunk ch, the previous chunk's accumulator
-            // (its products were issued a chunk earlier) goes into the sum
-            if ((kb % kChunkKb == kChunkKb - 1 || kb == nk - 1) && kb / kChunkKb >= 1 &&
-                !drain_chunk(kb / kChunkKb - 1, tmem, chunk_done, drained, warp, lane, g.err)) {
+            if (*s_err) break;
+            if (!drain_chunk(gch + nch - 1, nch == 1, tmem, chunk_done, drained, warp, lane, g.err) ||
+                !mbar_wait(done, tiles & 1, g.err)) {
                 *s_err = 1;
                 break;
             }
-        }
-        const int nch = (nk + kChunkKb - 1) / kChunkKb;
-        if (!*s_err && !drain_chunk(nch - 1, tmem, chunk_done, drained, warp, lane, g.err)) *s_err = 1;
-        if (mbar_wait(done, 0, g.err) && !*s_err) {
             tc_fence_after();
-            // Every product has completed, so no copy or product touches the
-            // operand boxes any more: each warp stages its 32 x 32 blocks in
-            // a_hi (33-float rows, conflict-free both ways) and writes C a
-            // row at a time, 32 consecutive columns per warp instruction.
-            const int q = warp & 3;  // this warp's 32-lane quarter of tensor memory
-            const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-            float* stage = a_hi + q * 32 * 33;
+            // Every product of this tile has completed (the next tile's boxes
+            // may already be landing in the ring): each warp stages its
+            // 32 x 32 blocks in its own staging block (33-float rows,
+            // conflict-free both ways) and writes C a row at a time, 32
+            // consecutive columns per warp instruction.
 #pragma unroll 1
-            for (int c = 0; c < kBN / 32; ++c) {
+            for (int cc = 0; cc < kBN / 32; ++cc) {
                 float v[32], w[32];
-                tmem_ld32(lane_base + kColSum + 32 * c, v);
-                tmem_ld32(lane_base + kColCorr + 32 * c, w);
+                tmem_ld32(lane_base + kColSum + 32 * cc, v);
+                tmem_ld32(lane_base + kColCorr + 32 * cc, w);
 #pragma unroll
-                for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = v[j] + w[j];
+                for (int j = 0; j < 32; ++j) st[lane * 33 + j] = v[j] + w[j];
                 __syncwarp();
-                const int col = col0 + 32 * c + lane;
+                const int col = col0 + 32 * cc + lane;
                 // the 32 old values first, all loads in flight together
                 float old[32];
 #pragma unroll
-                for (int r = 0; r < 32; ++r) {
-                    const int row = row0 + 32 * q + r;
-                    old[r] = (g.beta != 0.f && row < g.M && col < g.N && (!g.lower || col <= row))
-                                 ? __ldcg(g.C + (int64_t)row * g.ldc + col)
-                                 : 0.f;
+                for (int rr = 0; rr < 32; ++rr) {
+                    const int row = row0 + 32 * q + rr;
+                    old[rr] = (g.beta != 0.f && row < g.M && col < g.N && (!g.lower || col <= row))
+                                  ? __ldcg(g.C + (int64_t)row * g.ldc + col)
+                                  : 0.f;
                 }
 #pragma unroll
-                for (int r = 0; r < 32; ++r) {
-                    const int row = row0 + 32 * q + r;
+                for (int rr = 0; rr < 32; ++rr) {
+                    const int row = row0 + 32 * q + rr;
                     if (row < g.M && col < g.N && (!g.lower || col <= row))
-                        g.C[(int64_t)row * g.ldc + col] = g.alpha * stage[r * 33 + lane] + g.beta * old[r];
+                        g.C[(int64_t)row * g.ldc + col] = g.alpha * st[rr * 33 + lane] + g.beta * old[rr];
                 }
                 __syncwarp();
             }
+            tc_fence_before();
+            mbar_arrive(tmem_free);
         }
     }
     // teardown: copies still in flight land before the CTA leaves; products
     // finish before their tensor memory is freed
     if (warp == 0 && lane == 0 && *s_err) {
-        for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb)
-            mbar_wait(full + kb % kStages, (kb / kStages) & 1, g.err);
+        for (int k = (issued > kStages ? issued - kStages : 0); k < issued; ++k)
+            mbar_wait(full + k % kStages, (k / kStages) & 1, g.err);
     }
-    if (warp == 1 && lane == 0 && *s_err) mbar_wait(done, 0, g.err);
     if (threadIdx.x == 0 && *s_err && g.st) g.st->solve_ok = 0;
     tc_fence_before();
     __syncthreads();
@@ -421,7 +493,8 @@ bool tc_gemm_supported(int lda, int ldb, const float* A, const float* B) {
 }
 
 cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                              float alpha, float beta, bool lower, int* err, cudaStream_t s, LmState* st) {
+                              float alpha, float beta, bool lower, int* err, cudaStream_t s, LmState* st,
+                              int max_ctas) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     if (K <= 0 || !tc_gemm_supported(lda, ldb, A, B)) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
@@ -429,8 +502,11 @@ cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, cons
     cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
     if (e != cudaSuccess) return e;
     TcArgs g{M, N, K, C, ldc, alpha, beta, lower ? 1 : 0, err, st};
-    const dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
-    k_tc_gemm_nt<<<grid, kTcThreads, kTcSmem, s>>>(ta, tb, g);
+    const int ntm = (M + kBM - 1) / kBM, ntn = (N + kBN - 1) / kBN;
+    if (lower && M < N) return cudaErrorInvalidValue;  // lower: C square or taller than wide
+    int tiles = lower ? ntn * (ntn + 1) / 2 + (ntm - ntn) * ntn : ntm * ntn;
+    if (max_ctas > 0 && tiles > max_ctas) tiles = max_ctas;
+    k_tc_gemm_nt<<<tiles, kTcThreads, kTcSmem, s>>>(ta, tb, g);
     note_launch();
     return cudaGetLastError();
 }
@@ -443,9 +519,9 @@ cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, cons
 #include "../../include/zeroslam_ba.h"
 
 extern "C" int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C, int M, int N, int K, int lower,
-                                       double* ms) {
+                                       int max_ctas, double* ms) {
     using namespace zs;
-    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0) return ZS_ERR_INVALID;
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || max_ctas < 0 || (lower && M < N)) return ZS_ERR_INVALID;
     const int ld = (K + 3) & ~3;  // device rows padded to 16 bytes
     float *dA = nullptr, *dB = nullptr, *dC = nullptr;
     int* derr = nullptr;
@@ -466,7 +542,8 @@ extern "C" int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C,
                (e = cudaMemcpyAsync(dC, C, 4ull * M * N, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
                (e = cudaMemsetAsync(derr, 0, sizeof(int), s)) != cudaSuccess ||
                (e = cudaEventRecord(e0, s)) != cudaSuccess ||
-               (e = launch_tc_gemm_nt(M, N, K, dA, ld, dB, ld, dC, N, 1.f, 0.f, lower != 0, derr, s)) != cudaSuccess ||
+               (e = launch_tc_gemm_nt(M, N, K, dA, ld, dB, ld, dC, N, 1.f, 0.f, lower != 0, derr, s, nullptr,
+                                      max_ctas)) != cudaSuccess ||
                (e = cudaEventRecord(e1, s)) != cudaSuccess ||
                (e = cudaMemcpyAsync(C, dC, 4ull * M * N, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
                (e = cudaStreamSynchronize(s)) != cudaSuccess) {
