@@ -106,7 +106,7 @@ struct DevWork {
     double* partial = nullptr; // [nsegs*36] Schur segment sums (FP64)
     void* lm_part = nullptr;   // plain form: [M*12] per-observation landmark records (9 used)
     ObsJac* jac = nullptr;     // mixed form: [M] per-observation Jacobian records
-    float4* jp_pm = nullptr;   // mixed form: [3M] J_p of each record again, pose-major positions
+    float4* jp_pm = nullptr;   // mixed form: [3M] J_p of each record again, pose-major positions, three planes
     double* pcg = nullptr;     // mixed form: PCG vectors and operator scratch (pcg_doubles)
     void* pose_part = nullptr; // [M*28] T, per-observation pose records (27 used), pose-major positions
     double* hpp = nullptr;     // [K*36]

@@ -344,7 +344,7 @@ __device__ void op_pose_chunks(const DevProblem& P, const float4* __restrict__ j
         const int q1 = P.opch_q[ch + 1];
         df_dot acc[6];
         for (int q = P.opch_q[ch] + lane; q < q1; q += 32) {
-            const float4 a = __ldg(jp_pm + 3LL * q), b = __ldg(jp_pm + 3LL * q + 1), d = __ldg(jp_pm + 3LL * q + 2);
+            const float4 a = __ldg(jp_pm + q), b = __ldg(jp_pm + P.M + q), d = __ldg(jp_pm + 2 * P.M + q);
             const float4 sv = __ldcg(wsp + q);
             const df s0{sv.x, sv.y}, s1{sv.z, sv.w};
             const float j0[6] = {a.x, a.y, a.z, a.w, b.x, b.y}, j1[6] = {b.z, b.w, d.x, d.y, d.z, d.w};

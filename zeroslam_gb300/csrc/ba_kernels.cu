@@ -281,9 +281,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 3 : 0) k_linearize(
                 d[1] = j0;
                 d[2] = j1;
                 d[3] = j2;
-                jp_pm[3 * q] = j0;  // pose-major copy for the operator's pose pass
-                jp_pm[3 * q + 1] = j1;
-                jp_pm[3 * q + 2] = j2;
+                jp_pm[q] = j0;  // pose-major copy for the operator's pose pass, three planes
+                jp_pm[P.M + q] = j1;
+                jp_pm[2 * P.M + q] = j2;
             }
             d[4] = make_float4(jl[0], jl[1], jl[2], jl[3]);
             d[5] = make_float4(jl[4], jl[5], (float)W00, (float)W01);
