@@ -40,7 +40,7 @@ class Options(C.Structure):
                 ("diagonal_clamp", C.c_double), ("legacy_stop", C.c_double), ("relative_tolerance", C.c_double),
                 ("chi2_floor", C.c_double), ("refine_iterations", C.c_int32), ("refine_tolerance", C.c_double),
                 ("device", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32),
-                ("batch_graph", C.c_int32), ("autotune_cache", C.c_char_p)]
+                ("batch_graph", C.c_int32), ("autotune_cache", C.c_char_p), ("pose_only_path", C.c_int32)]
 
 
 class Problem(C.Structure):

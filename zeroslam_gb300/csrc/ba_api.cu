@@ -378,6 +378,12 @@ struct zs_ba_handle {
     // handle's lifetime and sized for the largest n seen
     TcStreams tcs;
     int tcs_n = 0;
+    // pose-only problems in one launch: free landmarks of the problem, and
+    // the launch's report and attempt records (device, handle lifetime)
+    int free_landmarks = 0;
+    PoseOnlyOut* po_out = nullptr;
+    zs_ba_attempt* po_hist = nullptr;
+    int po_hist_cap = 0;
 
     void release_graph() {
         if (bexec) cudaGraphExecDestroy(bexec);
@@ -487,6 +493,7 @@ void zs_ba_default_options(zs_ba_options* o) {
     o->verbose = 0;
     o->batch_graph = 1;
     o->autotune_cache = nullptr;
+    o->pose_only_path = 1;
 }
 
 const char* zs_ba_status_string(int s) {
@@ -565,6 +572,8 @@ void zs_ba_destroy(zs_ba_handle* h) {
     h->release_problem();
     h->hscratch.release();
     if (h->aux_buf) cudaFree(h->aux_buf);
+    if (h->po_out) cudaFree(h->po_out);
+    if (h->po_hist) cudaFree(h->po_hist);
     if (h->st) cudaFree(h->st);
     if (h->st_host) cudaFreeHost(h->st_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -872,6 +881,8 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     for (int l = 0; l < L; ++l)
         for (int i = 0; i < 3; ++i) lm4[(size_t)l * kLmStride + i] = p->landmarks[3LL * l + i];
     std::vector<uint8_t> pf(p->pose_fixed, p->pose_fixed + K), lf(p->landmark_fixed, p->landmark_fixed + L);
+    h->free_landmarks = 0;
+    for (int l = 0; l < L; ++l) h->free_landmarks += lf[l] == 0;
 
     auto& own = h->owned;
     P.pose = upload(pose8, own, s);
@@ -1292,6 +1303,60 @@ int linear_step_impl(zs_ba_handle* h, double lambda, double* S, double* bs, doub
 // meeting the mixed form's 1e-6 agreement.
 bool mixed_tukey(const zs_ba_handle* h) { return h->tsize == 4 && h->P.loss.kind == ZS_LOSS_TUKEY; }
 
+// A single problem whose landmarks are all fixed, small enough for one CTA's
+// per-pose blocks: the pose-only path (ba_pose_only.cu).
+bool pose_only(const zs_ba_handle* h) {
+    return h->opt.pose_only_path != 0 && !h->batch && h->free_landmarks == 0 && h->P.K <= kPoseOnlyMaxK;
+}
+
+int pose_only_solve(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report* rep) {
+    cudaStream_t s = h->stream;
+    const zs_ba_options& o = h->opt;
+    const long long launches0 = launch_counter();
+    const int cap = std::max(1, iterations * std::max(1, o.max_failures));
+    if (!h->po_out) ZS_CUDA(cudaMalloc(&h->po_out, sizeof(PoseOnlyOut)));
+    if (h->po_hist_cap < cap) {
+        if (h->po_hist) ZS_CUDA(cudaFree(h->po_hist));
+        h->po_hist = nullptr;
+        h->po_hist_cap = 0;
+        ZS_CUDA(cudaMalloc(&h->po_hist, sizeof(zs_ba_attempt) * (size_t)cap));
+        h->po_hist_cap = cap;
+    }
+    PoseOnlyCtl ctl{o.tau, o.diagonal_clamp, o.legacy_stop, o.relative_tolerance, o.chi2_floor,
+                    o.max_failures, iterations, use_relative ? 1 : 0, h->po_hist_cap};
+    ZS_CUDA(cudaEventRecord(h->ev0, s));
+    ZS_CUDA(launch_pose_only_lm(h->P, ctl, h->po_out, h->po_hist, s));
+    ZS_CUDA(cudaEventRecord(h->ev1, s));
+    PoseOnlyOut out{};
+    ZS_CUDA(cudaMemcpyAsync(&out, h->po_out, sizeof(out), cudaMemcpyDeviceToHost, s));
+    ZS_CUDA(cudaStreamSynchronize(s));
+    const int nh = std::min(out.history, h->po_hist_cap);
+    h->history.assign((size_t)nh, zs_ba_attempt{});
+    if (nh > 0)
+        ZS_CUDA(cudaMemcpy(h->history.data(), h->po_hist, sizeof(zs_ba_attempt) * (size_t)nh,
+                           cudaMemcpyDeviceToHost));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    zs_ba_report r{};
+    r.status = ZS_OK;
+    r.iterations = out.iterations;
+    r.accepted = out.accepted;
+    r.attempts = out.attempts;
+    r.cholesky_failures = out.cholesky_failures;
+    r.chi2_initial = out.chi2_initial;
+    r.chi2_final = out.chi2_final;
+    r.lambda_final = out.lambda_final;
+    r.ms_total = ms;
+    r.kernel_launches = launch_counter() - launches0;
+    if (o.verbose)
+        for (const zs_ba_attempt& a : h->history)
+            std::fprintf(stderr, "[%s] iter: % 3d, attempt % 3d, chi2 = % 7.7f, rho = % 7.7f, next lambda = % 8.7f\n",
+                         a.accepted ? "GOOD" : (a.solved ? " BAD" : "FAIL"), a.iteration, a.attempt, a.chi2, a.rho,
+                         a.lambda);
+    if (rep) *rep = r;
+    return out.accepted;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1301,12 +1366,17 @@ int zs_ba_solve(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report*
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
     if (h->batch) return ZS_ERR_UNSUPPORTED;  // zs_ba_solve_batch
-    if (mixed_tukey(h)) return ZS_ERR_UNSUPPORTED;
+    if (mixed_tukey(h) && !pose_only(h)) return ZS_ERR_UNSUPPORTED;
     // source/factor_graph.hpp:494-499: nothing to do without edges or vertices
     if (h->P.M == 0 || (h->P.K == 0 && h->P.L == 0)) return 0;
     if (iterations < 0) return ZS_ERR_INVALID;
     try {
         ZS_CUDA(cudaSetDevice(h->device));
+        if (pose_only(h)) {
+            const int v = pose_only_solve(h, iterations, use_relative != 0, rep);
+            ZS_CUDA(cudaGetLastError());
+            return v;
+        }
         const int v = h->tsize == 8 ? solve_impl<double>(h, iterations, use_relative != 0, rep)
                                     : solve_impl<float>(h, iterations, use_relative != 0, rep);
         ZS_CUDA(cudaGetLastError());

@@ -9,6 +9,8 @@
 
 #include "ba_common.cuh"
 
+struct zs_ba_attempt;
+
 namespace zs {
 
 // Device-resident problem and structure. Observations are stored
@@ -406,6 +408,22 @@ cudaError_t launch_factor_dag(int n, const double* S, float* F, float* X, float*
 // diagonal (source/matrix_decomposition_cholesky.hpp:74,80,89).
 cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, float* XT, float* scratch,
                                   TcStreams* ts, LmState* st, double mu, int* flags, int* epoch, cudaStream_t s);
+
+// ---- pose-only problems in one launch (ba_pose_only.cu) ----
+// Every landmark fixed and at most kPoseOnlyMaxK poses: one CTA runs the
+// whole LM loop (FP64) on the poses in P.pose; out and hist (hist_cap
+// attempt records) are device memory.
+constexpr int kPoseOnlyMaxK = 64;
+struct PoseOnlyCtl {
+    double tau, clamp, legacy_stop, rel_tol, floor;
+    int max_failures, iterations, use_relative, hist_cap;
+};
+struct PoseOnlyOut {
+    int iterations, attempts, accepted, cholesky_failures, history;
+    double chi2_initial, chi2_final, lambda_final;
+};
+cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,
+                                cudaStream_t s);
 
 // ---- FP32 products on the tensor cores (ba_tc_gemm.cu) ----
 // C (M x N, row stride ldc) = alpha A B^T + beta C, A (M x K) and B (N x K)

@@ -179,6 +179,13 @@ __device__ __forceinline__ int64_t next_chunk(int* queue) {
     return __shfl_sync(0xffffffffu, c, 0);
 }
 
+// The claim of a warp's next chunk, issued before the current chunk's work
+// and read after it, so that the atomic's round trip overlaps the work.
+__device__ __forceinline__ int claim_chunk(int* queue) {
+    return (threadIdx.x & 31) == 0 ? atomicAdd(queue, 1) : 0;
+}
+__device__ __forceinline__ int64_t claimed_chunk(int c) { return __shfl_sync(0xffffffffu, c, 0); }
+
 __device__ __forceinline__ df ld_df(const df* p) {
     const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
     return df{v.x, v.y};
@@ -200,7 +207,8 @@ template <bool kIdW>
 __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac, const df* hinv, const df* v, bool c,
                              float4* ws, float4* wsp, df* yst, int* queue) {
     const int lane = threadIdx.x & 31;
-    for (int64_t ch = next_chunk(queue); ch < P.nlmch; ch = next_chunk(queue)) {
+    for (int64_t ch = next_chunk(queue), nxt; ch < P.nlmch; ch = claimed_chunk(nxt)) {
+        nxt = claim_chunk(queue);
         const int l0 = P.lmch_l[ch], l1 = P.lmch_l[ch + 1];
         const int O0 = P.lm_ptr[l0], O1 = P.lm_ptr[l1];
         df carry[3] = {df_zero(), df_zero(), df_zero()};
@@ -340,7 +348,8 @@ __device__ void op_landmarks(const DevProblem& P, const ObsJac* __restrict__ jac
 __device__ void op_pose_chunks(const DevProblem& P, const float4* __restrict__ jp_pm, const float4* wsp, df* part,
                                int* queue) {
     const int lane = threadIdx.x & 31;
-    for (int64_t ch = next_chunk(queue); ch < P.nopch; ch = next_chunk(queue)) {
+    for (int64_t ch = next_chunk(queue), nxt; ch < P.nopch; ch = claimed_chunk(nxt)) {
+        nxt = claim_chunk(queue);
         const int q1 = P.opch_q[ch + 1];
         df_dot acc[6];
         for (int q = P.opch_q[ch] + lane; q < q1; q += 32) {

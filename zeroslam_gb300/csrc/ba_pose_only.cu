@@ -1,0 +1,412 @@
+// Pose-only problems (every landmark fixed: zeroslam's tracking mode,
+// map optimise(1, true, 50), source/slam.hpp:316,387,469) solved in one
+// launch: one CTA runs the whole Levenberg-Marquardt loop of
+// factor_graph::solve (source/factor_graph.hpp:489-615) on the device, with no
+// host round trip per attempt.
+//
+// With every landmark fixed the landmark blocks vanish: no H_ll, no H_pl, and
+// the reduced system is H_pp + lambda I, block diagonal with one 6 x 6 block
+// per pose. Per attempt the CTA
+//   * sums each pose's J_p^T W J_p and -J_p^T g over its observations
+//     (per-observation terms exactly as k_linearize forms them in FP64;
+//     thread-strided partial sums, then warp butterflies and the warps in a
+//     fixed order: the solve repeats bit for bit),
+//   * factors each damped 6 x 6 block with the reference's pivot test
+//     (d > 1e-14 max |S_ii|, source/matrix_decomposition_cholesky.hpp:41-57)
+//     and solve test (|L_ii| > 1e-7 max |L_ii|, :74-89), a thread per pose,
+//     and solves for the step,
+//   * applies the step (pose_plus), evaluates the cost at the trial state
+//     and takes the reference's accept / reject decision
+//     (source/factor_graph.hpp:542-606), rolling back a rejected step.
+// The outer loop, its stopping rules and the attempt history follow the
+// host loop of the general path (solve_impl). Both precisions take this path
+// in FP64: there is no Schur complement or dense factor to make cheaper.
+#include "../../include/zeroslam_ba.h"
+#include "ba_internal.h"
+
+namespace zs {
+
+namespace {
+
+constexpr int kPoWarps = kThreads / 32;
+
+__constant__ int8_t kPoUp6[21][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 5}, {1, 1}, {1, 2}, {1, 3}, {1, 4},
+                                      {1, 5}, {2, 2}, {2, 3}, {2, 4}, {2, 5}, {3, 3}, {3, 4}, {3, 5}, {4, 4}, {4, 5},
+                                      {5, 5}};
+__constant__ int kDiag6[6] = {0, 6, 11, 15, 18, 20};  // the diagonal's places in that order
+
+// Observation o's 27 pose terms: J_p^T W J_p (upper triangle, row by row)
+// and -J_p^T g, formed as the plain form's k_linearize forms them.
+__device__ void pose_record(const DevProblem& P, int64_t o, double rec[27]) {
+    const int pi = P.obs_pose[o], li = P.obs_lm[o];
+    const double* pp = P.pose + (int64_t)pi * kPoseStride;
+    const double* xp = P.lm + (int64_t)li * kLmStride;
+    const double2 uv = P.obs_uv[o];
+    const double* om = P.obs_info ? P.obs_info + 4 * o : nullptr;
+    double p[7], X[3], Xc[3], r[2], Jc[6];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) p[i] = pp[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) X[i] = xp[i];
+    const int front = residual(p, X, uv.x, uv.y, P.intr, Xc, r);
+    if (front) {
+        const double iz = 1.0 / Xc[2];
+        const double iz2 = iz * iz;
+        const double fx = P.intr.fx, fy = P.intr.fy;
+        Jc[0] = fx * iz; Jc[1] = 0.0; Jc[2] = -fx * Xc[0] * iz2;
+        Jc[3] = 0.0; Jc[4] = fy * iz; Jc[5] = -fy * Xc[1] * iz2;
+    } else {
+        Jc[0] = 0.0; Jc[1] = 0.0; Jc[2] = kBehindPenalty;
+        Jc[3] = 0.0; Jc[4] = 0.0; Jc[5] = kBehindPenalty;
+    }
+    const double Xv = Xc[0], Yv = Xc[1], Zv = Xc[2];
+    double Wd[4] = {1.0, 0.0, 0.0, 1.0};
+    if (om) {
+        Wd[0] = om[0]; Wd[1] = om[1]; Wd[2] = om[2]; Wd[3] = om[3];
+    }
+    double orr0 = r[0], orr1 = r[1];
+    if (om) {
+        orr0 = om[0] * r[0] + om[1] * r[1];
+        orr1 = om[2] * r[0] + om[3] * r[1];
+    }
+    double drho = 1.0;
+    if (P.loss.kind) {
+        const double e2 = chi2_of(r, om);
+        double rho[3];
+        loss_rho(P.loss, e2, rho);
+        drho = rho[1];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Wd[i] *= rho[1];
+        // rho' + 2 rho'' e2 as separately rounded multiply and add (no FMA),
+        // as the reference evaluates it (its sign decides the rank-one term)
+        if (__dadd_rn(rho[1], __dmul_rn(2.0 * rho[2], e2)) > 0.0) {
+            const double k2 = 2.0 * rho[2];
+            Wd[0] += k2 * orr0 * orr0;
+            Wd[1] += k2 * orr0 * orr1;
+            Wd[2] += k2 * orr1 * orr0;
+            Wd[3] += k2 * orr1 * orr1;
+        }
+    }
+    double Jp[12];
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+        const double c0 = Jc[rr * 3], c1 = Jc[rr * 3 + 1], c2 = Jc[rr * 3 + 2];
+        Jp[rr * 6 + 0] = -(c2 * Yv - c1 * Zv);
+        Jp[rr * 6 + 1] = -(c0 * Zv - c2 * Xv);
+        Jp[rr * 6 + 2] = -(c1 * Xv - c0 * Yv);
+        Jp[rr * 6 + 3] = -c0;
+        Jp[rr * 6 + 4] = -c1;
+        Jp[rr * 6 + 5] = -c2;
+    }
+    const double g0 = drho * orr0, g1 = drho * orr1;
+    double A0[6], A1[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+        A0[a] = Jp[a] * Wd[0] + Jp[6 + a] * Wd[2];
+        A1[a] = Jp[a] * Wd[1] + Jp[6 + a] * Wd[3];
+    }
+#pragma unroll
+    for (int k = 0; k < 21; ++k) {
+        const int a = kPoUp6[k][0], c = kPoUp6[k][1];
+        rec[k] = A0[a] * Jp[c] + A1[a] * Jp[6 + c];
+    }
+#pragma unroll
+    for (int a = 0; a < 6; ++a) rec[21 + a] = -(Jp[a] * g0 + Jp[6 + a] * g1);
+}
+
+// Observation o's cost term (k_cost_partial's).
+__device__ double obs_cost(const DevProblem& P, int64_t o) {
+    const int pi = P.obs_pose[o], li = P.obs_lm[o];
+    const double* pp = P.pose + (int64_t)pi * kPoseStride;
+    const double* xp = P.lm + (int64_t)li * kLmStride;
+    double p[7], X[3];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) p[i] = pp[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) X[i] = xp[i];
+    const double2 uv = P.obs_uv[o];
+    double Xc[3], r[2];
+    residual(p, X, uv.x, uv.y, P.intr, Xc, r);
+    const double e2 = chi2_of(r, P.obs_info ? P.obs_info + 4 * o : nullptr);
+    if (P.loss.kind) {
+        double rho[3];
+        loss_rho(P.loss, e2, rho);
+        return rho[0];
+    }
+    return e2;
+}
+
+struct Shared {
+    double H[kPoseOnlyMaxK][27];      // per pose: the 21 upper entries of J^T W J, then b
+    double delta[kPoseOnlyMaxK][6];
+    double bk[kPoseOnlyMaxK][kPoseStride];
+    double wpart[kPoWarps][27];
+    double red[kThreads];
+    double lambda, nu, chi2, chi2_new, scale, rho, eps_factor, eps_solve;
+    int solve_ok, good;
+};
+
+// H and b of every pose at the current state.
+__device__ void assemble(const DevProblem& P, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < P.K; ++k) {
+        double acc[27];
+#pragma unroll
+        for (int e = 0; e < 27; ++e) acc[e] = 0.0;
+        if (!P.pose_fixed[k]) {
+            for (int q = P.pose_ptr[k] + threadIdx.x; q < P.pose_ptr[k + 1]; q += blockDim.x) {
+                double rec[27];
+                pose_record(P, P.pose_obs[q], rec);
+#pragma unroll
+                for (int e = 0; e < 27; ++e) acc[e] += rec[e];
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 27; ++e) {
+            double v = acc[e];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) sh.wpart[warp][e] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 27) {
+            double v = 0.0;
+            for (int w = 0; w < kPoWarps; ++w) v += sh.wpart[w][threadIdx.x];
+            sh.H[k][threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ double cost(const DevProblem& P, Shared& sh) {
+    double v = 0.0;
+    for (int64_t o = threadIdx.x; o < P.M; o += blockDim.x) v += obs_cost(P, o);
+    return block_sum(v, sh.red);
+}
+
+__device__ double cta_max(double v, double* red) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double out = red[0];
+    __syncthreads();
+    return out;
+}
+
+// The damped blocks' factors and the step delta (sh.solve_ok, sh.delta).
+__device__ void solve_step(const DevProblem& P, Shared& sh) {
+    const int k = threadIdx.x;
+    const bool mine = k < P.K;
+    const double lam = sh.lambda;
+    double a[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) a[i][j] = 0.0;
+    double dmax = 0.0;
+    if (mine) {
+#pragma unroll
+        for (int e = 0; e < 21; ++e) {
+            const int i = kPoUp6[e][0], j = kPoUp6[e][1];
+            a[i][j] = sh.H[k][e];
+            a[j][i] = sh.H[k][e];
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            a[i][i] += lam;
+            dmax = fmax(dmax, fabs(a[i][i]));
+        }
+    }
+    const double eps_f = cta_max(dmax, sh.red) * 1e-14;
+    int ok = 1;
+    double lmax = 0.0;
+    if (mine) {
+        // right-looking, as the general path's diagonal blocks; after a
+        // failed pivot the remaining columns are skipped
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double d = a[c][c];
+            if (!(d > eps_f)) ok = 0;
+            if (ok) {
+                const double piv = sqrt(d), inv = 1.0 / piv;
+                a[c][c] = piv;
+#pragma unroll
+                for (int i = c + 1; i < 6; ++i) a[i][c] *= inv;
+#pragma unroll
+                for (int i = c + 1; i < 6; ++i)
+#pragma unroll
+                    for (int m = c + 1; m <= i; ++m) a[i][m] -= a[i][c] * a[m][c];
+            }
+        }
+        if (ok)
+#pragma unroll
+            for (int i = 0; i < 6; ++i) lmax = fmax(lmax, fabs(a[i][i]));
+    }
+    ok = __syncthreads_and(ok);
+    const double eps_s = cta_max(lmax, sh.red) * 1e-7;
+    if (ok && mine) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (!(fabs(a[i][i]) > eps_s)) ok = 0;
+    }
+    ok = __syncthreads_and(ok);
+    if (ok && mine) {
+        double y[6], x[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            double v = sh.H[k][21 + i];
+#pragma unroll
+            for (int m = 0; m < i; ++m) v -= a[i][m] * y[m];
+            y[i] = v / a[i][i];
+        }
+#pragma unroll
+        for (int i = 5; i >= 0; --i) {
+            double v = y[i];
+#pragma unroll
+            for (int m = i + 1; m < 6; ++m) v -= a[m][i] * x[m];
+            x[i] = v / a[i][i];
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sh.delta[k][i] = x[i];
+    }
+    if (threadIdx.x == 0) sh.solve_ok = ok;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnlyCtl ctl, PoseOnlyOut* out,
+                                                           zs_ba_attempt* hist) {
+    __shared__ Shared sh;
+    const int t = threadIdx.x;
+    // the initial system, cost and damping (tau min(clamp, max diag H))
+    assemble(P, sh);
+    const double c0 = cost(P, sh);
+    double dmax = 0.0;
+    if (t < P.K)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(sh.H[t][kDiag6[i]]));
+    const double mdiag = cta_max(dmax, sh.red);
+    if (t == 0) {
+        sh.chi2 = c0;
+        sh.lambda = ctl.tau * fmin(ctl.clamp, mdiag);
+        sh.nu = 2.0;
+    }
+    __syncthreads();
+    int iterations = 0, attempts = 0, accepted = 0, chol_fail = 0, nhist = 0;
+    const double legacy = ctl.legacy_stop * c0;
+    for (int it = 0; it < ctl.iterations; ++it) {
+        iterations = it + 1;
+        const double last = sh.chi2;
+        int failures = 0;
+        while (failures < ctl.max_failures) {
+            solve_step(P, sh);
+            const bool ok = sh.solve_ok != 0;
+            double chi2_new = sh.chi2;
+            if (ok) {
+                // trial state (poses; every landmark is fixed), the model's
+                // gain delta^T (lambda delta + b) + 1e-3 and the cost there
+                double sc = 0.0;
+                if (t < P.K) {
+                    double* pp = P.pose + (int64_t)t * kPoseStride;
+                    for (int i = 0; i < kPoseStride; ++i) sh.bk[t][i] = pp[i];
+                    for (int i = 0; i < 6; ++i) {
+                        const double d = sh.delta[t][i];
+                        sc += d * (sh.lambda * d + sh.H[t][21 + i]);
+                    }
+                    if (!P.pose_fixed[t]) pose_plus(pp, sh.delta[t]);
+                }
+                const double scale = block_sum(sc, sh.red) + 1e-3;
+                chi2_new = cost(P, sh);
+                if (t == 0) {
+                    sh.scale = scale;
+                    sh.chi2_new = chi2_new;
+                }
+            }
+            // source/factor_graph.hpp:542-591 (k_decide)
+            if (t == 0) {
+                if (!ok) {
+                    sh.lambda *= sh.nu;
+                    sh.nu *= 2.0;
+                    sh.good = 0;
+                } else {
+                    const double rho = (sh.chi2 - sh.chi2_new) / sh.scale;
+                    sh.rho = rho;
+                    if (rho > 0 && isfinite(sh.chi2_new)) {
+                        double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
+                        alpha = fmin(alpha, 2.0 / 3.0);
+                        sh.lambda *= fmax(1.0 / 3.0, alpha);
+                        sh.nu = 2.0;
+                        sh.chi2 = sh.chi2_new;
+                        sh.good = 1;
+                    } else {
+                        sh.lambda *= sh.nu;
+                        sh.nu *= 2.0;
+                        sh.good = 0;
+                    }
+                }
+            }
+            __syncthreads();
+            const bool good = sh.good != 0;
+            const double lam = sh.lambda;
+            // a rejected step is rolled back while lambda stays finite (k_rollback)
+            if (ok && !good && isfinite(lam) && t < P.K) {
+                double* pp = P.pose + (int64_t)t * kPoseStride;
+                for (int i = 0; i < kPoseStride; ++i) pp[i] = sh.bk[t][i];
+            }
+            ++attempts;
+            if (t == 0 && nhist < ctl.hist_cap) {
+                zs_ba_attempt a{};
+                a.iteration = it;
+                a.attempt = failures;
+                a.solved = ok ? 1 : 0;
+                a.accepted = ok && good ? 1 : 0;
+                a.chi2 = ok ? chi2_new : sh.chi2;
+                a.rho = ok ? sh.rho : 0.0;
+                a.lambda = lam;
+                hist[nhist] = a;
+            }
+            ++nhist;
+            __syncthreads();
+            if (!ok) {
+                ++chol_fail;
+                ++failures;
+                if (!isfinite(lam)) break;
+                continue;
+            }
+            if (good) {
+                ++accepted;
+                if (!isfinite(lam)) break;
+                assemble(P, sh);  // the next iteration's system at the accepted state
+                break;
+            }
+            if (!isfinite(lam)) break;
+            ++failures;
+        }
+        const double thr = ctl.use_relative ? ctl.rel_tol * fmax(last, ctl.floor) : legacy;
+        if (failures >= ctl.max_failures || (last - sh.chi2) < thr || !isfinite(sh.lambda)) break;
+    }
+    if (t == 0) {
+        out->iterations = iterations;
+        out->attempts = attempts;
+        out->accepted = accepted;
+        out->cholesky_failures = chol_fail;
+        out->history = nhist;
+        out->chi2_initial = c0;
+        out->chi2_final = sh.chi2;
+        out->lambda_final = sh.lambda;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,
+                                cudaStream_t s) {
+    if (P.K > kPoseOnlyMaxK) return cudaErrorInvalidValue;
+    k_pose_only_lm<<<1, kThreads, 0, s>>>(P, ctl, out, hist);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace zs
