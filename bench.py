@@ -16,8 +16,9 @@ collective): value = iterations of all ranks / max-over-ranks time.
 The same JSON line carries the other configurations and rows as sections:
 batched_windows (256 local windows, with a CPU baseline over every host
 core), loop_4m (the 4M-observation loop), adjoint (gradients of the solved
-state), map_cull (map::cull), map_optimise (map::optimise over map arrays)
-and matching (feature::find_matches). --map-only prints the last three
+state), pose_only (a tracking solve in one launch against the general path),
+map_cull (map::cull), map_optimise (map::optimise over map arrays) and
+matching (feature::find_matches). --map-only prints the last three
 alone; --no-batch / --no-loop / --no-adjoint / --no-cull skip sections.
 """
 
@@ -486,6 +487,35 @@ def adjoint_section(args, dist: Dist) -> dict:
             "observations": sc.M}
 
 
+def pose_only_section(args, dist: Dist) -> dict:
+    """zeroslam's tracking solve (map optimise(1, true, 50)): one free pose among
+    four fixed ones, every landmark fixed, 50 LM iterations; the one-launch
+    path (k_pose_only_lm) against the general path on the same handle type
+    (device time of zs_ba_solve, FP64; one warm-up, `steps` timed solves)."""
+    from zeroslam_gb300 import ba, scenes
+
+    sc = scenes.arc_scene(5, 1500, seed=51)
+    sc.landmark_fixed[:] = 1
+    sc.pose_fixed[:] = 1
+    sc.pose_fixed[2] = 0
+    out = {"workload": f"tracking: 1 free pose of {sc.K}, {sc.L} fixed landmarks, M={sc.M} observations, "
+                       "50 LM iterations, FP64"}
+    for name, path in (("one_launch", 1), ("general_path", 0)):
+        with ba.BundleAdjuster(precision=ba.FP64, device=dist.local, pose_only_path=path) as h:
+            h.set_problem(sc)
+            h.solve(50)
+            ms, launches = [], 0
+            for _ in range(max(1, args.steps)):
+                h.reset_state()
+                r = h.solve(50)
+                ms.append(r.ms_total)
+                launches = r.kernel_launches
+            out[name] = {"ms_per_solve": dist.max(float(np.mean(ms))), "kernel_launches": int(launches),
+                         "attempts": r.attempts, "chi2_final": r.chi2_final}
+    out["speedup"] = out["general_path"]["ms_per_solve"] / out["one_launch"]["ms_per_solve"]
+    return out
+
+
 # Per observation that reaches the cull's error pass: R X + t, projection and
 # distance in FP64, 35 operations (9 mul + 12 add for R X + t, 1 div + 4 mul +
 # 2 add for the projection, 2 sub + 2 mul + 2 add + 1 sqrt for the distance;
@@ -792,6 +822,7 @@ def ours_arm(args, dist: Dist):
     batch = None if args.no_batch else batch_section(args, dist)
     loop = None if args.no_loop else loop_section(args, dist)
     adjoint = None if args.no_adjoint else adjoint_section(args, dist)
+    pose_only = pose_only_section(args, dist)
     cull = None if args.no_cull else cull_section(args, dist, peaks, hbm, sc)
     mapopt = None if args.no_cull else map_section(args, dist, sc)
     matching = None if args.no_cull else match_section(args, dist)
@@ -845,6 +876,7 @@ def ours_arm(args, dist: Dist):
         "batched_windows": batch,
         "loop_4m": loop,
         "adjoint": adjoint,
+        "pose_only": pose_only,
         "map_cull": cull,
         "map_optimise": mapopt,
         "matching": matching,

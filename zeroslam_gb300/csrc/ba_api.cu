@@ -384,6 +384,8 @@ struct zs_ba_handle {
     PoseOnlyOut* po_out = nullptr;
     zs_ba_attempt* po_hist = nullptr;
     int po_hist_cap = 0;
+    double* po_scratch = nullptr;  // partial sums: [grid * 64 * 27] + [64 * 27] + [grid]
+    size_t po_scratch_cap = 0;
 
     void release_graph() {
         if (bexec) cudaGraphExecDestroy(bexec);
@@ -574,6 +576,7 @@ void zs_ba_destroy(zs_ba_handle* h) {
     if (h->aux_buf) cudaFree(h->aux_buf);
     if (h->po_out) cudaFree(h->po_out);
     if (h->po_hist) cudaFree(h->po_hist);
+    if (h->po_scratch) cudaFree(h->po_scratch);
     if (h->st) cudaFree(h->st);
     if (h->st_host) cudaFreeHost(h->st_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1322,10 +1325,22 @@ int pose_only_solve(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_re
         ZS_CUDA(cudaMalloc(&h->po_hist, sizeof(zs_ba_attempt) * (size_t)cap));
         h->po_hist_cap = cap;
     }
+    const int grid = pose_only_grid(h->P.M);
+    const size_t need = (size_t)grid * kPoseOnlyMaxK * 27 + (size_t)kPoseOnlyMaxK * 27 + (size_t)grid;
+    if (h->po_scratch_cap < need) {
+        if (h->po_scratch) ZS_CUDA(cudaFree(h->po_scratch));
+        h->po_scratch = nullptr;
+        h->po_scratch_cap = 0;
+        ZS_CUDA(cudaMalloc(&h->po_scratch, sizeof(double) * need));
+        h->po_scratch_cap = need;
+    }
+    double* part = h->po_scratch;
+    double* sums = part + (size_t)grid * kPoseOnlyMaxK * 27;
+    double* cpart = sums + (size_t)kPoseOnlyMaxK * 27;
     PoseOnlyCtl ctl{o.tau, o.diagonal_clamp, o.legacy_stop, o.relative_tolerance, o.chi2_floor,
                     o.max_failures, iterations, use_relative ? 1 : 0, h->po_hist_cap};
     ZS_CUDA(cudaEventRecord(h->ev0, s));
-    ZS_CUDA(launch_pose_only_lm(h->P, ctl, h->po_out, h->po_hist, s));
+    ZS_CUDA(launch_pose_only_lm(h->P, ctl, h->po_out, h->po_hist, part, sums, cpart, grid, s));
     ZS_CUDA(cudaEventRecord(h->ev1, s));
     PoseOnlyOut out{};
     ZS_CUDA(cudaMemcpyAsync(&out, h->po_out, sizeof(out), cudaMemcpyDeviceToHost, s));

@@ -410,9 +410,10 @@ cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, fl
                                   TcStreams* ts, LmState* st, double mu, int* flags, int* epoch, cudaStream_t s);
 
 // ---- pose-only problems in one launch (ba_pose_only.cu) ----
-// Every landmark fixed and at most kPoseOnlyMaxK poses: one CTA runs the
-// whole LM loop (FP64) on the poses in P.pose; out and hist (hist_cap
-// attempt records) are device memory.
+// Every landmark fixed and at most kPoseOnlyMaxK poses: one cooperative
+// launch of `grid` CTAs (pose_only_grid(M)) runs the whole LM loop (FP64) on
+// the poses in P.pose. Device memory: out, hist (hist_cap attempt records),
+// part [grid * K * 27], sums [K * 27], cpart [grid].
 constexpr int kPoseOnlyMaxK = 64;
 struct PoseOnlyCtl {
     double tau, clamp, legacy_stop, rel_tol, floor;
@@ -422,8 +423,9 @@ struct PoseOnlyOut {
     int iterations, attempts, accepted, cholesky_failures, history;
     double chi2_initial, chi2_final, lambda_final;
 };
+int pose_only_grid(int64_t M);
 cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,
-                                cudaStream_t s);
+                                double* part, double* sums, double* cpart, int grid, cudaStream_t s);
 
 // ---- FP32 products on the tensor cores (ba_tc_gemm.cu) ----
 // C (M x N, row stride ldc) = alpha A B^T + beta C, A (M x K) and B (N x K)

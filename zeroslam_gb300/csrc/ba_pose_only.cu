@@ -1,28 +1,42 @@
 // Pose-only problems (every landmark fixed: zeroslam's tracking mode,
 // map optimise(1, true, 50), source/slam.hpp:316,387,469) solved in one
-// launch: one CTA runs the whole Levenberg-Marquardt loop of
+// cooperative launch that runs the whole Levenberg-Marquardt loop of
 // factor_graph::solve (source/factor_graph.hpp:489-615) on the device, with no
 // host round trip per attempt.
 //
 // With every landmark fixed the landmark blocks vanish: no H_ll, no H_pl, and
 // the reduced system is H_pp + lambda I, block diagonal with one 6 x 6 block
-// per pose. Per attempt the CTA
-//   * sums each pose's J_p^T W J_p and -J_p^T g over its observations
-//     (per-observation terms exactly as k_linearize forms them in FP64;
-//     thread-strided partial sums, then warp butterflies and the warps in a
-//     fixed order: the solve repeats bit for bit),
-//   * factors each damped 6 x 6 block with the reference's pivot test
-//     (d > 1e-14 max |S_ii|, source/matrix_decomposition_cholesky.hpp:41-57)
-//     and solve test (|L_ii| > 1e-7 max |L_ii|, :74-89), a thread per pose,
-//     and solves for the step,
-//   * applies the step (pose_plus), evaluates the cost at the trial state
-//     and takes the reference's accept / reject decision
-//     (source/factor_graph.hpp:542-606), rolling back a rejected step.
-// The outer loop, its stopping rules and the attempt history follow the
-// host loop of the general path (solve_impl). Both precisions take this path
-// in FP64: there is no Schur complement or dense factor to make cheaper.
+// per pose. Per attempt:
+//   * every CTA sums its share of each pose's observations into 27 terms
+//     (J_p^T W J_p upper triangle and -J_p^T g, each observation's terms
+//     formed exactly as the plain form's k_linearize forms them); after a
+//     grid barrier a warp per sum adds the CTAs' partials (lanes over the
+//     CTAs, then a butterfly), and after another every CTA reads the sums;
+//   * every CTA factors the damped 6 x 6 blocks (a thread per pose) with the
+//     reference's pivot test (d > 1e-14 max |S_ii|,
+//     source/matrix_decomposition_cholesky.hpp:41-57) and solve test
+//     (|L_ii| > 1e-7 max |L_ii|, :74-89) and solves for the step: the same
+//     arithmetic on the same values in every CTA, so all of them take the
+//     same decisions without exchanging them;
+//   * CTA 0 backs up and updates the poses (pose_plus); after a barrier the
+//     CTAs evaluate the trial cost (per-CTA partials, then every CTA adds
+//     them the same way), take the reference's accept / reject decision
+//     (source/factor_graph.hpp:542-606) and CTA 0 rolls a rejected step back.
+// The FP64 pipe of one SM is far too slow for the per-observation work on
+// GB300 (measured: one CTA took 1.30 ms for a 6,802-observation tracking
+// solve, the general path 0.81 ms), hence the whole grid. The outer loop, its
+// stopping rules and the attempt history follow the host loop of the general
+// path (solve_impl). Both precisions take this path in FP64: there is no
+// Schur complement or dense factor to make cheaper. Every sum has a fixed
+// order for a given grid size: results repeat bit for bit.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
 #include "../../include/zeroslam_ba.h"
 #include "ba_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace zs {
 
@@ -142,46 +156,84 @@ struct Shared {
     double bk[kPoseOnlyMaxK][kPoseStride];
     double wpart[kPoWarps][27];
     double red[kThreads];
-    double lambda, nu, chi2, chi2_new, scale, rho, eps_factor, eps_solve;
+    double lambda, nu, chi2, rho;
     int solve_ok, good;
 };
 
-// H and b of every pose at the current state.
-__device__ void assemble(const DevProblem& P, Shared& sh) {
+// Warp butterflies and the warps in order: the CTA's 27 sums into sh.wpart[0].
+__device__ void cta_sum27(double acc[27], Shared& sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int e = 0; e < 27; ++e) {
+        double v = acc[e];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) sh.wpart[warp][e] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        double v = 0.0;
+        for (int w = 0; w < kPoWarps; ++w) v += sh.wpart[w][threadIdx.x];
+        sh.wpart[0][threadIdx.x] = v;  // (warp 0's slot, read only after the barrier below)
+    }
+    __syncthreads();
+}
+
+// H and b of every pose at the current state into sh.H (every CTA).
+// part: [G][K][27] per-CTA partials, sums: [K][27].
+__device__ void assemble(cg::grid_group& grid, const DevProblem& P, Shared& sh, double* part, double* sums) {
+    const int G = gridDim.x, c = blockIdx.x;
     for (int k = 0; k < P.K; ++k) {
         double acc[27];
 #pragma unroll
         for (int e = 0; e < 27; ++e) acc[e] = 0.0;
         if (!P.pose_fixed[k]) {
-            for (int q = P.pose_ptr[k] + threadIdx.x; q < P.pose_ptr[k + 1]; q += blockDim.x) {
+            const int q0 = P.pose_ptr[k], q1 = P.pose_ptr[k + 1];
+            for (int q = q0 + c * blockDim.x + threadIdx.x; q < q1; q += G * blockDim.x) {
                 double rec[27];
                 pose_record(P, P.pose_obs[q], rec);
 #pragma unroll
                 for (int e = 0; e < 27; ++e) acc[e] += rec[e];
             }
         }
-#pragma unroll
-        for (int e = 0; e < 27; ++e) {
-            double v = acc[e];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-            if (lane == 0) sh.wpart[warp][e] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < 27) {
-            double v = 0.0;
-            for (int w = 0; w < kPoWarps; ++w) v += sh.wpart[w][threadIdx.x];
-            sh.H[k][threadIdx.x] = v;
-        }
+        cta_sum27(acc, sh);
+        if (threadIdx.x < 27) part[((int64_t)c * P.K + k) * 27 + threadIdx.x] = sh.wpart[0][threadIdx.x];
         __syncthreads();
     }
+    grid.sync();
+    // entry i of the 27 K sums: a warp adds the G partials, lane l those of
+    // CTAs l, l + 32, ..., then a butterfly (a fixed order for a given G)
+    {
+        const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        for (int i = c * nw + (threadIdx.x >> 5); i < 27 * P.K; i += G * nw) {
+            double v = 0.0;
+            for (int b = lane; b < G; b += 32) v += __ldcg(part + (int64_t)b * 27 * P.K + i);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) sums[i] = v;
+        }
+    }
+    grid.sync();
+    for (int i = threadIdx.x; i < 27 * P.K; i += blockDim.x) sh.H[i / 27][i % 27] = __ldcg(sums + i);
+    __syncthreads();
 }
 
-__device__ double cost(const DevProblem& P, Shared& sh) {
+// The cost at the current state (every CTA gets the same value).
+__device__ double cost(cg::grid_group& grid, const DevProblem& P, Shared& sh, double* cpart) {
+    const int G = gridDim.x;
     double v = 0.0;
-    for (int64_t o = threadIdx.x; o < P.M; o += blockDim.x) v += obs_cost(P, o);
-    return block_sum(v, sh.red);
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < P.M; o += (int64_t)G * blockDim.x)
+        v += obs_cost(P, o);
+    v = block_sum(v, sh.red);
+    if (threadIdx.x == 0) cpart[blockIdx.x] = v;
+    grid.sync();
+    // every warp adds the G partials the same way: lane l those of CTAs l,
+    // l + 32, ..., then a butterfly
+    double t = 0.0;
+    for (int b = threadIdx.x & 31; b < G; b += 32) t += __ldcg(cpart + b);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    return t;
 }
 
 __device__ double cta_max(double v, double* red) {
@@ -277,12 +329,15 @@ __device__ void solve_step(const DevProblem& P, Shared& sh) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnlyCtl ctl, PoseOnlyOut* out,
-                                                           zs_ba_attempt* hist) {
+                                                           zs_ba_attempt* hist, double* part, double* sums,
+                                                           double* cpart) {
+    cg::grid_group grid = cg::this_grid();
     __shared__ Shared sh;
     const int t = threadIdx.x;
+    const bool lead = blockIdx.x == 0;  // the CTA that writes poses, history and the report
     // the initial system, cost and damping (tau min(clamp, max diag H))
-    assemble(P, sh);
-    const double c0 = cost(P, sh);
+    assemble(grid, P, sh, part, sums);
+    const double c0 = cost(grid, P, sh, cpart);
     double dmax = 0.0;
     if (t < P.K)
 #pragma unroll
@@ -303,42 +358,41 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
         while (failures < ctl.max_failures) {
             solve_step(P, sh);
             const bool ok = sh.solve_ok != 0;
-            double chi2_new = sh.chi2;
+            double chi2_new = sh.chi2, scale = 0.0;
             if (ok) {
                 // trial state (poses; every landmark is fixed), the model's
                 // gain delta^T (lambda delta + b) + 1e-3 and the cost there
                 double sc = 0.0;
                 if (t < P.K) {
                     double* pp = P.pose + (int64_t)t * kPoseStride;
+#pragma unroll
                     for (int i = 0; i < kPoseStride; ++i) sh.bk[t][i] = pp[i];
+#pragma unroll
                     for (int i = 0; i < 6; ++i) {
                         const double d = sh.delta[t][i];
                         sc += d * (sh.lambda * d + sh.H[t][21 + i]);
                     }
-                    if (!P.pose_fixed[t]) pose_plus(pp, sh.delta[t]);
                 }
-                const double scale = block_sum(sc, sh.red) + 1e-3;
-                chi2_new = cost(P, sh);
-                if (t == 0) {
-                    sh.scale = scale;
-                    sh.chi2_new = chi2_new;
-                }
+                scale = block_sum(sc, sh.red) + 1e-3;
+                if (lead && t < P.K && !P.pose_fixed[t]) pose_plus(P.pose + (int64_t)t * kPoseStride, sh.delta[t]);
+                grid.sync();  // the trial poses are visible to every CTA
+                chi2_new = cost(grid, P, sh, cpart);
             }
-            // source/factor_graph.hpp:542-591 (k_decide)
+            // source/factor_graph.hpp:542-591 (k_decide), in every CTA
             if (t == 0) {
                 if (!ok) {
                     sh.lambda *= sh.nu;
                     sh.nu *= 2.0;
                     sh.good = 0;
                 } else {
-                    const double rho = (sh.chi2 - sh.chi2_new) / sh.scale;
+                    const double rho = (sh.chi2 - chi2_new) / scale;
                     sh.rho = rho;
-                    if (rho > 0 && isfinite(sh.chi2_new)) {
+                    if (rho > 0 && isfinite(chi2_new)) {
                         double alpha = 1.0 - pow(2.0 * rho - 1.0, 3.0);
                         alpha = fmin(alpha, 2.0 / 3.0);
                         sh.lambda *= fmax(1.0 / 3.0, alpha);
                         sh.nu = 2.0;
-                        sh.chi2 = sh.chi2_new;
+                        sh.chi2 = chi2_new;
                         sh.good = 1;
                     } else {
                         sh.lambda *= sh.nu;
@@ -350,13 +404,8 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
             __syncthreads();
             const bool good = sh.good != 0;
             const double lam = sh.lambda;
-            // a rejected step is rolled back while lambda stays finite (k_rollback)
-            if (ok && !good && isfinite(lam) && t < P.K) {
-                double* pp = P.pose + (int64_t)t * kPoseStride;
-                for (int i = 0; i < kPoseStride; ++i) pp[i] = sh.bk[t][i];
-            }
             ++attempts;
-            if (t == 0 && nhist < ctl.hist_cap) {
+            if (lead && t == 0 && nhist < ctl.hist_cap) {
                 zs_ba_attempt a{};
                 a.iteration = it;
                 a.attempt = failures;
@@ -368,7 +417,16 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
                 hist[nhist] = a;
             }
             ++nhist;
-            __syncthreads();
+            if (ok) {
+                // a rejected step is rolled back while lambda stays finite
+                // (k_rollback); every CTA waits for the poses it will read
+                if (lead && !good && isfinite(lam) && t < P.K) {
+                    double* pp = P.pose + (int64_t)t * kPoseStride;
+#pragma unroll
+                    for (int i = 0; i < kPoseStride; ++i) pp[i] = sh.bk[t][i];
+                }
+                grid.sync();
+            }
             if (!ok) {
                 ++chol_fail;
                 ++failures;
@@ -378,7 +436,7 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
             if (good) {
                 ++accepted;
                 if (!isfinite(lam)) break;
-                assemble(P, sh);  // the next iteration's system at the accepted state
+                assemble(grid, P, sh, part, sums);  // the next iteration's system at the accepted state
                 break;
             }
             if (!isfinite(lam)) break;
@@ -387,7 +445,7 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
         const double thr = ctl.use_relative ? ctl.rel_tol * fmax(last, ctl.floor) : legacy;
         if (failures >= ctl.max_failures || (last - sh.chi2) < thr || !isfinite(sh.lambda)) break;
     }
-    if (t == 0) {
+    if (lead && t == 0) {
         out->iterations = iterations;
         out->attempts = attempts;
         out->accepted = accepted;
@@ -401,12 +459,29 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
 
 }  // namespace
 
+int pose_only_grid(int64_t M) {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pose_only_lm, kThreads, 0);
+        cached = std::max(1, std::min(sms, sms * per));
+        cudaGetLastError();
+    }
+    // about 64 observations per CTA and pass, at most one CTA per SM
+    return (int)std::max<int64_t>(1, std::min<int64_t>(cached, (M + 63) / 64));
+}
+
 cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,
-                                cudaStream_t s) {
-    if (P.K > kPoseOnlyMaxK) return cudaErrorInvalidValue;
-    k_pose_only_lm<<<1, kThreads, 0, s>>>(P, ctl, out, hist);
-    note_launch();
-    return cudaGetLastError();
+                                double* part, double* sums, double* cpart, int grid, cudaStream_t s) {
+    if (P.K > kPoseOnlyMaxK || grid < 1) return cudaErrorInvalidValue;
+    DevProblem Pv = P;
+    PoseOnlyCtl c = ctl;
+    void* args[] = {(void*)&Pv, (void*)&c, (void*)&out, (void*)&hist, (void*)&part, (void*)&sums, (void*)&cpart};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pose_only_lm, dim3(grid), dim3(kThreads), args, 0, s);
+    if (e == cudaSuccess) note_launch();
+    return e;
 }
 
 }  // namespace zs
