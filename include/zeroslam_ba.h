@@ -86,9 +86,10 @@ typedef struct zs_ba_options {
                                    node over attempt rounds), 0 = host loop over rounds (1) */
     const char* autotune_cache; /* batched solve: file of autotuned block sizes (read, and written
                                    after tuning), or NULL for a per-process cache only */
-    int32_t pose_only_path;     /* 1: a single problem with every landmark fixed and at most 64 poses
-                                   (zeroslam's tracking mode) runs its whole LM loop in one launch,
-                                   in FP64 in both precisions; 0: the general path (1) */
+    int32_t pose_only_path;     /* 1: a single problem with every landmark fixed, at most 64 poses and
+                                   at most 4 of them free (zeroslam's tracking mode) runs its whole LM
+                                   loop in one launch, in FP64 in both precisions; 0: the general
+                                   path (1) */
 } zs_ba_options;
 
 /* A bundle-adjustment problem as structure of arrays (host pointers).

@@ -55,7 +55,7 @@ def test_pose_only_batch(zs_lib, oracle):
             assert abs(reps[w].chi2_final - ro.chi2_final) <= tol * ro.chi2_final + 1e-12, (precision, w)
 
 
-# ---- the one-launch path (every landmark fixed, at most 64 poses) ----
+# ---- the one-launch path (every landmark fixed, at most 64 poses, at most 4 free) ----
 
 
 def _tracking(seed, n_fixed=4, L=1500):
@@ -86,8 +86,11 @@ def test_one_launch_against_oracle(zs_lib, oracle, precision):
 
 def test_one_launch_matches_general_path(zs_lib):
     """Same decisions as the general path (Schur, dense factor) on a pose-only
-    problem with several free poses: every attempt's outcome, and the cost."""
+    problem with four free poses among twelve: every attempt's outcome, and
+    the cost."""
     sc = _pose_only(scenes.arc_scene(12, 800, seed=53))
+    sc.pose_fixed[:] = 1
+    sc.pose_fixed[[2, 5, 7, 10]] = 0
     out = []
     for path in (1, 0):
         with _ba(0, pose_only_path=path) as h:
@@ -105,6 +108,8 @@ def test_one_launch_matches_general_path(zs_lib):
 def test_one_launch_robust_information(zs_lib, oracle):
     """Huber loss and per-observation information matrices, against the oracle."""
     sc = _pose_only(scenes.arc_scene(8, 1200, seed=57, huber=True))
+    sc.pose_fixed[:] = 1
+    sc.pose_fixed[[1, 4, 6]] = 0
     rng = np.random.default_rng(58)
     s = rng.uniform(0.5, 2.0, size=(sc.M, 1))
     sc.obs_info = np.concatenate([1.0 * s, 0.2 * s, 0.2 * s, 0.6 * s], axis=1)
@@ -118,7 +123,8 @@ def test_one_launch_robust_information(zs_lib, oracle):
 
 
 def test_one_launch_repeats_and_limits(zs_lib):
-    """Bit-for-bit repetition; more than 64 poses take the general path."""
+    """Bit-for-bit repetition; more than 64 poses, or more than 4 free ones,
+    take the general path."""
     sc = _tracking(59)
     res = []
     for _ in range(2):
@@ -130,5 +136,12 @@ def test_one_launch_repeats_and_limits(zs_lib):
     big = _pose_only(scenes.arc_scene(70, 600, seed=61))
     with _ba(0) as h:
         h.set_problem(big)
+        r = h.solve(3)
+    assert r.kernel_launches > 1 and r.accepted >= 1
+    five = _pose_only(scenes.arc_scene(8, 600, seed=63))
+    five.pose_fixed[:] = 1
+    five.pose_fixed[1:6] = 0
+    with _ba(0) as h:
+        h.set_problem(five)
         r = h.solve(3)
     assert r.kernel_launches > 1 and r.accepted >= 1

@@ -380,7 +380,7 @@ struct zs_ba_handle {
     int tcs_n = 0;
     // pose-only problems in one launch: free landmarks of the problem, and
     // the launch's report and attempt records (device, handle lifetime)
-    int free_landmarks = 0;
+    int free_landmarks = 0, free_poses = 0;
     PoseOnlyOut* po_out = nullptr;
     zs_ba_attempt* po_hist = nullptr;
     int po_hist_cap = 0;
@@ -886,6 +886,8 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     std::vector<uint8_t> pf(p->pose_fixed, p->pose_fixed + K), lf(p->landmark_fixed, p->landmark_fixed + L);
     h->free_landmarks = 0;
     for (int l = 0; l < L; ++l) h->free_landmarks += lf[l] == 0;
+    h->free_poses = 0;
+    for (int k = 0; k < K; ++k) h->free_poses += pf[k] == 0;
 
     auto& own = h->owned;
     P.pose = upload(pose8, own, s);
@@ -1306,10 +1308,12 @@ int linear_step_impl(zs_ba_handle* h, double lambda, double* S, double* bs, doub
 // meeting the mixed form's 1e-6 agreement.
 bool mixed_tukey(const zs_ba_handle* h) { return h->tsize == 4 && h->P.loss.kind == ZS_LOSS_TUKEY; }
 
-// A single problem whose landmarks are all fixed, small enough for one CTA's
-// per-pose blocks: the pose-only path (ba_pose_only.cu).
+// A single problem whose landmarks are all fixed, with at most
+// kPoseOnlyMaxK poses of which at most kPoseOnlyMaxFree free: the pose-only
+// path (ba_pose_only.cu).
 bool pose_only(const zs_ba_handle* h) {
-    return h->opt.pose_only_path != 0 && !h->batch && h->free_landmarks == 0 && h->P.K <= kPoseOnlyMaxK;
+    return h->opt.pose_only_path != 0 && !h->batch && h->free_landmarks == 0 && h->P.K <= kPoseOnlyMaxK &&
+           h->free_poses <= kPoseOnlyMaxFree;
 }
 
 int pose_only_solve(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report* rep) {

@@ -415,6 +415,10 @@ cudaError_t launch_preconditioner(int n, const double* S, float* F, float* X, fl
 // the poses in P.pose. Device memory: out, hist (hist_cap attempt records),
 // part [grid * K * 27], sums [K * 27], cpart [grid].
 constexpr int kPoseOnlyMaxK = 64;
+// At most this many free poses: each free pose's sums take one pass of the
+// grid (the FP64 pipe bounds it), so problems with more free poses are
+// faster on the general path (measured: 16 free poses 2.42 against 2.03 ms).
+constexpr int kPoseOnlyMaxFree = 4;
 struct PoseOnlyCtl {
     double tau, clamp, legacy_stop, rel_tol, floor;
     int max_failures, iterations, use_relative, hist_cap;

@@ -184,17 +184,16 @@ __device__ void cta_sum27(double acc[27], Shared& sh) {
 __device__ void assemble(cg::grid_group& grid, const DevProblem& P, Shared& sh, double* part, double* sums) {
     const int G = gridDim.x, c = blockIdx.x;
     for (int k = 0; k < P.K; ++k) {
+        if (P.pose_fixed[k]) continue;  // (uniform) a fixed pose's sums are zero
         double acc[27];
 #pragma unroll
         for (int e = 0; e < 27; ++e) acc[e] = 0.0;
-        if (!P.pose_fixed[k]) {
-            const int q0 = P.pose_ptr[k], q1 = P.pose_ptr[k + 1];
-            for (int q = q0 + c * blockDim.x + threadIdx.x; q < q1; q += G * blockDim.x) {
-                double rec[27];
-                pose_record(P, P.pose_obs[q], rec);
+        const int q0 = P.pose_ptr[k], q1 = P.pose_ptr[k + 1];
+        for (int q = q0 + c * blockDim.x + threadIdx.x; q < q1; q += G * blockDim.x) {
+            double rec[27];
+            pose_record(P, P.pose_obs[q], rec);
 #pragma unroll
-                for (int e = 0; e < 27; ++e) acc[e] += rec[e];
-            }
+            for (int e = 0; e < 27; ++e) acc[e] += rec[e];
         }
         cta_sum27(acc, sh);
         if (threadIdx.x < 27) part[((int64_t)c * P.K + k) * 27 + threadIdx.x] = sh.wpart[0][threadIdx.x];
@@ -207,7 +206,8 @@ __device__ void assemble(cg::grid_group& grid, const DevProblem& P, Shared& sh, 
         const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
         for (int i = c * nw + (threadIdx.x >> 5); i < 27 * P.K; i += G * nw) {
             double v = 0.0;
-            for (int b = lane; b < G; b += 32) v += __ldcg(part + (int64_t)b * 27 * P.K + i);
+            if (!P.pose_fixed[i / 27])
+                for (int b = lane; b < G; b += 32) v += __ldcg(part + (int64_t)b * 27 * P.K + i);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
             if (lane == 0) sums[i] = v;
@@ -306,20 +306,24 @@ __device__ void solve_step(const DevProblem& P, Shared& sh) {
     }
     ok = __syncthreads_and(ok);
     if (ok && mine) {
-        double y[6], x[6];
+        // forward and back substitution with the pivots' reciprocals (FP64
+        // division is a long instruction sequence on this GPU's slow FP64 pipe)
+        double y[6], x[6], rd[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) rd[i] = 1.0 / a[i][i];
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
             double v = sh.H[k][21 + i];
 #pragma unroll
             for (int m = 0; m < i; ++m) v -= a[i][m] * y[m];
-            y[i] = v / a[i][i];
+            y[i] = v * rd[i];
         }
 #pragma unroll
         for (int i = 5; i >= 0; --i) {
             double v = y[i];
 #pragma unroll
             for (int m = i + 1; m < 6; ++m) v -= a[m][i] * x[m];
-            x[i] = v / a[i][i];
+            x[i] = v * rd[i];
         }
 #pragma unroll
         for (int i = 0; i < 6; ++i) sh.delta[k][i] = x[i];
