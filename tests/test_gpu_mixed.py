@@ -137,3 +137,19 @@ def test_mixed_robust_with_information(zs_lib, oracle):
         h.set_problem(sc)
         r = h.solve(8)
     assert abs(r.chi2_final - ro.chi2_final) <= 1e-5 * ro.chi2_final
+
+
+def test_mixed_blocked_preconditioner_ragged(zs_lib):
+    """A mixed solve whose reduced system (n = 3600: 600 poses) takes the
+    blocked tensor-core preconditioner with a 16-column last panel: the same
+    accepted steps and the cost within the mixed form's 1e-6 of the FP64
+    solve."""
+    sc = scenes.walk_scene(K=600, L=20000, seed=71)  # M = 438,946
+    res = []
+    for precision in (0, 1):
+        with _ba(precision) as h:
+            h.set_problem(sc)
+            res.append(h.solve(4))
+    r64, r32 = res
+    assert r32.accepted == r64.accepted and r32.cholesky_failures == 0
+    assert abs(r32.chi2_final - r64.chi2_final) <= MIXED_COST_TOL * r64.chi2_final

@@ -63,6 +63,18 @@ def test_blocked_matches_numpy(zs_lib, n):
     assert _rel(X.astype(np.float64), X1.astype(np.float64)) < 1e-4
 
 
+def test_solve_form_3600(zs_lib):
+    """The form the solves choose at n = 3600: blocked (n >= 3072), 14 panels
+    of 256 and a last panel of 16 columns (a dataflow launch of one tile, the
+    products with K = 16)."""
+    from zeroslam_gb300 import ba
+
+    A = _spd(3600, 3600)
+    st, L, X, _ = ba.dense_chol_inverse_f32(A, form=0)
+    assert st == ba.ZS_OK
+    _check(A, L, X)
+
+
 def test_blocked_6000(zs_lib):
     """The size of the loop workload's reduced camera system: 24 panels."""
     from zeroslam_gb300 import ba

@@ -541,17 +541,28 @@ cudaError_t launch_chol_inverse_dag_ld(int n, int ld, float* F, float* X, float*
                                        int* epoch, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     static const int stall = stall_task_from_env();
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    static std::atomic<int> resident[kMaxDevices];
     const size_t smem = sizeof(Smem);
-    cudaError_t e = cudaFuncSetAttribute(k_chol_inverse_dag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_inverse_dag, t64::kThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    // co-resident CTAs of the launch on this device (the attribute set and the
+    // occupancy query once per device)
+    const int co = per_device(resident, [&] {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaFuncSetAttribute(k_chol_inverse_dag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_inverse_dag, t64::kThreads, smem) !=
+                cudaSuccess)
+            return 0;
+        return sms * per_sm;
+    });
+    if (co < 1) {
+        const cudaError_t e = cudaGetLastError();
+        return e != cudaSuccess ? e : cudaErrorInvalidConfiguration;
+    }
+    cudaError_t e;
     const int N = (n + kP - 1) / kP;
-    int blocks = sms * per_sm;
+    int blocks = co;
     if (blocks > N * N) blocks = N * N;
     Dag d;
     d.n = n;

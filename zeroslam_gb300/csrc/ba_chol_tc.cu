@@ -156,9 +156,14 @@ unsigned grid_of(int64_t items) { return (unsigned)std::max<int64_t>(1, std::min
 cudaError_t launch_gemm_nt64(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
                              float alpha, float beta, bool lower, const LmState* st, cudaStream_t s) {
     if (M <= 0 || N <= 0) return cudaSuccess;
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_gemm_nt64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemm64Smem);
-    if (attr != cudaSuccess) return attr;
+    static std::atomic<int> attr_set[kMaxDevices];
+    if (per_device(attr_set, [] {
+            return cudaFuncSetAttribute(k_gemm_nt64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kGemm64Smem) == cudaSuccess
+                       ? 1
+                       : 0;
+        }) < 1)
+        return cudaErrorInvalidConfiguration;
     const dim3 grid((N + t64::kP - 1) / t64::kP, (M + t64::kP - 1) / t64::kP);
     k_gemm_nt64<<<grid, t64::kThreads, kGemm64Smem, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta, lower ? 1 : 0,
                                                           st);
@@ -213,9 +218,13 @@ cudaError_t launch_chol_inverse_tc(int n, float* F, float* X, float* XT, float* 
     int* err = &st->timeout;
     // the bulk stream's products leave 16 SMs to the dataflow launches of the
     // chain (measured at n = 6000: 4.46 ms against 4.80 with no cap)
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    static std::atomic<int> sm_cache[kMaxDevices];
+    const int sms = per_device(sm_cache, [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n;
+    });
     const int lo_cap = sms > 32 ? sms - 16 : 0;
     cudaError_t e;
 #define ZS_TRY(x)                               \

@@ -9,9 +9,29 @@
 
 #include "ba_common.cuh"
 
+#include <atomic>
+
 struct zs_ba_attempt;
 
 namespace zs {
+
+// A value computed once per device (launch configurations: SM counts,
+// occupancies, function attributes) so that the launch paths of the solve
+// loop make no runtime queries: f() runs on the first call for the current
+// device and must return a positive value, or a non-positive one that is
+// not cached.
+constexpr int kMaxDevices = 64;
+template <typename F>
+int per_device(std::atomic<int> (&slot)[kMaxDevices], F f) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices) return f();
+    int v = slot[dev].load(std::memory_order_acquire);
+    if (v > 0) return v;
+    v = f();
+    if (v > 0) slot[dev].store(v, std::memory_order_release);
+    return v;
+}
 
 // Device-resident problem and structure. Observations are stored
 // landmark-major (sorted by landmark, then pose); "blocks" are the

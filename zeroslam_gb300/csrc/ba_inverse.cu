@@ -121,10 +121,14 @@ __global__ void __launch_bounds__(kThreads) k_refine(int n, const TS* __restrict
 }
 
 static int sm_count() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms > 0 ? sms : 1;
+    static std::atomic<int> cache[kMaxDevices];
+    const int v = per_device(cache, [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return sms;
+    });
+    return v > 0 ? v : 1;
 }
 
 template <typename TS, typename TX>
@@ -617,9 +621,16 @@ cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it,
     // the operator skips the weight products
     const bool id_w = P.loss.kind == 0 && P.obs_info == nullptr;  // 0: no robust loss
     const void* kern = id_w ? (const void*)k_pcg<true> : (const void*)k_pcg<false>;
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, 0);
-    if (e != cudaSuccess) return e;
+    static std::atomic<int> occ_cache[2][kMaxDevices];
+    const int occ = per_device(occ_cache[id_w ? 1 : 0], [&] {
+        int o = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kThreads, 0) == cudaSuccess ? o : 0;
+    });
+    if (occ < 1) {
+        const cudaError_t err = cudaGetLastError();
+        return err != cudaSuccess ? err : cudaErrorInvalidConfiguration;
+    }
+    cudaError_t e;
     const int blocks = std::max(1, std::min(kPcgMaxBlocks, occ * sm_count()));
     DevProblem Pv = P;
     const ObsJac* jac = W.jac;

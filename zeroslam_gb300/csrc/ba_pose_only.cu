@@ -464,17 +464,17 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
 }  // namespace
 
 int pose_only_grid(int64_t M) {
-    static int cached = 0;
-    if (!cached) {
+    static std::atomic<int> cache[kMaxDevices];
+    const int co = per_device(cache, [] {
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pose_only_lm, kThreads, 0);
-        cached = std::max(1, std::min(sms, sms * per));
         cudaGetLastError();
-    }
+        return std::max(1, std::min(sms, sms * per));
+    });
     // about 64 observations per CTA and pass, at most one CTA per SM
-    return (int)std::max<int64_t>(1, std::min<int64_t>(cached, (M + 63) / 64));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(co, (M + 63) / 64));
 }
 
 cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,

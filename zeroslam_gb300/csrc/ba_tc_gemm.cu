@@ -499,8 +499,14 @@ cudaError_t launch_tc_gemm_nt(int M, int N, int K, const float* A, int lda, cons
     if (K <= 0 || !tc_gemm_supported(lda, ldb, A, B)) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     if (!make_map(&ta, A, M, K, lda) || !make_map(&tb, B, N, K, ldb)) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-    if (e != cudaSuccess) return e;
+    static std::atomic<int> attr_set[kMaxDevices];
+    if (per_device(attr_set, [] {
+            return cudaFuncSetAttribute(k_tc_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem) ==
+                           cudaSuccess
+                       ? 1
+                       : 0;
+        }) < 1)
+        return cudaGetLastError() != cudaSuccess ? cudaErrorInvalidValue : cudaErrorInvalidConfiguration;
     TcArgs g{M, N, K, C, ldc, alpha, beta, lower ? 1 : 0, err, st};
     const int ntm = (M + kBM - 1) / kBM, ntn = (N + kBN - 1) / kBN;
     if (lower && M < N) return cudaErrorInvalidValue;  // lower: C square or taller than wide
