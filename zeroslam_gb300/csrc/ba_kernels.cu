@@ -578,12 +578,20 @@ __global__ void __launch_bounds__(kThreads) k_reduce_pose_runs(DevProblem P, con
             }
         }
     }
+    // The warps that took no chunk hold zeros: they skip their 27 FP64
+    // butterflies (warp-uniform) and their totals are written as the zeros
+    // the butterflies would have produced, so the sums are unchanged.
+    const int nchunks = e > s0 ? ((e - 1) >> 5) - (s0 >> 5) + 1 : 0;
+    if (warp * 32 < nchunks) {
 #pragma unroll
-    for (int c = 0; c < 27; ++c) {
-        double v = acc[c];
+        for (int c = 0; c < 27; ++c) {
+            double v = acc[c];
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) sh[warp][c] = v;
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) sh[warp][c] = v;
+        }
+    } else if (lane < 27) {
+        sh[warp][lane] = 0.0;
     }
     __syncthreads();
     if (threadIdx.x < 27) {
