@@ -160,15 +160,21 @@ struct Shared {
     int solve_ok, good;
 };
 
-// Warp butterflies and the warps in order: the CTA's 27 sums into sh.wpart[0].
-__device__ void cta_sum27(double acc[27], Shared& sh) {
+// Warp butterflies and the warps in order: the CTA's 27 sums into
+// sh.wpart[0]. Threads from `active` on took no observation: the warps made
+// of them skip their FP64 butterflies and give the zeros those would give.
+__device__ void cta_sum27(double acc[27], int active, Shared& sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp * 32 < active) {
 #pragma unroll
-    for (int e = 0; e < 27; ++e) {
-        double v = acc[e];
+        for (int e = 0; e < 27; ++e) {
+            double v = acc[e];
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) sh.wpart[warp][e] = v;
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) sh.wpart[warp][e] = v;
+        }
+    } else if (lane < 27) {
+        sh.wpart[warp][lane] = 0.0;
     }
     __syncthreads();
     if (threadIdx.x < 27) {
@@ -195,7 +201,8 @@ __device__ void assemble(cg::grid_group& grid, const DevProblem& P, Shared& sh, 
 #pragma unroll
             for (int e = 0; e < 27; ++e) acc[e] += rec[e];
         }
-        cta_sum27(acc, sh);
+        const int span = q1 - (q0 + c * (int)blockDim.x);  // this CTA's first pass covers min(span, blockDim)
+        cta_sum27(acc, span <= 0 ? 0 : min(span, (int)blockDim.x), sh);
         if (threadIdx.x < 27) part[((int64_t)c * P.K + k) * 27 + threadIdx.x] = sh.wpart[0][threadIdx.x];
         __syncthreads();
     }
