@@ -468,7 +468,8 @@ int zs_dense_cholesky_solve_noalloc(const double* A, int n, const double* b, dou
 int zs_dense_gemm_nt_tf32x3(const float* A, const float* B, float* C, int M, int N, int K, int lower, int max_ctas,
                             double* ms);
 
-/* The mixed form's FP32 preconditioner on a row-major n x n host matrix S:
+/* The mixed form's FP32 preconditioner on a row-major n x n host matrix S
+ * (only its lower triangle is read, as matrix::decompose_cholesky reads it):
  * the factor S = L L^T and X = L^-1 (both lower triangular; the upper
  * triangles of L and X come back zero; either may be NULL). form 0: as the
  * mixed solve chooses; 1: the dataflow kernel alone (64 x 64 tiles, any n);

@@ -99,6 +99,23 @@ def test_blocked_form_rules(zs_lib):
     _check(A, L, X)
 
 
+@pytest.mark.parametrize("n,form", [(200, 1), (640, 1), (1024, 2), (2100, 2)])
+def test_reads_lower_triangle_only(zs_lib, n, form):
+    """matrix::decompose_cholesky reads only S's lower triangle
+    (source/matrix_decomposition_cholesky.hpp:42-50); so do both forms (the
+    blocked form's trailing updates write only the lower triangle of the
+    diagonal blocks the dataflow kernel then factors). Garbage above the
+    diagonal leaves the factor and inverse unchanged."""
+    from zeroslam_gb300 import ba
+
+    A = _spd(n, n + 7)
+    rng = np.random.default_rng(n)
+    B = np.tril(A) + np.triu(3.0 + rng.random((n, n)), 1)
+    st, L, X, _ = ba.dense_chol_inverse_f32(B, form=form)
+    assert st == ba.ZS_OK
+    _check(A, L, X)
+
+
 @pytest.mark.parametrize("form", [1, 2])
 def test_indefinite_fails(zs_lib, form):
     """A matrix with negative eigenvalues fails a pivot in some panel: the

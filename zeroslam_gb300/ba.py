@@ -648,7 +648,8 @@ def dense_gemm_tf32x3(A, B, lower: bool = False, max_ctas: int = 0):
 
 def dense_chol_inverse_f32(S, form: int = 0):
     """(status, L, X = L^-1, device ms) of the mixed form's FP32
-    preconditioner on the symmetric matrix S; form 0 as the solve chooses,
+    preconditioner on the symmetric matrix S (its lower triangle is read);
+    form 0 as the solve chooses,
     1 the dataflow kernel alone, 2 the blocked tensor-core form."""
     lib = load()
     S = np.ascontiguousarray(S, dtype=np.float32)

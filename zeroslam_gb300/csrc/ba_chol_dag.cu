@@ -37,7 +37,6 @@
 
 #include "ba_internal.h"
 #include "ba_tile64.cuh"
-#include "ba_tiles.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -82,14 +81,17 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 }
 
 // Shared memory of one CTA.
+// A published row of the diagonal factor: four owner groups of 16 values,
+// kRowQ apart (20: the four groups' 16-byte reads fall in distinct banks).
+constexpr int kRowQ = 20;
+
 struct Smem {
     float a[2][kTileFloats];
     float b[2][kTileFloats];
-    float T[3 * kTile];  // the diagonal tile as three 32 x 32 tiles (ba_tiles.cuh)
     float inv[kTileFloats];
-    float dinv[kP];
-    float epsr[kP];
-    int flag;
+    __align__(16) float rowbuf[2][8 * kRowQ];  // row c of [C | I] (both halves), double-buffered
+    float pinv[2];                             // 1 / d_c
+    float rs[kP];                              // d_c^-1/2
 };
 
 // Thread 0 waits for *f == epoch; false when the launch was aborted (or this
@@ -206,94 +208,118 @@ __device__ bool accumulate(const Dag& d, int nq, Term term, Smem& sm, float acc[
                            [&](const float* A, const float* B, int kk) { tile_nt_acc(A, B, kk, acc); });
 }
 
-// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows):
-// L_jj stays in sm.T (store_diag_factor writes it out), L_jj^-1 goes into
-// X's tile (zeros above the diagonal) and its transpose into XT's. Returns 0
-// when a pivot fails its test (uniform).
-__device__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float eps, Smem& sm) {
-    const int ld = d.ld, k0 = kP * jb;
-    const int nbw = (kb + 31) >> 5;
-    float* T = sm.T;
-    float* Inv = sm.inv;
-    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
-        const int i = e >> 6, j = e & 63;
-        if (j > i || (i >> 5) >= nbw) continue;
-        const float v = (i < kb && j < kb) ? C[i * kPL + j] : (i == j ? 1.f : 0.f);
-        tile_at(T, i >> 5, j >> 5)[(i & 31) * kLd + (j & 31)] = v;
-    }
-    if (threadIdx.x < kP) sm.epsr[threadIdx.x] = eps;
-    __syncthreads();
-    if (!cta_cholesky<float>(T, nbw, kb, sm.epsr, sm.dinv, &sm.flag)) return 0;
-    // the inverse [Xa 0; -Xc Lb Xa  Xc] from the 32 x 32 tile inverses
-    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
-        const int r = e >> 6, c = e & 63;
-        float v = 0.f;
-        if ((r >> 5) == (c >> 5) && (r >> 5) < nbw) {
-            const int b = r >> 5, rr = r & 31, cc = c & 31;
-            v = rr == cc ? sm.dinv[r] : (cc < rr ? tile_at(T, b, b)[cc * kLd + rr] : 0.f);
-        }
-        Inv[r * kPL + c] = v;
-    }
-    __syncthreads();
-    if (nbw == 2) {
-        float w[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
+// Factors the diagonal tile C (64 x kPL in shared memory, kb valid rows) by
+// elimination on the augmented block [C | I]: at step c the raw row c is
+// published with the reciprocal of its pivot d_c, and every row r > c takes
+// m_rc = a_rc / d_c times it away from itself in both halves. After the 64
+// steps the right half is E = L'^-1 for C = L' D L'^T (L' unit lower), so
+// L^-1 = D^-1/2 E and L_rc = a_rc d_c^-1/2 (a_rc: row r's value in column c
+// when step c ran). The square roots and the final scaling stay off the
+// step-to-step path, which is one barrier, the pivot's reciprocal and one
+// fused multiply-add per step.
+//
+// Thread t owns row r = t / 4 and the columns j = 4 m + (t % 4), m < 16, of
+// both halves in registers (so a column's owner and register are fixed when
+// the step loop is unrolled); a published row is laid out by owner (q-major,
+// stride kRowQ) for 16-byte broadcast reads. Pivot test at the real rows:
+// d_c > eps (the reference's test, source/matrix_decomposition_cholesky.hpp:40,53).
+// L_jj^-1 goes into X's tile (zeros above the diagonal) and its transpose
+// into XT's; L_jj stays in sm.a[0] for store_diag_factor. Returns 0 when a
+// pivot fails its test (uniform).
+// (One out-of-line copy for both callers: the unrolled steps are long.)
+__device__ __noinline__ int eliminate_diag(float* X, float* XT, int ld, int k0, int kb, const float* C, float eps,
+                                           Smem& sm) {
+    const int t = threadIdx.x, r = t >> 2, q = t & 3, lane = t & 31;
+    const int grp = lane & ~3;
+    float a[16], v[16];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int e = threadIdx.x + q * blockDim.x;
-                w[q] = fmaf(tile_at(T, 1, 0)[(e >> 5) * kLd + m], Inv[m * kPL + (e & 31)], w[q]);
+    for (int m = 0; m < 16; ++m) {
+        const int j = 4 * m + q;
+        // from C's lower triangle only (the blocked form updates no more of a
+        // diagonal block): row r right of the diagonal is column r below it
+        a[m] = (r < kb && j < kb) ? (j <= r ? C[r * kPL + j] : C[j * kPL + r]) : (r == j ? 1.f : 0.f);
+        v[m] = r == j ? 1.f : 0.f;
+    }
+    int fail = 0;
+    float arc = __shfl_sync(0xffffffffu, a[0], grp);  // row r's column-0 value
+#pragma unroll
+    for (int c = 0; c < kP; ++c) {
+        constexpr int kHalf = 4 * kRowQ;
+        float* rowA = sm.rowbuf[c & 1];
+        float* rowE = rowA + kHalf;
+        const int mc = c >> 2;  // register of column c (owner q == c % 4)
+        if (r == c) {
+            float4* pa = reinterpret_cast<float4*>(rowA + q * kRowQ);
+#pragma unroll
+            for (int g = mc >> 2; g < 4; ++g) pa[g] = make_float4(a[4 * g], a[4 * g + 1], a[4 * g + 2], a[4 * g + 3]);
+            float4* pe = reinterpret_cast<float4*>(rowE + q * kRowQ);
+#pragma unroll
+            for (int g = 0; g <= (mc >> 2); ++g) pe[g] = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
+            if (q == (c & 3)) {
+                const float dc = a[mc];
+                if (c < kb && !(dc > eps)) fail = 1;
+                sm.pinv[c & 1] = __frcp_rn(dc);
+                const float rs = rsqrtf(dc);
+                sm.rs[c] = rs;
+                a[mc] = dc * rs;  // L_cc
             }
         }
         __syncthreads();
+        if (r > c) {
+            const float coef = arc * sm.pinv[c & 1];
+            const float4* pa = reinterpret_cast<const float4*>(rowA + q * kRowQ);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * blockDim.x;
-            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = w[q];
-        }
-        __syncthreads();
+            for (int g = mc >> 2; g < 4; ++g) {
+                const float4 u = pa[g];
+                const float uu[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = 0.f;
-#pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int e = threadIdx.x + q * blockDim.x;
-                w[q] = fmaf(Inv[(32 + (e >> 5)) * kPL + 32 + m], Inv[(32 + m) * kPL + (e & 31)], w[q]);
+                for (int k = 0; k < 4; ++k) {
+                    const int m = 4 * g + k;
+                    if (m > mc || (m == mc && q > (c & 3))) a[m] = fmaf(-coef, uu[k], a[m]);
+                }
             }
-        }
-        __syncthreads();
+            const float4* pe = reinterpret_cast<const float4*>(rowE + q * kRowQ);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = threadIdx.x + q * blockDim.x;
-            Inv[(32 + (e >> 5)) * kPL + (e & 31)] = -w[q];
+            for (int g = 0; g <= (mc >> 2); ++g) {
+                const float4 u = pe[g];
+                const float uu[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int m = 4 * g + k;
+                    if (m < mc || (m == mc && q <= (c & 3))) v[m] = fmaf(-coef, uu[k], v[m]);
+                }
+            }
+            if (q == (c & 3)) a[mc] = arc * sm.rs[c];  // L_rc
         }
-        __syncthreads();
+        if (c + 1 < kP) arc = __shfl_sync(0xffffffffu, a[(c + 1) >> 2], grp | ((c + 1) & 3));
     }
-    // the inverse out (row-major, zeros above the diagonal) and its transpose
-    // into XT: what the other tiles wait for (L_jj itself follows the flag)
-    for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
-        const int i = e >> 6, j = e & 63;
-        if (i >= kb || j >= kb) continue;
-        d.X[(int64_t)(k0 + i) * ld + k0 + j] = j <= i ? Inv[i * kPL + j] : 0.f;
-        d.XT[(int64_t)(k0 + i) * ld + k0 + j] = i <= j ? Inv[j * kPL + i] : 0.f;
+    if (__syncthreads_or(fail)) return 0;
+    const float rr = sm.rs[r];
+    float* Lout = sm.a[0];  // C is no longer read
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+        const int j = 4 * m + q;
+        v[m] *= rr;  // (L^-1)_rj, zero above the diagonal
+        Lout[r * kPL + j] = j <= r ? a[m] : 0.f;
+        if (r < kb && j < kb) {
+            X[(int64_t)(k0 + r) * ld + k0 + j] = v[m];
+            XT[(int64_t)(k0 + j) * ld + k0 + r] = v[m];
+        }
     }
     return 1;
 }
 
-// L_jj (row-major, zeros above the diagonal) into F from the factored tiles.
-// No task reads F's diagonal tiles; the solve test after the launch does.
+__device__ __forceinline__ int factor_diag(const Dag& d, int jb, int kb, const float* C, float eps, Smem& sm) {
+    return eliminate_diag(d.X, d.XT, d.ld, kP * jb, kb, C, eps, sm);
+}
+
+// L_jj (row-major, zeros above the diagonal) into F from sm.a[0]. No task
+// reads F's diagonal tiles; the solve test after the launch does.
 __device__ void store_diag_factor(const Dag& d, int jb, int kb, const Smem& sm) {
     const int ld = d.ld, k0 = kP * jb;
     for (int e = threadIdx.x; e < kP * kP; e += blockDim.x) {
         const int i = e >> 6, j = e & 63;
-        if (i >= kb || j >= kb) continue;
-        float l = 0.f;
-        if (j <= i) {
-            const float* Tb = tile_at(sm.T, i >> 5, j >> 5);
-            l = (j == i) ? Tb[(i & 31) * (kLd + 1)] : Tb[(i & 31) * kLd + (j & 31)];
-        }
-        d.F[(int64_t)(k0 + i) * ld + k0 + j] = l;
+        if (i < kb && j < kb) d.F[(int64_t)(k0 + i) * ld + k0 + j] = sm.a[0][i * kPL + j];
     }
 }
 
