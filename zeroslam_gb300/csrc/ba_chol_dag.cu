@@ -258,10 +258,7 @@ __device__ __noinline__ int eliminate_diag(float* X, float* XT, int ld, int k0, 
             if (q == (c & 3)) {
                 const float dc = a[mc];
                 if (c < kb && !(dc > eps)) fail = 1;
-                sm.pinv[c & 1] = __frcp_rn(dc);
-                const float rs = rsqrtf(dc);
-                sm.rs[c] = rs;
-                a[mc] = dc * rs;  // L_cc
+                sm.pinv[c & 1] = __fdividef(1.f, dc);
             }
         }
         __syncthreads();
@@ -289,10 +286,13 @@ __device__ __noinline__ int eliminate_diag(float* X, float* XT, int ld, int k0, 
                     if (m < mc || (m == mc && q <= (c & 3))) v[m] = fmaf(-coef, uu[k], v[m]);
                 }
             }
-            if (q == (c & 3)) a[mc] = arc * sm.rs[c];  // L_rc
         }
         if (c + 1 < kP) arc = __shfl_sync(0xffffffffu, a[(c + 1) >> 2], grp | ((c + 1) & 3));
     }
+    // d_r^-1/2 from each row's pivot, still in its owner's register
+#pragma unroll
+    for (int m = 0; m < 16; ++m)
+        if (4 * m + q == r) sm.rs[r] = rsqrtf(a[m]);
     if (__syncthreads_or(fail)) return 0;
     const float rr = sm.rs[r];
     float* Lout = sm.a[0];  // C is no longer read
@@ -300,7 +300,7 @@ __device__ __noinline__ int eliminate_diag(float* X, float* XT, int ld, int k0, 
     for (int m = 0; m < 16; ++m) {
         const int j = 4 * m + q;
         v[m] *= rr;  // (L^-1)_rj, zero above the diagonal
-        Lout[r * kPL + j] = j <= r ? a[m] : 0.f;
+        Lout[r * kPL + j] = j <= r ? a[m] * sm.rs[j] : 0.f;
         if (r < kb && j < kb) {
             X[(int64_t)(k0 + r) * ld + k0 + j] = v[m];
             XT[(int64_t)(k0 + j) * ld + k0 + r] = v[m];
