@@ -16,7 +16,8 @@ collective): value = iterations of all ranks / max-over-ranks time.
 The same JSON line carries the other configurations and rows as sections:
 batched_windows (256 local windows, with a CPU baseline over every host
 core), loop_4m (the 4M-observation loop), adjoint (gradients of the solved
-state), pose_only (a tracking solve in one launch against the general path),
+state), pose_only (a tracking solve in one launch against the general path, and 256
+tracking windows in one launch against the general batched path),
 map_cull (map::cull), map_optimise (map::optimise over map arrays) and
 matching (feature::find_matches). --map-only prints the last three
 alone; --no-batch / --no-loop / --no-adjoint / --no-cull skip sections.
@@ -491,7 +492,9 @@ def pose_only_section(args, dist: Dist) -> dict:
     """zeroslam's tracking solve (map optimise(1, true, 50)): one free pose among
     four fixed ones, every landmark fixed, 50 LM iterations; the one-launch
     path (k_pose_only_lm) against the general path on the same handle type
-    (device time of zs_ba_solve, FP64; one warm-up, `steps` timed solves)."""
+    (device time of zs_ba_solve, FP64; one warm-up, `steps` timed solves);
+    then 256 such problems as one batch (k_pose_only_windows, a CTA per
+    window) against the general batched path."""
     from zeroslam_gb300 import ba, scenes
 
     sc = scenes.arc_scene(5, 1500, seed=51)
@@ -513,6 +516,33 @@ def pose_only_section(args, dist: Dist) -> dict:
             out[name] = {"ms_per_solve": dist.max(float(np.mean(ms))), "kernel_launches": int(launches),
                          "attempts": r.attempts, "chi2_final": r.chi2_final}
     out["speedup"] = out["general_path"]["ms_per_solve"] / out["one_launch"]["ms_per_solve"]
+    # many tracking problems at once (zs_ba_solve_batch): 256 windows of 5
+    # poses (1 free) and 1,500 fixed landmarks, one CTA per window, against
+    # the general batched path
+    wins = []
+    for i in range(256):
+        w = scenes.arc_scene(5, 1500, seed=1000 + i)
+        w.landmark_fixed[:] = 1
+        w.pose_fixed[:] = 1
+        w.pose_fixed[2] = 0
+        wins.append(w)
+    bat = {"workload": f"{len(wins)} tracking windows: 1 free pose of 5, 1500 fixed landmarks each, "
+                       f"M={sum(w.M for w in wins)} observations, 50 LM iterations, FP64"}
+    for name, path in (("one_launch", 1), ("general_batched", 0)):
+        with ba.BundleAdjuster(precision=ba.FP64, device=dist.local, pose_only_path=path) as h:
+            h.set_batch(wins)
+            h.solve_batch(50)
+            ms, launches = [], 0
+            for _ in range(max(1, args.steps)):
+                h.reset_state()
+                _, _, br = h.solve_batch(50)
+                ms.append(br.ms_total)
+                launches = br.kernel_launches
+            t = dist.max(float(np.mean(ms)))
+            bat[name] = {"ms_per_batch": t, "windows_per_s": len(wins) / (t * 1e-3), "kernel_launches": int(launches),
+                         "attempts": int(br.attempts)}
+    bat["speedup"] = bat["general_batched"]["ms_per_batch"] / bat["one_launch"]["ms_per_batch"]
+    out["batched"] = bat
     return out
 
 

@@ -88,7 +88,8 @@ typedef struct zs_ba_options {
                                    after tuning), or NULL for a per-process cache only */
     int32_t pose_only_path;     /* 1: a single problem with every landmark fixed, at most 64 poses and
                                    at most 4 of them free (zeroslam's tracking mode) runs its whole LM
-                                   loop in one launch, in FP64 in both precisions; 0: the general
+                                   loop in one launch, in FP64 in both precisions; so does a batch whose
+                                   landmarks are all fixed, one CTA per window; 0: the general
                                    path (1) */
 } zs_ba_options;
 
@@ -223,7 +224,9 @@ int zs_ba_set_batch(zs_ba_handle* h, int num_windows, const zs_ba_problem* windo
 /* Solves every window of the batch as zs_ba_solve would (same iterations /
  * use_relative semantics per window). window_reports (may be NULL): one
  * report per window; rep (may be NULL): the batch summary. Returns the
- * accepted steps summed over windows, or a negative status. */
+ * accepted steps summed over windows, or a negative status. A batch whose
+ * landmarks are all fixed (tracking problems) takes the pose-only path
+ * (options.pose_only_path): one launch, one CTA per window, in FP64. */
 int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_report* window_reports,
                       zs_ba_batch_report* rep);
 /* With options.profile: per window, the SM cycles the last zs_ba_solve_batch

@@ -2,7 +2,9 @@
 map optimise(1, true, 50), source/slam.hpp:316,387,469): the landmark blocks
 vanish (zero H_ll inverses, no H_pl), S is block diagonal (one 6 x 6 block
 per pose) and the solve reduces to independent pose updates. Single problems
-in both forms and batched windows are compared with the oracle."""
+in both forms and batched windows are compared with the oracle; the
+one-launch paths (a single problem over the whole grid, a batch with one
+CTA per window) with the oracle and with the general paths."""
 
 import numpy as np
 import pytest
@@ -145,3 +147,100 @@ def test_one_launch_repeats_and_limits(zs_lib):
         h.set_problem(five)
         r = h.solve(3)
     assert r.kernel_launches > 1 and r.accepted >= 1
+
+
+# ---- batches of pose-only windows: one CTA per window ----
+
+
+def _tracking_batch(seed):
+    """Tracking windows of several shapes: one to four free poses among up
+    to 32, a window with every pose fixed, a lone fixed pose and a window
+    without observations (every landmark fixed throughout)."""
+    rng = np.random.default_rng(seed)
+    wins = []
+    for i in range(10):
+        k = int(rng.integers(2, 33))
+        sc = _pose_only(scenes.arc_scene(k, int(rng.integers(200, 1500)), seed=seed + i))
+        sc.pose_fixed[:] = 1
+        free = rng.choice(k, size=min(k, 1 + i % 4), replace=False)
+        sc.pose_fixed[free] = 0
+        wins.append(sc)
+    allfixed = _pose_only(scenes.arc_scene(6, 300, seed=seed + 20))
+    allfixed.pose_fixed[:] = 1
+    lone = _pose_only(scenes.arc_scene(1, 40, seed=seed + 21))
+    empty = _pose_only(scenes.arc_scene(4, 50, seed=seed + 22))
+    empty.obs_pose = empty.obs_pose[:0]
+    empty.obs_landmark = empty.obs_landmark[:0]
+    empty.obs_uv = empty.obs_uv[:0]
+    return wins[:4] + [allfixed, lone] + wins[4:7] + [empty] + wins[7:]
+
+
+def _run_batch(wins, iterations, precision=0, use_relative=False, **kw):
+    with _ba(precision, **kw) as h:
+        h.set_batch(wins)
+        acc, reps, brep = h.solve_batch(iterations, use_relative)
+        states = [h.get_window_state(w) for w in range(len(wins))]
+    return acc, reps, brep, states
+
+
+@pytest.mark.parametrize("use_relative", [False, True])
+def test_windows_match_general_batch(zs_lib, use_relative):
+    """The one-launch batch takes the general batched path's decisions in
+    every window (same accepted steps, attempts, iterations and Cholesky
+    failures) and reaches its cost and poses; empty and fully fixed windows
+    report as the general path reports them."""
+    wins = _tracking_batch(71)
+    a1, r1, b1, s1 = _run_batch(wins, 30, use_relative=use_relative)
+    a0, r0, b0, s0 = _run_batch(wins, 30, use_relative=use_relative, pose_only_path=0)
+    assert b1.kernel_launches == 1 and b1.graph_launches == 0 and b0.graph_launches == 1
+    assert a1 == a0
+    for w in range(len(wins)):
+        x, y = r1[w], r0[w]
+        assert (x.accepted, x.attempts, x.iterations, x.cholesky_failures) == \
+            (y.accepted, y.attempts, y.iterations, y.cholesky_failures), w
+        assert abs(x.chi2_initial - y.chi2_initial) <= 1e-12 * abs(y.chi2_initial) + 1e-300, w
+        assert abs(x.chi2_final - y.chi2_final) <= 1e-11 * abs(y.chi2_final) + 1e-300, w
+        assert rel_err(s1[w][0], s0[w][0]) < 1e-9, w
+        assert np.array_equal(s1[w][1], wins[w].landmarks)  # fixed landmarks do not move
+        fixed = wins[w].pose_fixed.astype(bool)
+        assert np.array_equal(s1[w][0][fixed], wins[w].poses[fixed]), w
+
+
+def test_windows_against_oracle(zs_lib, oracle):
+    """Every attempt's decision over the first three iterations (steps far
+    above rounding: converged tracking problems reach trial steps that change
+    the cost by ~1e-16 relative, where accept or reject follows the last bit
+    of either implementation), and the cost and poses after twenty."""
+    wins = _tracking_batch(73)[:6]
+    _, reps, _, _ = _run_batch(wins, 3)
+    _, reps20, _, states = _run_batch(wins, 20)
+    for w, sc in enumerate(wins):
+        _, _, ro = oracle.solve(sc, 3)
+        r = reps[w]
+        assert (r.accepted, r.attempts, r.iterations, r.cholesky_failures) == \
+            (ro.accepted, ro.attempts, ro.iterations, ro.chol_failures), w
+        poses, _, ro = oracle.solve(sc, 20)
+        assert abs(reps20[w].chi2_final - ro.chi2_final) <= COST_TOL * ro.chi2_final + 1e-300, w
+        assert rel_err(states[w][0], poses) < 1e-7, w
+
+
+def test_windows_robust_information_and_forms(zs_lib):
+    """Huber loss with information matrices, against the general batched
+    path; the mixed-form handle takes the same FP64 path (identical bits)."""
+    wins = []
+    for i in range(6):
+        sc = _pose_only(scenes.arc_scene(5 + i, 600, seed=80 + i, huber=True))
+        sc.pose_fixed[:] = 1
+        sc.pose_fixed[[0, 2 + i % 3]] = 0
+        rng = np.random.default_rng(90 + i)
+        s = rng.uniform(0.5, 2.0, size=(sc.M, 1))
+        sc.obs_info = np.concatenate([1.0 * s, 0.2 * s, 0.2 * s, 0.6 * s], axis=1)
+        wins.append(sc)
+    _, r1, _, s1 = _run_batch(wins, 15)
+    _, r0, _, _ = _run_batch(wins, 15, pose_only_path=0)
+    _, rm, bm, sm = _run_batch(wins, 15, precision=1)
+    assert bm.kernel_launches == 1
+    for w in range(len(wins)):
+        assert (r1[w].accepted, r1[w].attempts) == (r0[w].accepted, r0[w].attempts), w
+        assert abs(r1[w].chi2_final - r0[w].chi2_final) <= 1e-11 * r0[w].chi2_final, w
+        assert rm[w].chi2_final == r1[w].chi2_final and np.array_equal(sm[w][0], s1[w][0]), w

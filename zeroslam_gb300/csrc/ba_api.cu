@@ -1316,6 +1316,13 @@ bool pose_only(const zs_ba_handle* h) {
            h->free_poses <= kPoseOnlyMaxFree;
 }
 
+// A batch whose landmarks are all fixed (every window at most
+// ZS_BATCH_MAX_POSES <= kPoseOnlyMaxK poses): one CTA per window
+// (k_pose_only_windows).
+bool pose_only_batch(const zs_ba_handle* h) {
+    return h->opt.pose_only_path != 0 && h->batch && h->free_landmarks == 0;
+}
+
 int pose_only_solve(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_report* rep) {
     cudaStream_t s = h->stream;
     const zs_ba_options& o = h->opt;
@@ -2052,7 +2059,8 @@ int solve_batch_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_r
     cudaStream_t s = h->stream;
     zs_ba_batch_report r{};
     r.windows = P.nwin;
-    batch_tune<T>(h);
+    const bool po = pose_only_batch(h);
+    if (!po) batch_tune<T>(h);
     for (int b = 0; b < kBatchBuckets; ++b) {
         r.bucket_windows[b] = B.bucket_off[b + 1] - B.bucket_off[b];
         r.bucket_threads[b] = B.threads[b];
@@ -2065,7 +2073,14 @@ int solve_batch_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_r
     }
     if (B.prof) ZS_CUDA(cudaMemsetAsync(B.prof, 0, sizeof(long long) * P.nwin * kBatchProfSlots, s));
     const long long launches0 = launch_counter();
-    if (h->opt.batch_graph) {
+    if (po) {
+        const zs_ba_options& o = h->opt;
+        PoseOnlyCtl ctl{o.tau, o.diagonal_clamp, o.legacy_stop, o.relative_tolerance, o.chi2_floor,
+                        o.max_failures, iterations, use_relative ? 1 : 0, 0};
+        ZS_CUDA(cudaEventRecord(h->ev0, s));
+        ZS_CUDA(launch_pose_only_windows(h->P, ctl, B.ctl, B.st, s));
+        ZS_CUDA(cudaEventRecord(h->ev1, s));
+    } else if (h->opt.batch_graph) {
         if (!h->bexec || h->bgraph_iters != iterations || h->bgraph_rel != (int)use_relative) {
             h->release_graph();
             build_batch_graph<T>(h, prm);
@@ -2096,8 +2111,10 @@ int solve_batch_impl(zs_ba_handle* h, int iterations, bool use_relative, zs_ba_r
     int rounds = 0;
     ZS_CUDA(cudaMemcpyAsync(st.data(), B.st, sizeof(LmState) * P.nwin, cudaMemcpyDeviceToHost, s));
     ZS_CUDA(cudaMemcpyAsync(ctl.data(), B.ctl, sizeof(WinCtl) * P.nwin, cudaMemcpyDeviceToHost, s));
-    ZS_CUDA(cudaMemcpyAsync(&rounds, B.rounds, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!po) ZS_CUDA(cudaMemcpyAsync(&rounds, B.rounds, sizeof(int), cudaMemcpyDeviceToHost, s));
     ZS_CUDA(cudaStreamSynchronize(s));
+    if (po)  // a window's attempts run back to back in its CTA: the longest is the rounds' count
+        for (const WinCtl& c : ctl) rounds = std::max(rounds, c.attempts);
     r.rounds = rounds;
     r.ms_total = ms;
     r.kernel_launches = r.graph_launches ? h->bpro_launches + (long long)rounds * h->bbody_launches
@@ -2249,7 +2266,7 @@ int zs_ba_solve_batch(zs_ba_handle* h, int iterations, int use_relative, zs_ba_r
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h->has_problem) return ZS_ERR_NO_PROBLEM;
     if (!h->batch) return ZS_ERR_INVALID;
-    if (mixed_tukey(h)) return ZS_ERR_UNSUPPORTED;
+    if (mixed_tukey(h) && !pose_only_batch(h)) return ZS_ERR_UNSUPPORTED;
     if (iterations < 0) return ZS_ERR_INVALID;
     try {
         ZS_CUDA(cudaSetDevice(h->device));

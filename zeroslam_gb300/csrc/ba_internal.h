@@ -448,6 +448,11 @@ struct PoseOnlyOut {
     double chi2_initial, chi2_final, lambda_final;
 };
 int pose_only_grid(int64_t M);
+// A batch whose landmarks are all fixed: one CTA per window (at most
+// kPoseOnlyMaxK poses each), reports into wctl / wst as the general batched
+// path's per-window control and state.
+cudaError_t launch_pose_only_windows(const DevProblem& P, const PoseOnlyCtl& ctl, WinCtl* wctl, LmState* wst,
+                                    cudaStream_t s);
 cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,
                                 double* part, double* sums, double* cpart, int grid, cudaStream_t s);
 

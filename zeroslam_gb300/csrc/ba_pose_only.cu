@@ -256,9 +256,9 @@ __device__ double cta_max(double v, double* red) {
 }
 
 // The damped blocks' factors and the step delta (sh.solve_ok, sh.delta).
-__device__ void solve_step(const DevProblem& P, Shared& sh) {
+__device__ void solve_step(int K, Shared& sh) {
     const int k = threadIdx.x;
-    const bool mine = k < P.K;
+    const bool mine = k < K;
     const double lam = sh.lambda;
     double a[6][6];
 #pragma unroll
@@ -339,18 +339,73 @@ __device__ void solve_step(const DevProblem& P, Shared& sh) {
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnlyCtl ctl, PoseOnlyOut* out,
-                                                           zs_ba_attempt* hist, double* part, double* sums,
-                                                           double* cpart) {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ Shared sh;
+// The window's H and b (its poses k0 .. k1, sh.H[k - k0]) by one CTA.
+__device__ void assemble_window(const DevProblem& P, int k0, int k1, Shared& sh) {
+    for (int k = k0; k < k1; ++k) {
+        if (!P.pose_fixed[k]) {  // (uniform) a fixed pose's sums are zero
+            double acc[27];
+#pragma unroll
+            for (int e = 0; e < 27; ++e) acc[e] = 0.0;
+            const int q0 = P.pose_ptr[k], q1 = P.pose_ptr[k + 1];
+            for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+                double rec[27];
+                pose_record(P, P.pose_obs[q], rec);
+#pragma unroll
+                for (int e = 0; e < 27; ++e) acc[e] += rec[e];
+            }
+            cta_sum27(acc, min(max(q1 - q0, 0), (int)blockDim.x), sh);
+            if (threadIdx.x < 27) sh.H[k - k0][threadIdx.x] = sh.wpart[0][threadIdx.x];
+        } else if (threadIdx.x < 27) {
+            sh.H[k - k0][threadIdx.x] = 0.0;
+        }
+        __syncthreads();
+    }
+}
+
+// The cost of the window's observations (pose-major positions q0 .. q1), by
+// one CTA; every thread gets it.
+__device__ double cost_window(const DevProblem& P, int64_t q0, int64_t q1, Shared& sh) {
+    double v = 0.0;
+    for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) v += obs_cost(P, P.pose_obs[q]);
+    return block_sum(v, sh.red);
+}
+
+// Who works on one problem: the whole cooperative grid (a single problem,
+// poses 0 .. P.K) or one CTA (a window of a batch, poses k0 .. k0 + K).
+struct GridTeam {
+    cg::grid_group grid;
+    double* part;
+    double* sums;
+    double* cpart;
+    __device__ void sync() { grid.sync(); }
+    __device__ bool lead() const { return blockIdx.x == 0; }
+    __device__ void assemble(const DevProblem& P, Shared& sh) { zs::assemble(grid, P, sh, part, sums); }
+    __device__ double cost(const DevProblem& P, Shared& sh) { return zs::cost(grid, P, sh, cpart); }
+};
+struct WindowTeam {
+    int k0, k1;
+    int64_t q0, q1;
+    __device__ void sync() { __syncthreads(); }
+    __device__ bool lead() const { return true; }
+    __device__ void assemble(const DevProblem& P, Shared& sh) { assemble_window(P, k0, k1, sh); }
+    __device__ double cost(const DevProblem& P, Shared& sh) { return cost_window(P, q0, q1, sh); }
+};
+
+// The Levenberg-Marquardt loop of factor_graph::solve
+// (source/factor_graph.hpp:506-615) over poses k0 .. k0 + K (every landmark
+// fixed). active = false skips the loop (the window reports no iteration).
+// hist (may be null): the attempts, up to ctl.hist_cap. The lead CTA updates
+// and restores the poses; every CTA takes the same decisions.
+template <typename Team>
+__device__ PoseOnlyOut lm_loop(const DevProblem& P, int k0, int K, const PoseOnlyCtl& ctl, bool active, Team& team,
+                               Shared& sh, zs_ba_attempt* hist) {
     const int t = threadIdx.x;
-    const bool lead = blockIdx.x == 0;  // the CTA that writes poses, history and the report
+    const bool lead = team.lead();
     // the initial system, cost and damping (tau min(clamp, max diag H))
-    assemble(grid, P, sh, part, sums);
-    const double c0 = cost(grid, P, sh, cpart);
+    team.assemble(P, sh);
+    const double c0 = team.cost(P, sh);
     double dmax = 0.0;
-    if (t < P.K)
+    if (t < K)
 #pragma unroll
         for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(sh.H[t][kDiag6[i]]));
     const double mdiag = cta_max(dmax, sh.red);
@@ -362,20 +417,20 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
     __syncthreads();
     int iterations = 0, attempts = 0, accepted = 0, chol_fail = 0, nhist = 0;
     const double legacy = ctl.legacy_stop * c0;
-    for (int it = 0; it < ctl.iterations; ++it) {
+    for (int it = 0; active && it < ctl.iterations; ++it) {
         iterations = it + 1;
         const double last = sh.chi2;
         int failures = 0;
         while (failures < ctl.max_failures) {
-            solve_step(P, sh);
+            solve_step(K, sh);
             const bool ok = sh.solve_ok != 0;
             double chi2_new = sh.chi2, scale = 0.0;
             if (ok) {
                 // trial state (poses; every landmark is fixed), the model's
                 // gain delta^T (lambda delta + b) + 1e-3 and the cost there
                 double sc = 0.0;
-                if (t < P.K) {
-                    double* pp = P.pose + (int64_t)t * kPoseStride;
+                if (t < K) {
+                    double* pp = P.pose + (int64_t)(k0 + t) * kPoseStride;
 #pragma unroll
                     for (int i = 0; i < kPoseStride; ++i) sh.bk[t][i] = pp[i];
 #pragma unroll
@@ -385,9 +440,10 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
                     }
                 }
                 scale = block_sum(sc, sh.red) + 1e-3;
-                if (lead && t < P.K && !P.pose_fixed[t]) pose_plus(P.pose + (int64_t)t * kPoseStride, sh.delta[t]);
-                grid.sync();  // the trial poses are visible to every CTA
-                chi2_new = cost(grid, P, sh, cpart);
+                if (lead && t < K && !P.pose_fixed[k0 + t])
+                    pose_plus(P.pose + (int64_t)(k0 + t) * kPoseStride, sh.delta[t]);
+                team.sync();  // the trial poses are visible to every CTA
+                chi2_new = team.cost(P, sh);
             }
             // source/factor_graph.hpp:542-591 (k_decide), in every CTA
             if (t == 0) {
@@ -416,7 +472,7 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
             const bool good = sh.good != 0;
             const double lam = sh.lambda;
             ++attempts;
-            if (lead && t == 0 && nhist < ctl.hist_cap) {
+            if (hist && lead && t == 0 && nhist < ctl.hist_cap) {
                 zs_ba_attempt a{};
                 a.iteration = it;
                 a.attempt = failures;
@@ -431,12 +487,12 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
             if (ok) {
                 // a rejected step is rolled back while lambda stays finite
                 // (k_rollback); every CTA waits for the poses it will read
-                if (lead && !good && isfinite(lam) && t < P.K) {
-                    double* pp = P.pose + (int64_t)t * kPoseStride;
+                if (lead && !good && isfinite(lam) && t < K) {
+                    double* pp = P.pose + (int64_t)(k0 + t) * kPoseStride;
 #pragma unroll
                     for (int i = 0; i < kPoseStride; ++i) pp[i] = sh.bk[t][i];
                 }
-                grid.sync();
+                team.sync();
             }
             if (!ok) {
                 ++chol_fail;
@@ -447,7 +503,7 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
             if (good) {
                 ++accepted;
                 if (!isfinite(lam)) break;
-                assemble(grid, P, sh, part, sums);  // the next iteration's system at the accepted state
+                team.assemble(P, sh);  // the next iteration's system at the accepted state
                 break;
             }
             if (!isfinite(lam)) break;
@@ -456,15 +512,60 @@ __global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnl
         const double thr = ctl.use_relative ? ctl.rel_tol * fmax(last, ctl.floor) : legacy;
         if (failures >= ctl.max_failures || (last - sh.chi2) < thr || !isfinite(sh.lambda)) break;
     }
-    if (lead && t == 0) {
-        out->iterations = iterations;
-        out->attempts = attempts;
-        out->accepted = accepted;
-        out->cholesky_failures = chol_fail;
-        out->history = nhist;
-        out->chi2_initial = c0;
-        out->chi2_final = sh.chi2;
-        out->lambda_final = sh.lambda;
+    PoseOnlyOut o;
+    o.iterations = iterations;
+    o.attempts = attempts;
+    o.accepted = accepted;
+    o.cholesky_failures = chol_fail;
+    o.history = nhist;
+    o.chi2_initial = c0;
+    o.chi2_final = sh.chi2;
+    o.lambda_final = sh.lambda;
+    return o;
+}
+
+__global__ void __launch_bounds__(kThreads) k_pose_only_lm(DevProblem P, PoseOnlyCtl ctl, PoseOnlyOut* out,
+                                                           zs_ba_attempt* hist, double* part, double* sums,
+                                                           double* cpart) {
+    __shared__ Shared sh;
+    GridTeam team{cg::this_grid(), part, sums, cpart};
+    const PoseOnlyOut o = lm_loop(P, 0, P.K, ctl, true, team, sh, hist);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = o;
+}
+
+// A batch of windows whose landmarks are all fixed (tracking problems solved
+// together): one CTA per window runs the loop above on the window's poses,
+// each window with its own damping, decisions and stops, as the general
+// batched path (ba_batch.cu) runs them, and reports into the batch's
+// per-window control and state. A window without observations, or with
+// neither poses nor landmarks, runs no iteration (k_binit's rule).
+__global__ void __launch_bounds__(kThreads) k_pose_only_windows(DevProblem P, PoseOnlyCtl ctl, WinCtl* wctl,
+                                                                LmState* wst) {
+    __shared__ Shared sh;
+    const int w = blockIdx.x;
+    const int k0 = P.win_pose0[w], k1 = P.win_pose0[w + 1];
+    WindowTeam team{k0, k1, P.pose_ptr[k0], P.pose_ptr[k1]};
+    const bool has_obs = team.q1 > team.q0;
+    const bool active = ctl.iterations > 0 && ctl.max_failures > 0 && has_obs &&
+                        (k1 > k0 || P.win_lm0[w + 1] > P.win_lm0[w]);
+    const PoseOnlyOut o = lm_loop(P, k0, k1 - k0, ctl, active, team, sh, nullptr);
+    if (threadIdx.x == 0) {
+        WinCtl c{};
+        c.iterations = o.iterations;
+        c.it = o.iterations;
+        c.accepted = o.accepted;
+        c.attempts = o.attempts;
+        c.chol_failures = o.cholesky_failures;
+        c.last = o.chi2_final;
+        c.legacy = ctl.legacy_stop * o.chi2_initial;
+        c.chi2_initial = o.chi2_initial;
+        wctl[w] = c;
+        LmState st{};
+        st.chi2 = o.chi2_final;
+        st.chi2_new = o.chi2_final;
+        st.lambda = o.lambda_final;
+        st.solve_ok = 1;
+        wst[w] = st;
     }
 }
 
@@ -482,6 +583,14 @@ int pose_only_grid(int64_t M) {
     });
     // about 64 observations per CTA and pass, at most one CTA per SM
     return (int)std::max<int64_t>(1, std::min<int64_t>(co, (M + 63) / 64));
+}
+
+cudaError_t launch_pose_only_windows(const DevProblem& P, const PoseOnlyCtl& ctl, WinCtl* wctl, LmState* wst,
+                                    cudaStream_t s) {
+    if (P.nwin < 1) return cudaSuccess;
+    k_pose_only_windows<<<P.nwin, kThreads, 0, s>>>(P, ctl, wctl, wst);
+    note_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_pose_only_lm(const DevProblem& P, const PoseOnlyCtl& ctl, PoseOnlyOut* out, zs_ba_attempt* hist,
