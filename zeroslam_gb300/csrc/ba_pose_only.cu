@@ -29,6 +29,11 @@
 // path (solve_impl). Both precisions take this path in FP64: there is no
 // Schur complement or dense factor to make cheaper. Every sum has a fixed
 // order for a given grid size: results repeat bit for bit.
+//
+// Batches of such windows (many tracking problems at once) run the same loop
+// with one CTA per window (k_pose_only_windows): the window's sums stay in
+// its CTA, and the loop is shared with the single-problem kernel through a
+// team type (GridTeam / WindowTeam: who sums, who synchronises).
 #include <cooperative_groups.h>
 
 #include <algorithm>
