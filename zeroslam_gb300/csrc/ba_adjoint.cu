@@ -163,22 +163,23 @@ __global__ void __launch_bounds__(kThreads) k_adj_reduce_lm(DevProblem P, const 
     for (int i = 0; i < 3; ++i) out[P.n + 3LL * l + i] = P.lm_fixed[l] ? 0.0 : a[P.n + 3LL * l + i] - s[i];
 }
 
-__global__ void __launch_bounds__(kThreads) k_adj_reduce_pose(DevProblem P, const double* __restrict__ part,
-                                                              const double* __restrict__ a, double* out) {
-    __shared__ double sh[kThreads];
-    const int k = blockIdx.x;
-    double s[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = P.pose_ptr[k] + threadIdx.x; i < P.pose_ptr[k + 1]; i += blockDim.x) {
-        const int64_t o = P.pose_obs[i];
+// The pose rows of a - H v (launch_pose_sums6): position q's six pose terms
+// of H v, and the pose's output (zero for a fixed pose).
+struct AdjPoseTerm {
+    const double* part;
+    __device__ void operator()(const DevProblem& P, int q, double s[6]) const {
+        const int64_t o = P.pose_obs[q];
 #pragma unroll
         for (int c = 0; c < 6; ++c) s[c] += part[(int64_t)c * P.M + o];
     }
-#pragma unroll 1
-    for (int c = 0; c < 6; ++c) {
-        const double v = block_sum(s[c], sh);
-        if (threadIdx.x == 0) out[6LL * k + c] = P.pose_fixed[k] ? 0.0 : a[6LL * k + c] - v;
+};
+struct AdjPoseOut {
+    const double* a;
+    double* out;
+    __device__ void operator()(const DevProblem& P, int k, int c, double v) const {
+        out[6LL * k + c] = P.pose_fixed[k] ? 0.0 : a[6LL * k + c] - v;
     }
-}
+};
 
 // y = alpha x + beta y
 __global__ void __launch_bounds__(kThreads) k_adj_axpby(int64_t N, double alpha, const double* __restrict__ x,
@@ -331,9 +332,9 @@ void launch_adj_prep(const DevProblem& P, double* rec, cudaStream_t s) {
     }
 }
 
-// out = a - H v (fixed vertices zero) using part [9*M] scratch.
+// out = a - H v (fixed vertices zero) using part [9*M] and csum [6 nopch] scratch.
 void launch_adj_residual(const DevProblem& P, const double* rec, const double* v, const double* a, double* part,
-                         double* out, cudaStream_t s) {
+                         double* csum, double* out, cudaStream_t s) {
     if (P.M > 0) {
         k_adj_matvec<<<grid_for(P.M), kThreads, 0, s>>>(P, rec, v, part);
         note_launch();
@@ -342,10 +343,7 @@ void launch_adj_residual(const DevProblem& P, const double* rec, const double* v
         k_adj_reduce_lm<<<grid_for(P.L), kThreads, 0, s>>>(P, part, a, out);
         note_launch();
     }
-    if (P.K > 0) {
-        k_adj_reduce_pose<<<P.K, kThreads, 0, s>>>(P, part, a, out);
-        note_launch();
-    }
+    launch_pose_sums6(P, csum, AdjPoseTerm{part}, AdjPoseOut{a, out}, s);
 }
 
 void launch_adj_axpby(int64_t N, double alpha, const double* x, double beta, double* y, cudaStream_t s) {

@@ -960,6 +960,7 @@ static void build_problem(zs_ba_handle* h, const zs_ba_problem* p, const std::ve
     W.W = dalloc<char>(ts * rs * M, own);
     W.pose_aux = dalloc<double>((size_t)K * 24, own);
     W.partial = dalloc<double>(36 * (size_t)P.nsegs, own);
+    W.opch_sum = dalloc<double>(6 * (size_t)std::max<int64_t>(P.nopch, 1), own);
     if (h->tsize == 4) {
         W.jac = dalloc<ObsJac>((size_t)M, own);
         W.jp_pm = dalloc<float4>(3 * (size_t)M, own);
@@ -1726,7 +1727,7 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
                 launch_backsub<double>(P, W, h->st, s);
                 launch_adj_copy(N, W.delta, out, s);
             };
-            launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, r, s);  // r = a, fixed entries zeroed
+            launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, W.opch_sum, r, s);  // r = a, fixed entries zeroed
             const double anorm = std::sqrt(dot(r, r));
             double rn = anorm;
             int it = 0;
@@ -1754,7 +1755,7 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
                 constexpr int kAdjBatch = 8;
                 while (!ch.done) {
                     for (int b = 0; b < kAdjBatch; ++b) {
-                        launch_adj_residual(P, h->adj_rec, pv, zero, h->adj_part, q, s);  // q = -H p
+                        launch_adj_residual(P, h->adj_rec, pv, zero, h->adj_part, W.opch_sum, q, s);  // q = -H p
                         launch_adj_dot(N, pv, q, red2, s);
                         launch_adj_cg_pap(red2, cg, s);                // alpha = rz / p.Hp
                         launch_adj_cg_axpby(N, cg, 0, pv, v, s);       // v += alpha p
@@ -1774,7 +1775,7 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
                 }
                 it = ch.it;
                 // the true residual of the returned v
-                launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, r, s);
+                launch_adj_residual(P, h->adj_rec, v, a, h->adj_part, W.opch_sum, r, s);
                 rn = std::sqrt(dot(r, r));
             }
             // outputs from v

@@ -149,6 +149,7 @@ struct DevWork {
     TcStreams* tc_streams = nullptr;  // and its streams (owned by the handle)
     double* delta = nullptr;   // [n + 3L]
     double* red = nullptr;     // [kReduceBlocks * 4] reduction partials
+    double* opch_sum = nullptr; // [6 nopch] per-chunk partial sums of per-pose reductions (launch_pose_sums6)
     int32_t* ired = nullptr;   // [kReduceBlocks]
 };
 
@@ -303,7 +304,7 @@ int bsolve_max_blocks_per_sm(int bucket, int threads);
 constexpr int kAdjRecord = 64;  // doubles per observation in the adjoint record
 void launch_adj_prep(const DevProblem& P, double* rec, cudaStream_t s);
 void launch_adj_residual(const DevProblem& P, const double* rec, const double* v, const double* a, double* part,
-                         double* out, cudaStream_t s);
+                         double* csum, double* out, cudaStream_t s);
 void launch_adj_axpby(int64_t N, double alpha, const double* x, double beta, double* y, cudaStream_t s);
 void launch_adj_dot(int64_t N, const double* x, const double* y, double* red, cudaStream_t s);
 void launch_adj_copy(int64_t N, const double* src, double* dst, cudaStream_t s);
@@ -485,5 +486,50 @@ cudaError_t launch_refine(int n, const TS* S, const TX* X, const TX* XT, const d
 // or max_it iterations.
 cudaError_t launch_pcg(const DevProblem& P, DevWork& W, LmState* st, int max_it, double tol, cudaStream_t s);
 size_t pcg_doubles(const DevProblem& P);
+
+// Per-pose sums of six values over each pose's observations, spread over the
+// whole GPU (a CTA per pose leaves most SMs idle at a few hundred poses) in a
+// fixed order: a warp per pose-major chunk (<= kOpChunk positions of one
+// pose, P.opch_q; lane i takes positions i, i + 32, then a butterfly) into
+// part[6 c + a], then a thread per (pose, value) adds its pose's chunks in
+// chunk order and hands the total to out(P, k, a, total). term(P, q, s) adds
+// position q's six values to s.
+template <typename Term>
+__global__ void __launch_bounds__(kThreads) k_chunk_sums6(DevProblem P, Term term, double* __restrict__ part) {
+    const int lane = threadIdx.x & 31;
+    const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (c >= P.nopch) return;
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int q = P.opch_q[c] + lane; q < P.opch_q[c + 1]; q += 32) term(P, q, s);
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s[a] += __shfl_xor_sync(0xffffffffu, s[a], off);
+    if (lane == 0)
+#pragma unroll
+        for (int a = 0; a < 6; ++a) part[6 * c + a] = s[a];
+}
+
+template <typename Out>
+__global__ void __launch_bounds__(kThreads) k_chunk_finish6(DevProblem P, const double* __restrict__ part, Out out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= 6LL * P.K) return;
+    const int k = (int)(i / 6), a = (int)(i % 6);
+    double v = 0.0;
+    for (int c = P.pose_opch[k]; c < P.pose_opch[k + 1]; ++c) v += part[6LL * c + a];
+    out(P, k, a, v);
+}
+
+// part: [6 P.nopch] scratch.
+template <typename Term, typename Out>
+void launch_pose_sums6(const DevProblem& P, double* part, Term term, Out out, cudaStream_t s) {
+    if (P.K <= 0) return;
+    if (P.nopch > 0) {
+        k_chunk_sums6<<<grid_for(P.nopch * 32), kThreads, 0, s>>>(P, term, part);
+        note_launch();
+    }
+    k_chunk_finish6<<<grid_for(6LL * P.K), kThreads, 0, s>>>(P, part, out);
+    note_launch();
+}
 
 }  // namespace zs

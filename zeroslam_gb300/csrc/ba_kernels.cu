@@ -798,43 +798,44 @@ __global__ void __launch_bounds__(kThreads) k_s_init(DevProblem P, const double*
     S[idx] = v;
 }
 
+// b_s = b_p - W b_l per pose (launch_pose_sums6): position q's term W_q b_l
+// (pose-major W records) and the pose's output.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_bs(DevProblem P, const T* __restrict__ W, const double* __restrict__ b,
-                                                 double* bs) {
-    constexpr int RS = RecStride<T>::value;
-    __shared__ double sh[kThreads];
-    const int k = blockIdx.x;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    const int e = P.pose_ptr[k + 1];
-    for (int i = P.pose_ptr[k] + threadIdx.x; i < e; i += blockDim.x) {
-        const int64_t o = P.pose_obs[i];
-        if (!P.blk_valid[o]) continue;
-        const T* w = W + (int64_t)i * RS;  // pose-major records
+struct BsTerm {
+    const T* W;
+    const double* b;
+    __device__ void operator()(const DevProblem& P, int q, double s[6]) const {
+        constexpr int RS = RecStride<T>::value;
+        const int64_t o = P.pose_obs[q];
+        if (!P.blk_valid[o]) return;
+        const T* w = W + (int64_t)q * RS;
         const double* bl = b + P.n + 3LL * P.obs_lm[o];
         const T b0 = (T)bl[0], b1 = (T)bl[1], b2 = (T)bl[2];
 #pragma unroll
-        for (int a = 0; a < 6; ++a) acc[a] += (double)(w[a * 3] * b0 + w[a * 3 + 1] * b1 + w[a * 3 + 2] * b2);
+        for (int a = 0; a < 6; ++a) s[a] += (double)(w[a * 3] * b0 + w[a * 3 + 1] * b1 + w[a * 3 + 2] * b2);
     }
-#pragma unroll 1
-    for (int a = 0; a < 6; ++a) {
-        const double v = block_sum(acc[a], sh);
-        if (threadIdx.x == 0) bs[6LL * k + a] = b[6LL * k + a] - v;
-    }
-}
+};
+struct BsOut {
+    const double* b;
+    double* bs;
+    __device__ void operator()(const DevProblem&, int k, int a, double v) const { bs[6LL * k + a] = b[6LL * k + a] - v; }
+};
 
 // delta_l = H_ll^-1 (b_l - H_lp delta_p); delta[0..n) already holds delta_p.
+// A warp per landmark (lanes over its observations, then a butterfly: the
+// whole GPU busy at ten thousand landmarks, and a fixed order).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_backsub(DevProblem P, const T* __restrict__ hpl,
                                                       const double* __restrict__ hinv, const double* __restrict__ b,
                                                       double* delta, const LmState* st) {
     constexpr int RS = RecStride<T>::value;
     if (!st->solve_ok) return;
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t l = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (l >= P.L) return;
-    const double* bl = b + P.n + 3LL * l;
-    double v0 = bl[0], v1 = bl[1], v2 = bl[2];
+    double u0 = 0.0, u1 = 0.0, u2 = 0.0;
     const int e = P.lm_ptr[l + 1];
-    for (int o = P.lm_ptr[l]; o < e; ++o) {
+    for (int o = P.lm_ptr[l] + lane; o < e; o += 32) {
         if (!P.blk_valid[o]) continue;
         const T* h = hpl + (int64_t)P.pm[o] * RS;
         const double* dp = delta + 6LL * P.obs_pose[o];
@@ -846,8 +847,17 @@ __global__ void __launch_bounds__(kThreads) k_backsub(DevProblem P, const T* __r
             s1 += h[a * 3 + 1] * d;
             s2 += h[a * 3 + 2] * d;
         }
-        v0 -= s0; v1 -= s1; v2 -= s2;
+        u0 += s0; u1 += s1; u2 += s2;
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        u0 += __shfl_xor_sync(0xffffffffu, u0, off);
+        u1 += __shfl_xor_sync(0xffffffffu, u1, off);
+        u2 += __shfl_xor_sync(0xffffffffu, u2, off);
+    }
+    if (lane != 0) return;
+    const double* bl = b + P.n + 3LL * l;
+    const double v0 = bl[0] - u0, v1 = bl[1] - u1, v2 = bl[2] - u2;
     const double* I = hinv + (int64_t)l * 9;
     double* dl = delta + P.n + 3LL * l;
     dl[0] = I[0] * v0 + I[1] * v1 + I[2] * v2;
@@ -1111,12 +1121,12 @@ void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream
     if (nn > 0) { k_s_init<<<grid_for(nn), kThreads, 0, s>>>(P, W.hpp, (double*)W.S, st); note_launch(); }
     launch_schur_pairs<T>(P, W, nullptr, s);
     // (the mixed form's b_s comes from its FP64 operator, launch_pcg)
-    if (sizeof(T) == 8 && P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
+    if (sizeof(T) == 8) launch_bs<T>(P, W, s);
 }
 
 template <typename T>
 void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s) {
-    if (P.K > 0) { k_bs<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs); note_launch(); }
+    launch_pose_sums6(P, W.opch_sum, BsTerm<T>{(const T*)W.W, W.b}, BsOut{W.b, W.bs}, s);
 }
 
 template <typename T>
@@ -1130,7 +1140,10 @@ void launch_w(const DevProblem& P, DevWork& W, cudaStream_t s) {
 
 template <typename T>
 void launch_backsub(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
-    if (P.L > 0) { k_backsub<T><<<grid_for(P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st); note_launch(); }
+    if (P.L > 0) {
+        k_backsub<T><<<grid_for(32LL * P.L), kThreads, 0, s>>>(P, (const T*)W.hpl, W.hll_inv, W.b, W.delta, st);
+        note_launch();
+    }
 }
 
 void launch_update(const DevProblem& P, DevWork& W, const LmState* st, cudaStream_t s) {
