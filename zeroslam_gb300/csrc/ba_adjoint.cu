@@ -325,6 +325,66 @@ __global__ void __launch_bounds__(kThreads) k_adj_out(DevProblem P, const double
     }
 }
 
+// Xi = L^-1 of the reduced system's FP64 factor (row-major lower L, n x n)
+// and XiT = its transpose, for the preconditioner of the adjoint's conjugate
+// gradients, whose factor stays fixed for all its iterations: a warp per
+// column j, forward substitution x_i = (delta_ij - sum_{j<=k<i} L_ik x_k) /
+// L_ii with lanes over k and a butterfly (a fixed order), x in shared memory.
+__global__ void __launch_bounds__(kAdjInvWarps * 32) k_adj_tri_inverse(int n, const double* __restrict__ L,
+                                                                     double* __restrict__ Xi, double* __restrict__ XiT) {
+    extern __shared__ double xs[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = blockIdx.x * kAdjInvWarps + warp;
+    if (j >= n) return;  // (whole warps)
+    double* x = xs + (size_t)warp * n;
+    for (int i = j; i < n; ++i) {
+        double t = 0.0;
+        for (int k = j + lane; k < i; k += 32) t += L[(int64_t)i * n + k] * x[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        const double xi = ((i == j ? 1.0 : 0.0) - t) / L[(int64_t)i * n + i];
+        if (lane == 0) x[i] = xi;
+        __syncwarp();
+    }
+    for (int i = lane; i < n; i += 32) {
+        const double v = i >= j ? x[i] : 0.0;
+        Xi[(int64_t)i * n + j] = v;
+        XiT[(int64_t)j * n + i] = v;
+    }
+}
+
+// y = M x for a triangular M (upper = 0: columns <= row; 1: columns >= row),
+// a warp per row, lanes over the row, a butterfly.
+__global__ void __launch_bounds__(kThreads) k_adj_gemv_tri(int n, const double* __restrict__ M,
+                                                           const double* __restrict__ x, double* __restrict__ y,
+                                                           int upper) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const int lo = upper ? (int)i : 0, hi = upper ? n : (int)i + 1;
+    double t = 0.0;
+    for (int k = lo + lane; k < hi; k += 32) t += M[i * n + k] * x[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane == 0) y[i] = t;
+}
+
+void launch_adj_tri_inverse(int n, const double* L, double* Xi, double* XiT, cudaStream_t s) {
+    if (n <= 0) return;
+    const size_t smem = sizeof(double) * (size_t)kAdjInvWarps * n;
+    k_adj_tri_inverse<<<(n + kAdjInvWarps - 1) / kAdjInvWarps, kAdjInvWarps * 32, smem, s>>>(n, L, Xi, XiT);
+    note_launch();
+}
+
+// y = XiT (Xi b): the reduced solve L L^T y = b with the explicit inverse.
+void launch_adj_apply_inverse(int n, const double* Xi, const double* XiT, const double* b, double* tmp, double* y,
+                              cudaStream_t s) {
+    if (n <= 0) return;
+    k_adj_gemv_tri<<<grid_for(32LL * n), kThreads, 0, s>>>(n, Xi, b, tmp, 0);
+    k_adj_gemv_tri<<<grid_for(32LL * n), kThreads, 0, s>>>(n, XiT, tmp, y, 1);
+    note_launch(2);
+}
+
 void launch_adj_prep(const DevProblem& P, double* rec, cudaStream_t s) {
     if (P.M > 0) {
         k_adj_prep<<<grid_for(P.M), kThreads, 0, s>>>(P, rec);

@@ -359,6 +359,7 @@ struct zs_ba_handle {
     double* adj_rec = nullptr;   // adjoint buffers, allocated on first use (owned)
     double* adj_part = nullptr;
     double* adj_vec = nullptr;   // a, v, r, z, p, q, zero: 7 x (n + 3L)
+    double* adj_inv = nullptr;   // L^-1, its transpose and n doubles (n <= kAdjInvMaxN)
     std::vector<int64_t> perm;   // landmark-major position -> caller's observation index
     int tsize = 8;
     HostScratch hscratch;        // build_problem's host arrays (pinned, reused)
@@ -411,7 +412,7 @@ struct zs_ba_handle {
         else owned.release_all();
         P = DevProblem{};
         W = DevWork{};
-        adj_rec = adj_part = adj_vec = nullptr;
+        adj_rec = adj_part = adj_vec = adj_inv = nullptr;
         batch = false;
         B = BatchDev{};
         wpose0.clear();
@@ -1673,6 +1674,7 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
             h->adj_rec = dalloc<double>((size_t)std::max<int64_t>(P.M, 1) * kAdjRecord, h->owned);
             h->adj_part = dalloc<double>((size_t)std::max<int64_t>(P.M, 1) * 9, h->owned);
             h->adj_vec = dalloc<double>((size_t)std::max<int64_t>(N, 1) * 7, h->owned);
+            if (n > 0 && n <= kAdjInvMaxN) h->adj_inv = dalloc<double>((size_t)n * (2 * (size_t)n + 1), h->owned);
         }
         double* a = h->adj_vec;
         double* v = a + N;
@@ -1718,12 +1720,21 @@ int zs_ba_adjoint(zs_ba_handle* h, const double* dloss_dpose, const double* dlos
                 for (int i = 0; i < kReduceBlocks; ++i) t += red[i];
                 return t;
             };
-            // z = M^-1 x through the Schur complement and the reduced factor
+            // z = M^-1 x through the Schur complement and the reduced factor;
+            // up to kAdjInvMaxN the factor's inverse is formed once and each
+            // reduced solve is two triangular products
+            double* Xi = h->adj_inv;
+            double* XiT = Xi ? Xi + (size_t)n * n : nullptr;
+            if (Xi) launch_adj_tri_inverse(n, (const double*)W.F, Xi, XiT, s);
             auto precondition = [&](const double* x, double* out) {
                 launch_adj_copy(N, x, W.b, s);
                 launch_bs<double>(P, W, s);
-                ZS_CUDA((launch_solve_refine<double, double>(n, W.S, (const double*)W.F, (const double*)W.D, W.bs,
-                                                             W.delta, W.work, h->st, 0, 0.0, s)));
+                if (Xi) {
+                    launch_adj_apply_inverse(n, Xi, XiT, W.bs, XiT + (size_t)n * n, W.delta, s);
+                } else {
+                    ZS_CUDA((launch_solve_refine<double, double>(n, W.S, (const double*)W.F, (const double*)W.D,
+                                                                 W.bs, W.delta, W.work, h->st, 0, 0.0, s)));
+                }
                 launch_backsub<double>(P, W, h->st, s);
                 launch_adj_copy(N, W.delta, out, s);
             };

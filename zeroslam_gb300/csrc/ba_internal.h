@@ -305,6 +305,14 @@ constexpr int kAdjRecord = 64;  // doubles per observation in the adjoint record
 void launch_adj_prep(const DevProblem& P, double* rec, cudaStream_t s);
 void launch_adj_residual(const DevProblem& P, const double* rec, const double* v, const double* a, double* part,
                          double* csum, double* out, cudaStream_t s);
+// The adjoint's preconditioner with an explicit inverse of its fixed FP64
+// reduced factor (n <= kAdjInvMaxN): Xi = L^-1 and XiT once, then
+// y = XiT (Xi b) per application (tmp: n doubles).
+constexpr int kAdjInvMaxN = 1024;
+constexpr int kAdjInvWarps = 4;  // columns per CTA (shared memory: 8 n bytes each)
+void launch_adj_tri_inverse(int n, const double* L, double* Xi, double* XiT, cudaStream_t s);
+void launch_adj_apply_inverse(int n, const double* Xi, const double* XiT, const double* b, double* tmp, double* y,
+                              cudaStream_t s);
 void launch_adj_axpby(int64_t N, double alpha, const double* x, double beta, double* y, cudaStream_t s);
 void launch_adj_dot(int64_t N, const double* x, const double* y, double* red, cudaStream_t s);
 void launch_adj_copy(int64_t N, const double* src, double* dst, cudaStream_t s);
