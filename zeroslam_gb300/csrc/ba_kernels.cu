@@ -821,6 +821,23 @@ struct BsOut {
     __device__ void operator()(const DevProblem&, int k, int a, double v) const { bs[6LL * k + a] = b[6LL * k + a] - v; }
 };
 
+// The same with a CTA per pose, for batches of thousands of window poses
+// (the grid is full without the chunks, and it is one launch, not two).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bs_per_pose(DevProblem P, const T* __restrict__ W,
+                                                          const double* __restrict__ b, double* bs) {
+    __shared__ double sh[kThreads];
+    const int k = blockIdx.x;
+    const BsTerm<T> term{W, b};
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = P.pose_ptr[k] + threadIdx.x; q < P.pose_ptr[k + 1]; q += blockDim.x) term(P, q, acc);
+#pragma unroll 1
+    for (int a = 0; a < 6; ++a) {
+        const double v = block_sum(acc[a], sh);
+        if (threadIdx.x == 0) bs[6LL * k + a] = b[6LL * k + a] - v;
+    }
+}
+
 // delta_l = H_ll^-1 (b_l - H_lp delta_p); delta[0..n) already holds delta_p.
 // A warp per landmark (lanes over its observations, then a butterfly: the
 // whole GPU busy at ten thousand landmarks, and a fixed order).
@@ -1126,7 +1143,12 @@ void launch_schur(const DevProblem& P, DevWork& W, const LmState* st, cudaStream
 
 template <typename T>
 void launch_bs(const DevProblem& P, DevWork& W, cudaStream_t s) {
-    launch_pose_sums6(P, W.opch_sum, BsTerm<T>{(const T*)W.W, W.b}, BsOut{W.b, W.bs}, s);
+    if (P.K >= 1024) {
+        k_bs_per_pose<T><<<P.K, kThreads, 0, s>>>(P, (const T*)W.W, W.b, W.bs);
+        note_launch();
+    } else {
+        launch_pose_sums6(P, W.opch_sum, BsTerm<T>{(const T*)W.W, W.b}, BsOut{W.b, W.bs}, s);
+    }
 }
 
 template <typename T>
