@@ -67,8 +67,9 @@ def parse():
     ap.add_argument("--batch-graph", type=int, default=1, choices=[0, 1],
                     help="1: one graph launch per batched solve; 0: host loop over rounds (same kernels; "
                          "for profilers that cannot see kernels inside conditional graph nodes)")
-    ap.add_argument("--single", choices=["mixed", "fp64", "batch-mixed", "batch-fp64"], default=None,
-                    help="run one solve of --iterations (default 2) on the workload and exit; for profilers")
+    ap.add_argument("--single", choices=["mixed", "fp64", "batch-mixed", "batch-fp64", "adjoint"], default=None,
+                    help="run one solve of --iterations (default 2) on the workload and exit (adjoint: the "
+                         "configuration-3 forward solve and one adjoint); for profilers")
     return ap.parse_args()
 
 
@@ -936,6 +937,20 @@ def single_solve(args):
     """One solve on the workload, nothing else: the unit a profiler captures."""
     from zeroslam_gb300 import ba
 
+    if args.single == "adjoint":  # configuration 3's scene: the forward solve, then one adjoint
+        from zeroslam_gb300 import scenes
+
+        sc = scenes.adjoint_scene()
+        rng = np.random.default_rng(11)
+        a_pose = rng.normal(size=(sc.K, 6)) * (sc.pose_fixed[:, None] == 0)
+        a_lm = rng.normal(size=(sc.L, 3)) * (sc.landmark_fixed[:, None] == 0)
+        with ba.BundleAdjuster(precision=ba.FP64) as h:
+            h.set_problem(sc)
+            h.solve(sc.iterations)
+            _, _, rep = h.adjoint(a_pose, a_lm)
+        print(json.dumps({"single": "adjoint", "observations": sc.M, "ms_total": rep.ms_total,
+                          "cg_iterations": rep.iterations, "rel_residual": rep.rel_residual}), flush=True)
+        return
     prec = ba.MIXED if args.single.endswith("mixed") else ba.FP64
     if args.single.startswith("batch"):
         from zeroslam_gb300 import scenes
