@@ -191,18 +191,27 @@ __global__ void __launch_bounds__(kThreads) k_adj_axpby(int64_t N, double alpha,
 // ---- the conjugate-gradient loop's scalars on the device ----
 // The host enqueues iterations in batches and reads c->done once per batch;
 // every update below is skipped once done is set, so iterations enqueued past
-// the stop change nothing. The sums over the kReduceBlocks partials run in
-// block order on one thread: the same values a host-side sum gives.
+// the stop change nothing.
+
+// The kReduceBlocks partials of a dot product, added by one warp (lane l
+// takes partials l, l + 32, ..., then a butterfly): a fixed order, every lane
+// gets the sum. (One thread adding them in turn waited on 304 dependent FP64
+// additions, three times per iteration.)
 __device__ __forceinline__ double cg_sum(const double* red) {
+    const int lane = threadIdx.x & 31;
     double t = 0.0;
-    for (int i = 0; i < kReduceBlocks; ++i) t += red[i];
+    for (int i = lane; i < kReduceBlocks; i += 32) t += red[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
     return t;
 }
 
 // pAp = -(p . q) with q = -H p; stop (done = 2) unless pAp > 0, else alpha.
+// (One warp: the sum is the warp's, lane 0 writes.)
 __global__ void k_adj_cg_pap(const double* __restrict__ red, AdjCg* c) {
-    if (threadIdx.x || c->done) return;
+    if (c->done) return;  // (uniform)
     const double pAp = -cg_sum(red);
+    if (threadIdx.x) return;
     if (!(pAp > 0.0)) {
         c->done = 2;
         return;
@@ -213,8 +222,10 @@ __global__ void k_adj_cg_pap(const double* __restrict__ red, AdjCg* c) {
 // |r| after the update: one more iteration done; stop at the tolerance
 // (done = 1) or at the iteration limit (done = 3).
 __global__ void k_adj_cg_rn(const double* __restrict__ red, AdjCg* c) {
-    if (threadIdx.x || c->done) return;
-    c->rn = sqrt(cg_sum(red));
+    if (c->done) return;
+    const double rn = sqrt(cg_sum(red));
+    if (threadIdx.x) return;
+    c->rn = rn;
     c->it += 1;
     if (c->rn <= c->tol * c->anorm) c->done = 1;
     else if (c->it >= c->max_it) c->done = 3;
@@ -222,8 +233,9 @@ __global__ void k_adj_cg_rn(const double* __restrict__ red, AdjCg* c) {
 
 // r . z of the new preconditioned residual: beta and the new rz.
 __global__ void k_adj_cg_rz(const double* __restrict__ red, AdjCg* c) {
-    if (threadIdx.x || c->done) return;
+    if (c->done) return;
     const double rz_new = cg_sum(red);
+    if (threadIdx.x) return;
     c->beta = rz_new / c->rz;
     c->rz = rz_new;
 }
